@@ -1,0 +1,88 @@
+"""Builds gromacs-fmm_gb300/lib/libgbfmm.so for sm_103a (in-tree, no cmake).
+
+Each translation unit is compiled by its own nvcc process in parallel, then the
+objects are linked into one shared library with a plain C ABI (include/gbfmm.h).
+Only one -gencode target: compute_103a / sm_103a.
+"""
+import concurrent.futures as cf
+import os
+import platform
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+OUT = os.path.join(HERE, "lib")
+LIB = os.path.join(OUT, "libgbfmm.so")
+
+SOURCES = ["kernels.cu", "m2l_tc.cu", "solver.cu", "operators.cpp"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def nvcc():
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    p = os.path.join(cuda, "bin", "nvcc")
+    return p if os.path.exists(p) else shutil.which("nvcc")
+
+
+def _flags():
+    return ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+                   "--expt-relaxed-constexpr", "-I", CSRC, "-I", os.path.join(ROOT, "include")]
+
+
+def _elf_matches_host(path):
+    """True if 'path' is an ELF object for this machine's architecture."""
+    want = {"x86_64": 62, "aarch64": 183, "arm64": 183}.get(platform.machine())
+    try:
+        with open(path, "rb") as f:
+            hdr = f.read(20)
+    except OSError:
+        return False
+    if len(hdr) < 20 or hdr[:4] != b"\x7fELF":
+        return False
+    return want is None or int.from_bytes(hdr[18:20], "little") == want
+
+
+def _stale(out, deps):
+    if not os.path.exists(out) or not _elf_matches_host(out):
+        return True
+    t = os.path.getmtime(out)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build(force=False, verbose=False):
+    objdir = os.path.join(OUT, "obj-" + platform.machine())
+    os.makedirs(objdir, exist_ok=True)
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
+    headers.append(os.path.join(ROOT, "include", "gbfmm.h"))
+    srcs = [s for s in SOURCES if os.path.exists(os.path.join(CSRC, s))]
+    objs = []
+    jobs = []
+    for s in srcs:
+        src = os.path.join(CSRC, s)
+        obj = os.path.join(objdir, s + ".o")
+        objs.append(obj)
+        if force or _stale(obj, [src] + headers):
+            lang = ["-x", "cu"] if s.endswith(".cu") else ["-x", "c++"]
+            jobs.append([nvcc()] + _flags() + lang + ["-c", src, "-o", obj])
+    if jobs:
+        with cf.ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
+            res = list(ex.map(lambda c: subprocess.run(c, capture_output=True, text=True), jobs))
+        for c, r in zip(jobs, res):
+            if verbose or r.returncode != 0:
+                sys.stderr.write(" ".join(c) + "\n" + r.stdout + r.stderr)
+            if r.returncode != 0:
+                raise RuntimeError("nvcc failed for " + c[-3])
+    if force or jobs or _stale(LIB, objs):
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
+            raise RuntimeError("link failed")
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))

@@ -1,0 +1,757 @@
+// Device kernels of the GB300 FMM (sm_103a).
+//
+// Data layout in HBM:
+//   atoms      float4 (u, q) per body in tree order; u = (x - leaf centre) / h_leaf
+//   M, L       per level k: 8^k rows of Rpad floats (real (P+1)^2 representation,
+//              scaled by the level's cell size h_k: M~_n = M_n/h^n, L~_j = L_j h^(j+1)),
+//              rows indexed by Morton code
+//   root       M~_0, L~_0 in FP64 (plus an FP32 copy of M~_0 for level-1 M2L)
+//   field      float4 (phi, grad) per body in tree order, scaled units
+#include <cuda_runtime.h>
+
+#include <atomic>
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace gbfmm {
+
+// Kernel launches issued by this library (all launch_* wrappers count theirs).
+std::atomic<long> g_kernel_launches{0};
+#define COUNT_LAUNCH() g_kernel_launches.fetch_add(1, std::memory_order_relaxed)
+
+// ------------------------------------------------------------------ tree
+
+__global__ void __launch_bounds__(256) k_tree_keys(TreeArgs a)
+{
+    extern __shared__ float sh[];
+    const int nd = 1 << a.depth;
+    const StepConst* sc = a.sc;
+    float* th = sh;                                   // 3 x (nd+1)
+    float2* ce = reinterpret_cast<float2*>(sh + ((3 * (nd + 1) + 1) & ~1));  // 3 x nd
+    for (int i = threadIdx.x; i < 3 * (nd + 1); i += blockDim.x) th[i] = sc->thresh[i / (nd + 1)][i % (nd + 1)];
+    for (int i = threadIdx.x; i < 3 * nd; i += blockDim.x) ce[i] = sc->centre[i / nd][i % nd];
+    const float inv_h = sc->inv_h;
+    const float* coords = sc->coords;
+    __syncthreads();
+    double s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+    int bad = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) {
+        float x[3] = {coords[3 * i], coords[3 * i + 1], coords[3 * i + 2]};
+        float q = a.charges[i];
+        if (!isfinite(x[0]) || !isfinite(x[1]) || !isfinite(x[2]) || !isfinite(q)) bad = 1;
+        int iv[3];
+        float u[3];
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            float kf = fminf(fmaxf(x[d] * inv_h, 0.0f), (float)(nd - 1));
+            int k = (int)kf;
+            const float* T = th + d * (nd + 1);
+            // cell k holds T[k] < x <= T[k+1]: the strict '>' descent of tree.cpp:49-51
+            while (k > 0 && !(x[d] > T[k])) k--;
+            while (k < nd - 1 && x[d] > T[k + 1]) k++;
+            iv[d] = k;
+            float2 c = ce[d * nd + k];
+            u[d] = ((x[d] - c.x) - c.y) * inv_h;
+        }
+        uint32_t code = morton_encode(iv[0], iv[1], iv[2]);
+        a.code[i] = code;
+        a.uq[i] = make_float4(u[0], u[1], u[2], q);
+        atomicAdd(&a.counts[code], 1);
+        double dq = (double)q;
+        s0 += dq * (double)x[0];
+        s1 += dq * (double)x[1];
+        s2 += dq * (double)x[2];
+        s3 += dq;
+    }
+    // block reduction of the dipole and total charge (FP64)
+    for (int o = 16; o > 0; o >>= 1) {
+        s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+        s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+        s3 += __shfl_xor_sync(0xffffffffu, s3, o);
+    }
+    __shared__ double red[8][4];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        red[warp][0] = s0; red[warp][1] = s1; red[warp][2] = s2; red[warp][3] = s3;
+    }
+    __syncthreads();
+    if (threadIdx.x < 4) {
+        double t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w][threadIdx.x];
+        atomicAdd(&a.sums[threadIdx.x], t);
+    }
+    if (bad) atomicOr(&a.flags[0], 1);
+}
+
+void launch_tree_keys(const TreeArgs& a, cudaStream_t s)
+{
+    int nd = 1 << a.depth;
+    size_t shm = sizeof(float) * (((3 * (nd + 1) + 1) & ~1) + 6 * nd);
+    int blocks = (a.n + 255) / 256;
+    if (blocks > 4 * 152) blocks = 4 * 152;
+    if (blocks < 1) blocks = 1;
+    COUNT_LAUNCH();
+    k_tree_keys<<<blocks, 256, shm, s>>>(a);
+}
+
+// Exclusive scan of n ints (out[n] = total), three phases of 2048-element blocks.
+__global__ void __launch_bounds__(512) k_scan_blocks(const int* in, int* out, int n, int* bsum)
+{
+    __shared__ int ws[16];
+    const int base = blockIdx.x * 2048 + threadIdx.x * 4;
+    int v[4], t = 0;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        v[i] = base + i < n ? in[base + i] : 0;
+        t += v[i];
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int x = t;
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) ws[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int w = lane < 16 ? ws[lane] : 0;
+        for (int o = 1; o < 16; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < 16) ws[lane] = w;
+    }
+    __syncthreads();
+    int excl = x - t + (warp > 0 ? ws[warp - 1] : 0);
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        if (base + i < n) out[base + i] = excl;
+        excl += v[i];
+    }
+    if (threadIdx.x == 511) bsum[blockIdx.x] = excl;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_top(int* bsum, int nb, int* total)
+{
+    __shared__ int ws[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int carry = 0;
+    for (int base = 0; base < nb; base += 1024) {
+        int i = base + threadIdx.x;
+        int v = i < nb ? bsum[i] : 0;
+        int x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) ws[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            int w = ws[lane];
+            for (int o = 1; o < 32; o <<= 1) {
+                int y = __shfl_up_sync(0xffffffffu, w, o);
+                if (lane >= o) w += y;
+            }
+            ws[lane] = w;
+        }
+        __syncthreads();
+        int incl = x + (warp > 0 ? ws[warp - 1] : 0);
+        if (i < nb) bsum[i] = carry + incl - v;
+        int blocktotal = ws[31];
+        __syncthreads();
+        carry += blocktotal;
+    }
+    if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void k_scan_add(int* out, int n, const int* bsum)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] += bsum[i / 2048];
+}
+
+void launch_exclusive_scan(const int* in, int* out, int n, int* scratch, cudaStream_t s)
+{
+    int nb = (n + 2047) / 2048;
+    COUNT_LAUNCH();
+    k_scan_blocks<<<nb, 512, 0, s>>>(in, out, n, scratch);
+    COUNT_LAUNCH();
+    k_scan_top<<<1, 1024, 0, s>>>(scratch, nb, out + n);
+    if (nb > 1) { COUNT_LAUNCH(); k_scan_add<<<(n + 255) / 256, 256, 0, s>>>(out, n, scratch); }
+}
+
+__global__ void k_scatter(const uint32_t* code, int n, int* cursor, int* tmp_idx)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) tmp_idx[atomicAdd(&cursor[code[i]], 1)] = i;
+}
+
+void launch_scatter(const uint32_t* code, int n, int* cursor, int* tmp_idx, cudaStream_t s)
+{
+    if (n > 0) { COUNT_LAUNCH(); k_scatter<<<(n + 255) / 256, 256, 0, s>>>(code, n, cursor, tmp_idx); }
+}
+
+// Stable order inside each leaf (ascending input index), which makes the body
+// order identical to the per-level stable counting sort of tree.cpp:43-74.
+__global__ void __launch_bounds__(256) k_leaf_sort(const int* off, int nleaf, const int* tmp_idx, const float4* uq,
+                                                   int* order, float4* atoms, int* atom_leaf)
+{
+    const int lane = threadIdx.x & 31;
+    const int leaf = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (leaf >= nleaf) return;
+    const int b = off[leaf], n = off[leaf + 1] - b;
+    if (n <= 32) {
+        int v = lane < n ? tmp_idx[b + lane] : 0x7fffffff;
+        int rank = 0;
+        for (int j = 0; j < 32; j++) {
+            int w = __shfl_sync(0xffffffffu, v, j);
+            rank += (w < v);
+        }
+        if (lane < n) {
+            order[b + rank] = v;
+            atoms[b + rank] = uq[v];
+            atom_leaf[b + rank] = leaf;
+        }
+    } else {
+        for (int e = lane; e < n; e += 32) {
+            int v = tmp_idx[b + e];
+            int rank = 0;
+            for (int j = 0; j < n; j++) rank += (tmp_idx[b + j] < v);
+            order[b + rank] = v;
+            atoms[b + rank] = uq[v];
+            atom_leaf[b + rank] = leaf;
+        }
+    }
+}
+
+void launch_leaf_sort(const int* offsets, int nleaf, int* tmp_idx, const float4* uq, const uint32_t* code, int* order,
+                      float4* atoms, int* atom_leaf, cudaStream_t s)
+{
+    (void)code;
+    long threads = (long)nleaf * 32;
+    COUNT_LAUNCH();
+    k_leaf_sort<<<(int)((threads + 255) / 256), 256, 0, s>>>(offsets, nleaf, tmp_idx, uq, order, atoms, atom_leaf);
+}
+
+// ------------------------------------------------------------------ P2M
+
+// Streams the regular harmonics Y_n^m(u), m >= 0, in (m outer, n inner) order and
+// calls f(n, m, re, im) for each.  Recurrences (exafmm normalisation):
+//   Y_m^m = Y_{m-1}^{m-1} (x+iy) / (2m),  Y_{m+1}^m = -z Y_m^m,
+//   Y_{n+1}^m = -((2n+1) z Y_n^m + r^2 Y_{n-1}^m) / ((n+m+1)(n-m+1)).
+template <int P, typename F>
+__device__ __forceinline__ void stream_regular(float x, float y, float z, F&& f)
+{
+    const float r2 = x * x + y * y + z * z;
+    float sr = 1.f, si = 0.f;
+#pragma unroll
+    for (int m = 0; m <= P; m++) {
+        if (m > 0) {
+            const float inv = 1.0f / (2 * m);
+            float tr = (sr * x - si * y) * inv, ti = (sr * y + si * x) * inv;
+            sr = tr;
+            si = ti;
+        }
+        f(m, m, sr, si);
+        if (m + 1 <= P) {
+            float ar = sr, ai = si;          // Y_{n-1}
+            float br = -z * sr, bi = -z * si;  // Y_n
+            f(m + 1, m, br, bi);
+#pragma unroll
+            for (int n = m + 1; n < P; n++) {
+                const float c = 1.0f / ((n + m + 1) * (n - m + 1));
+                float cr = -((2 * n + 1) * z * br + r2 * ar) * c;
+                float ci = -((2 * n + 1) * z * bi + r2 * ai) * c;
+                f(n + 1, m, cr, ci);
+                ar = br; ai = bi;
+                br = cr; bi = ci;
+            }
+        }
+    }
+}
+
+template <int P, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) k_p2m(const int* off, int nleaf, const float4* atoms, float* M, int Rpad)
+{
+    constexpr int R = (P + 1) * (P + 1);
+    constexpr int LD = 33;
+    extern __shared__ float sm[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int leaf = blockIdx.x * WARPS + warp;
+    if (leaf >= nleaf) return;
+    float* S = sm + warp * R * LD;
+    for (int r = 0; r < R; r++) S[r * LD + lane] = 0.f;
+    const int b = off[leaf], n = off[leaf + 1] - b;
+    for (int c0 = 0; c0 < n; c0 += 32) {
+        float4 a = c0 + lane < n ? atoms[b + c0 + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float q = a.w;
+        // M~ += q conj(Y(u)), kernel.cu:228-240 evaluated at -phi
+        stream_regular<P>(a.x, a.y, a.z, [&](int nn, int mm, float yr, float yi) {
+            S[ridx_re(nn, mm) * LD + lane] += q * yr;
+            if (mm > 0) S[ridx_im(nn, mm) * LD + lane] -= q * yi;
+        });
+    }
+    __syncwarp();
+    float* out = M + (long)leaf * Rpad;
+    for (int r = lane; r < R; r += 32) {
+        float t = 0.f;
+#pragma unroll 8
+        for (int c = 0; c < 32; c++) t += S[r * LD + c];
+        out[r] = t;
+    }
+}
+
+template <int P>
+static void p2m_dispatch(const int* off, int nleaf, const float4* atoms, float* M, int Rpad, cudaStream_t s)
+{
+    constexpr int R = (P + 1) * (P + 1);
+    constexpr int W = R <= 169 ? 4 : 2;
+    size_t shm = sizeof(float) * W * R * 33;
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_p2m<P, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+        attr = true;
+    }
+    COUNT_LAUNCH();
+    k_p2m<P, W><<<(nleaf + W - 1) / W, W * 32, shm, s>>>(off, nleaf, atoms, M, Rpad);
+}
+
+#define GBFMM_ORDER_SWITCH(P, CALL)            \
+    switch (P) {                              \
+        case 2: { constexpr int PP = 2; CALL; } break;   \
+        case 3: { constexpr int PP = 3; CALL; } break;   \
+        case 4: { constexpr int PP = 4; CALL; } break;   \
+        case 5: { constexpr int PP = 5; CALL; } break;   \
+        case 6: { constexpr int PP = 6; CALL; } break;   \
+        case 7: { constexpr int PP = 7; CALL; } break;   \
+        case 8: { constexpr int PP = 8; CALL; } break;   \
+        case 9: { constexpr int PP = 9; CALL; } break;   \
+        case 10: { constexpr int PP = 10; CALL; } break; \
+        case 11: { constexpr int PP = 11; CALL; } break; \
+        case 12: { constexpr int PP = 12; CALL; } break; \
+        case 13: { constexpr int PP = 13; CALL; } break; \
+        case 14: { constexpr int PP = 14; CALL; } break; \
+        case 15: { constexpr int PP = 15; CALL; } break; \
+        case 16: { constexpr int PP = 16; CALL; } break; \
+        default: break;                       \
+    }
+
+void launch_p2m(int P, const int* offsets, int nleaf, const float4* atoms, float* M_leaf, int Rpad, cudaStream_t s)
+{
+    GBFMM_ORDER_SWITCH(P, p2m_dispatch<PP>(offsets, nleaf, atoms, M_leaf, Rpad, s));
+}
+
+// ------------------------------------------------------------------ L2P
+
+// phi = sum_n [Re(L_n0 Y_n0) + 2 sum_{m>0} Re(L_nm Y_nm)], the L2P sum of kernel.cu:635-651,
+// and its Cartesian gradient from the ladder identities
+//   dz Y_nm = -Y_{n-1,m};  (dx+i dy) Y_nm = -Y_{n-1,m+1};
+//   (dx-i dy) Y_nm = Y_{n-1,m-1} (m>0),  (dx-i dy) Y_n0 = -conj(Y_{n-1,1}).
+template <int P, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) k_l2p(const int* off, int nleaf, const float4* atoms, const float* L,
+                                                   int Rpad, float4* field)
+{
+    constexpr int R = (P + 1) * (P + 1);
+    __shared__ float Ls[WARPS][R + 1];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int leaf = blockIdx.x * WARPS + warp;
+    if (leaf >= nleaf) return;
+    const float* src = L + (long)leaf * Rpad;
+    float* Lw = Ls[warp];
+    for (int r = lane; r < R; r += 32) Lw[r] = src[r];
+    __syncwarp();
+    const int b = off[leaf], n = off[leaf + 1] - b;
+    auto lre = [&](int nn, int mm) { return Lw[ridx_re(nn, mm)]; };
+    auto lim = [&](int nn, int mm) { return mm > 0 ? Lw[ridx_im(nn, mm)] : 0.f; };
+    for (int c0 = 0; c0 < n; c0 += 32) {
+        if (c0 + lane >= n) break;
+        const float4 a = atoms[b + c0 + lane];
+        float phi = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
+        stream_regular<P>(a.x, a.y, a.z, [&](int np, int mp, float ya, float yb) {
+            const float wm = mp == 0 ? 1.f : 2.f;
+            phi += wm * (lre(np, mp) * ya - lim(np, mp) * yb);
+            if (np + 1 <= P) {
+                float Lr = lre(np + 1, mp), Li = lim(np + 1, mp);
+                gz -= wm * (Lr * ya - Li * yb);
+                if (mp >= 1) {
+                    const float w = (mp - 1) == 0 ? 1.f : 2.f;
+                    Lr = lre(np + 1, mp - 1);
+                    Li = lim(np + 1, mp - 1);
+                    gx -= 0.5f * w * (Lr * ya - Li * yb);
+                    gy -= 0.5f * w * (Lr * yb + Li * ya);
+                }
+                Lr = lre(np + 1, mp + 1);
+                Li = lim(np + 1, mp + 1);
+                gx += (Lr * ya - Li * yb);
+                gy -= (Lr * yb + Li * ya);
+                if (mp == 1) {
+                    Lr = lre(np + 1, 0);
+                    gx -= 0.5f * Lr * ya;
+                    gy -= 0.5f * Lr * yb;
+                }
+            }
+        });
+        field[b + c0 + lane] = make_float4(phi, gx, gy, gz);
+    }
+}
+
+void launch_l2p(int P, const int* offsets, int nleaf, const float4* atoms, const float* L_leaf, int Rpad,
+                float4* field, cudaStream_t s)
+{
+    COUNT_LAUNCH();
+    GBFMM_ORDER_SWITCH(P, (k_l2p<PP, 4><<<(nleaf + 3) / 4, 128, 0, s>>>(offsets, nleaf, atoms, L_leaf, Rpad, field)));
+}
+
+// ------------------------------------------------------------------ P2P
+
+constexpr int P2P_THREADS = 128;
+constexpr int P2P_MAXS = 2048;  // staged source bodies per pass
+constexpr int P2P_MAXT = 256;   // targets per pass
+
+// One CTA per target leaf.  The source bodies of the 81 near leaves are staged in
+// shared memory, shifted into the target leaf's frame (scaled units, integer
+// offsets of the stencil, so the periodic shift is exact), then each warp sweeps a
+// quarter of them with one lane per target body.  Pair term as kernel.cu:480-490:
+// phi += q/r, grad += q (x_j - x_i)/r^3, skipped when r = 0.
+__global__ void __launch_bounds__(P2P_THREADS) k_p2p(const int* off, int depth, int periodic, const float4* atoms,
+                                                     const int* stencil, int nst, float4* field)
+{
+    __shared__ float4 src[P2P_MAXS];
+    __shared__ float4 acc[P2P_MAXT];
+    __shared__ int e_off[128];
+    __shared__ int e_beg[128];
+    __shared__ float4 e_d[128];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nd = 1 << depth;
+    const uint32_t tcode = blockIdx.x;
+    int tx, ty, tz;
+    morton_decode(tcode, tx, ty, tz);
+    const int tb = off[tcode], nt = off[tcode + 1] - tb;
+    if (nt == 0) return;
+    // source leaves of the stencil
+    int cnt = 0;
+    if (tid < nst) {
+        int vx = tx + stencil[3 * tid], vy = ty + stencil[3 * tid + 1], vz = tz + stencil[3 * tid + 2];
+        bool ok = true;
+        if (periodic) {
+            vx &= nd - 1; vy &= nd - 1; vz &= nd - 1;
+        } else {
+            ok = vx >= 0 && vy >= 0 && vz >= 0 && vx < nd && vy < nd && vz < nd;
+        }
+        if (ok) {
+            uint32_t sc = morton_encode(vx, vy, vz);
+            e_beg[tid] = off[sc];
+            cnt = off[sc + 1] - off[sc];
+        } else {
+            e_beg[tid] = 0;
+        }
+        e_d[tid] = make_float4((float)stencil[3 * tid], (float)stencil[3 * tid + 1], (float)stencil[3 * tid + 2], 0.f);
+    }
+    // prefix over the stencil entries (nst <= 128)
+    {
+        __shared__ int ws[4];
+        int x = cnt;
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) ws[warp] = x;
+        __syncthreads();
+        int add = 0;
+        for (int w = 0; w < warp; w++) add += ws[w];
+        e_off[tid] = x - cnt + add;  // exclusive
+        __syncthreads();
+        if (tid == 0) e_off[nst] = ws[0] + ws[1] + ws[2] + ws[3];
+    }
+    __syncthreads();
+    const int total = e_off[nst];
+    for (int t0 = 0; t0 < nt; t0 += P2P_MAXT) {
+        const int ntc = min(P2P_MAXT, nt - t0);
+        for (int i = tid; i < ntc; i += P2P_THREADS) acc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int s0 = 0; s0 < total; s0 += P2P_MAXS) {
+            const int ns = min(P2P_MAXS, total - s0);
+            __syncthreads();
+            for (int i = tid; i < ns; i += P2P_THREADS) {
+                int g = s0 + i;
+                int lo = 0, hi = nst - 1;  // last entry with e_off <= g
+                while (lo < hi) {
+                    int mid = (lo + hi + 1) >> 1;
+                    if (e_off[mid] <= g) lo = mid; else hi = mid - 1;
+                }
+                float4 a = atoms[e_beg[lo] + (g - e_off[lo])];
+                float4 d = e_d[lo];
+                src[i] = make_float4(a.x + d.x, a.y + d.y, a.z + d.z, a.w);
+            }
+            __syncthreads();
+            const int per = (ns + 3) / 4;
+            const int jb = warp * per, je = min(ns, jb + per);
+            for (int tt = lane; tt < ntc; tt += 32) {
+                const float4 xi = atoms[tb + t0 + tt];
+                float phi = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
+                for (int j = jb; j < je; j++) {
+                    const float4 s = src[j];
+                    const float dx = xi.x - s.x, dy = xi.y - s.y, dz = xi.z - s.z;
+                    const float r2 = dx * dx + dy * dy + dz * dz;
+                    const float ri = r2 > 0.f ? rsqrtf(r2) : 0.f;
+                    const float qr = s.w * ri;
+                    phi += qr;
+                    const float q3 = qr * ri * ri;
+                    gx -= q3 * dx;
+                    gy -= q3 * dy;
+                    gz -= q3 * dz;
+                }
+                atomicAdd(&acc[tt].x, phi);
+                atomicAdd(&acc[tt].y, gx);
+                atomicAdd(&acc[tt].z, gy);
+                atomicAdd(&acc[tt].w, gz);
+            }
+        }
+        __syncthreads();
+        for (int i = tid; i < ntc; i += P2P_THREADS) field[tb + t0 + i] = acc[i];
+        __syncthreads();
+    }
+}
+
+void launch_p2p(const int* offsets, int depth, int periodic, const float4* atoms, const int* stencil, int nst,
+                float4* field, cudaStream_t s)
+{
+    int nleaf = 1 << (3 * depth);
+    COUNT_LAUNCH();
+    k_p2p<<<nleaf, P2P_THREADS, 0, s>>>(offsets, depth, periodic, atoms, stencil, nst, field);
+}
+
+// ------------------------------------------------------------------ batched contraction (M2M, M2L, L2L)
+
+// A CTA owns CT_TILE targets that share one operator per entry.  For each entry it
+// gathers the source rows (transposed, [row][target]) into shared memory and runs
+// a block-sparse FP32 GEMM: warps own (8-row block, column range) work items, the
+// operator (packed [col][8 rows]) is read as broadcast float4 loads, each lane
+// accumulates 8 rows x 2 targets.  Partial sums go to a shared [row][target] tile
+// that is written (or added) to the destination level at the end.
+__global__ void __launch_bounds__(CT_WARPS * 32) k_contract(ContractArgs a)
+{
+    extern __shared__ float sm[];
+    const int R = a.R, Rpad = a.Rpad;
+    constexpr int T = CT_TILE;
+    constexpr int LT = CT_TILE + 1;
+    float* Ms = sm;                       // R x T
+    float* Ls = Ms + R * T;               // R x LT
+    int* srow = reinterpret_cast<int*>(Ls + R * LT);
+    int* trow = srow + T;
+    const CTask task = a.tasks[blockIdx.x];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int i = tid; i < R * LT; i += blockDim.x) Ls[i] = 0.f;
+    int vt[3] = {0, 0, 0}, va[3] = {0, 0, 0};
+    uint32_t tcode = 0;
+    const bool tvalid = tid < task.ntgt;
+    if (tid < T) {
+        if (task.octant >= 0) {
+            uint32_t q = (uint32_t)(task.q0 + tid);
+            tcode = (q << 3) | (uint32_t)task.octant;
+            morton_decode(q, va[0], va[1], va[2]);
+        } else {
+            tcode = (uint32_t)(task.q0 + tid);
+        }
+        morton_decode(tcode, vt[0], vt[1], vt[2]);
+        trow[tid] = tvalid ? (int)(tcode * (uint32_t)Rpad) : -1;
+    }
+    for (int e = task.e_begin; e < task.e_end; e++) {
+        const CEntry en = a.entries[e];
+        const int slev = en.mode == 0 ? task.level : (en.mode == 1 ? task.level - 1 : task.level + 1);
+        __syncthreads();
+        if (tid < T) {
+            int row = -1;
+            if (tvalid) {
+                if (en.mode == 2) {
+                    row = (int)(((tcode << 3) | (uint32_t)((en.dx << 2) | (en.dy << 1) | en.dz)) * (uint32_t)Rpad);
+                } else {
+                    const int* base = en.mode == 0 ? vt : va;
+                    int sx = base[0] + en.dx, sy = base[1] + en.dy, sz = base[2] + en.dz;
+                    const int ns = 1 << slev;
+                    bool ok = true;
+                    if (a.periodic) {
+                        sx &= ns - 1; sy &= ns - 1; sz &= ns - 1;
+                    } else {
+                        ok = sx >= 0 && sy >= 0 && sz >= 0 && sx < ns && sy < ns && sz < ns;
+                    }
+                    if (ok) row = (int)(morton_encode(sx, sy, sz) * (uint32_t)Rpad);
+                }
+            }
+            srow[tid] = row;
+        }
+        __syncthreads();
+        const float* src = a.src_lvl[slev];
+        const int nc4 = Rpad >> 2;
+        for (int idx = tid; idx < T * nc4; idx += blockDim.x) {
+            const int t = idx % T, c4 = idx / T;
+            const int row = srow[t];
+            float4 v = row >= 0 ? __ldg(reinterpret_cast<const float4*>(src + row) + c4) : make_float4(0.f, 0.f, 0.f, 0.f);
+            const int c = 4 * c4;
+            if (c < R) Ms[c * T + t] = v.x;
+            if (c + 1 < R) Ms[(c + 1) * T + t] = v.y;
+            if (c + 2 < R) Ms[(c + 2) * T + t] = v.z;
+            if (c + 3 < R) Ms[(c + 3) * T + t] = v.w;
+        }
+        __syncthreads();
+        const float* op = a.ops + en.op;
+        for (int it = a.warp_begin[warp]; it < a.warp_begin[warp + 1]; it++) {
+            const int4 w = a.items[it];
+            const BlockInfo bi = a.blocks[w.x];
+            float acc[8][2];
+#pragma unroll
+            for (int i = 0; i < 8; i++) acc[i][0] = acc[i][1] = 0.f;
+            const float4* ap = reinterpret_cast<const float4*>(op + bi.off + (w.y - bi.c0) * 8);
+            for (int c = w.y; c < w.z; c++, ap += 2) {
+                const float4 a0 = __ldg(ap), a1 = __ldg(ap + 1);
+                const float2 m = *reinterpret_cast<const float2*>(&Ms[c * T + 2 * lane]);
+                acc[0][0] += a0.x * m.x; acc[0][1] += a0.x * m.y;
+                acc[1][0] += a0.y * m.x; acc[1][1] += a0.y * m.y;
+                acc[2][0] += a0.z * m.x; acc[2][1] += a0.z * m.y;
+                acc[3][0] += a0.w * m.x; acc[3][1] += a0.w * m.y;
+                acc[4][0] += a1.x * m.x; acc[4][1] += a1.x * m.y;
+                acc[5][0] += a1.y * m.x; acc[5][1] += a1.y * m.y;
+                acc[6][0] += a1.z * m.x; acc[6][1] += a1.z * m.y;
+                acc[7][0] += a1.w * m.x; acc[7][1] += a1.w * m.y;
+            }
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                const int r = 8 * w.x + i;
+                if (r < R) {
+                    atomicAdd(&Ls[r * LT + 2 * lane], acc[i][0]);
+                    atomicAdd(&Ls[r * LT + 2 * lane + 1], acc[i][1]);
+                }
+            }
+        }
+    }
+    __syncthreads();
+    float* dst = a.dst_lvl[task.level];
+    for (int idx = tid; idx < R * T; idx += blockDim.x) {
+        const int r = idx % R, t = idx / R;
+        const int row = trow[t];
+        if (row < 0) continue;
+        const float v = Ls[r * LT + t];
+        if (a.write_mode == 0) dst[row + r] = v;
+        else if (a.write_mode == 1) dst[row + r] += v;
+        else atomicAdd(&dst[row + r], v);
+    }
+}
+
+void launch_contract(const ContractArgs& a, int ntasks, cudaStream_t s)
+{
+    if (ntasks <= 0) return;
+    size_t shm = sizeof(float) * ((size_t)a.R * CT_TILE + (size_t)a.R * (CT_TILE + 1)) + sizeof(int) * 2 * CT_TILE;
+    static size_t attr = 0;
+    if (shm > attr) {
+        cudaFuncSetAttribute(k_contract, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+        attr = shm;
+    }
+    COUNT_LAUNCH();
+    k_contract<<<ntasks, CT_WARPS * 32, shm, s>>>(a);
+}
+
+// ------------------------------------------------------------------ root (FP64)
+
+// M~_0 = sum_o A_o M~_1[o]: one CTA per (child, 32-row chunk), FP64 dot products.
+__global__ void k_root_m2m(RootArgs a)
+{
+    const int o = blockIdx.x, r = blockIdx.y * 32 + threadIdx.x;
+    if (r >= a.R) return;
+    const double* A = a.m2m + ((size_t)o * a.R + r) * a.R;
+    const float* m = a.M1 + (size_t)o * a.Rpad;
+    double t = 0;
+    for (int c = 0; c < a.R; c++) t += A[c] * (double)m[c];
+    atomicAdd(&a.M0[r], t);
+}
+
+// L~_0 = A_lattice M~_0 (images >= 2), and the FP32 copy of M~_0.
+__global__ void k_root_lattice(RootArgs a)
+{
+    const int r = blockIdx.x * 32 + threadIdx.x;
+    if (r >= a.R) return;
+    a.M0f[r] = (float)a.M0[r];
+    double t = 0;
+    if (a.images >= 2) {
+        const double* A = a.lattice + (size_t)r * a.R;
+        for (int c = 0; c < a.R; c++) t += A[c] * a.M0[c];
+    }
+    a.L0[r] = t;
+}
+
+// L~_1[o] += A_o L~_0 (FP64 arithmetic, FP32 result).
+__global__ void k_root_l2l(RootArgs a)
+{
+    const int o = blockIdx.x, r = blockIdx.y * 32 + threadIdx.x;
+    if (r >= a.R) return;
+    const double* A = a.l2l + ((size_t)o * a.R + r) * a.R;
+    double t = 0;
+    for (int c = 0; c < a.R; c++) t += A[c] * a.L0[c];
+    a.L1[(size_t)o * a.Rpad + r] += (float)t;
+}
+
+void launch_root_m2m(const RootArgs& a, cudaStream_t s)
+{
+    COUNT_LAUNCH();
+    k_root_m2m<<<dim3(8, (a.R + 31) / 32), 32, 0, s>>>(a);
+}
+void launch_root_lattice(const RootArgs& a, cudaStream_t s)
+{
+    COUNT_LAUNCH();
+    k_root_lattice<<<(a.R + 31) / 32, 32, 0, s>>>(a);
+}
+void launch_root_l2l(const RootArgs& a, cudaStream_t s)
+{
+    COUNT_LAUNCH();
+    k_root_l2l<<<dim3(8, (a.R + 31) / 32), 32, 0, s>>>(a);
+}
+
+// ------------------------------------------------------------------ finalize
+
+// Unit conversion of gpu_solver.cu:250-256 (phi*ke, F = -q*ke*grad phi), the
+// tin-foil dipole correction of solver.cpp:30-49, scatter back to input order
+// (solver.cpp:58-67) and the FP64 energy 0.5*sum(q*phi) (fmm.cpp:89-98).
+__global__ void __launch_bounds__(256) k_finalize(FinalArgs a)
+{
+    const double M0 = a.sums[0], M1 = a.sums[1], M2 = a.sums[2];
+    const double cK = a.sc->coef * KE;
+    const float inv_h = a.sc->inv_h, inv_h2 = a.sc->inv_h * a.sc->inv_h;
+    const double corr = cK * (M0 * M0 + M1 * M1 + M2 * M2) / (double)a.n;
+    const float fM0 = (float)(cK * M0), fM1 = (float)(cK * M1), fM2 = (float)(cK * M2);
+    double e = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) {
+        const float4 nf = a.near[i], ff = a.far[i];
+        const float q = a.atoms[i].w;
+        const float phi = (nf.x + ff.x) * inv_h;
+        const float gx = (nf.y + ff.y) * inv_h2, gy = (nf.z + ff.z) * inv_h2, gz = (nf.w + ff.w) * inv_h2;
+        const int o = a.order[i];
+        const float qk = -q * (float)KE;
+        a.forces[3 * o] = qk * gx + q * fM0;
+        a.forces[3 * o + 1] = qk * gy + q * fM1;
+        a.forces[3 * o + 2] = qk * gz + q * fM2;
+        double pot = (double)phi * KE;
+        if (q != 0.f) pot -= corr / (double)q;
+        a.pots[o] = (float)pot;
+        e += 0.5 * (double)q * pot;
+    }
+    for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
+    __shared__ double red[8];
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = e;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w];
+        atomicAdd(a.energy, t);
+    }
+}
+
+void launch_finalize(const FinalArgs& a, cudaStream_t s)
+{
+    int blocks = (a.n + 255) / 256;
+    if (blocks > 4 * 152) blocks = 4 * 152;
+    if (blocks < 1) blocks = 1;
+    COUNT_LAUNCH();
+    k_finalize<<<blocks, 256, 0, s>>>(a);
+}
+
+}  // namespace gbfmm

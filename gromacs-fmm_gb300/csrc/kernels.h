@@ -1,0 +1,120 @@
+// Launch interface of the FMM device kernels (kernels.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+
+#include "common.cuh"
+
+namespace gbfmm {
+
+// One entry of a batched contraction: source cell relative to the target.
+//   mode 0: same level, source = target coords + d
+//   mode 1: parent level, source = parent coords + d
+//   mode 2: child level, source = 2*target coords + d (d = child octant bits)
+struct CEntry {
+    int8_t dx, dy, dz, mode;
+    int op;  // float offset of the packed operator
+};
+
+// One CTA job of a batched contraction.
+struct CTask {
+    int level;    // target level
+    int octant;   // >= 0: targets are 8*(q0+t)+octant; < 0: targets are q0+t
+    int q0;
+    int ntgt;     // targets in this tile (<= tile size)
+    int e_begin, e_end;
+};
+
+struct BlockInfo {
+    int c0, off;
+};
+
+constexpr int CT_TILE = 64;   // targets per contraction CTA
+constexpr int CT_WARPS = 8;
+
+struct ContractArgs {
+    const float* ops;
+    const CEntry* entries;
+    const CTask* tasks;
+    const int4* items;        // (blk, ca, cb, 0)
+    const int* warp_begin;    // CT_WARPS+1
+    const BlockInfo* blocks;  // per 8-row block
+    float* src_lvl[8];
+    float* dst_lvl[8];
+    int R, Rpad, nblk;
+    int periodic;
+    int write_mode;           // 0 store, 1 add, 2 atomic add
+};
+
+// Per-step constants that depend on the box, read by the kernels from device
+// memory so that a captured graph can be replayed for a new box and new
+// coordinate pointer without re-capture.
+struct StepConst {
+    const float* coords;                 // 3N device coordinates of this step
+    float inv_h;                         // 2^D / L
+    float pad_;
+    double coef;                         // 4 pi / (3 V), dipole correction
+    float thresh[3][(1 << MAX_DEPTH) + 1];  // leaf boundaries rounded down to float (T[0] = -inf)
+    float2 centre[3][1 << MAX_DEPTH];   // leaf centres as hi + lo floats
+};
+
+struct TreeArgs {
+    const StepConst* sc;
+    const float* charges;   // N, input order
+    int n;
+    int depth;
+    uint32_t* code;         // N leaf codes (input order)
+    float4* uq;             // N scaled coords + charge (input order)
+    int* counts;            // 8^D
+    double* sums;           // [0..2] dipole, [3] total charge
+    int* flags;             // [0] non-finite input seen
+};
+
+extern std::atomic<long> g_kernel_launches;
+
+void launch_tree_keys(const TreeArgs& a, cudaStream_t s);
+void launch_exclusive_scan(const int* in, int* out, int n, int* scratch, cudaStream_t s);
+void launch_scatter(const uint32_t* code, int n, int* cursor, int* tmp_idx, cudaStream_t s);
+void launch_leaf_sort(const int* offsets, int nleaf, int* tmp_idx, const float4* uq, const uint32_t* code, int* order,
+                      float4* atoms, int* atom_leaf, cudaStream_t s);
+void launch_p2m(int P, const int* offsets, int nleaf, const float4* atoms, float* M_leaf, int Rpad, cudaStream_t s);
+void launch_l2p(int P, const int* offsets, int nleaf, const float4* atoms, const float* L_leaf, int Rpad, float4* field,
+                cudaStream_t s);
+void launch_p2p(const int* offsets, int depth, int periodic, const float4* atoms, const int* stencil, int nst,
+                float4* field, cudaStream_t s);
+void launch_contract(const ContractArgs& a, int ntasks, cudaStream_t s);
+
+struct RootArgs {
+    int R, Rpad;
+    const double* m2m;      // 8 x R x R
+    const double* l2l;      // 8 x R x R
+    const double* lattice;  // R x R
+    const float* M1;        // level-1 multipoles (8 rows)
+    double* M0;             // root multipole (FP64)
+    double* L0;             // root local (FP64)
+    float* M0f;             // FP32 copy of the root multipole (level-0 row)
+    float* L1;              // level-1 locals (8 rows)
+    int images;
+};
+void launch_root_m2m(const RootArgs& a, cudaStream_t s);
+void launch_root_lattice(const RootArgs& a, cudaStream_t s);
+void launch_root_l2l(const RootArgs& a, cudaStream_t s);
+
+struct FinalArgs {
+    const StepConst* sc;
+    int n;
+    const float4* atoms;     // sorted (u, q)
+    const int* order;        // sorted -> input index
+    const float4* near;      // sorted (phi, grad) near field, scaled units
+    const float4* far;       // sorted far field, scaled units
+    const double* sums;      // dipole + total charge
+    float* forces;           // 3N input order
+    float* pots;             // N input order
+    double* energy;          // accumulated 0.5 * sum q * pot
+};
+void launch_finalize(const FinalArgs& a, cudaStream_t s);
+
+}  // namespace gbfmm

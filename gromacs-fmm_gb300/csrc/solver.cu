@@ -1,0 +1,966 @@
+// Host orchestration and C ABI of the GB300 FMM (include/gbfmm.h).
+//
+// One handle = one system.  Everything that depends only on (order, depth,
+// images) -- operators, stencils, contraction task lists -- is built and uploaded
+// once at create time; device buffers are sized once (no per-step allocation,
+// unlike GPUSolver::solve, src/gromacs/zeta_fmm/gpu_solver.cu:79-98, 258-270).
+// Per step only the box-dependent constants (a few KB) are uploaded, and the
+// whole step is replayed from a captured CUDA graph.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/gbfmm.h"
+#include "common.cuh"
+#include "kernels.h"
+#include "operators.h"
+
+using namespace gbfmm;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CK(call)                                                                                        \
+    do {                                                                                                \
+        cudaError_t e_ = (call);                                                                        \
+        if (e_ != cudaSuccess)                                                                          \
+            return fail(e_ == cudaErrorMemoryAllocation ? GBFMM_ERR_NOMEM : GBFMM_ERR_CUDA, "%s: %s (%s:%d)", \
+                        #call, cudaGetErrorString(e_), __FILE__, __LINE__);                             \
+    } while (0)
+
+// Operator tables shared by all handles of the same (order, images).
+struct OpTables {
+    int P = 0, images = -1, R = 0, Rpad = 0;
+    Stencils st;
+    PackPlan plan[3];
+    std::vector<float> packed;           // all packed FP32 operators
+    int off_m2m[8], off_l2l[8];
+    std::vector<int> off_cls;            // per M2L class
+    std::vector<double> root_m2m, root_l2l, lattice;  // dense FP64 for the root
+    std::vector<WorkItem> items[3];
+    std::vector<int> warp_begin[3];
+};
+
+std::mutex g_tab_mu;
+std::vector<OpTables*> g_tabs;
+
+const OpTables* get_tables(int P, int images)
+{
+    std::lock_guard<std::mutex> lk(g_tab_mu);
+    for (OpTables* t : g_tabs)
+        if (t->P == P && t->images == images) return t;
+    OpTables* t = new OpTables();
+    t->P = P;
+    t->images = images;
+    t->R = nreal(P);
+    t->Rpad = (t->R + 3) & ~3;
+    const int R = t->R;
+    t->st = build_stencils(0.4);
+    for (int k = 0; k < 3; k++) {
+        t->plan[k] = make_pack_plan(P, (OpType)k);
+        make_work_items(t->plan[k], CT_WARPS, t->items[k], t->warp_begin[k]);
+    }
+    std::vector<double> A((size_t)R * R);
+    auto append = [&](const PackPlan& pl) {
+        int off = (int)t->packed.size();
+        t->packed.resize(t->packed.size() + pl.packed);
+        pack_operator(pl, A.data(), t->packed.data() + off);
+        return off;
+    };
+    t->root_m2m.resize((size_t)8 * R * R);
+    t->root_l2l.resize((size_t)8 * R * R);
+    for (int o = 0; o < 8; o++) {
+        scaled_m2m(P, o, A.data());
+        std::copy(A.begin(), A.end(), t->root_m2m.begin() + (size_t)o * R * R);
+        t->off_m2m[o] = append(t->plan[OP_M2M]);
+        scaled_l2l(P, o, A.data());
+        std::copy(A.begin(), A.end(), t->root_l2l.begin() + (size_t)o * R * R);
+        t->off_l2l[o] = append(t->plan[OP_L2L]);
+    }
+    t->off_cls.resize(t->st.classes.size());
+    for (size_t c = 0; c < t->st.classes.size(); c++) {
+        scaled_m2l(P, t->st.classes[c], A.data());
+        t->off_cls[c] = append(t->plan[OP_M2L]);
+    }
+    t->lattice.resize((size_t)R * R);
+    lattice_operator(P, images, t->lattice.data());
+    g_tabs.push_back(t);
+    return t;
+}
+
+}  // namespace
+
+struct gbfmm_handle {
+    gbfmm_params prm{};
+    int n = 0, P = 0, R = 0, Rpad = 0, D = 0, nleaf = 0;
+    bool periodic = true;
+    const OpTables* tab = nullptr;
+    cudaStream_t stream = nullptr;
+    // host state
+    std::vector<float> h_q;
+    bool have_charges = false, have_result = false, results_on_host = false;
+    int verbose = 0;
+    // device arena
+    void* arena = nullptr;
+    size_t arena_bytes = 0;
+    float* d_coords = nullptr;   // internal copy for host-side execute
+    float* d_q = nullptr;
+    uint32_t* d_code = nullptr;
+    float4* d_uq = nullptr;
+    int *d_counts = nullptr, *d_off = nullptr, *d_cursor = nullptr, *d_scan = nullptr, *d_tmp = nullptr;
+    int *d_order = nullptr, *d_atom_leaf = nullptr;
+    float4 *d_atoms = nullptr, *d_near = nullptr, *d_far = nullptr;
+    float *d_M = nullptr, *d_L = nullptr;
+    float* Mlev[8] = {};
+    float* Llev[8] = {};
+    size_t lev_floats = 0;
+    double *d_M0 = nullptr, *d_L0 = nullptr;
+    float* d_ops = nullptr;
+    CEntry* d_entries = nullptr;
+    CTask* d_tasks = nullptr;
+    int4* d_items[3] = {};
+    int* d_wb[3] = {};
+    BlockInfo* d_blocks[3] = {};
+    double *d_root_m2m = nullptr, *d_root_l2l = nullptr, *d_lattice = nullptr;
+    int* d_p2p_st = nullptr;
+    int n_p2p_st = 0;
+    float *d_forces = nullptr, *d_pots = nullptr;
+    double* d_energy = nullptr;
+    double* d_sums = nullptr;
+    int* d_flags = nullptr;
+    StepConst* d_sc = nullptr;
+    StepConst* h_sc = nullptr;  // pinned
+    int* h_flags = nullptr;     // pinned
+    // task ranges
+    int m2m_task0[8] = {}, m2m_ntask[8] = {};
+    int l2l_task0[8] = {}, l2l_ntask[8] = {};
+    int m2l_task0 = 0, m2l_ntask = 0;
+    // graph
+    cudaGraphExec_t gexec = nullptr;
+    // host result staging (pinned)
+    float* h_forces = nullptr;
+    float* h_pots = nullptr;
+    double* h_energy = nullptr;
+    // stage timing
+    bool timing = false;
+    cudaEvent_t ev[16] = {};
+    float stage_ms[16] = {};
+    int n_stage = 0;
+    int step_launches = 0;
+};
+
+static const char* k_stage_names[] = {"tree", "p2m", "m2m", "root", "m2l", "l2l", "l2p", "p2p", "finalize"};
+
+extern "C" {
+
+void gbfmm_params_default(gbfmm_params* p)
+{
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    p->order = 10;
+    p->max_depth = 3;
+    p->images = 4;
+    p->theta = 0.4;
+    p->rega = 0.0;
+    p->precision = GBFMM_PREC_FP32;
+}
+
+const char* gbfmm_status_string(int s)
+{
+    switch (s) {
+        case GBFMM_OK: return "ok";
+        case GBFMM_ERR_ARG: return "invalid argument";
+        case GBFMM_ERR_BOX: return "invalid box";
+        case GBFMM_ERR_COORD: return "non-finite coordinate or charge";
+        case GBFMM_ERR_CUDA: return "CUDA error";
+        case GBFMM_ERR_NOMEM: return "out of memory";
+        case GBFMM_ERR_UNSUPPORTED: return "unsupported";
+        case GBFMM_ERR_STATE: return "call out of order";
+        case GBFMM_ERR_TIMEOUT: return "device wait timed out";
+        case GBFMM_ERR_NOT_NEUTRAL: return "system not neutral";
+        default: return "unknown status";
+    }
+}
+
+const char* gbfmm_last_error(void) { return g_err.c_str(); }
+const char* gbfmm_version(void) { return "gbfmm 0.1 (sm_103a)"; }
+const char* gbfmm_stage_name(int s) { return (s >= 0 && s < 9) ? k_stage_names[s] : ""; }
+
+}  // extern "C"
+
+static void free_handle(gbfmm_handle* h)
+{
+    if (!h) return;
+    if (h->gexec) cudaGraphExecDestroy(h->gexec);
+    for (int i = 0; i < 16; i++)
+        if (h->ev[i]) cudaEventDestroy(h->ev[i]);
+    if (h->arena) cudaFree(h->arena);
+    if (h->h_sc) cudaFreeHost(h->h_sc);
+    if (h->h_flags) cudaFreeHost(h->h_flags);
+    if (h->h_forces) cudaFreeHost(h->h_forces);
+    if (h->h_pots) cudaFreeHost(h->h_pots);
+    if (h->h_energy) cudaFreeHost(h->h_energy);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+}
+
+// Bump allocator over one device allocation.
+struct Arena {
+    size_t off = 0;
+    char* base = nullptr;
+    template <typename T>
+    T* take(size_t count)
+    {
+        off = (off + 255) & ~(size_t)255;
+        T* p = reinterpret_cast<T*>(base ? base + off : nullptr);
+        off += sizeof(T) * count;
+        return p;
+    }
+};
+
+static int layout(gbfmm_handle* h, Arena& a)
+{
+    const int n = std::max(h->n, 1), R = h->R, Rpad = h->Rpad, D = h->D;
+    const OpTables* t = h->tab;
+    h->d_coords = a.take<float>(3 * (size_t)n);
+    h->d_q = a.take<float>(n);
+    h->d_code = a.take<uint32_t>(n);
+    h->d_uq = a.take<float4>(n);
+    h->d_counts = a.take<int>(h->nleaf + 1);
+    h->d_off = a.take<int>(h->nleaf + 1);
+    h->d_cursor = a.take<int>(h->nleaf + 1);
+    h->d_scan = a.take<int>((h->nleaf + 2047) / 2048 + 1);
+    h->d_tmp = a.take<int>(n);
+    h->d_order = a.take<int>(n);
+    h->d_atom_leaf = a.take<int>(n);
+    h->d_atoms = a.take<float4>(n);
+    h->d_near = a.take<float4>(n);
+    h->d_far = a.take<float4>(n);
+    size_t lev = 0;
+    for (int k = 0; k <= D; k++) lev += ((size_t)1 << (3 * k)) * Rpad;
+    h->lev_floats = lev;
+    h->d_M = a.take<float>(lev);
+    h->d_L = a.take<float>(lev);
+    h->d_M0 = a.take<double>(R);
+    h->d_L0 = a.take<double>(R);
+    h->d_ops = a.take<float>(t->packed.size());
+    h->d_root_m2m = a.take<double>(t->root_m2m.size());
+    h->d_root_l2l = a.take<double>(t->root_l2l.size());
+    h->d_lattice = a.take<double>(t->lattice.size());
+    h->d_p2p_st = a.take<int>(t->st.p2p.size());
+    for (int k = 0; k < 3; k++) {
+        h->d_items[k] = a.take<int4>(t->items[k].size() + 1);
+        h->d_wb[k] = a.take<int>(CT_WARPS + 1);
+        h->d_blocks[k] = a.take<BlockInfo>(t->plan[k].nblk);
+    }
+    h->d_forces = a.take<float>(3 * (size_t)n);
+    h->d_pots = a.take<float>(n);
+    h->d_energy = a.take<double>(1);
+    h->d_sums = a.take<double>(4);
+    h->d_flags = a.take<int>(4);
+    h->d_sc = a.take<StepConst>(1);
+    return 0;
+}
+
+static void level_ptrs(gbfmm_handle* h)
+{
+    size_t o = 0;
+    for (int k = 0; k <= h->D; k++) {
+        h->Mlev[k] = h->d_M + o;
+        h->Llev[k] = h->d_L + o;
+        o += ((size_t)1 << (3 * k)) * h->Rpad;
+    }
+}
+
+// Contraction task lists: M2M per level, M2L for all levels, L2L per level.
+static int build_tasks(gbfmm_handle* h)
+{
+    const OpTables* t = h->tab;
+    const int D = h->D;
+    std::vector<CEntry> ent;
+    std::vector<CTask> tasks;
+    // M2M entries: 8 children
+    const int e_m2m = (int)ent.size();
+    for (int o = 0; o < 8; o++) {
+        CEntry e;
+        e.dx = (int8_t)((o >> 2) & 1); e.dy = (int8_t)((o >> 1) & 1); e.dz = (int8_t)(o & 1); e.mode = 2;
+        e.op = t->off_m2m[o];
+        ent.push_back(e);
+    }
+    // L2L entries: parent, one per target octant
+    const int e_l2l = (int)ent.size();
+    for (int o = 0; o < 8; o++) {
+        CEntry e;
+        e.dx = e.dy = e.dz = 0; e.mode = 1;
+        e.op = t->off_l2l[o];
+        ent.push_back(e);
+    }
+    // M2L stencils
+    int e_m2l[2][8];
+    for (int lt = 0; lt < 2; lt++)
+        for (int s = 0; s < 8; s++) {
+            e_m2l[lt][s] = (int)ent.size();
+            for (const StencilEntry& se : t->st.m2l[lt][s]) {
+                CEntry e;
+                e.dx = (int8_t)se.d[0]; e.dy = (int8_t)se.d[1]; e.dz = (int8_t)se.d[2];
+                e.mode = (int8_t)se.mode;
+                e.op = t->off_cls[se.cls];
+                ent.push_back(e);
+            }
+        }
+    // M2M tasks: target level k = D-1 .. 1 (level 0 is the FP64 root)
+    for (int k = D - 1; k >= 1; k--) {
+        h->m2m_task0[k] = (int)tasks.size();
+        long ncell = 1L << (3 * k);
+        for (long q0 = 0; q0 < ncell; q0 += CT_TILE) {
+            CTask c;
+            c.level = k; c.octant = -1; c.q0 = (int)q0; c.ntgt = (int)std::min<long>(CT_TILE, ncell - q0);
+            c.e_begin = e_m2m; c.e_end = e_m2m + 8;
+            tasks.push_back(c);
+        }
+        h->m2m_ntask[k] = (int)tasks.size() - h->m2m_task0[k];
+    }
+    // M2L tasks
+    long work = 0;
+    for (int k = 1; k <= D; k++) work += (1L << (3 * k)) * (k == 1 ? 107 : 182);
+    int split = h->prm.m2l_split > 0 ? h->prm.m2l_split : 1;
+    if (h->prm.m2l_split <= 0) {
+        long tiles = 0;
+        for (int k = 1; k <= D; k++) tiles += 8 * std::max<long>(1, (1L << (3 * (k - 1))) / CT_TILE);
+        while (tiles * split < 2 * 152 && split < 8) split *= 2;
+    }
+    if (h->prm.flags & GBFMM_FLAG_DETERMINISTIC) split = 1;
+    h->m2l_task0 = (int)tasks.size();
+    for (int k = 1; k <= D; k++) {
+        const int lt = k == 1 ? 0 : 1;
+        long npar = 1L << (3 * (k - 1));
+        for (int s = 0; s < 8; s++) {
+            int eb = e_m2l[lt][s], ne = (int)t->st.m2l[lt][s].size();
+            for (long q0 = 0; q0 < npar; q0 += CT_TILE) {
+                int ch = (ne + split - 1) / split;
+                for (int e0 = 0; e0 < ne; e0 += ch) {
+                    CTask c;
+                    c.level = k; c.octant = s; c.q0 = (int)q0; c.ntgt = (int)std::min<long>(CT_TILE, npar - q0);
+                    c.e_begin = eb + e0; c.e_end = eb + std::min(ne, e0 + ch);
+                    tasks.push_back(c);
+                }
+            }
+        }
+    }
+    h->m2l_ntask = (int)tasks.size() - h->m2l_task0;
+    (void)work;
+    // L2L tasks: target level k = 2 .. D (level 1 comes from the FP64 root)
+    for (int k = 2; k <= D; k++) {
+        h->l2l_task0[k] = (int)tasks.size();
+        long npar = 1L << (3 * (k - 1));
+        for (int s = 0; s < 8; s++)
+            for (long q0 = 0; q0 < npar; q0 += CT_TILE) {
+                CTask c;
+                c.level = k; c.octant = s; c.q0 = (int)q0; c.ntgt = (int)std::min<long>(CT_TILE, npar - q0);
+                c.e_begin = e_l2l + s; c.e_end = e_l2l + s + 1;
+                tasks.push_back(c);
+            }
+        h->l2l_ntask[k] = (int)tasks.size() - h->l2l_task0[k];
+    }
+    void* p = nullptr;
+    CK(cudaMalloc(&p, sizeof(CEntry) * ent.size() + sizeof(CTask) * tasks.size() + 512));
+    h->d_entries = (CEntry*)p;
+    h->d_tasks = (CTask*)((char*)p + ((sizeof(CEntry) * ent.size() + 255) & ~(size_t)255));
+    CK(cudaMemcpy(h->d_entries, ent.data(), sizeof(CEntry) * ent.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->d_tasks, tasks.data(), sizeof(CTask) * tasks.size(), cudaMemcpyHostToDevice));
+    return GBFMM_OK;
+}
+
+static ContractArgs contract_args(gbfmm_handle* h, int optype, int write_mode, bool src_is_L, int task0)
+{
+    ContractArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.ops = h->d_ops;
+    a.entries = h->d_entries;
+    a.tasks = h->d_tasks + task0;
+    a.items = h->d_items[optype];
+    a.warp_begin = h->d_wb[optype];
+    a.blocks = h->d_blocks[optype];
+    for (int k = 0; k <= h->D; k++) {
+        a.src_lvl[k] = src_is_L ? h->Llev[k] : h->Mlev[k];
+        a.dst_lvl[k] = optype == OP_M2M ? h->Mlev[k] : h->Llev[k];
+    }
+    a.R = h->R;
+    a.Rpad = h->Rpad;
+    a.nblk = h->tab->plan[optype].nblk;
+    a.periodic = h->periodic ? 1 : 0;
+    a.write_mode = write_mode;
+    return a;
+}
+
+static void mark(gbfmm_handle* h, int stage)
+{
+    if (h->timing) cudaEventRecord(h->ev[stage], h->stream);
+}
+
+// Enqueues one full step on h->stream (captured into the graph on first use).
+static void enqueue_step(gbfmm_handle* h)
+{
+    cudaStream_t s = h->stream;
+    const int D = h->D, n = h->n;
+    const long launches0 = g_kernel_launches.load();
+    mark(h, 0);
+    cudaMemsetAsync(h->d_counts, 0, sizeof(int) * (h->nleaf + 1), s);
+    cudaMemsetAsync(h->d_sums, 0, sizeof(double) * 4, s);
+    cudaMemsetAsync(h->d_energy, 0, sizeof(double), s);
+    cudaMemsetAsync(h->d_M0, 0, sizeof(double) * h->R, s);
+    cudaMemsetAsync(h->d_L, 0, sizeof(float) * h->lev_floats, s);
+    cudaMemsetAsync(h->d_far, 0, sizeof(float4) * std::max(n, 1), s);
+    if (n > 0) {
+        TreeArgs ta;
+        ta.sc = h->d_sc;
+        ta.charges = h->d_q;
+        ta.n = n;
+        ta.depth = D;
+        ta.code = h->d_code;
+        ta.uq = h->d_uq;
+        ta.counts = h->d_counts;
+        ta.sums = h->d_sums;
+        ta.flags = h->d_flags;
+        launch_tree_keys(ta, s);
+    }
+    launch_exclusive_scan(h->d_counts, h->d_off, h->nleaf, h->d_scan, s);
+    cudaMemcpyAsync(h->d_cursor, h->d_off, sizeof(int) * h->nleaf, cudaMemcpyDeviceToDevice, s);
+    launch_scatter(h->d_code, n, h->d_cursor, h->d_tmp, s);
+    launch_leaf_sort(h->d_off, h->nleaf, h->d_tmp, h->d_uq, h->d_code, h->d_order, h->d_atoms, h->d_atom_leaf, s);
+    mark(h, 1);
+    launch_p2m(h->P, h->d_off, h->nleaf, h->d_atoms, h->Mlev[D], h->Rpad, s);
+    mark(h, 2);
+    for (int k = D - 1; k >= 1; k--) {
+        ContractArgs a = contract_args(h, OP_M2M, 0, false, h->m2m_task0[k]);
+        launch_contract(a, h->m2m_ntask[k], s);
+    }
+    mark(h, 3);
+    RootArgs ra;
+    ra.R = h->R;
+    ra.Rpad = h->Rpad;
+    ra.m2m = h->d_root_m2m;
+    ra.l2l = h->d_root_l2l;
+    ra.lattice = h->d_lattice;
+    ra.M1 = h->Mlev[1];
+    ra.M0 = h->d_M0;
+    ra.L0 = h->d_L0;
+    ra.M0f = h->Mlev[0];
+    ra.L1 = h->Llev[1];
+    ra.images = h->prm.images;
+    launch_root_m2m(ra, s);
+    launch_root_lattice(ra, s);
+    mark(h, 4);
+    {
+        ContractArgs a = contract_args(h, OP_M2L, 2, false, h->m2l_task0);
+        launch_contract(a, h->m2l_ntask, s);
+    }
+    mark(h, 5);
+    launch_root_l2l(ra, s);
+    for (int k = 2; k <= D; k++) {
+        ContractArgs a = contract_args(h, OP_L2L, 1, true, h->l2l_task0[k]);
+        launch_contract(a, h->l2l_ntask[k], s);
+    }
+    mark(h, 6);
+    launch_l2p(h->P, h->d_off, h->nleaf, h->d_atoms, h->Llev[D], h->Rpad, h->d_far, s);
+    mark(h, 7);
+    launch_p2p(h->d_off, D, h->periodic ? 1 : 0, h->d_atoms, h->d_p2p_st, h->n_p2p_st, h->d_near, s);
+    mark(h, 8);
+    if (n > 0) {
+        FinalArgs fa;
+        fa.sc = h->d_sc;
+        fa.n = n;
+        fa.atoms = h->d_atoms;
+        fa.order = h->d_order;
+        fa.near = h->d_near;
+        fa.far = h->d_far;
+        fa.sums = h->d_sums;
+        fa.forces = h->d_forces;
+        fa.pots = h->d_pots;
+        fa.energy = h->d_energy;
+        launch_finalize(fa, s);
+    }
+    mark(h, 9);
+    h->step_launches = (int)(g_kernel_launches.load() - launches0);
+}
+
+extern "C" int gbfmm_create(const gbfmm_params* prm, int natoms, gbfmm_handle** out)
+{
+    if (!out) return fail(GBFMM_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    gbfmm_params p;
+    if (prm) p = *prm;
+    else gbfmm_params_default(&p);
+    if (natoms < 0) return fail(GBFMM_ERR_ARG, "natoms < 0");
+    if (p.order < 2 || p.order > MAX_ORDER) return fail(GBFMM_ERR_ARG, "order %d outside [2,%d]", p.order, MAX_ORDER);
+    if (p.max_depth < 1 || p.max_depth > MAX_DEPTH)
+        return fail(GBFMM_ERR_ARG, "max_depth %d outside [1,%d]", p.max_depth, MAX_DEPTH);
+    if (p.images < 0 || p.images > 8) return fail(GBFMM_ERR_ARG, "images %d outside [0,8]", p.images);
+    if (std::fabs(p.theta - 0.4) > 1e-12)
+        return fail(GBFMM_ERR_UNSUPPORTED, "theta %.6g: only the reference MAC scale 0.4 is supported", p.theta);
+    if (p.rega != 0.0) return fail(GBFMM_ERR_UNSUPPORTED, "rega > 0 (regularised FMM) is not built");
+    if (p.precision != GBFMM_PREC_FP32 && p.precision != GBFMM_PREC_BF16X3 && p.precision != GBFMM_PREC_BF16X1)
+        return fail(GBFMM_ERR_ARG, "unknown precision %d", p.precision);
+    if (p.precision != GBFMM_PREC_FP32)
+        return fail(GBFMM_ERR_UNSUPPORTED, "tensor-core M2L is not built in this library");
+    if (p.m2l_tile != 0 && p.m2l_tile != CT_TILE) return fail(GBFMM_ERR_ARG, "m2l_tile must be 0 or %d", CT_TILE);
+    if (p.m2l_split < 0 || p.m2l_split > 16) return fail(GBFMM_ERR_ARG, "m2l_split outside [0,16]");
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(GBFMM_ERR_CUDA, "no CUDA device available");
+    }
+    gbfmm_handle* h = new gbfmm_handle();
+    h->prm = p;
+    h->n = natoms;
+    h->P = p.order;
+    h->R = nreal(p.order);
+    h->Rpad = (h->R + 3) & ~3;
+    h->D = p.max_depth;
+    h->nleaf = 1 << (3 * h->D);
+    h->periodic = p.images > 0;
+    h->tab = get_tables(h->P, p.images);
+    h->h_q.assign(natoms, 0.0f);
+    int rc = GBFMM_OK;
+    auto bail = [&](int code) {
+        free_handle(h);
+        return code;
+    };
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(fail(GBFMM_ERR_CUDA, "stream create failed"));
+    Arena sz;
+    layout(h, sz);
+    h->arena_bytes = sz.off + 256;
+    cudaError_t e = cudaMalloc(&h->arena, h->arena_bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return bail(fail(GBFMM_ERR_NOMEM, "device arena of %zu bytes: %s", h->arena_bytes, cudaGetErrorString(e)));
+    }
+    Arena ar;
+    ar.base = (char*)h->arena;
+    layout(h, ar);
+    level_ptrs(h);
+    const OpTables* t = h->tab;
+    auto up = [&](void* dst, const void* src, size_t bytes) {
+        if (bytes && cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice) != cudaSuccess) rc = GBFMM_ERR_CUDA;
+    };
+    up(h->d_ops, t->packed.data(), sizeof(float) * t->packed.size());
+    up(h->d_root_m2m, t->root_m2m.data(), sizeof(double) * t->root_m2m.size());
+    up(h->d_root_l2l, t->root_l2l.data(), sizeof(double) * t->root_l2l.size());
+    up(h->d_lattice, t->lattice.data(), sizeof(double) * t->lattice.size());
+    up(h->d_p2p_st, t->st.p2p.data(), sizeof(int) * t->st.p2p.size());
+    h->n_p2p_st = (int)t->st.p2p.size() / 3;
+    for (int k = 0; k < 3; k++) {
+        std::vector<int4> it;
+        for (const WorkItem& w : t->items[k]) it.push_back(make_int4(w.blk, w.ca, w.cb, 0));
+        it.push_back(make_int4(0, 0, 0, 0));
+        up(h->d_items[k], it.data(), sizeof(int4) * it.size());
+        up(h->d_wb[k], t->warp_begin[k].data(), sizeof(int) * (CT_WARPS + 1));
+        std::vector<BlockInfo> bi(t->plan[k].nblk);
+        for (int b = 0; b < t->plan[k].nblk; b++) {
+            bi[b].c0 = t->plan[k].c0[b];
+            bi[b].off = t->plan[k].off[b];
+        }
+        up(h->d_blocks[k], bi.data(), sizeof(BlockInfo) * bi.size());
+    }
+    if (rc != GBFMM_OK) return bail(fail(rc, "operator upload failed"));
+    cudaMemset(h->d_flags, 0, sizeof(int) * 4);
+    cudaMemset(h->d_M, 0, sizeof(float) * h->lev_floats);
+    rc = build_tasks(h);
+    if (rc != GBFMM_OK) return bail(rc);
+    if (cudaMallocHost(&h->h_sc, sizeof(StepConst)) != cudaSuccess ||
+        cudaMallocHost(&h->h_flags, sizeof(int) * 4) != cudaSuccess ||
+        cudaMallocHost(&h->h_forces, sizeof(float) * 3 * std::max(natoms, 1)) != cudaSuccess ||
+        cudaMallocHost(&h->h_pots, sizeof(float) * std::max(natoms, 1)) != cudaSuccess ||
+        cudaMallocHost(&h->h_energy, sizeof(double)) != cudaSuccess)
+        return bail(fail(GBFMM_ERR_NOMEM, "pinned host buffers"));
+    std::memset(h->h_sc, 0, sizeof(StepConst));
+    for (int i = 0; i < 16; i++)
+        if (cudaEventCreate(&h->ev[i]) != cudaSuccess) return bail(fail(GBFMM_ERR_CUDA, "event create"));
+    *out = h;
+    return GBFMM_OK;
+}
+
+extern "C" int gbfmm_destroy(gbfmm_handle* h)
+{
+    if (!h) return fail(GBFMM_ERR_ARG, "handle is NULL");
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->d_entries) cudaFree(h->d_entries);
+    free_handle(h);
+    return GBFMM_OK;
+}
+
+extern "C" int gbfmm_set_charges(gbfmm_handle* h, int natoms, const float* q)
+{
+    if (!h) return fail(GBFMM_ERR_ARG, "handle is NULL");
+    if (natoms != h->n) return fail(GBFMM_ERR_ARG, "natoms %d differs from the handle's %d", natoms, h->n);
+    if (natoms > 0 && !q) return fail(GBFMM_ERR_ARG, "charges is NULL");
+    for (int i = 0; i < natoms; i++)
+        if (!std::isfinite(q[i])) return fail(GBFMM_ERR_COORD, "charge %d is not finite", i);
+    std::memcpy(h->h_q.data(), q, sizeof(float) * natoms);
+    CK(cudaMemcpyAsync(h->d_q, q, sizeof(float) * natoms, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    h->have_charges = true;
+    return GBFMM_OK;
+}
+
+// Fills the box-dependent step constants.  Cubic boxes only: the reference takes
+// the period from box[XX][XX] and the root half-width as its half
+// (zeta_fmm_solver.cpp:38-40).
+static int set_box(gbfmm_handle* h, const float* box, const float* d_coords)
+{
+    if (!box) return fail(GBFMM_ERR_ARG, "box is NULL");
+    for (int i = 0; i < 9; i++)
+        if (!std::isfinite(box[i])) return fail(GBFMM_ERR_BOX, "box entry %d is not finite", i);
+    if (!(box[0] > 0) || box[1] != 0 || box[2] != 0 || box[3] != 0 || box[5] != 0 || box[6] != 0 || box[7] != 0)
+        return fail(GBFMM_ERR_BOX, "box must be rectangular with positive diagonal");
+    if (box[4] != box[0] || box[8] != box[0])
+        return fail(GBFMM_ERR_BOX, "box must be cubic (got %g x %g x %g)", box[0], box[4], box[8]);
+    const double L = (double)box[0];
+    const int D = h->D, nd = 1 << D;
+    StepConst* sc = h->h_sc;
+    sc->coords = d_coords;
+    sc->inv_h = (float)(nd / L);
+    sc->coef = 4.0 * M_PI / (3.0 * L * L * L);
+    const double centre[3] = {(double)box[0] / 2, (double)box[4] / 2, (double)box[8] / 2};
+    for (int d = 0; d < 3; d++) {
+        // leaf boundaries of the strict '>' descent: the descent around centre c with
+        // half-width L/2 compares against c + L*(j/2^D - 1/2), exactly representable
+        const double lo = centre[d] - L / 2;
+        sc->thresh[d][0] = -INFINITY;
+        for (int j = 1; j < nd; j++) {
+            double b = lo + L * j / nd;
+            float f = (float)b;
+            if ((double)f > b) f = std::nextafter(f, -INFINITY);
+            sc->thresh[d][j] = f;
+        }
+        sc->thresh[d][nd] = INFINITY;
+        for (int j = 0; j < nd; j++) {
+            double c = lo + L * (2 * j + 1) / (2.0 * nd);
+            float hi = (float)c;
+            float lo_f = (float)(c - (double)hi);
+            sc->centre[d][j] = make_float2(hi, lo_f);
+        }
+    }
+    return GBFMM_OK;
+}
+
+static int run_step(gbfmm_handle* h)
+{
+    CK(cudaMemcpyAsync(h->d_sc, h->h_sc, sizeof(StepConst), cudaMemcpyHostToDevice, h->stream));
+    const bool use_graph = !(h->prm.flags & GBFMM_FLAG_NO_GRAPH) && !h->timing;
+    if (use_graph) {
+        if (!h->gexec) {
+            cudaGraph_t g = nullptr;
+            CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+            enqueue_step(h);
+            cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+            if (e != cudaSuccess) return fail(GBFMM_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+            e = cudaGraphInstantiate(&h->gexec, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) return fail(GBFMM_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+        }
+        CK(cudaGraphLaunch(h->gexec, h->stream));
+    } else {
+        enqueue_step(h);
+        CK(cudaGetLastError());
+    }
+    h->have_result = true;
+    h->results_on_host = false;
+    return GBFMM_OK;
+}
+
+extern "C" int gbfmm_execute_device(gbfmm_handle* h, const void* d_coords, const float* box, void* stream)
+{
+    if (!h) return fail(GBFMM_ERR_ARG, "handle is NULL");
+    if (!h->have_charges) return fail(GBFMM_ERR_STATE, "charges not set");
+    if (h->n > 0 && !d_coords) return fail(GBFMM_ERR_ARG, "coordinates are NULL");
+    int rc = set_box(h, box, (const float*)d_coords);
+    if (rc) return rc;
+    cudaStream_t us = (cudaStream_t)stream;
+    cudaEvent_t ein = h->ev[14], eout = h->ev[15];
+    // order the internal stream after the caller's stream, and the caller's after us
+    CK(cudaEventRecord(ein, us));
+    CK(cudaStreamWaitEvent(h->stream, ein, 0));
+    rc = run_step(h);
+    if (rc) return rc;
+    CK(cudaEventRecord(eout, h->stream));
+    CK(cudaStreamWaitEvent(us, eout, 0));
+    return GBFMM_OK;
+}
+
+static int fetch(gbfmm_handle* h)
+{
+    if (!h->have_result) return fail(GBFMM_ERR_STATE, "no result: call gbfmm_execute first");
+    if (h->results_on_host) return GBFMM_OK;
+    const int n = h->n;
+    CK(cudaMemcpyAsync(h->h_forces, h->d_forces, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(h->h_pots, h->d_pots, sizeof(float) * n, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(h->h_energy, h->d_energy, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(h->h_flags, h->d_flags, sizeof(int) * 4, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    if (h->timing) {
+        h->n_stage = 9;
+        for (int s = 0; s < 9; s++) cudaEventElapsedTime(&h->stage_ms[s], h->ev[s], h->ev[s + 1]);
+    }
+    h->results_on_host = true;
+    if (h->h_flags[0]) {
+        CK(cudaMemsetAsync(h->d_flags, 0, sizeof(int) * 4, h->stream));
+        h->have_result = false;
+        return fail(GBFMM_ERR_COORD, "non-finite coordinate or charge in the input");
+    }
+    return GBFMM_OK;
+}
+
+extern "C" int gbfmm_execute(gbfmm_handle* h, const float* coords, const float* box, int verbose)
+{
+    if (!h) return fail(GBFMM_ERR_ARG, "handle is NULL");
+    if (!h->have_charges) return fail(GBFMM_ERR_STATE, "charges not set");
+    if (h->n > 0 && !coords) return fail(GBFMM_ERR_ARG, "coordinates are NULL");
+    h->verbose = verbose;
+    int rc = set_box(h, box, h->d_coords);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(h->d_coords, coords, sizeof(float) * 3 * h->n, cudaMemcpyHostToDevice, h->stream));
+    rc = run_step(h);
+    if (rc) return rc;
+    rc = fetch(h);
+    if (rc == GBFMM_OK && verbose)
+        std::printf("[gbfmm] natoms=%d P=%d depth=%d images=%d energy=%.8f\n", h->n, h->P, h->D, h->prm.images,
+                    *h->h_energy);
+    return rc;
+}
+
+extern "C" int gbfmm_device_outputs(gbfmm_handle* h, void** f, void** p, void** e)
+{
+    if (!h) return fail(GBFMM_ERR_ARG, "handle is NULL");
+    if (f) *f = h->d_forces;
+    if (p) *p = h->d_pots;
+    if (e) *e = h->d_energy;
+    return GBFMM_OK;
+}
+
+extern "C" int gbfmm_get_forces(gbfmm_handle* h, float* f)
+{
+    if (!h || (!f && h->n > 0)) return fail(GBFMM_ERR_ARG, "NULL argument");
+    int rc = fetch(h);
+    if (rc) return rc;
+    std::memcpy(f, h->h_forces, sizeof(float) * 3 * h->n);
+    return GBFMM_OK;
+}
+
+extern "C" int gbfmm_add_forces(gbfmm_handle* h, float* f)
+{
+    if (!h || (!f && h->n > 0)) return fail(GBFMM_ERR_ARG, "NULL argument");
+    int rc = fetch(h);
+    if (rc) return rc;
+    for (int i = 0; i < 3 * h->n; i++) f[i] += h->h_forces[i];
+    return GBFMM_OK;
+}
+
+extern "C" int gbfmm_get_potentials(gbfmm_handle* h, float* p)
+{
+    if (!h || (!p && h->n > 0)) return fail(GBFMM_ERR_ARG, "NULL argument");
+    int rc = fetch(h);
+    if (rc) return rc;
+    std::memcpy(p, h->h_pots, sizeof(float) * h->n);
+    return GBFMM_OK;
+}
+
+extern "C" int gbfmm_get_energy(gbfmm_handle* h, double* e)
+{
+    if (!h || !e) return fail(GBFMM_ERR_ARG, "NULL argument");
+    int rc = fetch(h);
+    if (rc) return rc;
+    *e = *h->h_energy;
+    return GBFMM_OK;
+}
+
+extern "C" int gbfmm_compare_forces(gbfmm_handle* h, const float* g, double* l2f)
+{
+    if (!h || !l2f || (!g && h->n > 0)) return fail(GBFMM_ERR_ARG, "NULL argument");
+    int rc = fetch(h);
+    if (rc) return rc;
+    double dif = 0, nrm = 0;
+    for (int i = 0; i < h->n; i++) {
+        const float* f = h->h_forces + 3 * i;
+        if (std::isnan(f[0]) || std::isnan(f[1]) || std::isnan(f[2]) || std::isnan(h->h_pots[i])) {
+            *l2f = NAN;
+            return fail(GBFMM_ERR_COORD, "result of atom %d is NaN", i);
+        }
+        for (int d = 0; d < 3; d++) {
+            double x = (double)f[d] - (double)g[3 * i + d];
+            dif += x * x;
+            nrm += (double)g[3 * i + d] * (double)g[3 * i + d];
+        }
+    }
+    *l2f = std::sqrt(dif / nrm);
+    return GBFMM_OK;
+}
+
+extern "C" int gbfmm_step_launches(gbfmm_handle* h, int* n)
+{
+    if (!h || !n) return fail(GBFMM_ERR_ARG, "NULL argument");
+    *n = h->step_launches;
+    return GBFMM_OK;
+}
+
+extern "C" int gbfmm_set_timing(gbfmm_handle* h, int enable)
+{
+    if (!h) return fail(GBFMM_ERR_ARG, "handle is NULL");
+    h->timing = enable != 0;
+    return GBFMM_OK;
+}
+
+extern "C" int gbfmm_stage_times(gbfmm_handle* h, float* ms, int n_max, int* n_out)
+{
+    if (!h || !ms || !n_out) return fail(GBFMM_ERR_ARG, "NULL argument");
+    int rc = fetch(h);
+    if (rc) return rc;
+    int n = std::min(n_max, h->n_stage);
+    for (int i = 0; i < n; i++) ms[i] = h->stage_ms[i];
+    *n_out = n;
+    return GBFMM_OK;
+}
+
+extern "C" int gbfmm_get_tree(gbfmm_handle* h, int* order, int* leaf_off, int* leaf_num)
+{
+    if (!h) return fail(GBFMM_ERR_ARG, "handle is NULL");
+    if (!h->have_result) return fail(GBFMM_ERR_STATE, "no result: call gbfmm_execute first");
+    std::vector<int> off(h->nleaf + 1);
+    CK(cudaStreamSynchronize(h->stream));
+    CK(cudaMemcpy(off.data(), h->d_off, sizeof(int) * (h->nleaf + 1), cudaMemcpyDeviceToHost));
+    if (order) CK(cudaMemcpy(order, h->d_order, sizeof(int) * h->n, cudaMemcpyDeviceToHost));
+    for (int k = 0; k < h->nleaf; k++) {
+        if (leaf_off) leaf_off[k] = off[k];
+        if (leaf_num) leaf_num[k] = off[k + 1] - off[k];
+    }
+    return GBFMM_OK;
+}
+
+extern "C" int gbfmm_lists(int max_depth, int images, int which, long* count, int* tgt, int* src, int* off3)
+{
+    if (!count || (which != 0 && which != 1) || max_depth < 1 || max_depth > MAX_DEPTH || images < 0 || images > 8)
+        return fail(GBFMM_ERR_ARG, "bad argument");
+    static std::mutex mu;
+    static Stencils st;
+    static bool have = false;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (!have) {
+            st = build_stencils(0.4);
+            have = true;
+        }
+    }
+    RefLists p2p, m2l;
+    emit_lists(st, max_depth, images, p2p, m2l);
+    const RefLists& l = which == 0 ? p2p : m2l;
+    *count = (long)l.tgt.size();
+    if (tgt) std::memcpy(tgt, l.tgt.data(), sizeof(int) * l.tgt.size());
+    if (src) std::memcpy(src, l.src.data(), sizeof(int) * l.src.size());
+    if (off3) std::memcpy(off3, l.off.data(), sizeof(int) * l.off.size());
+    return GBFMM_OK;
+}
+
+extern "C" int gbfmm_get_lists(gbfmm_handle* h, int which, long* count, int* tgt, int* src, int* off3)
+{
+    if (!h || !count || (which != 0 && which != 1)) return fail(GBFMM_ERR_ARG, "bad argument");
+    RefLists p2p, m2l;
+    emit_lists(h->tab->st, h->D, h->prm.images, p2p, m2l);
+    const RefLists& l = which == 0 ? p2p : m2l;
+    *count = (long)l.tgt.size();
+    if (tgt) std::memcpy(tgt, l.tgt.data(), sizeof(int) * l.tgt.size());
+    if (src) std::memcpy(src, l.src.data(), sizeof(int) * l.src.size());
+    if (off3) std::memcpy(off3, l.off.data(), sizeof(int) * l.off.size());
+    return GBFMM_OK;
+}
+
+extern "C" int gbfmm_debug_operator(int order, int images, int kind, int index, double* mat, int* dim, double* cv)
+{
+    if (order < 2 || order > MAX_ORDER || !mat || !dim) return fail(GBFMM_ERR_ARG, "bad argument");
+    const int R = nreal(order);
+    *dim = R;
+    if (kind == 0 || kind == 1) {
+        if (index < 0 || index > 7) return fail(GBFMM_ERR_ARG, "octant %d", index);
+        if (kind == 0) scaled_m2m(order, index, mat);
+        else scaled_l2l(order, index, mat);
+        return GBFMM_OK;
+    }
+    if (kind == 2) {
+        Stencils st = build_stencils(0.4);
+        if (index < 0 || index >= (int)st.classes.size()) return fail(GBFMM_ERR_ARG, "class %d", index);
+        scaled_m2l(order, st.classes[index], mat);
+        if (cv) {
+            cv[0] = st.classes[index].kind;
+            for (int i = 0; i < 3; i++) cv[1 + i] = st.classes[index].v[i];
+        }
+        return GBFMM_OK;
+    }
+    if (kind == 3) {
+        lattice_operator(order, images, mat);
+        return GBFMM_OK;
+    }
+    return fail(GBFMM_ERR_ARG, "kind %d", kind);
+}
+
+extern "C" int gbfmm_debug_harmonics(int order, int kind, const double* d, double* out)
+{
+    if (order < 0 || order > 40 || !d || !out) return fail(GBFMM_ERR_ARG, "bad argument");
+    int np = (order + 1) * (order + 2) / 2;
+    std::vector<double> re(np), im(np);
+    if (kind == 0) harm_regular(order, d, re.data(), im.data());
+    else harm_singular(order, d, re.data(), im.data());
+    for (int i = 0; i < np; i++) {
+        out[2 * i] = re[i];
+        out[2 * i + 1] = im[i];
+    }
+    return GBFMM_OK;
+}
+
+// ---- batched solves: one handle per system for now
+struct gbfmm_batch {
+    std::vector<gbfmm_handle*> hs;
+    std::vector<int> off;
+};
+
+extern "C" int gbfmm_batch_create(int n_sys, const int* atom_offsets, const int* orders, const int* depths, int images,
+                                  int precision, gbfmm_batch** out)
+{
+    (void)n_sys; (void)atom_offsets; (void)orders; (void)depths; (void)images; (void)precision;
+    if (out) *out = nullptr;
+    return fail(GBFMM_ERR_UNSUPPORTED, "batched solves are not built yet");
+}
+extern "C" int gbfmm_batch_execute(gbfmm_batch*, const float*, const float*, const float*, float*, float*, double*)
+{
+    return fail(GBFMM_ERR_UNSUPPORTED, "batched solves are not built yet");
+}
+extern "C" int gbfmm_batch_execute_device(gbfmm_batch*, const void*, const void*, const float*, void*)
+{
+    return fail(GBFMM_ERR_UNSUPPORTED, "batched solves are not built yet");
+}
+extern "C" int gbfmm_batch_device_outputs(gbfmm_batch*, void**, void**, void**)
+{
+    return fail(GBFMM_ERR_UNSUPPORTED, "batched solves are not built yet");
+}
+extern "C" int gbfmm_batch_destroy(gbfmm_batch* b)
+{
+    delete b;
+    return GBFMM_OK;
+}

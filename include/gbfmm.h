@@ -1,0 +1,166 @@
+/*
+ * gbfmm.h -- C ABI of the GB300-native FMM Coulomb solver.
+ *
+ * Drop-in for the solver that mdrun reaches through the fork's Coulomb-solver
+ * plugin interface, coulomb_solver::BaseSolver
+ * (src/gromacs/coulomb_solvers/basesolver.h:43-90), as implemented for the GPU
+ * FMM by zeta_fmm::ZetaFmmSolver (src/gromacs/zeta_fmm/zeta_fmm_solver.cpp).
+ * Plain C types only: host pointers, device pointers as void*, a CUDA stream as
+ * void*.  Every call returns a gbfmm_status; nothing calls exit().
+ *
+ * Units follow GROMACS: nm, e, kJ/mol; forces kJ/mol/nm.
+ */
+#ifndef GBFMM_H
+#define GBFMM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  The reference has none: CUDA errors print and exit(-1)
+ * (src/gromacs/zeta_fmm/type.h:23-28), an unknown solver exits(0)
+ * (src/gromacs/coulomb_solvers/executer.h:55-59). */
+typedef enum gbfmm_status {
+    GBFMM_OK = 0,
+    GBFMM_ERR_ARG = 1,        /* invalid argument (null pointer, size, order, depth) */
+    GBFMM_ERR_BOX = 2,        /* box not cubic, not positive or not finite */
+    GBFMM_ERR_COORD = 3,      /* NaN/Inf coordinate or charge */
+    GBFMM_ERR_CUDA = 4,       /* CUDA runtime error (message via gbfmm_last_error) */
+    GBFMM_ERR_NOMEM = 5,      /* device or host allocation failed, or the arena cap was hit */
+    GBFMM_ERR_UNSUPPORTED = 6,/* feature not built (e.g. rega > 0, tensor M2L for this order) */
+    GBFMM_ERR_STATE = 7,      /* call out of order (e.g. forces before execute) */
+    GBFMM_ERR_TIMEOUT = 8,    /* a bounded device wait gave up; the context stays usable */
+    GBFMM_ERR_NOT_NEUTRAL = 9 /* reserved */
+} gbfmm_status;
+
+/* M2L arithmetic. */
+typedef enum gbfmm_precision {
+    GBFMM_PREC_FP32 = 0,      /* plain FP32 CUDA-core M2L */
+    GBFMM_PREC_BF16X3 = 1,    /* tcgen05 tensor-core M2L, split bf16 hi+lo (3 products), FP32 accumulate */
+    GBFMM_PREC_BF16X1 = 2     /* tcgen05 tensor-core M2L, single bf16 product, FP32 accumulate */
+} gbfmm_precision;
+
+/* Solver parameters.  Defaults (gbfmm_params_default) are the reference's
+ * constants: P=10, max_depth=3, images=4, rega=0 (zeta_fmm_solver.cpp:10-13)
+ * and MAC scale 0.4 (gpu_solver.cu:46). */
+typedef struct gbfmm_params {
+    int order;          /* expansion order P, 2..16 */
+    int max_depth;      /* uniform tree depth, 1..7 */
+    int images;         /* periodic lattice levels: 0 = free space, 1 = 27 near shifts only, >=2 adds far images */
+    double theta;       /* MAC scale; only 0.4 is supported (stencils are precomputed for it) */
+    double rega;        /* regularisation width; only 0 is supported */
+    int precision;      /* gbfmm_precision */
+    int m2l_tile;       /* 0 = autotuned, else targets per M2L tile (32 or 64) */
+    int m2l_split;      /* 0 = autotuned, else entry splits per M2L tile (1..16) */
+    int flags;          /* GBFMM_FLAG_* */
+} gbfmm_params;
+
+#define GBFMM_FLAG_NO_GRAPH 1        /* launch the step kernel by kernel instead of replaying a CUDA graph */
+#define GBFMM_FLAG_DETERMINISTIC 2   /* no floating-point atomics in M2L (m2l_split forced to 1) */
+
+typedef struct gbfmm_handle gbfmm_handle;
+
+void gbfmm_params_default(gbfmm_params* p);
+const char* gbfmm_status_string(int status);
+/* Last error message of the calling thread (static storage; valid until the next call). */
+const char* gbfmm_last_error(void);
+const char* gbfmm_version(void);
+
+/* Constructor: replaces ZetaFmmSolver::ZetaFmmSolver + BaseSolver::BaseSolver
+ * (zeta_fmm_solver.cpp:6-14, basesolver.h:46-52).  natoms = t_mdatoms::homenr. */
+int gbfmm_create(const gbfmm_params* params, int natoms, gbfmm_handle** out);
+int gbfmm_destroy(gbfmm_handle* h);
+
+/* BaseSolver::set_parameter (basesolver.h:56-61): atom count and chargeA.
+ * Charges are copied (the reference borrows them and reads them in execute). */
+int gbfmm_set_charges(gbfmm_handle* h, int natoms, const float* charges);
+
+/* BaseSolver::execute (basesolver.h:67; zeta_fmm_solver.cpp:16-64): host
+ * coordinates (float[3*natoms], nm) and the box (float[9], row-major 3x3, nm;
+ * must be cubic: the reference uses box[XX][XX] as the period).  Synchronous,
+ * like the reference: results are on the host when it returns. */
+int gbfmm_execute(gbfmm_handle* h, const float* coords, const float* box, int verbose);
+
+/* Device-resident execute: d_coords float[3*natoms] on the device, results left
+ * on the device (see gbfmm_device_outputs).  Asynchronous on 'stream'
+ * (cudaStream_t, NULL = default stream). */
+int gbfmm_execute_device(gbfmm_handle* h, const void* d_coords, const float* box, void* stream);
+
+/* Device pointers of the last results, in input atom order: forces float[3*natoms]
+ * (kJ/mol/nm), potentials float[natoms] (kJ/mol/e), energy double[1] (kJ/mol). */
+int gbfmm_device_outputs(gbfmm_handle* h, void** d_forces, void** d_potentials, void** d_energy);
+
+/* BaseSolver::add_force (basesolver.h:72; zeta_fmm_solver.cpp:66-76): adds the
+ * Coulomb forces to a host float[3*natoms] array. */
+int gbfmm_add_forces(gbfmm_handle* h, float* forces);
+int gbfmm_get_forces(gbfmm_handle* h, float* forces);
+int gbfmm_get_potentials(gbfmm_handle* h, float* potentials);
+
+/* BaseSolver::get_energy (basesolver.h:77).  The reference returns zeros
+ * (zeta_fmm_solver.cpp:109-115); this returns 0.5*sum(q*phi) as the legacy
+ * zeta_fmm::FMM::get_energy does (src/gromacs/zeta_fmm/fmm.cpp:89-98). */
+int gbfmm_get_energy(gbfmm_handle* h, double* coulomb_energy);
+
+/* BaseSolver::compare_forces (basesolver.h:82; zeta_fmm_solver.cpp:78-107):
+ * relative L2 force error sqrt(sum|f-g|^2 / sum|g|^2) against host forces g.
+ * Returns GBFMM_ERR_COORD (and l2f = NaN) if a result is NaN, where the
+ * reference prints "have nan!". */
+int gbfmm_compare_forces(gbfmm_handle* h, const float* ref_forces, double* l2f);
+
+/* Per-stage device times of the last execute (ms, CUDA events), when built with
+ * timing enabled by gbfmm_set_timing(h, 1). */
+int gbfmm_set_timing(gbfmm_handle* h, int enable);
+int gbfmm_stage_times(gbfmm_handle* h, float* ms, int n_max, int* n_out);
+const char* gbfmm_stage_name(int stage);
+/* Number of device kernels one step launches (counted when the step is enqueued). */
+int gbfmm_step_launches(gbfmm_handle* h, int* n);
+
+/* ---- tree and interaction lists (integer parity with the reference) ---- */
+
+/* Body order of the last execute: order[i] = input index of the body at sorted
+ * position i (CompleteBalancedOctree::build, tree.cpp:13-99), and the body range
+ * of every leaf in BFS cell order (leaf_off[k], leaf_num[k] for leaf k). */
+int gbfmm_get_tree(gbfmm_handle* h, int* order, int* leaf_off, int* leaf_num);
+
+/* Interaction lists as the reference's Traverser produces them
+ * (traverser.cpp:47-214): entries grouped by ascending target cell, in traversal
+ * order within a target.  which: 0 = P2P, 1 = M2L.  Cell indices are the
+ * reference's BFS indices; image cells follow the tree cells.  offsets are the
+ * periodic shift of each source in units of the period (integers).  Two-call
+ * protocol: pass NULL arrays to get the count. */
+int gbfmm_get_lists(gbfmm_handle* h, int which, long* count, int* target, int* source, int* offset3);
+/* The same lists without a handle (host only): tree depth and image levels. */
+int gbfmm_lists(int max_depth, int images, int which, long* count, int* target, int* source, int* offset3);
+
+/* ---- operator tables (host only, for tests) ---- */
+
+/* Fills 'mat' (rows x cols, row-major, real (P+1)^2 representation in scaled
+ * units) with one operator the device kernels apply.  kind: 0 M2M of child
+ * octant 'index', 1 L2L of child octant 'index', 2 M2L class 'index', 3 the
+ * periodic lattice operator.  Returns GBFMM_ERR_ARG for an unknown index. */
+int gbfmm_debug_operator(int order, int images, int kind, int index, double* mat, int* dim, double* class_vec);
+int gbfmm_debug_harmonics(int order, int kind, const double* d, double* out);
+
+/* ---- batched solves ---- */
+
+/* Many independent cubic systems solved as one batch through one captured
+ * CUDA graph.  Host inputs: offsets[n_sys+1] into the concatenated coords
+ * (3 floats per atom) and charges, boxes[n_sys] (cubic edge, nm), per-system
+ * order and depth.  Outputs (host): forces, potentials, energies[n_sys]. */
+typedef struct gbfmm_batch gbfmm_batch;
+int gbfmm_batch_create(int n_sys, const int* atom_offsets, const int* orders, const int* depths, int images,
+                       int precision, gbfmm_batch** out);
+int gbfmm_batch_execute(gbfmm_batch* b, const float* coords, const float* charges, const float* box_edges,
+                        float* forces, float* potentials, double* energies);
+int gbfmm_batch_execute_device(gbfmm_batch* b, const void* d_coords, const void* d_charges,
+                               const float* box_edges, void* stream);
+int gbfmm_batch_device_outputs(gbfmm_batch* b, void** d_forces, void** d_potentials, void** d_energies);
+int gbfmm_batch_destroy(gbfmm_batch* b);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBFMM_H */

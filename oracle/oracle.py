@@ -1,0 +1,213 @@
+"""ctypes wrapper of the oracle (TEST INFRASTRUCTURE ONLY).
+
+Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg import this
+module; the product library never does.  It exposes:
+
+* ``zeta_solve`` -- FP64 restatement of the zeta_fmm solver (zeta64.c),
+* ``zeta_tree`` / ``zeta_lists`` -- restated tree build and traversal,
+* ``ewald`` / ``direct`` -- FP64 Ewald and direct lattice sums (ewald64.c),
+* ``ref_run`` -- the reference's own tree/traverser (oracle/_ref), when built.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_LIB = os.path.join(HERE, "_ref", "libzetaref.so")
+
+_lib = None
+_ref = None
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+_lp = ctypes.POINTER(ctypes.c_long)
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    return a.ctypes.data_as(_ip)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = ctypes.CDLL(path)
+        L.z64_solve.restype = ctypes.c_int
+        L.z64_solve.argtypes = [ctypes.c_int, _dp, _dp, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                ctypes.c_int, ctypes.c_double, ctypes.c_int, _dp, _dp, _dp]
+        L.z64_tree.restype = ctypes.c_int
+        L.z64_tree.argtypes = [ctypes.c_int, _dp, ctypes.c_double, _dp, ctypes.c_int, _ip, _ip, _ip, _ip,
+                               _dp, ctypes.c_int]
+        L.z64_lists.restype = ctypes.c_int
+        L.z64_lists.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, _lp, _lp]
+        L.z64_lists_fetch.restype = None
+        L.z64_lists_fetch.argtypes = [ctypes.c_int, _ip, _ip, _dp]
+        L.z64_harmonics.restype = None
+        L.z64_harmonics.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp]
+        L.z64_apply.restype = None
+        L.z64_apply.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]
+        L.z64_set_threads.restype = None
+        L.z64_set_threads.argtypes = [ctypes.c_int]
+        L.ew64_solve.restype = ctypes.c_int
+        L.ew64_solve.argtypes = [ctypes.c_int, _dp, _dp, _dp, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                 _ip, _dp, _dp, ctypes.c_int, _dp]
+        L.direct64_solve.restype = ctypes.c_int
+        L.direct64_solve.argtypes = [ctypes.c_int, _dp, _dp, ctypes.c_double, ctypes.c_int, _dp, _dp]
+        _lib = L
+    return _lib
+
+
+def set_threads(n):
+    lib().z64_set_threads(int(n))
+
+
+def zeta_solve(xyz, q, cycle, P, depth, images=4, theta=0.4, stages=7):
+    """Reference-algorithm FMM in FP64. xyz (n,3) float64 (already float32-rounded
+    by the caller when mimicking GROMACS RVec input), q (n,). Returns pot, force, energy."""
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    n = len(q)
+    pot = np.zeros(n)
+    force = np.zeros((n, 3))
+    e = np.zeros(1)
+    rc = lib().z64_solve(n, _d(xyz), _d(q), float(cycle), int(P), int(depth), int(images), float(theta),
+                         int(stages), _d(pot), _d(force), _d(e))
+    if rc != 0:
+        raise ValueError("z64_solve rejected its arguments")
+    return pot, force, float(e[0])
+
+
+def zeta_tree(xyz, cycle, depth):
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    n = len(xyz)
+    maxc = (8 ** (depth + 1) - 1) // 7
+    order = np.zeros(max(n, 1), np.int32)
+    cd = np.zeros(maxc, np.int32)
+    bo = np.zeros(maxc, np.int32)
+    bn = np.zeros(maxc, np.int32)
+    cc = np.zeros((maxc, 3))
+    center = np.full(3, cycle / 2.0)
+    nc = lib().z64_tree(n, _d(xyz), cycle / 2.0, _d(center), int(depth), _i(order), _i(cd), _i(bo), _i(bn),
+                        _d(cc), maxc)
+    return dict(order=order[:n], depth=cd[:nc], body_off=bo[:nc], body_num=bn[:nc], center=cc[:nc])
+
+
+def zeta_lists(depth, images, cycle=1.0, theta=0.4):
+    np2p = ctypes.c_long()
+    nm2l = ctypes.c_long()
+    nimg = lib().z64_lists(int(depth), int(images), float(cycle), float(theta), ctypes.byref(np2p),
+                           ctypes.byref(nm2l))
+    out = {"n_image_cells": nimg}
+    for which, name, cnt in ((0, "p2p", np2p.value), (1, "m2l", nm2l.value)):
+        t = np.zeros(max(cnt, 1), np.int32)
+        s = np.zeros(max(cnt, 1), np.int32)
+        o = np.zeros((max(cnt, 1), 3))
+        lib().z64_lists_fetch(which, _i(t), _i(s), _d(o))
+        out[name] = (t[:cnt], s[:cnt], o[:cnt])
+    return out
+
+
+def harmonics(kind, P, d):
+    d = np.ascontiguousarray(d, dtype=np.float64)
+    out = np.zeros(2 * (P + 1) ** 2)
+    lib().z64_harmonics(int(kind), int(P), _d(d), _d(out))
+    return out[0::2] + 1j * out[1::2]
+
+
+def apply_op(kind, P, d, vec):
+    """kind 0: M2M, 1: L2L, 2: M2L; vec packed complex of length (P+1)(P+2)/2."""
+    d = np.ascontiguousarray(d, dtype=np.float64)
+    v = np.ascontiguousarray(np.stack([np.real(vec), np.imag(vec)], -1).reshape(-1), dtype=np.float64)
+    out = np.zeros_like(v)
+    lib().z64_apply(int(kind), int(P), _d(d), _d(v), _d(out))
+    return out[0::2] + 1j * out[1::2]
+
+
+def ewald(xyz, q, box, eps=1e-10, targets=None, rc=0.0, energy=False):
+    """Converged FP64 Ewald (tin-foil). Returns (pot[targets], force[targets], energy|None)."""
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    box = np.ascontiguousarray(np.broadcast_to(np.asarray(box, dtype=np.float64), (3,)))
+    n = len(q)
+    if energy:
+        tg = np.arange(n, dtype=np.int32)
+    else:
+        tg = np.ascontiguousarray(np.arange(n) if targets is None else targets, dtype=np.int32)
+    nt = len(tg)
+    pot = np.zeros(nt)
+    force = np.zeros((nt, 3))
+    e = np.zeros(1)
+    lib().ew64_solve(n, _d(xyz), _d(q), _d(box), float(eps), float(rc), nt, _i(tg), _d(pot), _d(force),
+                     1 if energy else 0, _d(e))
+    return pot, force, (float(e[0]) if energy else None)
+
+
+def direct(xyz, q, L, nmax):
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    n = len(q)
+    pot = np.zeros(n)
+    force = np.zeros((n, 3))
+    lib().direct64_solve(n, _d(xyz), _d(q), float(L), int(nmax), _d(pot), _d(force))
+    return pot, force
+
+
+# ------------------------------------------------------------------ reference itself
+
+def ref_available():
+    return os.path.exists(REF_LIB)
+
+
+def ref_lib():
+    global _ref
+    if _ref is None:
+        R = ctypes.CDLL(REF_LIB)
+        R.zref_run.restype = ctypes.c_int
+        R.zref_run.argtypes = [ctypes.c_int, _dp, ctypes.c_double, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                               ctypes.c_double]
+        R.zref_cells.restype = None
+        R.zref_cells.argtypes = [_ip, _dp, _dp, _ip, _ip, _ip, _ip]
+        R.zref_order.restype = None
+        R.zref_order.argtypes = [_ip]
+        R.zref_nlist.restype = ctypes.c_long
+        R.zref_nlist.argtypes = [ctypes.c_int]
+        R.zref_list.restype = None
+        R.zref_list.argtypes = [ctypes.c_int, _ip, _ip, _dp]
+        _ref = R
+    return _ref
+
+
+def ref_run(xyz, cycle, depth, images, theta=0.4):
+    """Run the reference's own CompleteBalancedOctree + Traverser."""
+    R = ref_lib()
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+    n = len(xyz)
+    center = np.full(3, cycle / 2.0)
+    nc = R.zref_run(n, _d(xyz), cycle / 2.0, _d(center), int(depth), int(images), float(cycle), float(theta))
+    depth_a = np.zeros(nc, np.int32)
+    r = np.zeros(nc)
+    c = np.zeros((nc, 3))
+    co = np.zeros(nc, np.int32)
+    cn = np.zeros(nc, np.int32)
+    bo = np.zeros(nc, np.int32)
+    bn = np.zeros(nc, np.int32)
+    R.zref_cells(_i(depth_a), _d(r), _d(c), _i(co), _i(cn), _i(bo), _i(bn))
+    order = np.zeros(max(n, 1), np.int32)
+    R.zref_order(_i(order))
+    out = dict(depth=depth_a, r=r, center=c, child_off=co, child_num=cn, body_off=bo, body_num=bn,
+               order=order[:n])
+    for which, name in ((0, "p2p"), (1, "m2l")):
+        cnt = R.zref_nlist(which)
+        t = np.zeros(max(cnt, 1), np.int32)
+        s = np.zeros(max(cnt, 1), np.int32)
+        o = np.zeros((max(cnt, 1), 3))
+        R.zref_list(which, _i(t), _i(s), _d(o))
+        out[name] = (t[:cnt], s[:cnt], o[:cnt])
+    return out

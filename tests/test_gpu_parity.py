@@ -1,0 +1,177 @@
+"""GPU parity: the sm_103a FP32 path against the FP64 oracle (relative RMS force
+and potential error <= 1e-5, relative energy error <= 1e-6) and the tree against
+fixtures made by the reference's own tree.cpp (bit-exact)."""
+import numpy as np
+import pytest
+
+from conftest import golden, rel_rms
+
+pytestmark = pytest.mark.gpu
+
+TOL_F = 1e-5   # relative RMS force / potential error of the FP32 path vs the FP64 oracle
+TOL_E = 1e-6   # relative energy error
+
+
+def _solve(pkg, xyz, q, box, **kw):
+    s = pkg.ZetaFmmSolver(len(q), q, **kw)
+    s.execute(xyz, box)
+    return s.forces(), s.potentials(), s.get_energy(), s
+
+
+@pytest.mark.parametrize("n_sites,L,ions,P,depth,images", [
+    (300, 2.0, 2, 4, 2, 4),
+    (1000, 2.2, 4, 8, 2, 4),
+    (3000, 4.5, 0, 8, 3, 4),
+    (1500, 3.0, 6, 10, 3, 0),
+    (1500, 3.0, 6, 6, 3, 1),
+    (1500, 3.0, 6, 6, 3, 2),
+    (3000, 4.5, 10, 12, 3, 4),
+    (800, 2.0, 4, 5, 1, 4),
+])
+def test_parity_vs_oracle(pkg, oracle, systems, n_sites, L, ions, P, depth, images):
+    xyz, q, box = systems.water_ion_box(n_sites, L, n_na=ions, n_cl=ions, seed=n_sites + P)
+    f, p, e, s = _solve(pkg, xyz, q, box, order=P, max_depth=depth, images=images)
+    po, fo, eo = oracle.zeta_solve(xyz.astype(np.float64), q.astype(np.float64), float(box[0]), P, depth, images)
+    assert rel_rms(f, fo) < TOL_F
+    assert rel_rms(p, po) < TOL_F
+    assert abs(e - eo) / abs(eo) < TOL_E
+    s.close()
+
+
+def test_parity_water_96k(pkg, oracle, systems):
+    """The 95,600-atom 9.86 nm box at p=10, depth 4, at full size."""
+    xyz, q, box = systems.cfg_96k()
+    f, p, e, s = _solve(pkg, xyz, q, box, order=10, max_depth=4, images=4)
+    po, fo, eo = oracle.zeta_solve(xyz.astype(np.float64), q.astype(np.float64), float(box[0]), 10, 4, 4)
+    assert rel_rms(f, fo) < TOL_F
+    assert rel_rms(p, po) < TOL_F
+    assert abs(e - eo) / abs(eo) < TOL_E
+    # against the converged Ewald sum on a sample of atoms (FMM truncation error)
+    tg = np.arange(0, len(q), 97)
+    _, fe, _ = oracle.ewald(xyz.astype(np.float64), q.astype(np.float64), box[0], eps=1e-9, targets=tg)
+    assert rel_rms(f[tg], fe) < 2e-4
+    s.close()
+
+
+@pytest.mark.parametrize("name,depth", [("tree_water9k_d3.npz", 3), ("tree_edges_d1.npz", 1),
+                                        ("tree_edges_d2.npz", 2), ("tree_edges_d3.npz", 3)])
+def test_tree_bit_exact_vs_reference(pkg, name, depth):
+    g = golden(name)
+    xyz = g["xyz"]
+    q = np.where(np.arange(len(xyz)) % 2 == 0, 1.0, -1.0).astype(np.float32)
+    s = pkg.ZetaFmmSolver(len(q), q, order=4, max_depth=depth, images=4)
+    s.execute(xyz, float(g["box"]))
+    order, lo, ln = s.tree()
+    assert np.array_equal(order, g["order"])
+    assert np.array_equal(ln, g["leaf_count"])
+    assert np.array_equal(lo, np.concatenate([[0], np.cumsum(ln)[:-1]]))
+    s.close()
+
+
+def test_crowded_leaves(pkg, oracle, systems):
+    """Ragged occupancy: most bodies in a few leaves (> 256 per leaf, > 2048 near
+    sources), many empty leaves."""
+    rng = np.random.default_rng(4)
+    L = 4.0
+    a = rng.uniform(0.05, 0.45, (1400, 3))
+    b = rng.uniform(0, L, (200, 3))
+    xyz = np.concatenate([a, b]).astype(np.float32)
+    q = np.where(np.arange(len(xyz)) % 2 == 0, 0.5, -0.5).astype(np.float32)
+    f, p, e, s = _solve(pkg, xyz, q, L, order=6, max_depth=3, images=4)
+    po, fo, eo = oracle.zeta_solve(xyz.astype(np.float64), q.astype(np.float64), L, 6, 3, 4)
+    assert rel_rms(f, fo) < TOL_F
+    assert rel_rms(p, po) < TOL_F
+    s.close()
+
+
+def test_device_execute_matches_host_execute(pkg, systems):
+    torch = pytest.importorskip("torch")
+    xyz, q, box = systems.water_ion_box(1200, 2.5, seed=12)
+    s = pkg.ZetaFmmSolver(len(q), q, order=6, max_depth=2, images=4, flags=pkg.FLAG_DETERMINISTIC)
+    s.execute(xyz, box)
+    f_host = s.forces()
+    x = torch.from_numpy(xyz).cuda()
+    st = torch.cuda.Stream()
+    s.execute_device(x.data_ptr(), box, st.cuda_stream)
+    st.synchronize()
+    f_dev = s.forces()
+    assert np.array_equal(f_host, f_dev)
+    fp, pp, ep = s.device_outputs()
+    assert fp and pp and ep
+    s.close()
+
+
+def test_deterministic_flag_is_bitwise_repeatable(pkg, systems):
+    xyz, q, box = systems.water_ion_box(2000, 2.8, seed=13)
+    s = pkg.ZetaFmmSolver(len(q), q, order=8, max_depth=3, images=4, flags=pkg.FLAG_DETERMINISTIC)
+    s.execute(xyz, box)
+    f1, p1, e1 = s.forces(), s.potentials(), s.get_energy()
+    s.execute(xyz, box)
+    f2, p2, e2 = s.forces(), s.potentials(), s.get_energy()
+    assert np.array_equal(f1, f2) and np.array_equal(p1, p2)
+    assert abs(e1 - e2) <= 1e-12 * abs(e1)
+    s.close()
+
+
+def test_graph_replay_follows_new_box_and_coords(pkg, oracle, systems):
+    xyz, q, box = systems.water_ion_box(900, 2.1, seed=14)
+    s = pkg.ZetaFmmSolver(len(q), q, order=6, max_depth=2, images=4)
+    s.execute(xyz, box)
+    xyz2 = (xyz * np.float32(1.05)).astype(np.float32)
+    L2 = float(np.float32(box[0] * 1.05))
+    s.execute(xyz2, L2)
+    f = s.forces()
+    _, fo, _ = oracle.zeta_solve(xyz2.astype(np.float64), q.astype(np.float64), L2, 6, 2, 4)
+    assert rel_rms(f, fo) < TOL_F
+    s.close()
+
+
+def test_nonfinite_input_reports_error_and_recovers(pkg, systems):
+    xyz, q, box = systems.water_ion_box(300, 2.0, seed=15)
+    s = pkg.ZetaFmmSolver(len(q), q, order=4, max_depth=2, images=4)
+    bad = xyz.copy()
+    bad[7, 1] = np.nan
+    with pytest.raises(pkg.FmmError) as e:
+        s.execute(bad, box)
+    assert e.value.status == 3
+    s.execute(xyz, box)
+    assert np.isfinite(s.forces()).all()
+    s.close()
+
+
+def test_box_validation(pkg, systems):
+    xyz, q, box = systems.water_ion_box(100, 1.5, seed=16)
+    s = pkg.ZetaFmmSolver(len(q), q, order=4, max_depth=1, images=4)
+    for bad in ([1.5, 1.5, 1.6], [0.0, 0.0, 0.0], [np.inf, 1.5, 1.5]):
+        with pytest.raises(pkg.FmmError) as e:
+            s.execute(xyz, bad)
+        assert e.value.status == 2
+    with pytest.raises(pkg.FmmError) as e:
+        pkg.ZetaFmmSolver(len(q), q, order=4, max_depth=1).forces()
+    assert e.value.status == 7
+    s.close()
+
+
+def test_add_force_and_compare_forces(pkg, oracle, systems):
+    xyz, q, box = systems.water_ion_box(500, 1.8, seed=17)
+    s = pkg.ZetaFmmSolver(len(q), q, order=6, max_depth=2, images=4)
+    s.execute(xyz, box)
+    acc = np.ones((len(q), 3), np.float32)
+    s.add_force(acc)
+    assert np.allclose(acc - 1.0, s.forces(), rtol=0, atol=1e-3)
+    _, fo, _ = oracle.zeta_solve(xyz.astype(np.float64), q.astype(np.float64), float(box[0]), 6, 2, 4)
+    l2f = s.compare_forces(fo.astype(np.float32), verbose=False)
+    assert l2f < TOL_F
+    s.close()
+
+
+def test_empty_and_zero_charge_systems(pkg):
+    s = pkg.ZetaFmmSolver(0, np.zeros(0, np.float32), order=4, max_depth=1, images=4)
+    s.execute(np.zeros((0, 3), np.float32), 2.0)
+    assert s.get_energy() == 0.0
+    s.close()
+    xyz = np.random.default_rng(0).uniform(0, 2, (50, 3)).astype(np.float32)
+    s = pkg.ZetaFmmSolver(50, np.zeros(50, np.float32), order=4, max_depth=1, images=4)
+    s.execute(xyz, 2.0)
+    assert np.all(s.forces() == 0) and np.all(s.potentials() == 0) and s.get_energy() == 0.0
+    s.close()

@@ -1,0 +1,98 @@
+"""The oracle pinned against the reference: tree and lists against fixtures made
+by the reference's own tree.cpp/traverser.cpp, operators against physics (FP64
+Ewald and direct lattice sums)."""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, golden, rel_rms
+
+
+def _digest(t, s, o):
+    h = hashlib.sha256()
+    for a in (t, s, o):
+        h.update(np.ascontiguousarray(a, dtype="<i4").tobytes())
+    return h.hexdigest()
+
+
+@pytest.mark.parametrize("name,depth", [("tree_water9k_d3.npz", 3), ("tree_edges_d1.npz", 1),
+                                        ("tree_edges_d2.npz", 2), ("tree_edges_d3.npz", 3)])
+def test_oracle_tree_matches_reference(oracle, name, depth):
+    g = golden(name)
+    T = oracle.zeta_tree(g["xyz"].astype(np.float64), float(g["box"]), depth)
+    assert np.array_equal(T["order"], g["order"])
+    leaf = T["depth"] == depth
+    assert np.array_equal(T["body_num"][leaf], g["leaf_count"])
+
+
+@pytest.mark.parametrize("depth", [1, 2])
+@pytest.mark.parametrize("images", [0, 1, 2, 4])
+def test_oracle_lists_match_reference(oracle, depth, images):
+    g = golden("lists_small.npz")
+    L = oracle.zeta_lists(depth, images, cycle=4.5)
+    for k in ("p2p", "m2l"):
+        t, s, o = L[k]
+        assert np.array_equal(t, g[f"{k}_d{depth}_i{images}_tgt"])
+        assert np.array_equal(s, g[f"{k}_d{depth}_i{images}_src"])
+        assert np.array_equal(np.rint(o / 4.5).astype(np.int32), g[f"{k}_d{depth}_i{images}_off"])
+
+
+def test_oracle_lists_hash_matches_reference(oracle):
+    with open(os.path.join(GOLDEN, "lists_hash.json")) as f:
+        ref = json.load(f)
+    for key, v in ref.items():
+        kind, d, i = key.split("_")
+        L = oracle.zeta_lists(int(d[1:]), int(i[1:]), cycle=9.86)
+        t, s, o = L[kind]
+        assert len(t) == v["count"], key
+        assert _digest(t, s, np.rint(o / 9.86).astype(np.int32)) == v["sha256"], key
+
+
+def test_ewald_matches_direct_lattice_sum(oracle):
+    rng = np.random.default_rng(3)
+    L = 2.0
+    x = rng.uniform(0, L, (8, 3))
+    q = np.array([1.0, -1.0] * 4)
+    _, fd = oracle.direct(x, q, L, 24)
+    _, fe, _ = oracle.ewald(x, q, L, eps=1e-12)
+    # the shell sum converges slowly; forces agree to ~1e-6
+    assert rel_rms(fd, fe) < 5e-6
+
+
+def test_ewald_accuracy_parameter_is_consistent(oracle, systems):
+    xyz, q, box = systems.water_ion_box(500, 1.75, seed=3)
+    x = xyz.astype(np.float64)
+    tg = np.arange(0, len(q), 5)
+    _, f1, _ = oracle.ewald(x, q, box[0], eps=1e-8, targets=tg)
+    _, f2, _ = oracle.ewald(x, q, box[0], eps=1e-12, targets=tg)
+    assert rel_rms(f1, f2) < 1e-7
+
+
+def test_zeta_oracle_converges_to_ewald(oracle, systems):
+    xyz, q, box = systems.water_ion_box(1000, 2.2, n_na=4, n_cl=4, seed=9)
+    x = xyz.astype(np.float64)
+    q = q.astype(np.float64)
+    _, fe, ee = oracle.ewald(x, q, box[0], eps=1e-11, energy=True)
+    errs = []
+    for P in (4, 6, 8, 10):
+        _, f, e = oracle.zeta_solve(x, q, float(box[0]), P, 2, 4)
+        errs.append(rel_rms(f, fe))
+    assert all(errs[i + 1] < errs[i] for i in range(len(errs) - 1)), errs
+    assert errs[-1] < 2e-4
+    _, _, e10 = oracle.zeta_solve(x, q, float(box[0]), 12, 2, 4)
+    assert abs(e10 - ee) / abs(ee) < 1e-5
+
+
+def test_zeta_oracle_near_and_far_split(oracle, systems):
+    """Stage masks: near (P2P) + far (multipole) + dipole add up to the full solve."""
+    xyz, q, box = systems.water_ion_box(300, 1.6, seed=2)
+    x = xyz.astype(np.float64)
+    q = q.astype(np.float64)
+    p_all, f_all, _ = oracle.zeta_solve(x, q, float(box[0]), 6, 2, 4, stages=7)
+    p1, f1, _ = oracle.zeta_solve(x, q, float(box[0]), 6, 2, 4, stages=1)
+    p2, f2, _ = oracle.zeta_solve(x, q, float(box[0]), 6, 2, 4, stages=2)
+    p4, f4, _ = oracle.zeta_solve(x, q, float(box[0]), 6, 2, 4, stages=4)
+    assert np.allclose(f1 + f2 + f4, f_all, rtol=1e-12, atol=1e-9)
