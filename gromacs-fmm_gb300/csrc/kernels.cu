@@ -80,18 +80,19 @@ __global__ void __launch_bounds__(256) k_tree_keys(TreeArgs a)
     if (threadIdx.x < 4) {
         double t = 0;
         for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w][threadIdx.x];
-        atomicAdd(&a.sums[threadIdx.x], t);
+        a.partials[4 * blockIdx.x + threadIdx.x] = t;
     }
     if (bad) atomicOr(&a.flags[0], 1);
 }
+
+int tree_blocks(int n) { return n <= 0 ? 1 : (n + 255) / 256 < TREE_MAX_BLOCKS ? (n + 255) / 256 : TREE_MAX_BLOCKS; }
+int final_blocks(int n) { return n <= 0 ? 1 : (n + 255) / 256 < FINAL_MAX_BLOCKS ? (n + 255) / 256 : FINAL_MAX_BLOCKS; }
 
 void launch_tree_keys(const TreeArgs& a, cudaStream_t s)
 {
     int nd = 1 << a.depth;
     size_t shm = sizeof(float) * (((3 * (nd + 1) + 1) & ~1) + 6 * nd);
-    int blocks = (a.n + 255) / 256;
-    if (blocks > 4 * 152) blocks = 4 * 152;
-    if (blocks < 1) blocks = 1;
+    int blocks = tree_blocks(a.n);
     COUNT_LAUNCH();
     k_tree_keys<<<blocks, 256, shm, s>>>(a);
 }
@@ -408,7 +409,7 @@ void launch_l2p(int P, const int* offsets, int nleaf, const float4* atoms, const
 
 constexpr int P2P_THREADS = 128;
 constexpr int P2P_MAXS = 2048;  // staged source bodies per pass
-constexpr int P2P_MAXT = 256;   // targets per pass
+constexpr int P2P_MAXT = 128;   // targets per pass
 
 // One CTA per target leaf.  The source bodies of the 81 near leaves are staged in
 // shared memory, shifted into the target leaf's frame (scaled units, integer
@@ -419,7 +420,7 @@ __global__ void __launch_bounds__(P2P_THREADS) k_p2p(const int* off, int depth, 
                                                      const int* stencil, int nst, float4* field)
 {
     __shared__ float4 src[P2P_MAXS];
-    __shared__ float4 acc[P2P_MAXT];
+    __shared__ float4 part[4][P2P_MAXT];  // per-warp partial sums, reduced in warp order
     __shared__ int e_off[128];
     __shared__ int e_beg[128];
     __shared__ float4 e_d[128];
@@ -469,7 +470,7 @@ __global__ void __launch_bounds__(P2P_THREADS) k_p2p(const int* off, int depth, 
     const int total = e_off[nst];
     for (int t0 = 0; t0 < nt; t0 += P2P_MAXT) {
         const int ntc = min(P2P_MAXT, nt - t0);
-        for (int i = tid; i < ntc; i += P2P_THREADS) acc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int i = tid; i < 4 * P2P_MAXT; i += P2P_THREADS) part[i / P2P_MAXT][i % P2P_MAXT] = make_float4(0.f, 0.f, 0.f, 0.f);
         for (int s0 = 0; s0 < total; s0 += P2P_MAXS) {
             const int ns = min(P2P_MAXS, total - s0);
             __syncthreads();
@@ -502,14 +503,25 @@ __global__ void __launch_bounds__(P2P_THREADS) k_p2p(const int* off, int depth, 
                     gy -= q3 * dy;
                     gz -= q3 * dz;
                 }
-                atomicAdd(&acc[tt].x, phi);
-                atomicAdd(&acc[tt].y, gx);
-                atomicAdd(&acc[tt].z, gy);
-                atomicAdd(&acc[tt].w, gz);
+                float4 pp = part[warp][tt];
+                pp.x += phi;
+                pp.y += gx;
+                pp.z += gy;
+                pp.w += gz;
+                part[warp][tt] = pp;
             }
         }
         __syncthreads();
-        for (int i = tid; i < ntc; i += P2P_THREADS) field[tb + t0 + i] = acc[i];
+        for (int i = tid; i < ntc; i += P2P_THREADS) {
+            float4 r = part[0][i];
+            for (int w = 1; w < 4; w++) {
+                r.x += part[w][i].x;
+                r.y += part[w][i].y;
+                r.z += part[w][i].z;
+                r.w += part[w][i].w;
+            }
+            field[tb + t0 + i] = r;
+        }
         __syncthreads();
     }
 }
@@ -557,6 +569,21 @@ __global__ void __launch_bounds__(CT_WARPS * 32) k_contract(ContractArgs a)
         morton_decode(tcode, vt[0], vt[1], vt[2]);
         trow[tid] = tvalid ? (int)(tcode * (uint32_t)Rpad) : -1;
     }
+    // this warp's work items (row block, column range) and their accumulators,
+    // kept in registers across all entries of the task
+    const int ib = a.warp_begin[task.group * (CT_WARPS + 1) + warp];
+    const int nit = min(CT_MAXI, a.warp_begin[task.group * (CT_WARPS + 1) + warp + 1] - ib);
+    int4 itm[CT_MAXI];
+    int bofs[CT_MAXI];
+    float acc[CT_MAXI][8][2];
+#pragma unroll
+    for (int k = 0; k < CT_MAXI; k++) {
+        itm[k] = k < nit ? a.items[ib + k] : make_int4(0, 0, 0, 0);
+        const BlockInfo bi = a.blocks[itm[k].x];
+        bofs[k] = bi.off + (itm[k].y - bi.c0) * 8;
+#pragma unroll
+        for (int i = 0; i < 8; i++) acc[k][i][0] = acc[k][i][1] = 0.f;
+    }
     for (int e = task.e_begin; e < task.e_end; e++) {
         const CEntry en = a.entries[e];
         const int slev = en.mode == 0 ? task.level : (en.mode == 1 ? task.level - 1 : task.level + 1);
@@ -596,39 +623,50 @@ __global__ void __launch_bounds__(CT_WARPS * 32) k_contract(ContractArgs a)
         }
         __syncthreads();
         const float* op = a.ops + en.op;
-        for (int it = a.warp_begin[warp]; it < a.warp_begin[warp + 1]; it++) {
-            const int4 w = a.items[it];
-            const BlockInfo bi = a.blocks[w.x];
-            float acc[8][2];
 #pragma unroll
-            for (int i = 0; i < 8; i++) acc[i][0] = acc[i][1] = 0.f;
-            const float4* ap = reinterpret_cast<const float4*>(op + bi.off + (w.y - bi.c0) * 8);
-            for (int c = w.y; c < w.z; c++, ap += 2) {
-                const float4 a0 = __ldg(ap), a1 = __ldg(ap + 1);
-                const float2 m = *reinterpret_cast<const float2*>(&Ms[c * T + 2 * lane]);
-                acc[0][0] += a0.x * m.x; acc[0][1] += a0.x * m.y;
-                acc[1][0] += a0.y * m.x; acc[1][1] += a0.y * m.y;
-                acc[2][0] += a0.z * m.x; acc[2][1] += a0.z * m.y;
-                acc[3][0] += a0.w * m.x; acc[3][1] += a0.w * m.y;
-                acc[4][0] += a1.x * m.x; acc[4][1] += a1.x * m.y;
-                acc[5][0] += a1.y * m.x; acc[5][1] += a1.y * m.y;
-                acc[6][0] += a1.z * m.x; acc[6][1] += a1.z * m.y;
-                acc[7][0] += a1.w * m.x; acc[7][1] += a1.w * m.y;
+        for (int k = 0; k < CT_MAXI; k++) {
+            if (k < nit) {
+                const float4* ap = reinterpret_cast<const float4*>(op + bofs[k]);
+                for (int c = itm[k].y; c < itm[k].z; c++, ap += 2) {
+                    const float4 a0 = __ldg(ap), a1 = __ldg(ap + 1);
+                    const float2 m = *reinterpret_cast<const float2*>(&Ms[c * T + 2 * lane]);
+                    acc[k][0][0] += a0.x * m.x; acc[k][0][1] += a0.x * m.y;
+                    acc[k][1][0] += a0.y * m.x; acc[k][1][1] += a0.y * m.y;
+                    acc[k][2][0] += a0.z * m.x; acc[k][2][1] += a0.z * m.y;
+                    acc[k][3][0] += a0.w * m.x; acc[k][3][1] += a0.w * m.y;
+                    acc[k][4][0] += a1.x * m.x; acc[k][4][1] += a1.x * m.y;
+                    acc[k][5][0] += a1.y * m.x; acc[k][5][1] += a1.y * m.y;
+                    acc[k][6][0] += a1.z * m.x; acc[k][6][1] += a1.z * m.y;
+                    acc[k][7][0] += a1.w * m.x; acc[k][7][1] += a1.w * m.y;
+                }
             }
+        }
+    }
+    // fixed-order reduction of the warps' partial sums (pieces of one row block
+    // may sit in different warps): warp 0 adds first, warp 7 last
+    for (int w = 0; w < CT_WARPS; w++) {
+        __syncthreads();
+        if (warp == w) {
 #pragma unroll
-            for (int i = 0; i < 8; i++) {
-                const int r = 8 * w.x + i;
-                if (r < R) {
-                    atomicAdd(&Ls[r * LT + 2 * lane], acc[i][0]);
-                    atomicAdd(&Ls[r * LT + 2 * lane + 1], acc[i][1]);
+            for (int k = 0; k < CT_MAXI; k++) {
+                if (k < nit) {
+#pragma unroll
+                    for (int i = 0; i < 8; i++) {
+                        const int r = 8 * itm[k].x + i;
+                        if (r < R) {
+                            Ls[r * LT + 2 * lane] += acc[k][i][0];
+                            Ls[r * LT + 2 * lane + 1] += acc[k][i][1];
+                        }
+                    }
                 }
             }
         }
     }
     __syncthreads();
     float* dst = a.dst_lvl[task.level];
-    for (int idx = tid; idx < R * T; idx += blockDim.x) {
-        const int r = idx % R, t = idx / R;
+    const int nr = task.r1 - task.r0;
+    for (int idx = tid; idx < nr * T; idx += blockDim.x) {
+        const int r = task.r0 + idx % nr, t = idx / nr;
         const int row = trow[t];
         if (row < 0) continue;
         const float v = Ls[r * LT + t];
@@ -653,16 +691,59 @@ void launch_contract(const ContractArgs& a, int ntasks, cudaStream_t s)
 
 // ------------------------------------------------------------------ root (FP64)
 
-// M~_0 = sum_o A_o M~_1[o]: one CTA per (child, 32-row chunk), FP64 dot products.
-__global__ void k_root_m2m(RootArgs a)
+// M~_0 = sum_o A_o M~_1[o] in FP64.  A CTA owns 8 output rows; its 256 threads
+// are (child o, row, quarter of the columns), reduced in a fixed order.  The
+// degree-0 and degree-1 moments (total charge and dipole about the box centre)
+// are then replaced by their exact FP64 sums over the bodies, which is what the
+// reference's FP64 P2M/M2M produces: the FP32 upward pass would otherwise leave
+// a monopole residual of ~1e-7 of sum|q| that the periodic lattice operator
+// (about 81 periods wide) turns into a constant shift of every potential.
+__global__ void __launch_bounds__(256) k_root_m2m(RootArgs a)
 {
-    const int o = blockIdx.x, r = blockIdx.y * 32 + threadIdx.x;
-    if (r >= a.R) return;
-    const double* A = a.m2m + ((size_t)o * a.R + r) * a.R;
-    const float* m = a.M1 + (size_t)o * a.Rpad;
+    __shared__ double part[8][8][4];
+    const int tid = threadIdx.x, p = tid & 3, rl = (tid >> 2) & 7, o = tid >> 5;
+    const int r = blockIdx.x * 8 + rl;
+    const int qc = (a.R + 3) / 4;
     double t = 0;
-    for (int c = 0; c < a.R; c++) t += A[c] * (double)m[c];
-    atomicAdd(&a.M0[r], t);
+    if (r < a.R) {
+        const double* A = a.m2m + ((size_t)o * a.R + r) * a.R;
+        const float* m = a.M1 + (size_t)o * a.Rpad;
+        for (int c = p * qc; c < min(a.R, (p + 1) * qc); c++) t += A[c] * (double)m[c];
+    }
+    part[o][rl][p] = t;
+    __syncthreads();
+    if (tid < 8) {
+        const int rr = blockIdx.x * 8 + tid;
+        if (rr < a.R) {
+            double s = 0;
+            for (int oo = 0; oo < 8; oo++)
+                for (int pp = 0; pp < 4; pp++) s += part[oo][tid][pp];
+            if (rr < 4) {
+                const double Q = a.sums[3], L = a.sc->box_len, c = 0.5 * L;
+                if (rr == 0) s = Q;
+                else if (rr == 1) s = -(a.sums[2] - Q * c) / L;
+                else if (rr == 2) s = (a.sums[0] - Q * c) / (2.0 * L);
+                else s = -(a.sums[1] - Q * c) / (2.0 * L);
+            }
+            a.M0[rr] = s;
+        }
+    }
+}
+
+// Fixed-order sum of per-block partials: out[j] = sum_b part[b*width + j].
+__global__ void k_sum_partials(const double* part, int nblocks, int width, double* out)
+{
+    const int j = threadIdx.x;
+    if (j >= width) return;
+    double s = 0;
+    for (int b = 0; b < nblocks; b++) s += part[(size_t)b * width + j];
+    out[j] = s;
+}
+
+void launch_sum_partials(const double* part, int nblocks, int width, double* out, cudaStream_t s)
+{
+    COUNT_LAUNCH();
+    k_sum_partials<<<1, 32, 0, s>>>(part, nblocks, width, out);
 }
 
 // L~_0 = A_lattice M~_0 (images >= 2), and the FP32 copy of M~_0.
@@ -693,7 +774,7 @@ __global__ void k_root_l2l(RootArgs a)
 void launch_root_m2m(const RootArgs& a, cudaStream_t s)
 {
     COUNT_LAUNCH();
-    k_root_m2m<<<dim3(8, (a.R + 31) / 32), 32, 0, s>>>(a);
+    k_root_m2m<<<(a.R + 7) / 8, 256, 0, s>>>(a);
 }
 void launch_root_lattice(const RootArgs& a, cudaStream_t s)
 {
@@ -741,15 +822,13 @@ __global__ void __launch_bounds__(256) k_finalize(FinalArgs a)
     if (threadIdx.x == 0) {
         double t = 0;
         for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w];
-        atomicAdd(a.energy, t);
+        a.partials[blockIdx.x] = t;
     }
 }
 
 void launch_finalize(const FinalArgs& a, cudaStream_t s)
 {
-    int blocks = (a.n + 255) / 256;
-    if (blocks > 4 * 152) blocks = 4 * 152;
-    if (blocks < 1) blocks = 1;
+    int blocks = final_blocks(a.n);
     COUNT_LAUNCH();
     k_finalize<<<blocks, 256, 0, s>>>(a);
 }

@@ -26,6 +26,8 @@ struct CTask {
     int q0;
     int ntgt;     // targets in this tile (<= tile size)
     int e_begin, e_end;
+    int group;    // row group (work-item set) of this CTA
+    int r0, r1;   // output rows written by this CTA
 };
 
 struct BlockInfo {
@@ -34,6 +36,7 @@ struct BlockInfo {
 
 constexpr int CT_TILE = 64;   // targets per contraction CTA
 constexpr int CT_WARPS = 8;
+constexpr int CT_MAXI = 6;    // work items per warp (register accumulators)
 
 struct ContractArgs {
     const float* ops;
@@ -57,6 +60,7 @@ struct StepConst {
     float inv_h;                         // 2^D / L
     float pad_;
     double coef;                         // 4 pi / (3 V), dipole correction
+    double box_len;                      // period L (nm)
     float thresh[3][(1 << MAX_DEPTH) + 1];  // leaf boundaries rounded down to float (T[0] = -inf)
     float2 centre[3][1 << MAX_DEPTH];   // leaf centres as hi + lo floats
 };
@@ -69,9 +73,14 @@ struct TreeArgs {
     uint32_t* code;         // N leaf codes (input order)
     float4* uq;             // N scaled coords + charge (input order)
     int* counts;            // 8^D
-    double* sums;           // [0..2] dipole, [3] total charge
+    double* partials;       // per block: dipole (3) and total charge, FP64
     int* flags;             // [0] non-finite input seen
 };
+constexpr int TREE_MAX_BLOCKS = 4 * 152;
+constexpr int FINAL_MAX_BLOCKS = 4 * 152;
+void launch_sum_partials(const double* part, int nblocks, int width, double* out, cudaStream_t s);
+int tree_blocks(int n);
+int final_blocks(int n);
 
 extern std::atomic<long> g_kernel_launches;
 
@@ -97,6 +106,8 @@ struct RootArgs {
     double* L0;             // root local (FP64)
     float* M0f;             // FP32 copy of the root multipole (level-0 row)
     float* L1;              // level-1 locals (8 rows)
+    const double* sums;     // dipole (3) and total charge of the bodies, FP64
+    const StepConst* sc;
     int images;
 };
 void launch_root_m2m(const RootArgs& a, cudaStream_t s);
@@ -113,7 +124,7 @@ struct FinalArgs {
     const double* sums;      // dipole + total charge
     float* forces;           // 3N input order
     float* pots;             // N input order
-    double* energy;          // accumulated 0.5 * sum q * pot
+    double* partials;        // per block: 0.5 * sum q * pot (FP64)
 };
 void launch_finalize(const FinalArgs& a, cudaStream_t s);
 

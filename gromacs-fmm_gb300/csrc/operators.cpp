@@ -407,37 +407,64 @@ void pack_operator(const PackPlan& pl, const double* A, float* out)
             }
 }
 
-void make_work_items(const PackPlan& pl, int n_warps, std::vector<WorkItem>& items, std::vector<int>& warp_begin)
+// Splits the row blocks into 'groups' contiguous row ranges of about equal work
+// (one CTA per group and target tile), then, inside each group, cuts blocks into
+// column pieces no larger than the per-warp share and assigns the pieces to warps
+// longest-first, at most max_items per warp.  Returns false if that cap cannot
+// be met.
+bool make_work_items(const PackPlan& pl, int n_warps, int groups, int max_items, WorkPartition& out)
 {
-    items.clear();
-    warp_begin.assign(n_warps + 1, 0);
+    out = WorkPartition();
+    out.groups = groups;
     long total = 0;
     for (int b = 0; b < pl.nblk; b++) total += pl.c1[b] - pl.c0[b];
-    long per = (total + n_warps - 1) / n_warps;
-    int w = 0;
-    long load = 0;
-    for (int b = 0; b < pl.nblk; b++) {
-        int c = pl.c0[b];
-        while (c < pl.c1[b]) {
-            long room = per - load;
-            if (room <= 0 && w < n_warps - 1) {
-                w++;
-                warp_begin[w] = (int)items.size();
-                load = 0;
-                room = per;
-            }
-            int take = (int)std::min<long>(room > 0 ? room : (pl.c1[b] - c), pl.c1[b] - c);
-            WorkItem it;
-            it.blk = (int16_t)b;
-            it.ca = (int16_t)c;
-            it.cb = (int16_t)(c + take);
-            it.pad = 0;
-            items.push_back(it);
-            c += take;
-            load += take;
+    // contiguous block ranges per group
+    std::vector<int> gb(groups + 1, pl.nblk);
+    gb[0] = 0;
+    {
+        long acc = 0;
+        int g = 1;
+        for (int b = 0; b < pl.nblk && g < groups; b++) {
+            acc += pl.c1[b] - pl.c0[b];
+            if (acc * groups >= total * g) gb[g++] = b + 1;
         }
+        for (; g < groups; g++) gb[g] = pl.nblk;
     }
-    for (int k = w + 1; k <= n_warps; k++) warp_begin[k] = (int)items.size();
+    for (int g = 0; g < groups; g++) {
+        out.row0.push_back(8 * gb[g]);
+        out.row1.push_back(std::min(pl.R, 8 * gb[g + 1]));
+        long gw = 0;
+        for (int b = gb[g]; b < gb[g + 1]; b++) gw += pl.c1[b] - pl.c0[b];
+        long share = std::max<long>(1, (gw + n_warps - 1) / n_warps);
+        std::vector<WorkItem> pieces;
+        for (int b = gb[g]; b < gb[g + 1]; b++)
+            for (int c = pl.c0[b]; c < pl.c1[b]; c += (int)share) {
+                WorkItem it;
+                it.blk = (int16_t)b;
+                it.ca = (int16_t)c;
+                it.cb = (int16_t)std::min<long>(pl.c1[b], c + share);
+                it.pad = 0;
+                pieces.push_back(it);
+            }
+        std::stable_sort(pieces.begin(), pieces.end(),
+                         [](const WorkItem& x, const WorkItem& y) { return (x.cb - x.ca) > (y.cb - y.ca); });
+        std::vector<std::vector<WorkItem>> per(n_warps);
+        std::vector<long> load(n_warps, 0);
+        for (const WorkItem& it : pieces) {
+            int best = -1;
+            for (int w = 0; w < n_warps; w++)
+                if ((int)per[w].size() < max_items && (best < 0 || load[w] < load[best])) best = w;
+            if (best < 0) return false;
+            per[best].push_back(it);
+            load[best] += it.cb - it.ca;
+        }
+        for (int w = 0; w < n_warps; w++) {
+            out.warp_begin.push_back((int)out.items.size());
+            for (const WorkItem& it : per[w]) out.items.push_back(it);
+        }
+        out.warp_begin.push_back((int)out.items.size());
+    }
+    return true;
 }
 
 // ------------------------------------------------------------------ reference lists
@@ -538,6 +565,102 @@ void emit_lists(const Stencils& st, int D, int images, RefLists& p2p, RefLists& 
                 p2p.off.push_back(x.ox);
                 p2p.off.push_back(x.oy);
                 p2p.off.push_back(x.oz);
+            }
+        }
+    }
+}
+
+}  // namespace gbfmm
+
+// ------------------------------------------------------------------ tensor-core M2L plan
+
+#include "m2l_tc.h"
+
+namespace gbfmm {
+
+static inline int round16(int x) { return (x + 15) & ~15; }
+
+// Degree chunks by dynamic programming: minimise sum(N*K) over contiguous degree
+// ranges, with N = rows padded to 16 (<= 256) and K = (P-j0+1)^2 padded to 16.
+TcPlan make_tc_plan(int P)
+{
+    TcPlan pl;
+    pl.P = P;
+    const int INF = 1 << 30;
+    std::vector<int> best(P + 2, INF), nxt(P + 2, -1);
+    best[P + 1] = 0;
+    for (int j0 = P; j0 >= 0; j0--) {
+        for (int j1 = j0; j1 <= P; j1++) {
+            int rows = (j1 + 1) * (j1 + 1) - j0 * j0;
+            int N = round16(rows);
+            if (N > 256) break;
+            int K = round16((P - j0 + 1) * (P - j0 + 1));
+            int cost = N * K + 256;  // small per-chunk overhead favours fewer MMAs
+            if (best[j1 + 1] < INF && cost + best[j1 + 1] < best[j0]) {
+                best[j0] = cost + best[j1 + 1];
+                nxt[j0] = j1 + 1;
+            }
+        }
+    }
+    int j0 = 0, col = 0, img = 0;
+    while (j0 <= P) {
+        int j1 = nxt[j0] - 1;
+        int c = pl.nchunk++;
+        pl.row0[c] = j0 * j0;
+        pl.rows[c] = (j1 + 1) * (j1 + 1) - j0 * j0;
+        pl.n[c] = round16(pl.rows[c]);
+        pl.k[c] = round16((P - j0 + 1) * (P - j0 + 1));
+        pl.col[c] = col;
+        pl.img[c] = img;
+        col += pl.n[c];
+        img += pl.n[c] * ((pl.k[c] + 63) / 64) * 128;
+        j0 = j1 + 1;
+    }
+    pl.img_bytes = img;
+    pl.k_atoms = (pl.k[0] + 63) / 64;
+    int t = 32;
+    while (t < col) t <<= 1;
+    pl.tmem_cols = t;
+    return pl;
+}
+
+static uint16_t f2bf(float f)
+{
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    if ((u & 0x7fffffffu) > 0x7f800000u) return 0x7fc0;
+    u += 0x7fffu + ((u >> 16) & 1u);
+    return (uint16_t)(u >> 16);
+}
+
+static float bf2f(uint16_t b)
+{
+    uint32_t u = (uint32_t)b << 16;
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+}
+
+// Operator chunk images in the canonical K-major 128-byte-swizzled shared-memory
+// layout: 64-element K atoms of N rows x 128 B; inside each 8-row group the
+// 16-byte column chunk c of row r sits at chunk position c ^ (r & 7).
+void append_tc_image(const TcPlan& pl, int R, const double* A, std::vector<uint8_t>& out)
+{
+    size_t base = out.size();
+    out.resize(base + 2 * (size_t)pl.img_bytes, 0);
+    for (int c = 0; c < pl.nchunk; c++) {
+        const int N = pl.n[c], atoms = (pl.k[c] + 63) / 64;
+        for (int nl = 0; nl < N; nl++) {
+            const int r = pl.row0[c] + nl;
+            for (int k = 0; k < atoms * 64; k++) {
+                double x = (nl < pl.rows[c] && k < pl.k[c] && k < R) ? A[(size_t)r * R + k] : 0.0;
+                uint16_t hi = f2bf((float)x);
+                uint16_t lo = f2bf((float)(x - (double)bf2f(hi)));
+                const int a = k / 64, kk = k % 64;
+                size_t off = (size_t)pl.img[c] + (size_t)a * N * 128 + (size_t)nl * 128 +
+                             (size_t)(((kk / 8) ^ (nl % 8)) * 16) + (size_t)(kk % 8) * 2;
+                std::memcpy(&out[base + off], &hi, 2);
+                std::memcpy(&out[base + pl.img_bytes + off], &lo, 2);
             }
         }
     }

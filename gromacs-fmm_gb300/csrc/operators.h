@@ -65,7 +65,13 @@ void pack_operator(const PackPlan& plan, const double* A, float* out);
 struct WorkItem {
     int16_t blk, ca, cb, pad;
 };
-void make_work_items(const PackPlan& plan, int n_warps, std::vector<WorkItem>& items, std::vector<int>& warp_begin);
+struct WorkPartition {
+    int groups = 0;
+    std::vector<WorkItem> items;
+    std::vector<int> warp_begin;  // groups x (n_warps + 1)
+    std::vector<int> row0, row1;  // output rows of each group
+};
+bool make_work_items(const PackPlan& plan, int n_warps, int groups, int max_items, WorkPartition& out);
 
 // Reference-ordered interaction lists for a complete tree of depth D.
 struct RefLists {

@@ -20,6 +20,7 @@
 #include "../../include/gbfmm.h"
 #include "common.cuh"
 #include "kernels.h"
+#include "m2l_tc.h"
 #include "operators.h"
 
 using namespace gbfmm;
@@ -56,9 +57,15 @@ struct OpTables {
     int off_m2m[8], off_l2l[8];
     std::vector<int> off_cls;            // per M2L class
     std::vector<double> root_m2m, root_l2l, lattice;  // dense FP64 for the root
-    std::vector<WorkItem> items[3];
-    std::vector<int> warp_begin[3];
+    WorkPartition part[3];
+    // tensor-core M2L (orders <= TC_MAX_ORDER): chunk plan and class images
+    TcPlan tc;
+    std::vector<uint8_t> tc_img;
 };
+
+// Row groups per contraction type: M2L has enough target tiles on its own;
+// M2M and L2L split the output rows so that small levels still fill the GPU.
+static const int k_groups[3] = {1, 4, 4};
 
 std::mutex g_tab_mu;
 std::vector<OpTables*> g_tabs;
@@ -77,7 +84,8 @@ const OpTables* get_tables(int P, int images)
     t->st = build_stencils(0.4);
     for (int k = 0; k < 3; k++) {
         t->plan[k] = make_pack_plan(P, (OpType)k);
-        make_work_items(t->plan[k], CT_WARPS, t->items[k], t->warp_begin[k]);
+        int g = k_groups[k];
+        while (!make_work_items(t->plan[k], CT_WARPS, g, CT_MAXI, t->part[k])) g++;
     }
     std::vector<double> A((size_t)R * R);
     auto append = [&](const PackPlan& pl) {
@@ -97,9 +105,11 @@ const OpTables* get_tables(int P, int images)
         t->off_l2l[o] = append(t->plan[OP_L2L]);
     }
     t->off_cls.resize(t->st.classes.size());
+    if (P <= TC_MAX_ORDER) t->tc = make_tc_plan(P);
     for (size_t c = 0; c < t->st.classes.size(); c++) {
         scaled_m2l(P, t->st.classes[c], A.data());
         t->off_cls[c] = append(t->plan[OP_M2L]);
+        if (P <= TC_MAX_ORDER) append_tc_image(t->tc, R, A.data(), t->tc_img);
     }
     t->lattice.resize((size_t)R * R);
     lattice_operator(P, images, t->lattice.data());
@@ -146,7 +156,17 @@ struct gbfmm_handle {
     float *d_forces = nullptr, *d_pots = nullptr;
     double* d_energy = nullptr;
     double* d_sums = nullptr;
+    double* d_partials = nullptr;
     int* d_flags = nullptr;
+    // tensor-core M2L
+    bool tc = false;
+    __nv_bfloat16 *d_mh = nullptr, *d_ml = nullptr;
+    uint8_t* d_img = nullptr;
+    long total_rows = 0;
+    long row_off[9] = {};
+    CEntry* d_tc_entries = nullptr;
+    CTask* d_tc_tasks = nullptr;
+    int tc_ntask = 0, tc_split = 1;
     StepConst* d_sc = nullptr;
     StepConst* h_sc = nullptr;  // pinned
     int* h_flags = nullptr;     // pinned
@@ -260,6 +280,16 @@ static int layout(gbfmm_handle* h, Arena& a)
     h->lev_floats = lev;
     h->d_M = a.take<float>(lev);
     h->d_L = a.take<float>(lev);
+    h->total_rows = 0;
+    for (int k = 0; k <= D; k++) {
+        h->row_off[k] = h->total_rows;
+        h->total_rows += 1L << (3 * k);
+    }
+    if (h->tc) {
+        h->d_mh = a.take<__nv_bfloat16>((size_t)h->total_rows * TC_KMAX);
+        h->d_ml = a.take<__nv_bfloat16>((size_t)h->total_rows * TC_KMAX);
+        h->d_img = a.take<uint8_t>(t->tc_img.size());
+    }
     h->d_M0 = a.take<double>(R);
     h->d_L0 = a.take<double>(R);
     h->d_ops = a.take<float>(t->packed.size());
@@ -268,14 +298,15 @@ static int layout(gbfmm_handle* h, Arena& a)
     h->d_lattice = a.take<double>(t->lattice.size());
     h->d_p2p_st = a.take<int>(t->st.p2p.size());
     for (int k = 0; k < 3; k++) {
-        h->d_items[k] = a.take<int4>(t->items[k].size() + 1);
-        h->d_wb[k] = a.take<int>(CT_WARPS + 1);
+        h->d_items[k] = a.take<int4>(t->part[k].items.size() + 1);
+        h->d_wb[k] = a.take<int>(t->part[k].warp_begin.size());
         h->d_blocks[k] = a.take<BlockInfo>(t->plan[k].nblk);
     }
     h->d_forces = a.take<float>(3 * (size_t)n);
     h->d_pots = a.take<float>(n);
     h->d_energy = a.take<double>(1);
     h->d_sums = a.take<double>(4);
+    h->d_partials = a.take<double>(4 * std::max(TREE_MAX_BLOCKS, FINAL_MAX_BLOCKS));
     h->d_flags = a.take<int>(4);
     h->d_sc = a.take<StepConst>(1);
     return 0;
@@ -331,12 +362,15 @@ static int build_tasks(gbfmm_handle* h)
     for (int k = D - 1; k >= 1; k--) {
         h->m2m_task0[k] = (int)tasks.size();
         long ncell = 1L << (3 * k);
-        for (long q0 = 0; q0 < ncell; q0 += CT_TILE) {
-            CTask c;
-            c.level = k; c.octant = -1; c.q0 = (int)q0; c.ntgt = (int)std::min<long>(CT_TILE, ncell - q0);
-            c.e_begin = e_m2m; c.e_end = e_m2m + 8;
-            tasks.push_back(c);
-        }
+        const WorkPartition& wp = t->part[OP_M2M];
+        for (long q0 = 0; q0 < ncell; q0 += CT_TILE)
+            for (int g = 0; g < wp.groups; g++) {
+                CTask c;
+                c.level = k; c.octant = -1; c.q0 = (int)q0; c.ntgt = (int)std::min<long>(CT_TILE, ncell - q0);
+                c.e_begin = e_m2m; c.e_end = e_m2m + 8;
+                c.group = g; c.r0 = wp.row0[g]; c.r1 = wp.row1[g];
+                tasks.push_back(c);
+            }
         h->m2m_ntask[k] = (int)tasks.size() - h->m2m_task0[k];
     }
     // M2L tasks
@@ -357,12 +391,15 @@ static int build_tasks(gbfmm_handle* h)
             int eb = e_m2l[lt][s], ne = (int)t->st.m2l[lt][s].size();
             for (long q0 = 0; q0 < npar; q0 += CT_TILE) {
                 int ch = (ne + split - 1) / split;
-                for (int e0 = 0; e0 < ne; e0 += ch) {
-                    CTask c;
-                    c.level = k; c.octant = s; c.q0 = (int)q0; c.ntgt = (int)std::min<long>(CT_TILE, npar - q0);
-                    c.e_begin = eb + e0; c.e_end = eb + std::min(ne, e0 + ch);
-                    tasks.push_back(c);
-                }
+                const WorkPartition& wp = t->part[OP_M2L];
+                for (int e0 = 0; e0 < ne; e0 += ch)
+                    for (int g = 0; g < wp.groups; g++) {
+                        CTask c;
+                        c.level = k; c.octant = s; c.q0 = (int)q0; c.ntgt = (int)std::min<long>(CT_TILE, npar - q0);
+                        c.e_begin = eb + e0; c.e_end = eb + std::min(ne, e0 + ch);
+                        c.group = g; c.r0 = wp.row0[g]; c.r1 = wp.row1[g];
+                        tasks.push_back(c);
+                    }
             }
         }
     }
@@ -373,21 +410,97 @@ static int build_tasks(gbfmm_handle* h)
         h->l2l_task0[k] = (int)tasks.size();
         long npar = 1L << (3 * (k - 1));
         for (int s = 0; s < 8; s++)
-            for (long q0 = 0; q0 < npar; q0 += CT_TILE) {
-                CTask c;
-                c.level = k; c.octant = s; c.q0 = (int)q0; c.ntgt = (int)std::min<long>(CT_TILE, npar - q0);
-                c.e_begin = e_l2l + s; c.e_end = e_l2l + s + 1;
-                tasks.push_back(c);
-            }
+            for (long q0 = 0; q0 < npar; q0 += CT_TILE)
+                for (int g = 0; g < t->part[OP_L2L].groups; g++) {
+                    CTask c;
+                    c.level = k; c.octant = s; c.q0 = (int)q0; c.ntgt = (int)std::min<long>(CT_TILE, npar - q0);
+                    c.e_begin = e_l2l + s; c.e_end = e_l2l + s + 1;
+                    c.group = g; c.r0 = t->part[OP_L2L].row0[g]; c.r1 = t->part[OP_L2L].row1[g];
+                    tasks.push_back(c);
+                }
         h->l2l_ntask[k] = (int)tasks.size() - h->l2l_task0[k];
+    }
+    // tensor-core M2L: entries carry the class index, tiles of TC_TILE targets
+    int tc_task0 = (int)tasks.size();
+    if (h->tc) {
+        int e_tc[2][8];
+        for (int lt = 0; lt < 2; lt++)
+            for (int s = 0; s < 8; s++) {
+                e_tc[lt][s] = (int)ent.size();
+                for (const StencilEntry& se : t->st.m2l[lt][s]) {
+                    CEntry e;
+                    e.dx = (int8_t)se.d[0]; e.dy = (int8_t)se.d[1]; e.dz = (int8_t)se.d[2];
+                    e.mode = (int8_t)se.mode;
+                    e.op = se.cls;
+                    ent.push_back(e);
+                }
+            }
+        long tiles = 0;
+        for (int k = 1; k <= D; k++) tiles += 8 * std::max<long>(1, ((1L << (3 * (k - 1))) + TC_TILE - 1) / TC_TILE);
+        int sp = h->prm.m2l_split > 0 ? h->prm.m2l_split : 1;
+        if (h->prm.m2l_split <= 0)
+            while (tiles * sp < 152 && sp < 8) sp *= 2;
+        if (h->prm.flags & GBFMM_FLAG_DETERMINISTIC) sp = 1;
+        h->tc_split = sp;
+        for (int k = 1; k <= D; k++) {
+            const int lt = k == 1 ? 0 : 1;
+            long npar = 1L << (3 * (k - 1));
+            for (int s = 0; s < 8; s++) {
+                int eb = e_tc[lt][s], ne = (int)t->st.m2l[lt][s].size();
+                int ch = (ne + sp - 1) / sp;
+                for (long q0 = 0; q0 < npar; q0 += TC_TILE)
+                    for (int e0 = 0; e0 < ne; e0 += ch) {
+                        CTask c;
+                        c.level = k; c.octant = s; c.q0 = (int)q0; c.ntgt = (int)std::min<long>(TC_TILE, npar - q0);
+                        c.e_begin = eb + e0; c.e_end = eb + std::min(ne, e0 + ch);
+                        c.group = 0; c.r0 = 0; c.r1 = h->R;
+                        tasks.push_back(c);
+                    }
+            }
+        }
+        h->tc_ntask = (int)tasks.size() - tc_task0;
     }
     void* p = nullptr;
     CK(cudaMalloc(&p, sizeof(CEntry) * ent.size() + sizeof(CTask) * tasks.size() + 512));
     h->d_entries = (CEntry*)p;
     h->d_tasks = (CTask*)((char*)p + ((sizeof(CEntry) * ent.size() + 255) & ~(size_t)255));
+    h->d_tc_tasks = h->d_tasks + tc_task0;
     CK(cudaMemcpy(h->d_entries, ent.data(), sizeof(CEntry) * ent.size(), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(h->d_tasks, tasks.data(), sizeof(CTask) * tasks.size(), cudaMemcpyHostToDevice));
     return GBFMM_OK;
+}
+
+static TcArgs tc_args(gbfmm_handle* h)
+{
+    TcArgs a;
+    std::memset(&a, 0, sizeof(a));
+    const TcPlan& pl = h->tab->tc;
+    for (int k = 0; k <= h->D; k++) {
+        a.mh[k] = h->d_mh + (size_t)h->row_off[k] * TC_KMAX;
+        a.ml[k] = h->d_ml + (size_t)h->row_off[k] * TC_KMAX;
+        a.dst_lvl[k] = h->Llev[k];
+    }
+    a.bimg = h->d_img;
+    a.entries = h->d_entries;
+    a.tasks = h->d_tc_tasks;
+    a.err = h->d_flags + 1;
+    a.Rpad = h->Rpad;
+    a.k_atoms = pl.k_atoms;
+    a.img_bytes = pl.img_bytes;
+    a.tmem_cols = pl.tmem_cols;
+    a.nchunk = pl.nchunk;
+    a.nprod = h->prm.precision == GBFMM_PREC_BF16X1 ? 1 : 3;
+    a.periodic = h->periodic ? 1 : 0;
+    a.atomic = h->tc_split > 1 ? 1 : 0;
+    for (int c = 0; c < pl.nchunk; c++) {
+        a.chunk_n[c] = pl.n[c];
+        a.chunk_k[c] = pl.k[c];
+        a.chunk_col[c] = pl.col[c];
+        a.chunk_row0[c] = pl.row0[c];
+        a.chunk_rows[c] = pl.rows[c];
+        a.chunk_img[c] = pl.img[c];
+    }
+    return a;
 }
 
 static ContractArgs contract_args(gbfmm_handle* h, int optype, int write_mode, bool src_is_L, int task0)
@@ -427,7 +540,6 @@ static void enqueue_step(gbfmm_handle* h)
     cudaMemsetAsync(h->d_counts, 0, sizeof(int) * (h->nleaf + 1), s);
     cudaMemsetAsync(h->d_sums, 0, sizeof(double) * 4, s);
     cudaMemsetAsync(h->d_energy, 0, sizeof(double), s);
-    cudaMemsetAsync(h->d_M0, 0, sizeof(double) * h->R, s);
     cudaMemsetAsync(h->d_L, 0, sizeof(float) * h->lev_floats, s);
     cudaMemsetAsync(h->d_far, 0, sizeof(float4) * std::max(n, 1), s);
     if (n > 0) {
@@ -439,9 +551,10 @@ static void enqueue_step(gbfmm_handle* h)
         ta.code = h->d_code;
         ta.uq = h->d_uq;
         ta.counts = h->d_counts;
-        ta.sums = h->d_sums;
+        ta.partials = h->d_partials;
         ta.flags = h->d_flags;
         launch_tree_keys(ta, s);
+        launch_sum_partials(h->d_partials, tree_blocks(n), 4, h->d_sums, s);
     }
     launch_exclusive_scan(h->d_counts, h->d_off, h->nleaf, h->d_scan, s);
     cudaMemcpyAsync(h->d_cursor, h->d_off, sizeof(int) * h->nleaf, cudaMemcpyDeviceToDevice, s);
@@ -466,11 +579,16 @@ static void enqueue_step(gbfmm_handle* h)
     ra.L0 = h->d_L0;
     ra.M0f = h->Mlev[0];
     ra.L1 = h->Llev[1];
+    ra.sums = h->d_sums;
+    ra.sc = h->d_sc;
     ra.images = h->prm.images;
     launch_root_m2m(ra, s);
     launch_root_lattice(ra, s);
     mark(h, 4);
-    {
+    if (h->tc) {
+        launch_split_bf16(h->d_M, h->Rpad, h->R, h->total_rows, h->d_mh, h->d_ml, s);
+        launch_m2l_tc(tc_args(h), h->tc_ntask, s);
+    } else {
         ContractArgs a = contract_args(h, OP_M2L, 2, false, h->m2l_task0);
         launch_contract(a, h->m2l_ntask, s);
     }
@@ -496,8 +614,9 @@ static void enqueue_step(gbfmm_handle* h)
         fa.sums = h->d_sums;
         fa.forces = h->d_forces;
         fa.pots = h->d_pots;
-        fa.energy = h->d_energy;
+        fa.partials = h->d_partials;
         launch_finalize(fa, s);
+        launch_sum_partials(h->d_partials, final_blocks(n), 1, h->d_energy, s);
     }
     mark(h, 9);
     h->step_launches = (int)(g_kernel_launches.load() - launches0);
@@ -520,8 +639,8 @@ extern "C" int gbfmm_create(const gbfmm_params* prm, int natoms, gbfmm_handle** 
     if (p.rega != 0.0) return fail(GBFMM_ERR_UNSUPPORTED, "rega > 0 (regularised FMM) is not built");
     if (p.precision != GBFMM_PREC_FP32 && p.precision != GBFMM_PREC_BF16X3 && p.precision != GBFMM_PREC_BF16X1)
         return fail(GBFMM_ERR_ARG, "unknown precision %d", p.precision);
-    if (p.precision != GBFMM_PREC_FP32)
-        return fail(GBFMM_ERR_UNSUPPORTED, "tensor-core M2L is not built in this library");
+    if (p.precision != GBFMM_PREC_FP32 && p.order > TC_MAX_ORDER)
+        return fail(GBFMM_ERR_UNSUPPORTED, "tensor-core M2L supports orders <= %d (got %d)", TC_MAX_ORDER, p.order);
     if (p.m2l_tile != 0 && p.m2l_tile != CT_TILE) return fail(GBFMM_ERR_ARG, "m2l_tile must be 0 or %d", CT_TILE);
     if (p.m2l_split < 0 || p.m2l_split > 16) return fail(GBFMM_ERR_ARG, "m2l_split outside [0,16]");
     int dev = 0;
@@ -538,6 +657,7 @@ extern "C" int gbfmm_create(const gbfmm_params* prm, int natoms, gbfmm_handle** 
     h->D = p.max_depth;
     h->nleaf = 1 << (3 * h->D);
     h->periodic = p.images > 0;
+    h->tc = p.precision != GBFMM_PREC_FP32;
     h->tab = get_tables(h->P, p.images);
     h->h_q.assign(natoms, 0.0f);
     int rc = GBFMM_OK;
@@ -566,14 +686,15 @@ extern "C" int gbfmm_create(const gbfmm_params* prm, int natoms, gbfmm_handle** 
     up(h->d_root_m2m, t->root_m2m.data(), sizeof(double) * t->root_m2m.size());
     up(h->d_root_l2l, t->root_l2l.data(), sizeof(double) * t->root_l2l.size());
     up(h->d_lattice, t->lattice.data(), sizeof(double) * t->lattice.size());
+    if (h->tc) up(h->d_img, t->tc_img.data(), t->tc_img.size());
     up(h->d_p2p_st, t->st.p2p.data(), sizeof(int) * t->st.p2p.size());
     h->n_p2p_st = (int)t->st.p2p.size() / 3;
     for (int k = 0; k < 3; k++) {
         std::vector<int4> it;
-        for (const WorkItem& w : t->items[k]) it.push_back(make_int4(w.blk, w.ca, w.cb, 0));
+        for (const WorkItem& w : t->part[k].items) it.push_back(make_int4(w.blk, w.ca, w.cb, 0));
         it.push_back(make_int4(0, 0, 0, 0));
         up(h->d_items[k], it.data(), sizeof(int4) * it.size());
-        up(h->d_wb[k], t->warp_begin[k].data(), sizeof(int) * (CT_WARPS + 1));
+        up(h->d_wb[k], t->part[k].warp_begin.data(), sizeof(int) * t->part[k].warp_begin.size());
         std::vector<BlockInfo> bi(t->plan[k].nblk);
         for (int b = 0; b < t->plan[k].nblk; b++) {
             bi[b].c0 = t->plan[k].c0[b];
@@ -640,6 +761,7 @@ static int set_box(gbfmm_handle* h, const float* box, const float* d_coords)
     sc->coords = d_coords;
     sc->inv_h = (float)(nd / L);
     sc->coef = 4.0 * M_PI / (3.0 * L * L * L);
+    sc->box_len = L;
     const double centre[3] = {(double)box[0] / 2, (double)box[4] / 2, (double)box[8] / 2};
     for (int d = 0; d < 3; d++) {
         // leaf boundaries of the strict '>' descent: the descent around centre c with
@@ -722,6 +844,11 @@ static int fetch(gbfmm_handle* h)
         for (int s = 0; s < 9; s++) cudaEventElapsedTime(&h->stage_ms[s], h->ev[s], h->ev[s + 1]);
     }
     h->results_on_host = true;
+    if (h->h_flags[1]) {
+        CK(cudaMemsetAsync(h->d_flags, 0, sizeof(int) * 4, h->stream));
+        h->have_result = false;
+        return fail(GBFMM_ERR_TIMEOUT, "a bounded device wait in the tensor-core M2L gave up");
+    }
     if (h->h_flags[0]) {
         CK(cudaMemsetAsync(h->d_flags, 0, sizeof(int) * 4, h->stream));
         h->have_result = false;
