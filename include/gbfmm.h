@@ -135,6 +135,27 @@ int gbfmm_get_lists(gbfmm_handle* h, int which, long* count, int* target, int* s
 /* The same lists without a handle (host only): tree depth and image levels. */
 int gbfmm_lists(int max_depth, int images, int which, long* count, int* target, int* source, int* offset3);
 
+/* ---- tree build without allocation ---- */
+
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory at call time (an MD engine whose own pool reserved the GPU's memory at
+ * start-up, or a time-stepping loop that must not call cudaMalloc because it can
+ * synchronise the device): builds the same tree as gbfmm_execute
+ * -- order[i] = input index of the body at sorted position i, leaf_offsets[k] =
+ * first body of leaf k in BFS order, leaf_offsets[8^depth] = natoms -- using
+ * only a fixed static device array for scratch.  Inputs and outputs are device
+ * pointers: coords float[3*natoms], charges float[natoms], order int[natoms],
+ * leaf_offsets int[8^depth + 1]; box float[9] on the host (cubic).
+ * Limits: natoms <= GBFMM_NOALLOC_MAX_ATOMS and depth <= GBFMM_NOALLOC_MAX_DEPTH;
+ * larger inputs return GBFMM_ERR_ARG.  The first call on a device looks up the
+ * array's device address (make it before any stream capture).  All calls share
+ * the scratch: calls that overlap on the GPU race.  Asynchronous on 'stream';
+ * non-finite coordinates are not reported (no host read-back). */
+#define GBFMM_NOALLOC_MAX_ATOMS 65536
+#define GBFMM_NOALLOC_MAX_DEPTH 4
+int gbfmm_tree_build_noalloc(const void* coords, const void* charges, int natoms, const float* box, int max_depth,
+                             void* order, void* leaf_offsets, void* stream);
+
 /* ---- operator tables (host only, for tests) ---- */
 
 /* Fills 'mat' (rows x cols, row-major, real (P+1)^2 representation in scaled
