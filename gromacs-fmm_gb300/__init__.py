@@ -247,6 +247,68 @@ class ZetaFmmSolver:
         return t[:n], s[:n], o[:n]
 
 
+class BatchSolver:
+    """Many independent cubic systems solved together through one CUDA graph
+    (gbfmm_batch_*).  systems: list of (coords (n,3), charges (n,), box edge);
+    orders/depths: one per system."""
+
+    def __init__(self, natoms_list, orders, depths, images=4, precision=PREC_FP32, flags=0):
+        L = lib()
+        vp = ctypes.c_void_p
+        ip = ctypes.POINTER(ctypes.c_int)
+        fp = ctypes.POINTER(ctypes.c_float)
+        dp = ctypes.POINTER(ctypes.c_double)
+        L.gbfmm_batch_create.restype = ctypes.c_int
+        L.gbfmm_batch_create.argtypes = [ctypes.c_int, ip, ip, ip, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                         ctypes.POINTER(vp)]
+        L.gbfmm_batch_execute.restype = ctypes.c_int
+        L.gbfmm_batch_execute.argtypes = [vp, fp, fp, fp, fp, fp, dp]
+        L.gbfmm_batch_execute_device.restype = ctypes.c_int
+        L.gbfmm_batch_execute_device.argtypes = [vp, vp, vp, fp, vp]
+        L.gbfmm_batch_device_outputs.restype = ctypes.c_int
+        L.gbfmm_batch_device_outputs.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp)]
+        L.gbfmm_batch_destroy.restype = ctypes.c_int
+        L.gbfmm_batch_destroy.argtypes = [vp]
+        self.n_sys = len(natoms_list)
+        self.offsets = np.concatenate([[0], np.cumsum(natoms_list)]).astype(np.int32)
+        o = np.ascontiguousarray(orders, dtype=np.int32)
+        d = np.ascontiguousarray(depths, dtype=np.int32)
+        h = ctypes.c_void_p()
+        _check(L.gbfmm_batch_create(self.n_sys, self.offsets.ctypes.data_as(ip), o.ctypes.data_as(ip),
+                                    d.ctypes.data_as(ip), images, precision, flags, ctypes.byref(h)))
+        self._b = h
+
+    def close(self):
+        if getattr(self, "_b", None):
+            lib().gbfmm_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def execute(self, coords, charges, box_edges):
+        """Host arrays (packed in system order); returns forces, potentials, energies."""
+        x = _f32(coords).reshape(-1)
+        q = _f32(charges)
+        b = _f32(box_edges)
+        n = int(self.offsets[-1])
+        f = np.zeros((n, 3), np.float32)
+        p = np.zeros(n, np.float32)
+        e = np.zeros(self.n_sys)
+        _check(lib().gbfmm_batch_execute(self._b, _fp(x), _fp(q), _fp(b), _fp(f), _fp(p),
+                                         e.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        return f, p, e
+
+    def execute_device(self, coords_ptr, charges_ptr, box_edges, stream_ptr=0):
+        b = _f32(box_edges)
+        _check(lib().gbfmm_batch_execute_device(self._b, ctypes.c_void_p(int(coords_ptr)),
+                                                ctypes.c_void_p(int(charges_ptr)), _fp(b),
+                                                ctypes.c_void_p(int(stream_ptr))))
+
+
 def lists(max_depth, images, which):
     """Reference-ordered interaction lists without a handle (host only)."""
     w = 0 if which == "p2p" else 1

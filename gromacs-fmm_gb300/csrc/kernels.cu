@@ -411,11 +411,82 @@ constexpr int P2P_THREADS = 128;
 constexpr int P2P_MAXS = 2048;  // staged source bodies per pass
 constexpr int P2P_MAXT = 128;   // targets per pass
 
+// 1/sqrt(x) by the PTX approximate instruction (relative error below 2^-22.9),
+// denormal inputs flushed to zero.
+__device__ __forceinline__ float rsqrt_approx(float x)
+{
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// K targets per thread (i, i+8, ..., i+8(K-1) of the cluster) against this
+// warp's source steps [sb, se); lane jj takes source 4 st + jj of each step.
+// Pair term as kernel.cu:480-490: phi += q/r, grad += q (x_j - x_i)/r^3,
+// skipped when r = 0 (a body with itself or a coincident body).
+template <int K>
+__device__ __forceinline__ void p2p_sweep(const float4* __restrict__ src, int sb, int se, int jj, const float4 (&xi)[K],
+                                          float (&acc)[K][4])
+{
+#pragma unroll 2
+    for (int st = sb; st < se; st++) {
+        const float4 s = src[4 * st + jj];
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const float dx = xi[k].x - s.x, dy = xi[k].y - s.y, dz = xi[k].z - s.z;
+            const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            const float ri = r2 > 0.f ? rsqrt_approx(r2) : 0.f;
+            const float qr = s.w * ri;
+            acc[k][0] += qr;
+            const float q3 = qr * ri * ri;
+            acc[k][1] = fmaf(-q3, dx, acc[k][1]);
+            acc[k][2] = fmaf(-q3, dy, acc[k][2]);
+            acc[k][3] = fmaf(-q3, dz, acc[k][3]);
+        }
+    }
+}
+
+// One cluster of up to 8K targets starting at c0 (of this pass's ntc).
+template <int K>
+__device__ __forceinline__ void p2p_cluster(const float4* __restrict__ src, const float4* __restrict__ tgt, int c0,
+                                            int ntc, int sb, int se, int lane, float4* part)
+{
+    const int ii = lane >> 2, jj = lane & 3;
+    float4 xi[K];
+    float acc[K][4];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        xi[k] = tgt[min(c0 + ii + 8 * k, ntc - 1)];
+        acc[k][0] = acc[k][1] = acc[k][2] = acc[k][3] = 0.f;
+    }
+    p2p_sweep<K>(src, sb, se, jj, xi, acc);
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        // fixed butterfly over the 4 source lanes of each target
+#pragma unroll
+        for (int o = 1; o < 4; o <<= 1)
+#pragma unroll
+            for (int c = 0; c < 4; c++) acc[k][c] += __shfl_xor_sync(0xffffffffu, acc[k][c], o);
+        const int t = c0 + ii + 8 * k;
+        if (jj == 0 && t < ntc) {
+            float4 pp = part[t];
+            pp.x += acc[k][0];
+            pp.y += acc[k][1];
+            pp.z += acc[k][2];
+            pp.w += acc[k][3];
+            part[t] = pp;
+        }
+    }
+}
+
 // One CTA per target leaf.  The source bodies of the 81 near leaves are staged in
 // shared memory, shifted into the target leaf's frame (scaled units, integer
-// offsets of the stencil, so the periodic shift is exact), then each warp sweeps a
-// quarter of them with one lane per target body.  Pair term as kernel.cu:480-490:
-// phi += q/r, grad += q (x_j - x_i)/r^3, skipped when r = 0.
+// offsets of the stencil, so the periodic shift is exact) and padded with zero
+// charges to a multiple of 4.  Lane = (target i = lane/4, source j = lane%4); a
+// thread carries up to 3 targets (clusters of 24), so every staged source it
+// loads serves 3 pairs.  Warp w sweeps a quarter of the sources; the 4 source
+// lanes of a target are reduced by shuffles and the per-warp partial sums are
+// added in warp order (deterministic).
 __global__ void __launch_bounds__(P2P_THREADS) k_p2p(const int* off, int depth, int periodic, const float4* atoms,
                                                      const int* stencil, int nst, float4* field)
 {
@@ -450,7 +521,7 @@ __global__ void __launch_bounds__(P2P_THREADS) k_p2p(const int* off, int depth, 
         }
         e_d[tid] = make_float4((float)stencil[3 * tid], (float)stencil[3 * tid + 1], (float)stencil[3 * tid + 2], 0.f);
     }
-    // prefix over the stencil entries (nst <= 128)
+    // exclusive prefix over the stencil entries (nst <= 128)
     {
         __shared__ int ws[4];
         int x = cnt;
@@ -462,7 +533,7 @@ __global__ void __launch_bounds__(P2P_THREADS) k_p2p(const int* off, int depth, 
         __syncthreads();
         int add = 0;
         for (int w = 0; w < warp; w++) add += ws[w];
-        e_off[tid] = x - cnt + add;  // exclusive
+        e_off[tid] = x - cnt + add;
         __syncthreads();
         if (tid == 0) e_off[nst] = ws[0] + ws[1] + ws[2] + ws[3];
     }
@@ -470,45 +541,34 @@ __global__ void __launch_bounds__(P2P_THREADS) k_p2p(const int* off, int depth, 
     const int total = e_off[nst];
     for (int t0 = 0; t0 < nt; t0 += P2P_MAXT) {
         const int ntc = min(P2P_MAXT, nt - t0);
+        const float4* tgt = atoms + tb + t0;
         for (int i = tid; i < 4 * P2P_MAXT; i += P2P_THREADS) part[i / P2P_MAXT][i % P2P_MAXT] = make_float4(0.f, 0.f, 0.f, 0.f);
         for (int s0 = 0; s0 < total; s0 += P2P_MAXS) {
             const int ns = min(P2P_MAXS, total - s0);
+            const int ns4 = (ns + 3) & ~3;
             __syncthreads();
-            for (int i = tid; i < ns; i += P2P_THREADS) {
-                int g = s0 + i;
-                int lo = 0, hi = nst - 1;  // last entry with e_off <= g
-                while (lo < hi) {
-                    int mid = (lo + hi + 1) >> 1;
-                    if (e_off[mid] <= g) lo = mid; else hi = mid - 1;
+            // warp w copies whole source leaves w, w+4, ...: lane = body of the leaf,
+            // clipped to this pass's window [s0, s0+ns); zero-charge padding to ns4
+            for (int e = warp; e < nst; e += 4) {
+                const int b0 = max(e_off[e], s0), b1 = min(e_off[e + 1], s0 + ns);
+                const float4 d = e_d[e];
+                const int gb = e_beg[e] - e_off[e];
+                for (int g = b0 + lane; g < b1; g += 32) {
+                    const float4 a = atoms[gb + g];
+                    src[g - s0] = make_float4(a.x + d.x, a.y + d.y, a.z + d.z, a.w);
                 }
-                float4 a = atoms[e_beg[lo] + (g - e_off[lo])];
-                float4 d = e_d[lo];
-                src[i] = make_float4(a.x + d.x, a.y + d.y, a.z + d.z, a.w);
             }
+            if (tid < ns4 - ns) src[ns + tid] = make_float4(0.f, 0.f, 0.f, 0.f);
             __syncthreads();
-            const int per = (ns + 3) / 4;
-            const int jb = warp * per, je = min(ns, jb + per);
-            for (int tt = lane; tt < ntc; tt += 32) {
-                const float4 xi = atoms[tb + t0 + tt];
-                float phi = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
-                for (int j = jb; j < je; j++) {
-                    const float4 s = src[j];
-                    const float dx = xi.x - s.x, dy = xi.y - s.y, dz = xi.z - s.z;
-                    const float r2 = dx * dx + dy * dy + dz * dz;
-                    const float ri = r2 > 0.f ? rsqrtf(r2) : 0.f;
-                    const float qr = s.w * ri;
-                    phi += qr;
-                    const float q3 = qr * ri * ri;
-                    gx -= q3 * dx;
-                    gy -= q3 * dy;
-                    gz -= q3 * dz;
-                }
-                float4 pp = part[warp][tt];
-                pp.x += phi;
-                pp.y += gx;
-                pp.z += gy;
-                pp.w += gz;
-                part[warp][tt] = pp;
+            // this warp's quarter of the sources, in steps of 4
+            const int nsteps = ns4 >> 2;
+            const int per = (nsteps + 3) >> 2;
+            const int sb = warp * per, se = min(nsteps, sb + per);
+            for (int c0 = 0; c0 < ntc; c0 += 24) {
+                const int rem = ntc - c0;
+                if (rem > 16) p2p_cluster<3>(src, tgt, c0, ntc, sb, se, lane, part[warp]);
+                else if (rem > 8) p2p_cluster<2>(src, tgt, c0, ntc, sb, se, lane, part[warp]);
+                else p2p_cluster<1>(src, tgt, c0, ntc, sb, se, lane, part[warp]);
             }
         }
         __syncthreads();
@@ -730,45 +790,55 @@ __global__ void __launch_bounds__(256) k_root_m2m(RootArgs a)
     }
 }
 
-// Fixed-order sum of per-block partials: out[j] = sum_b part[b*width + j].
+// Fixed-order sum of per-block partials: out[j] = sum_b part[b*width + j].  Warp
+// j reduces column j: lane l sums blocks l, l+32, ... then a fixed butterfly.
 __global__ void k_sum_partials(const double* part, int nblocks, int width, double* out)
 {
-    const int j = threadIdx.x;
+    const int j = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (j >= width) return;
     double s = 0;
-    for (int b = 0; b < nblocks; b++) s += part[(size_t)b * width + j];
-    out[j] = s;
+    for (int b = lane; b < nblocks; b += 32) s += part[(size_t)b * width + j];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) out[j] = s;
 }
 
 void launch_sum_partials(const double* part, int nblocks, int width, double* out, cudaStream_t s)
 {
     COUNT_LAUNCH();
-    k_sum_partials<<<1, 32, 0, s>>>(part, nblocks, width, out);
+    k_sum_partials<<<1, 32 * width, 0, s>>>(part, nblocks, width, out);
 }
 
-// L~_0 = A_lattice M~_0 (images >= 2), and the FP32 copy of M~_0.
-__global__ void k_root_lattice(RootArgs a)
+// L~_0 = A_lattice M~_0 (images >= 2), and the FP32 copy of M~_0.  One warp per
+// output row; lanes split the FP64 dot product, reduced by a fixed butterfly.
+__global__ void __launch_bounds__(256) k_root_lattice(RootArgs a)
 {
-    const int r = blockIdx.x * 32 + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int r = blockIdx.x * 8 + (threadIdx.x >> 5);
     if (r >= a.R) return;
-    a.M0f[r] = (float)a.M0[r];
     double t = 0;
     if (a.images >= 2) {
         const double* A = a.lattice + (size_t)r * a.R;
-        for (int c = 0; c < a.R; c++) t += A[c] * a.M0[c];
+        for (int c = lane; c < a.R; c += 32) t += A[c] * a.M0[c];
     }
-    a.L0[r] = t;
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) {
+        a.L0[r] = t;
+        a.M0f[r] = (float)a.M0[r];
+    }
 }
 
-// L~_1[o] += A_o L~_0 (FP64 arithmetic, FP32 result).
-__global__ void k_root_l2l(RootArgs a)
+// L~_1[o] += A_o L~_0 (FP64 arithmetic, FP32 result).  One warp per (child, row).
+__global__ void __launch_bounds__(256) k_root_l2l(RootArgs a)
 {
-    const int o = blockIdx.x, r = blockIdx.y * 32 + threadIdx.x;
-    if (r >= a.R) return;
+    const int lane = threadIdx.x & 31;
+    const int w = blockIdx.x * 8 + (threadIdx.x >> 5);
+    const int o = w / a.R, r = w % a.R;
+    if (o >= 8) return;
     const double* A = a.l2l + ((size_t)o * a.R + r) * a.R;
     double t = 0;
-    for (int c = 0; c < a.R; c++) t += A[c] * a.L0[c];
-    a.L1[(size_t)o * a.Rpad + r] += (float)t;
+    for (int c = lane; c < a.R; c += 32) t += A[c] * a.L0[c];
+    for (int k = 16; k > 0; k >>= 1) t += __shfl_xor_sync(0xffffffffu, t, k);
+    if (lane == 0) a.L1[(size_t)o * a.Rpad + r] += (float)t;
 }
 
 void launch_root_m2m(const RootArgs& a, cudaStream_t s)
@@ -779,12 +849,12 @@ void launch_root_m2m(const RootArgs& a, cudaStream_t s)
 void launch_root_lattice(const RootArgs& a, cudaStream_t s)
 {
     COUNT_LAUNCH();
-    k_root_lattice<<<(a.R + 31) / 32, 32, 0, s>>>(a);
+    k_root_lattice<<<(a.R + 7) / 8, 256, 0, s>>>(a);
 }
 void launch_root_l2l(const RootArgs& a, cudaStream_t s)
 {
     COUNT_LAUNCH();
-    k_root_l2l<<<dim3(8, (a.R + 31) / 32), 32, 0, s>>>(a);
+    k_root_l2l<<<(8 * a.R + 7) / 8, 256, 0, s>>>(a);
 }
 
 // ------------------------------------------------------------------ finalize
@@ -799,6 +869,7 @@ __global__ void __launch_bounds__(256) k_finalize(FinalArgs a)
     const float inv_h = a.sc->inv_h, inv_h2 = a.sc->inv_h * a.sc->inv_h;
     const double corr = cK * (M0 * M0 + M1 * M1 + M2 * M2) / (double)a.n;
     const float fM0 = (float)(cK * M0), fM1 = (float)(cK * M1), fM2 = (float)(cK * M2);
+    const float corr_f = (float)corr;
     double e = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) {
         const float4 nf = a.near[i], ff = a.far[i];
@@ -810,10 +881,11 @@ __global__ void __launch_bounds__(256) k_finalize(FinalArgs a)
         a.forces[3 * o] = qk * gx + q * fM0;
         a.forces[3 * o + 1] = qk * gy + q * fM1;
         a.forces[3 * o + 2] = qk * gz + q * fM2;
-        double pot = (double)phi * KE;
-        if (q != 0.f) pot -= corr / (double)q;
-        a.pots[o] = (float)pot;
-        e += 0.5 * (double)q * pot;
+        // FP32 per body (no FP64 division), FP64 accumulation of the energy
+        float pot = phi * (float)KE;
+        if (q != 0.f) pot -= corr_f / q;
+        a.pots[o] = pot;
+        e += (double)(0.5f * q) * (double)pot;
     }
     for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
     __shared__ double red[8];

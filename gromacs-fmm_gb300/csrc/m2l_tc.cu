@@ -77,11 +77,28 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
 
 __device__ __forceinline__ void cp_async16(void* dst, const void* src, bool valid)
 {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(valid ? 16 : 0)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(valid ? 16 : 0)
                  : "memory");
 }
 
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+// Arrives on the mbarrier once all of this thread's earlier cp.async copies have
+// landed (the barrier's expected count includes this arrival).
+__device__ __forceinline__ void cp_async_arrive_noinc(uint64_t* bar)
+{
+    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+// Waits until at most n of this thread's most recent cp.async groups are pending.
+__device__ __forceinline__ void cp_async_wait_pending(int n)
+{
+    switch (n) {
+        case 0: asm volatile("cp.async.wait_group 0;" ::: "memory"); break;
+        case 1: asm volatile("cp.async.wait_group 1;" ::: "memory"); break;
+        case 2: asm volatile("cp.async.wait_group 2;" ::: "memory"); break;
+        default: asm volatile("cp.async.wait_group 3;" ::: "memory"); break;
+    }
+}
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
@@ -157,29 +174,39 @@ void launch_split_bf16(const float* M, int Rpad, int R, long nrows, void* hi, vo
                                                                (__nv_bfloat16*)lo);
 }
 
-__global__ void __launch_bounds__(128, 1) k_m2l_tc(TcArgs a)
+// Warp-specialised pipeline, no block-wide barrier in the main loop:
+//   warps 0-3 (producers): thread t owns target row t; for entry i it waits until
+//     stage i%NS is free (the MMAs of entry i-NS committed), gathers its source
+//     row (cp.async, hi and lo bf16) into the 128B-swizzled A tile and arrives on
+//     the stage's full barrier when its copies land (cp.async.mbarrier.arrive);
+//     thread 0 also loads the operator images with one cp.async.bulk;
+//   warp 4 (MMA issuer, one lane): waits for the full barrier, issues the chunked
+//     tcgen05.mma sequence into TMEM and commits to the stage's empty barrier.
+// After the last commit, warps 0-3 read their 32 TMEM lanes (tcgen05.ld) and add
+// the results to the target locals.
+__global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(TcArgs a)
 {
     extern __shared__ uint8_t smraw[];
     uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~(uintptr_t)1023);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const bool split = a.nprod > 1;                    // lo halves are needed only for 3 products
     const int a_bytes = 128 * a.k_atoms * 128;        // one operand (hi or lo) of A
     const int b_bytes = a.img_bytes;                   // one operand of B
-    const int stage_bytes = 2 * a_bytes + 2 * b_bytes;
-    uint8_t* stage[2] = {sm, sm + stage_bytes};
-    uint64_t* bar_full = reinterpret_cast<uint64_t*>(sm + 2 * stage_bytes);
-    uint64_t* bar_empty = bar_full + 2;
-    int* srow = reinterpret_cast<int*>(bar_full + 4);
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(srow + 128);
+    const int stage_bytes = (split ? 2 : 1) * (a_bytes + b_bytes);
+    const int NS = a.nstage;
+    uint64_t* bar_full = reinterpret_cast<uint64_t*>(sm + NS * stage_bytes);
+    uint64_t* bar_empty = bar_full + TC_MAXSTAGE;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar_empty + TC_MAXSTAGE);
 
     const CTask task = a.tasks[blockIdx.x];
     if (tid == 0) {
-        mbar_init(&bar_full[0], 1);
-        mbar_init(&bar_full[1], 1);
-        mbar_init(&bar_empty[0], 1);
-        mbar_init(&bar_empty[1], 1);
+        for (int k = 0; k < NS; k++) {
+            mbar_init(&bar_full[k], 128 + 1);  // 128 producer copy arrivals + the bulk-copy expect_tx
+            mbar_init(&bar_empty[k], 1);
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == 0) {
+    if (warp == 4) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
                      "r"(a.tmem_cols)
                      : "memory");
@@ -189,34 +216,33 @@ __global__ void __launch_bounds__(128, 1) k_m2l_tc(TcArgs a)
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-
-    // target coordinates of row t = tid
-    const bool tvalid = tid < task.ntgt;
-    int vt[3], va[3];
-    const uint32_t q = (uint32_t)(task.q0 + tid);
-    const uint32_t tcode = (q << 3) | (uint32_t)task.octant;
-    morton_decode(q, va[0], va[1], va[2]);
-    morton_decode(tcode, vt[0], vt[1], vt[2]);
-
     const int ne = task.e_end - task.e_begin;
     bool ok = true;
-    for (int i = 0; i < ne; i++) {
-        const int e = task.e_begin + i, s = i & 1;
-        const CEntry en = a.entries[e];
-        // 1. the MMAs that last read this stage are complete
-        if (i >= 2) ok = mbar_wait(&bar_empty[s], ((i >> 1) - 1) & 1, a.err) && ok;
-        uint8_t* A_hi = stage[s];
-        uint8_t* A_lo = A_hi + a_bytes;
-        uint8_t* B = A_lo + a_bytes;
-        // 2. operator images (hi, lo) by the bulk-copy engine
-        if (tid == 0) {
-            mbar_expect_tx(&bar_full[s], 2u * b_bytes);
-            bulk_g2s(B, a.bimg + (size_t)en.op * 2 * b_bytes, 2u * b_bytes, &bar_full[s]);
-        }
-        // 3. source rows of the 128 targets
-        {
-            int row = -1;
+
+    if (warp < 4) {
+        // ---------------------------------------------------------------- producers
+        const int t = tid;
+        const bool tvalid = t < task.ntgt;
+        int vt[3], va[3];
+        const uint32_t q = (uint32_t)(task.q0 + t);
+        const uint32_t tcode = (q << 3) | (uint32_t)task.octant;
+        morton_decode(q, va[0], va[1], va[2]);
+        morton_decode(tcode, vt[0], vt[1], vt[2]);
+        const int chunks = a.k_atoms * 8;  // 16-byte chunks per row
+        for (int i = 0; i < ne; i++) {
+            const int st = i % NS, u = i / NS;
+            if (i >= NS) ok = mbar_wait(&bar_empty[st], (u - 1) & 1, a.err) && ok;
+            const CEntry en = a.entries[task.e_begin + i];
+            uint8_t* A_hi = sm + st * stage_bytes;
+            uint8_t* A_lo = A_hi + a_bytes;
+            if (t == 0) {
+                uint8_t* B = A_hi + (split ? 2 : 1) * a_bytes;
+                const uint32_t nb = (split ? 2u : 1u) * b_bytes;
+                mbar_expect_tx(&bar_full[st], nb);
+                bulk_g2s(B, a.bimg + (size_t)en.op * 2 * b_bytes, nb, &bar_full[st]);
+            }
             const int slev = en.mode == 0 ? task.level : task.level - 1;
+            int row = -1;
             if (tvalid) {
                 const int* base = en.mode == 0 ? vt : va;
                 int sx = base[0] + en.dx, sy = base[1] + en.dy, sz = base[2] + en.dz;
@@ -229,34 +255,26 @@ __global__ void __launch_bounds__(128, 1) k_m2l_tc(TcArgs a)
                 }
                 if (in) row = (int)morton_encode(sx, sy, sz);
             }
-            srow[tid] = row;
-        }
-        __syncthreads();
-        {
-            const int slev = en.mode == 0 ? task.level : task.level - 1;
-            const __nv_bfloat16* gh = a.mh[slev];
-            const __nv_bfloat16* gl = a.ml[slev];
-            const int chunks = a.k_atoms * 8;  // 16-byte chunks per row
-            for (int idx = tid; idx < 128 * chunks; idx += 128) {
-                const int r = idx / chunks, kc = idx % chunks;
-                const int row = srow[r];
-                const bool valid = row >= 0;
-                const size_t goff = (size_t)(valid ? row : 0) * TC_KMAX + kc * 8;
-                const int atom = kc >> 3, c = kc & 7;
-                const int soff = atom * (128 * 128) + r * 128 + ((c ^ (r & 7)) << 4);
-                cp_async16(A_hi + soff, gh + goff, valid);
-                cp_async16(A_lo + soff, gl + goff, valid);
+            const bool valid = row >= 0;
+            const size_t g0 = (size_t)(valid ? row : 0) * TC_KMAX;
+            const __nv_bfloat16* gh = a.mh[slev] + g0;
+            const __nv_bfloat16* gl = a.ml[slev] + g0;
+            for (int kc = 0; kc < chunks; kc++) {
+                const int soff = (kc >> 3) * (128 * 128) + t * 128 + (((kc & 7) ^ (t & 7)) << 4);
+                cp_async16(A_hi + soff, gh + kc * 8, valid);
+                if (split) cp_async16(A_lo + soff, gl + kc * 8, valid);
             }
+            cp_async_arrive_noinc(&bar_full[st]);
         }
-        cp_async_wait_all();
-        fence_proxy_async();
-        __syncthreads();
-        // 4. MMAs (one thread)
-        if (tid == 0) {
-            ok = mbar_wait(&bar_full[s], (i >> 1) & 1, a.err) && ok;
+    } else if (lane == 0) {
+        // ---------------------------------------------------------------- MMA issuer
+        for (int i = 0; i < ne; i++) {
+            const int st = i % NS, u = i / NS;
+            ok = mbar_wait(&bar_full[st], u & 1, a.err) && ok;
+            fence_proxy_async();
             tc_fence_after();
-            const uint32_t a_hi = smem_u32(A_hi), a_lo = smem_u32(A_lo), b_hi = smem_u32(B),
-                           b_lo = smem_u32(B) + (uint32_t)b_bytes;
+            const uint32_t a_hi = smem_u32(sm + st * stage_bytes), a_lo = a_hi + (uint32_t)a_bytes,
+                           b_hi = a_hi + (uint32_t)((split ? 2 : 1) * a_bytes), b_lo = b_hi + (uint32_t)b_bytes;
             for (int c = 0; c < a.nchunk; c++) {
                 const int N = a.chunk_n[c], K = a.chunk_k[c];
                 const uint32_t idesc = idesc_bf16(N);
@@ -264,23 +282,23 @@ __global__ void __launch_bounds__(128, 1) k_m2l_tc(TcArgs a)
                 for (int p = 0; p < a.nprod; p++) {
                     const uint32_t abase = p == 2 ? a_lo : a_hi;
                     const uint32_t bbase = (p == 1 ? b_lo : b_hi) + boff;
-                    for (int st = 0; st < K / 16; st++) {
-                        const uint32_t ao = (uint32_t)((st >> 2) * (128 * 128) + (st & 3) * 32);
-                        const uint32_t bo = (uint32_t)((st >> 2) * (N * 128) + (st & 3) * 32);
-                        const uint32_t acc = (i > 0 || p > 0 || st > 0) ? 1u : 0u;
+                    for (int kk = 0; kk < K / 16; kk++) {
+                        const uint32_t ao = (uint32_t)((kk >> 2) * (128 * 128) + (kk & 3) * 32);
+                        const uint32_t bo = (uint32_t)((kk >> 2) * (N * 128) + (kk & 3) * 32);
+                        const uint32_t acc = (i > 0 || p > 0 || kk > 0) ? 1u : 0u;
                         mma_bf16(tmem + (uint32_t)a.chunk_col[c], sw128_desc(abase + ao), sw128_desc(bbase + bo),
                                  idesc, acc);
                     }
                 }
             }
-            mma_commit(&bar_empty[s]);
+            mma_commit(&bar_empty[st]);
         }
     }
-    // all MMAs complete
-    if (ne > 0) ok = mbar_wait(&bar_empty[(ne - 1) & 1], ((ne - 1) >> 1) & 1, a.err) && ok;
+    // all MMAs complete (the last commit covers every earlier MMA of this thread)
+    if (warp < 4 && ne > 0) ok = mbar_wait(&bar_empty[(ne - 1) % NS], ((ne - 1) / NS) & 1, a.err) && ok;
     __syncthreads();
     tc_fence_after();
-    if (ne > 0) {
+    if (warp < 4 && ne > 0) {
         float* dst = a.dst_lvl[task.level];
         const int t = 32 * warp + lane;
         const bool wv = t < task.ntgt;
@@ -302,15 +320,31 @@ __global__ void __launch_bounds__(128, 1) k_m2l_tc(TcArgs a)
     }
     tc_fence_before();
     __syncthreads();
-    if (warp == 0)
+    if (warp == 4)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(a.tmem_cols) : "memory");
     (void)ok;
 }
 
+size_t tc_stage_bytes(int k_atoms, int img_bytes, int nprod)
+{
+    return (size_t)(nprod > 1 ? 2 : 1) * ((size_t)128 * k_atoms * 128 + (size_t)img_bytes);
+}
+
 size_t tc_smem_bytes(const TcArgs& a)
 {
-    size_t stage = 2 * (size_t)128 * a.k_atoms * 128 + 2 * (size_t)a.img_bytes;
-    return 1024 + 2 * stage + 4 * sizeof(uint64_t) + 128 * sizeof(int) + 16;
+    return 1024 + (size_t)a.nstage * tc_stage_bytes(a.k_atoms, a.img_bytes, a.nprod) +
+           2 * TC_MAXSTAGE * sizeof(uint64_t) + 16;
+}
+
+// Stages per CTA: aim at two CTAs per SM (about 110 KB each), at least 2 stages.
+int tc_pick_stages(int k_atoms, int img_bytes, int nprod)
+{
+    const size_t st = tc_stage_bytes(k_atoms, img_bytes, nprod);
+    int ns = (int)((110 * 1024) / st);
+    if (ns < 2) ns = 2;
+    if (ns > TC_MAXSTAGE) ns = TC_MAXSTAGE;
+    if (1024 + ns * st + 2 * TC_MAXSTAGE * sizeof(uint64_t) + 16 > 227 * 1024) ns = 1;
+    return ns;
 }
 
 void launch_m2l_tc(const TcArgs& a, int ntasks, cudaStream_t s)
@@ -323,7 +357,7 @@ void launch_m2l_tc(const TcArgs& a, int ntasks, cudaStream_t s)
         attr = shm;
     }
     g_kernel_launches.fetch_add(1, std::memory_order_relaxed);
-    k_m2l_tc<<<ntasks, 128, shm, s>>>(a);
+    k_m2l_tc<<<ntasks, TC_THREADS, shm, s>>>(a);
 }
 
 }  // namespace gbfmm

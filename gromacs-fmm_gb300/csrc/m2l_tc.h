@@ -15,6 +15,8 @@ constexpr int TC_KMAX = 128;     // length of a split (bf16) multipole row; orde
 constexpr int TC_MAX_ORDER = 10;
 constexpr int TC_MAXCHUNK = 8;
 constexpr int TC_TILE = 128;     // targets per CTA (MMA M)
+constexpr int TC_MAXSTAGE = 4;   // pipeline stages (operands of one entry each)
+constexpr int TC_THREADS = 160;  // 4 producer warps + 1 MMA warp
 
 // Degree chunks of the M2L operator: chunk c covers output rows [row0, row0+rows)
 // (whole degrees j0..j1), MMA N = n (rows padded to 16), K = k (inputs of degree
@@ -43,6 +45,7 @@ struct TcArgs {
     int Rpad;
     int k_atoms, img_bytes, tmem_cols, nchunk;
     int nprod;                   // 3: hi*hi + hi*lo + lo*hi, 1: hi*hi
+    int nstage;                  // pipeline stages, 2..TC_MAXSTAGE (tc_pick_stages)
     int periodic;
     int atomic;                  // 1: atomicAdd into L (split entry ranges), 0: plain add
     int chunk_n[TC_MAXCHUNK], chunk_k[TC_MAXCHUNK], chunk_col[TC_MAXCHUNK], chunk_row0[TC_MAXCHUNK],
@@ -50,6 +53,8 @@ struct TcArgs {
 };
 
 size_t tc_smem_bytes(const TcArgs& a);
+size_t tc_stage_bytes(int k_atoms, int img_bytes, int nprod);
+int tc_pick_stages(int k_atoms, int img_bytes, int nprod);
 void launch_m2l_tc(const TcArgs& a, int ntasks, cudaStream_t s);
 void launch_split_bf16(const float* M, int Rpad, int R, long nrows, void* hi, void* lo, cudaStream_t s);
 

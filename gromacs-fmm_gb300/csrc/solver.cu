@@ -490,6 +490,7 @@ static TcArgs tc_args(gbfmm_handle* h)
     a.tmem_cols = pl.tmem_cols;
     a.nchunk = pl.nchunk;
     a.nprod = h->prm.precision == GBFMM_PREC_BF16X1 ? 1 : 3;
+    a.nstage = tc_pick_stages(pl.k_atoms, pl.img_bytes, a.nprod);
     a.periodic = h->periodic ? 1 : 0;
     a.atomic = h->tc_split > 1 ? 1 : 0;
     for (int c = 0; c < pl.nchunk; c++) {
@@ -541,7 +542,6 @@ static void enqueue_step(gbfmm_handle* h)
     cudaMemsetAsync(h->d_sums, 0, sizeof(double) * 4, s);
     cudaMemsetAsync(h->d_energy, 0, sizeof(double), s);
     cudaMemsetAsync(h->d_L, 0, sizeof(float) * h->lev_floats, s);
-    cudaMemsetAsync(h->d_far, 0, sizeof(float4) * std::max(n, 1), s);
     if (n > 0) {
         TreeArgs ta;
         ta.sc = h->d_sc;
@@ -1061,33 +1061,227 @@ extern "C" int gbfmm_debug_harmonics(int order, int kind, const double* d, doubl
     return GBFMM_OK;
 }
 
-// ---- batched solves: one handle per system for now
+// ---- batched solves
+//
+// Many independent cubic systems solved together: each system keeps its own
+// operator set, stencils and tree (its own order and depth), but its inputs and
+// outputs are views into packed batch buffers and all systems' steps are captured
+// into ONE CUDA graph, forked over several streams so that independent systems
+// run concurrently.  Per call the host uploads the step constants of every system
+// in one copy and replays the graph.
 struct gbfmm_batch {
-    std::vector<gbfmm_handle*> hs;
+    int n_sys = 0;
+    long natoms = 0;
     std::vector<int> off;
+    std::vector<gbfmm_handle*> hs;
+    void* buf = nullptr;
+    float *d_coords = nullptr, *d_q = nullptr, *d_forces = nullptr, *d_pots = nullptr;
+    double* d_energy = nullptr;
+    StepConst* d_sc = nullptr;
+    StepConst* h_sc = nullptr;  // pinned
+    cudaStream_t master = nullptr;
+    std::vector<cudaStream_t> workers;
+    std::vector<cudaEvent_t> ev;
+    cudaEvent_t ein = nullptr, eout = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    bool have_result = false;
 };
 
+static void free_batch(gbfmm_batch* b)
+{
+    if (!b) return;
+    for (gbfmm_handle* h : b->hs)
+        if (h) gbfmm_destroy(h);
+    if (b->gexec) cudaGraphExecDestroy(b->gexec);
+    for (cudaStream_t s : b->workers) cudaStreamDestroy(s);
+    for (cudaEvent_t e : b->ev) cudaEventDestroy(e);
+    if (b->ein) cudaEventDestroy(b->ein);
+    if (b->eout) cudaEventDestroy(b->eout);
+    if (b->master) cudaStreamDestroy(b->master);
+    if (b->buf) cudaFree(b->buf);
+    if (b->h_sc) cudaFreeHost(b->h_sc);
+    delete b;
+}
+
 extern "C" int gbfmm_batch_create(int n_sys, const int* atom_offsets, const int* orders, const int* depths, int images,
-                                  int precision, gbfmm_batch** out)
+                                  int precision, int flags, gbfmm_batch** out)
 {
-    (void)n_sys; (void)atom_offsets; (void)orders; (void)depths; (void)images; (void)precision;
-    if (out) *out = nullptr;
-    return fail(GBFMM_ERR_UNSUPPORTED, "batched solves are not built yet");
+    if (!out) return fail(GBFMM_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    if (n_sys <= 0 || !atom_offsets || !orders || !depths) return fail(GBFMM_ERR_ARG, "bad batch description");
+    if (atom_offsets[0] != 0) return fail(GBFMM_ERR_ARG, "atom_offsets[0] must be 0");
+    for (int i = 0; i < n_sys; i++)
+        if (atom_offsets[i + 1] < atom_offsets[i]) return fail(GBFMM_ERR_ARG, "atom_offsets must not decrease");
+    gbfmm_batch* b = new gbfmm_batch();
+    b->n_sys = n_sys;
+    b->off.assign(atom_offsets, atom_offsets + n_sys + 1);
+    b->natoms = atom_offsets[n_sys];
+    const size_t N = (size_t)std::max<long>(b->natoms, 1);
+    auto bail = [&](int rc) {
+        free_batch(b);
+        return rc;
+    };
+    Arena sz;
+    sz.take<float>(3 * N);
+    sz.take<float>(N);
+    sz.take<float>(3 * N);
+    sz.take<float>(N);
+    sz.take<double>(n_sys);
+    sz.take<StepConst>(n_sys);
+    if (cudaMalloc(&b->buf, sz.off + 256) != cudaSuccess) {
+        cudaGetLastError();
+        return bail(fail(GBFMM_ERR_NOMEM, "batch buffers"));
+    }
+    Arena ar;
+    ar.base = (char*)b->buf;
+    b->d_coords = ar.take<float>(3 * N);
+    b->d_q = ar.take<float>(N);
+    b->d_forces = ar.take<float>(3 * N);
+    b->d_pots = ar.take<float>(N);
+    b->d_energy = ar.take<double>(n_sys);
+    b->d_sc = ar.take<StepConst>(n_sys);
+    if (cudaMallocHost(&b->h_sc, sizeof(StepConst) * n_sys) != cudaSuccess) return bail(fail(GBFMM_ERR_NOMEM, "pinned"));
+    std::memset(b->h_sc, 0, sizeof(StepConst) * n_sys);
+    for (int i = 0; i < n_sys; i++) {
+        gbfmm_params p;
+        gbfmm_params_default(&p);
+        p.order = orders[i];
+        p.max_depth = depths[i];
+        p.images = images;
+        p.precision = precision;
+        p.flags = flags & ~GBFMM_FLAG_NO_GRAPH;
+        gbfmm_handle* h = nullptr;
+        int rc = gbfmm_create(&p, atom_offsets[i + 1] - atom_offsets[i], &h);
+        if (rc != GBFMM_OK) return bail(rc);
+        b->hs.push_back(h);
+        // the system's inputs and outputs are views of the batch buffers
+        const int o = atom_offsets[i];
+        h->d_q = b->d_q + o;
+        h->d_forces = b->d_forces + 3 * (size_t)o;
+        h->d_pots = b->d_pots + o;
+        h->d_energy = b->d_energy + i;
+        h->d_sc = b->d_sc + i;
+        h->have_charges = true;
+    }
+    const int nw = std::min(n_sys, 8);
+    if (cudaStreamCreateWithFlags(&b->master, cudaStreamNonBlocking) != cudaSuccess)
+        return bail(fail(GBFMM_ERR_CUDA, "stream create"));
+    for (int w = 0; w < nw; w++) {
+        cudaStream_t s;
+        cudaEvent_t e;
+        if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+            return bail(fail(GBFMM_ERR_CUDA, "stream create"));
+        b->workers.push_back(s);
+        b->ev.push_back(e);
+    }
+    if (cudaEventCreateWithFlags(&b->ein, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->eout, cudaEventDisableTiming) != cudaSuccess)
+        return bail(fail(GBFMM_ERR_CUDA, "event create"));
+    *out = b;
+    return GBFMM_OK;
 }
-extern "C" int gbfmm_batch_execute(gbfmm_batch*, const float*, const float*, const float*, float*, float*, double*)
+
+static int batch_capture(gbfmm_batch* b)
 {
-    return fail(GBFMM_ERR_UNSUPPORTED, "batched solves are not built yet");
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(b->master, cudaStreamCaptureModeThreadLocal));
+    CK(cudaEventRecord(b->ein, b->master));
+    const int nw = (int)b->workers.size();
+    for (int w = 0; w < nw; w++) CK(cudaStreamWaitEvent(b->workers[w], b->ein, 0));
+    // largest systems first, round-robin over the worker streams
+    std::vector<int> ord(b->n_sys);
+    for (int i = 0; i < b->n_sys; i++) ord[i] = i;
+    std::sort(ord.begin(), ord.end(), [&](int x, int y) { return b->hs[x]->n > b->hs[y]->n; });
+    for (int k = 0; k < b->n_sys; k++) {
+        // the handle keeps (and later destroys) its own stream; only the capture
+        // goes to the worker stream
+        gbfmm_handle* h = b->hs[ord[k]];
+        cudaStream_t own = h->stream;
+        h->stream = b->workers[k % nw];
+        enqueue_step(h);
+        h->stream = own;
+    }
+    for (int w = 0; w < nw; w++) {
+        CK(cudaEventRecord(b->ev[w], b->workers[w]));
+        CK(cudaStreamWaitEvent(b->master, b->ev[w], 0));
+    }
+    cudaError_t e = cudaStreamEndCapture(b->master, &g);
+    if (e != cudaSuccess) return fail(GBFMM_ERR_CUDA, "batch graph capture: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&b->gexec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(GBFMM_ERR_CUDA, "batch graph instantiate: %s", cudaGetErrorString(e));
+    return GBFMM_OK;
 }
-extern "C" int gbfmm_batch_execute_device(gbfmm_batch*, const void*, const void*, const float*, void*)
+
+extern "C" int gbfmm_batch_execute_device(gbfmm_batch* b, const void* d_coords, const void* d_charges,
+                                          const float* box_edges, void* stream)
 {
-    return fail(GBFMM_ERR_UNSUPPORTED, "batched solves are not built yet");
+    if (!b || !box_edges || (b->natoms > 0 && (!d_coords || !d_charges))) return fail(GBFMM_ERR_ARG, "NULL argument");
+    for (int i = 0; i < b->n_sys; i++) {
+        gbfmm_handle* h = b->hs[i];
+        float box[9] = {box_edges[i], 0, 0, 0, box_edges[i], 0, 0, 0, box_edges[i]};
+        int rc = set_box(h, box, (const float*)d_coords + 3 * (size_t)b->off[i]);
+        if (rc) return rc;
+        b->h_sc[i] = *h->h_sc;
+    }
+    cudaStream_t us = (cudaStream_t)stream;
+    CK(cudaEventRecord(b->ein, us));
+    CK(cudaStreamWaitEvent(b->master, b->ein, 0));
+    if (d_charges != b->d_q)
+        CK(cudaMemcpyAsync(b->d_q, d_charges, sizeof(float) * b->natoms, cudaMemcpyDeviceToDevice, b->master));
+    CK(cudaMemcpyAsync(b->d_sc, b->h_sc, sizeof(StepConst) * b->n_sys, cudaMemcpyHostToDevice, b->master));
+    if (!b->gexec) {
+        int rc = batch_capture(b);
+        if (rc) return rc;
+    }
+    CK(cudaGraphLaunch(b->gexec, b->master));
+    CK(cudaEventRecord(b->eout, b->master));
+    CK(cudaStreamWaitEvent(us, b->eout, 0));
+    b->have_result = true;
+    return GBFMM_OK;
 }
-extern "C" int gbfmm_batch_device_outputs(gbfmm_batch*, void**, void**, void**)
+
+extern "C" int gbfmm_batch_execute(gbfmm_batch* b, const float* coords, const float* charges, const float* box_edges,
+                                   float* forces, float* potentials, double* energies)
 {
-    return fail(GBFMM_ERR_UNSUPPORTED, "batched solves are not built yet");
+    if (!b || !box_edges || (b->natoms > 0 && (!coords || !charges))) return fail(GBFMM_ERR_ARG, "NULL argument");
+    for (int i = 0; i < b->n_sys; i++)
+        for (int k = b->off[i]; k < b->off[i + 1]; k++)
+            if (!std::isfinite(charges[k])) return fail(GBFMM_ERR_COORD, "charge %d is not finite", k);
+    CK(cudaMemcpyAsync(b->d_coords, coords, sizeof(float) * 3 * b->natoms, cudaMemcpyHostToDevice, b->master));
+    CK(cudaMemcpyAsync(b->d_q, charges, sizeof(float) * b->natoms, cudaMemcpyHostToDevice, b->master));
+    int rc = gbfmm_batch_execute_device(b, b->d_coords, b->d_q, box_edges, b->master);
+    if (rc) return rc;
+    if (forces) CK(cudaMemcpyAsync(forces, b->d_forces, sizeof(float) * 3 * b->natoms, cudaMemcpyDeviceToHost, b->master));
+    if (potentials) CK(cudaMemcpyAsync(potentials, b->d_pots, sizeof(float) * b->natoms, cudaMemcpyDeviceToHost, b->master));
+    if (energies) CK(cudaMemcpyAsync(energies, b->d_energy, sizeof(double) * b->n_sys, cudaMemcpyDeviceToHost, b->master));
+    CK(cudaStreamSynchronize(b->master));
+    // non-finite coordinates: each system's flag
+    for (gbfmm_handle* h : b->hs) {
+        int fl[4];
+        CK(cudaMemcpy(fl, h->d_flags, sizeof(fl), cudaMemcpyDeviceToHost));
+        if (fl[0] || fl[1]) {
+            CK(cudaMemset(h->d_flags, 0, sizeof(int) * 4));
+            return fail(fl[1] ? GBFMM_ERR_TIMEOUT : GBFMM_ERR_COORD, "a system of the batch reported an error");
+        }
+    }
+    return GBFMM_OK;
 }
+
+extern "C" int gbfmm_batch_device_outputs(gbfmm_batch* b, void** f, void** p, void** e)
+{
+    if (!b) return fail(GBFMM_ERR_ARG, "batch is NULL");
+    if (f) *f = b->d_forces;
+    if (p) *p = b->d_pots;
+    if (e) *e = b->d_energy;
+    return GBFMM_OK;
+}
+
 extern "C" int gbfmm_batch_destroy(gbfmm_batch* b)
 {
-    delete b;
+    if (!b) return fail(GBFMM_ERR_ARG, "batch is NULL");
+    if (b->master) cudaStreamSynchronize(b->master);
+    free_batch(b);
     return GBFMM_OK;
 }

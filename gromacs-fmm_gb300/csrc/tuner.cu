@@ -1,0 +1,652 @@
+// Learned parameter selection: per-step statistics, a small MLP trained and
+// evaluated by this file's own CUDA kernels, and the proposal of (order, depth,
+// precision) for a requested force-error tolerance.
+//
+// Statistics (GBFMM_NFEAT floats, gbfmm_features):
+//   [0] log10 N   [1] log10 density (1/nm^3)   [2] log10 L   [3] mean q^2
+//   [4] |sum q| / sqrt(sum q^2)   [5] log10(|M|^2 / (V sum q^2) + 1e-12)
+//   [6 + 9(k-2) + b]  levels k = 2..6: fraction of cells whose body count is in
+//                     bin b = 0: empty, b >= 1: [2^(b-1), 2^b) (last bin open)
+//   [51 + (k-2)]      levels k = 2..6: log2 of the mean count of non-empty cells
+// MLP input = statistics ++ candidate (P/10, depth/6, precision, log2(N/8^depth)/5),
+// outputs = (log10 relative RMS force error, log10 step time in ms).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <random>
+#include <vector>
+
+#include "../../include/gbfmm.h"
+
+namespace gbfmm {
+extern std::atomic<long> g_kernel_launches;
+}
+using gbfmm::g_kernel_launches;
+
+namespace {
+
+constexpr int FL = 6;             // finest statistics level (64^3 cells)
+constexpr int NCELL = 1 << (3 * FL);
+constexpr int NBIN = 9;
+
+int status(cudaError_t e) { return e == cudaSuccess ? GBFMM_OK : (e == cudaErrorMemoryAllocation ? GBFMM_ERR_NOMEM : GBFMM_ERR_CUDA); }
+
+__device__ __forceinline__ int cell_index(float x, float inv)
+{
+    int k = (int)floorf(x * inv);
+    return min(max(k, 0), (1 << FL) - 1);
+}
+
+// Body counts of the 64^3 grid and FP64 charge moments (per-block partials).
+__global__ void k_feat_counts(const float* xyz, const float* q, int n, float inv, int* counts, double* part)
+{
+    double s[5] = {0, 0, 0, 0, 0};  // sum q, sum q^2, dipole x, y, z
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2], c = q[i];
+        const int ix = cell_index(x, inv), iy = cell_index(y, inv), iz = cell_index(z, inv);
+        atomicAdd(&counts[(ix << (2 * FL)) | (iy << FL) | iz], 1);
+        s[0] += c;
+        s[1] += (double)c * c;
+        s[2] += (double)c * x;
+        s[3] += (double)c * y;
+        s[4] += (double)c * z;
+    }
+    for (int k = 0; k < 5; k++)
+        for (int o = 16; o > 0; o >>= 1) s[k] += __shfl_xor_sync(0xffffffffu, s[k], o);
+    __shared__ double red[8][5];
+    if ((threadIdx.x & 31) == 0)
+        for (int k = 0; k < 5; k++) red[threadIdx.x >> 5][k] = s[k];
+    __syncthreads();
+    if (threadIdx.x < 5) {
+        double t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w][threadIdx.x];
+        part[5 * blockIdx.x + threadIdx.x] = t;
+    }
+}
+
+// Occupancy histogram of level k (cells of 2^(FL-k) fine cells per axis).
+__global__ void k_feat_hist(const int* counts, int k, int* hist, long long* sum_nonempty)
+{
+    const int nk = 1 << k, c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nk * nk * nk) return;
+    const int ix = c / (nk * nk), iy = (c / nk) % nk, iz = c % nk, w = 1 << (FL - k);
+    long long tot = 0;
+    for (int a = 0; a < w; a++)
+        for (int b = 0; b < w; b++)
+            for (int d = 0; d < w; d++)
+                tot += counts[((ix * w + a) << (2 * FL)) | ((iy * w + b) << FL) | (iz * w + d)];
+    int bin = 0;
+    if (tot > 0) {
+        bin = 1;
+        long long v = tot;
+        while (v > 1 && bin < NBIN - 1) {
+            v >>= 1;
+            bin++;
+        }
+    }
+    atomicAdd(&hist[bin], 1);
+    if (tot > 0) atomicAdd((unsigned long long*)sum_nonempty, (unsigned long long)tot);
+}
+
+// ---------------------------------------------------------------- MLP kernels
+
+// out[b][o] = act(sum_i W[o][i] in[b][i] + bias[o]); pre-activations kept for backward.
+__global__ void k_dense_fwd(const float* in, const float* W, const float* bias, float* pre, float* out, int B, int I,
+                            int O, int act)
+{
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= B * O) return;
+    const int b = idx / O, o = idx % O;
+    float s = bias[o];
+    for (int i = 0; i < I; i++) s += W[o * I + i] * in[b * I + i];
+    pre[idx] = s;
+    out[idx] = act ? tanhf(s) : s;
+}
+
+// d_pre = d_out * act'(pre) (in place on d_out).
+__global__ void k_act_bwd(float* dout, const float* pre, int n, int act)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !act) return;
+    const float t = tanhf(pre[i]);
+    dout[i] *= 1.f - t * t;
+}
+
+// dW[o][i] = sum_b dpre[b][o] in[b][i], db[o] = sum_b dpre[b][o] (fixed order over b).
+__global__ void k_dense_bwd_w(const float* dpre, const float* in, float* dW, float* db, int B, int I, int O)
+{
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= O * (I + 1)) return;
+    const int o = idx / (I + 1), i = idx % (I + 1);
+    float s = 0.f;
+    if (i < I)
+        for (int b = 0; b < B; b++) s += dpre[b * O + o] * in[b * I + i];
+    else
+        for (int b = 0; b < B; b++) s += dpre[b * O + o];
+    if (i < I) dW[o * I + i] = s;
+    else db[o] = s;
+}
+
+// din[b][i] = sum_o dpre[b][o] W[o][i].
+__global__ void k_dense_bwd_x(const float* dpre, const float* W, float* din, int B, int I, int O)
+{
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= B * I) return;
+    const int b = idx / I, i = idx % I;
+    float s = 0.f;
+    for (int o = 0; o < O; o++) s += dpre[b * O + o] * W[o * I + i];
+    din[idx] = s;
+}
+
+// Loss 1/B sum_b sum_j (y - t)^2 and its gradient 2 (y - t) / B; per-sample
+// losses in lossb (summed on the host in a fixed order).
+__global__ void k_mse(const float* y, const float* t, float* dy, float* lossb, int B, int O)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    float l = 0.f;
+    for (int j = 0; j < O; j++) {
+        const float d = y[b * O + j] - t[b * O + j];
+        dy[b * O + j] = 2.f * d / B;
+        l += d * d;
+    }
+    lossb[b] = l / B;
+}
+
+__global__ void k_adam(float* p, const float* g, float* m, float* v, int n, float lr, float b1, float b2, float eps,
+                       float c1, float c2)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = g[i];
+    m[i] = b1 * m[i] + (1.f - b1) * gi;
+    v[i] = b2 * v[i] + (1.f - b2) * gi * gi;
+    p[i] -= lr * (m[i] / c1) / (sqrtf(v[i] / c2) + eps);
+}
+
+inline unsigned blocks(long n, int t) { return (unsigned)((n + t - 1) / t); }
+
+}  // namespace
+
+// ------------------------------------------------------------------ statistics
+
+extern "C" int gbfmm_features(const void* d_coords, const void* d_charges, int n, const float* box, float* feat,
+                              void* stream)
+{
+    if (!feat || !box || n < 0 || (n > 0 && (!d_coords || !d_charges))) return GBFMM_ERR_ARG;
+    if (!(box[0] > 0) || box[4] != box[0] || box[8] != box[0]) return GBFMM_ERR_BOX;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int nb = std::max(1, std::min(608, (n + 255) / 256));
+    // one scratch allocation per call: counts + histograms + partials
+    size_t bytes = sizeof(int) * NCELL + sizeof(int) * 5 * NBIN + sizeof(long long) * 5 + sizeof(double) * 5 * nb + 64;
+    char* buf = nullptr;
+    cudaError_t e = cudaMallocAsync(&buf, bytes, s);
+    if (e != cudaSuccess) return status(e);
+    int* counts = (int*)buf;
+    int* hist = counts + NCELL;
+    long long* sums = (long long*)(hist + 5 * NBIN + 1);
+    sums = (long long*)(((uintptr_t)sums + 7) & ~(uintptr_t)7);
+    double* part = (double*)(sums + 5);
+    cudaMemsetAsync(buf, 0, sizeof(int) * NCELL + sizeof(int) * (5 * NBIN + 2) + sizeof(long long) * 5, s);
+    const float inv = (float)((1 << FL) / (double)box[0]);
+    if (n > 0) {
+        g_kernel_launches.fetch_add(1);
+        k_feat_counts<<<nb, 256, 0, s>>>((const float*)d_coords, (const float*)d_charges, n, inv, counts, part);
+    }
+    for (int k = 2; k <= FL; k++) {
+        g_kernel_launches.fetch_add(1);
+        k_feat_hist<<<blocks(1L << (3 * k), 128), 128, 0, s>>>(counts, k, hist + NBIN * (k - 2), sums + (k - 2));
+    }
+    int h_hist[5 * NBIN];
+    long long h_sums[5];
+    std::vector<double> h_part(5 * (size_t)nb, 0.0);
+    cudaMemcpyAsync(h_hist, hist, sizeof(h_hist), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(h_sums, sums, sizeof(h_sums), cudaMemcpyDeviceToHost, s);
+    if (n > 0) cudaMemcpyAsync(h_part.data(), part, sizeof(double) * 5 * nb, cudaMemcpyDeviceToHost, s);
+    e = cudaStreamSynchronize(s);
+    cudaFreeAsync(buf, s);
+    if (e != cudaSuccess) return status(e);
+    double m[5] = {0, 0, 0, 0, 0};
+    for (int b = 0; b < nb; b++)
+        for (int k = 0; k < 5; k++) m[k] += h_part[5 * b + k];
+    const double L = box[0], V = L * L * L, N = std::max(n, 1);
+    feat[0] = (float)std::log10(N);
+    feat[1] = (float)std::log10(N / V);
+    feat[2] = (float)std::log10(L);
+    feat[3] = (float)(m[1] / N);
+    feat[4] = (float)(std::fabs(m[0]) / std::sqrt(m[1] + 1e-30));
+    const double c = L / 2;
+    const double dx = m[2] - m[0] * c, dy = m[3] - m[0] * c, dz = m[4] - m[0] * c;
+    feat[5] = (float)std::log10((dx * dx + dy * dy + dz * dz) / (V * (m[1] + 1e-30)) + 1e-12);
+    for (int k = 2; k <= FL; k++) {
+        const double cells = std::pow(8.0, k);
+        int nonempty = 0;
+        for (int b = 0; b < NBIN; b++) {
+            feat[6 + NBIN * (k - 2) + b] = (float)(h_hist[NBIN * (k - 2) + b] / cells);
+            if (b > 0) nonempty += h_hist[NBIN * (k - 2) + b];
+        }
+        feat[6 + 5 * NBIN + (k - 2)] = (float)(nonempty ? std::log2((double)h_sums[k - 2] / nonempty) : 0.0);
+    }
+    return GBFMM_OK;
+}
+
+// ------------------------------------------------------------------ MLP
+
+struct gbfmm_mlp {
+    int I = 0, H = 0, O = 0, np = 0;
+    float* d_p = nullptr;  // W1 b1 W2 b2 W3 b3
+    float *d_g = nullptr, *d_m = nullptr, *d_v = nullptr;
+    std::vector<float> xm, xs, ym, ys;  // normalisation of inputs and outputs
+    long adam_t = 0;
+    // activations workspace for batch B
+    int cap = 0;
+    float* ws = nullptr;
+    cudaStream_t s = nullptr;
+};
+
+namespace {
+
+int offW1(const gbfmm_mlp* m) { return 0; }
+int offb1(const gbfmm_mlp* m) { return m->H * m->I; }
+int offW2(const gbfmm_mlp* m) { return offb1(m) + m->H; }
+int offb2(const gbfmm_mlp* m) { return offW2(m) + m->H * m->H; }
+int offW3(const gbfmm_mlp* m) { return offb2(m) + m->H; }
+int offb3(const gbfmm_mlp* m) { return offW3(m) + m->O * m->H; }
+
+// workspace: x, pre1, a1, pre2, a2, y(pre3), t, dy, d2, d1, dx, lossb
+int ensure_ws(gbfmm_mlp* m, int B)
+{
+    if (B <= m->cap) return GBFMM_OK;
+    if (m->ws) cudaFree(m->ws);
+    m->ws = nullptr;
+    size_t n = (size_t)B * (m->I * 2 + m->H * 6 + m->O * 4 + 1);
+    cudaError_t e = cudaMalloc(&m->ws, sizeof(float) * n);
+    if (e != cudaSuccess) return status(e);
+    m->cap = B;
+    return GBFMM_OK;
+}
+
+struct WS {
+    float *x, *pre1, *a1, *pre2, *a2, *y, *t, *dy, *d2, *d1, *dx, *lossb;
+};
+
+WS layout(gbfmm_mlp* m)
+{
+    const size_t B = m->cap;
+    WS w;
+    float* p = m->ws;
+    w.x = p; p += B * m->I;
+    w.pre1 = p; p += B * m->H;
+    w.a1 = p; p += B * m->H;
+    w.pre2 = p; p += B * m->H;
+    w.a2 = p; p += B * m->H;
+    w.y = p; p += B * m->O;
+    w.t = p; p += B * m->O;
+    w.dy = p; p += B * m->O;
+    w.d2 = p; p += B * m->H;
+    w.d1 = p; p += B * m->H;
+    w.dx = p; p += B * m->I;
+    w.lossb = p;
+    return w;
+}
+
+void forward(gbfmm_mlp* m, const WS& w, int B)
+{
+    const float* P = m->d_p;
+    g_kernel_launches.fetch_add(3);
+    k_dense_fwd<<<blocks((long)B * m->H, 128), 128, 0, m->s>>>(w.x, P + offW1(m), P + offb1(m), w.pre1, w.a1, B, m->I, m->H, 1);
+    k_dense_fwd<<<blocks((long)B * m->H, 128), 128, 0, m->s>>>(w.a1, P + offW2(m), P + offb2(m), w.pre2, w.a2, B, m->H, m->H, 1);
+    k_dense_fwd<<<blocks((long)B * m->O, 128), 128, 0, m->s>>>(w.a2, P + offW3(m), P + offb3(m), w.y, w.y, B, m->H, m->O, 0);
+}
+
+// gradient of the mean squared error into m->d_g; per-sample losses in w.lossb
+void backward(gbfmm_mlp* m, const WS& w, int B)
+{
+    const float* P = m->d_p;
+    float* G = m->d_g;
+    g_kernel_launches.fetch_add(8);
+    k_mse<<<blocks(B, 128), 128, 0, m->s>>>(w.y, w.t, w.dy, w.lossb, B, m->O);
+    k_dense_bwd_w<<<blocks((long)m->O * (m->H + 1), 128), 128, 0, m->s>>>(w.dy, w.a2, G + offW3(m), G + offb3(m), B, m->H, m->O);
+    k_dense_bwd_x<<<blocks((long)B * m->H, 128), 128, 0, m->s>>>(w.dy, P + offW3(m), w.d2, B, m->H, m->O);
+    k_act_bwd<<<blocks((long)B * m->H, 128), 128, 0, m->s>>>(w.d2, w.pre2, B * m->H, 1);
+    k_dense_bwd_w<<<blocks((long)m->H * (m->H + 1), 128), 128, 0, m->s>>>(w.d2, w.a1, G + offW2(m), G + offb2(m), B, m->H, m->H);
+    k_dense_bwd_x<<<blocks((long)B * m->H, 128), 128, 0, m->s>>>(w.d2, P + offW2(m), w.d1, B, m->H, m->H);
+    k_act_bwd<<<blocks((long)B * m->H, 128), 128, 0, m->s>>>(w.d1, w.pre1, B * m->H, 1);
+    k_dense_bwd_w<<<blocks((long)m->H * (m->I + 1), 128), 128, 0, m->s>>>(w.d1, w.x, G + offW1(m), G + offb1(m), B, m->I, m->H);
+}
+
+std::vector<float> normalise(const gbfmm_mlp* m, const float* x, int B, int D, const std::vector<float>& mu,
+                             const std::vector<float>& sd)
+{
+    std::vector<float> out((size_t)B * D);
+    for (int b = 0; b < B; b++)
+        for (int i = 0; i < D; i++) {
+            float s = sd.empty() ? 1.f : sd[i];
+            float u = mu.empty() ? 0.f : mu[i];
+            out[(size_t)b * D + i] = (x[(size_t)b * D + i] - u) / (s > 0 ? s : 1.f);
+        }
+    return out;
+}
+
+}  // namespace
+
+extern "C" int gbfmm_mlp_create(int n_in, int n_hidden, int n_out, unsigned long long seed, gbfmm_mlp** out)
+{
+    if (!out || n_in <= 0 || n_hidden <= 0 || n_out <= 0 || n_in > 4096 || n_hidden > 4096 || n_out > 64)
+        return GBFMM_ERR_ARG;
+    *out = nullptr;
+    gbfmm_mlp* m = new gbfmm_mlp();
+    m->I = n_in;
+    m->H = n_hidden;
+    m->O = n_out;
+    m->np = offb3(m) + n_out;
+    std::vector<float> p(m->np, 0.f);
+    std::mt19937_64 rng(seed);
+    auto fill = [&](int off, int fan_in, int count) {
+        std::normal_distribution<float> nd(0.f, 1.f / std::sqrt((float)fan_in));
+        for (int i = 0; i < count; i++) p[off + i] = nd(rng);
+    };
+    fill(offW1(m), n_in, n_hidden * n_in);
+    fill(offW2(m), n_hidden, n_hidden * n_hidden);
+    fill(offW3(m), n_hidden, n_out * n_hidden);
+    cudaError_t e = cudaStreamCreateWithFlags(&m->s, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&m->d_p, sizeof(float) * m->np * 4);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        if (m->s) cudaStreamDestroy(m->s);
+        delete m;
+        return status(e);
+    }
+    m->d_g = m->d_p + m->np;
+    m->d_m = m->d_g + m->np;
+    m->d_v = m->d_m + m->np;
+    cudaMemset(m->d_g, 0, sizeof(float) * m->np * 3);
+    cudaMemcpy(m->d_p, p.data(), sizeof(float) * m->np, cudaMemcpyHostToDevice);
+    *out = m;
+    return GBFMM_OK;
+}
+
+extern "C" int gbfmm_mlp_destroy(gbfmm_mlp* m)
+{
+    if (!m) return GBFMM_ERR_ARG;
+    cudaStreamSynchronize(m->s);
+    cudaFree(m->d_p);
+    if (m->ws) cudaFree(m->ws);
+    cudaStreamDestroy(m->s);
+    delete m;
+    return GBFMM_OK;
+}
+
+extern "C" int gbfmm_mlp_num_params(gbfmm_mlp* m, int* n)
+{
+    if (!m || !n) return GBFMM_ERR_ARG;
+    *n = m->np;
+    return GBFMM_OK;
+}
+
+extern "C" int gbfmm_mlp_get_params(gbfmm_mlp* m, float* p)
+{
+    if (!m || !p) return GBFMM_ERR_ARG;
+    return status(cudaMemcpy(p, m->d_p, sizeof(float) * m->np, cudaMemcpyDeviceToHost));
+}
+
+extern "C" int gbfmm_mlp_set_params(gbfmm_mlp* m, const float* p)
+{
+    if (!m || !p) return GBFMM_ERR_ARG;
+    return status(cudaMemcpy(m->d_p, p, sizeof(float) * m->np, cudaMemcpyHostToDevice));
+}
+
+extern "C" int gbfmm_mlp_set_normalization(gbfmm_mlp* m, const float* x_mean, const float* x_std, const float* y_mean,
+                                           const float* y_std)
+{
+    if (!m) return GBFMM_ERR_ARG;
+    m->xm.assign(x_mean, x_mean + m->I);
+    m->xs.assign(x_std, x_std + m->I);
+    m->ym.assign(y_mean, y_mean + m->O);
+    m->ys.assign(y_std, y_std + m->O);
+    return GBFMM_OK;
+}
+
+// Raw network (no normalisation): forward of B rows of x (host), y out (host).
+extern "C" int gbfmm_mlp_forward(gbfmm_mlp* m, const float* x, int B, float* y)
+{
+    if (!m || !x || !y || B <= 0) return GBFMM_ERR_ARG;
+    int rc = ensure_ws(m, B);
+    if (rc) return rc;
+    WS w = layout(m);
+    cudaMemcpyAsync(w.x, x, sizeof(float) * B * m->I, cudaMemcpyHostToDevice, m->s);
+    forward(m, w, B);
+    cudaMemcpyAsync(y, w.y, sizeof(float) * B * m->O, cudaMemcpyDeviceToHost, m->s);
+    return status(cudaStreamSynchronize(m->s));
+}
+
+// Raw network: loss = mean over rows of sum_j (y - t)^2 and its gradient w.r.t.
+// every parameter (grad may be NULL).
+extern "C" int gbfmm_mlp_loss_grad(gbfmm_mlp* m, const float* x, const float* t, int B, double* loss, float* grad)
+{
+    if (!m || !x || !t || B <= 0) return GBFMM_ERR_ARG;
+    int rc = ensure_ws(m, B);
+    if (rc) return rc;
+    WS w = layout(m);
+    cudaMemcpyAsync(w.x, x, sizeof(float) * B * m->I, cudaMemcpyHostToDevice, m->s);
+    cudaMemcpyAsync(w.t, t, sizeof(float) * B * m->O, cudaMemcpyHostToDevice, m->s);
+    forward(m, w, B);
+    backward(m, w, B);
+    std::vector<float> lb(B);
+    cudaMemcpyAsync(lb.data(), w.lossb, sizeof(float) * B, cudaMemcpyDeviceToHost, m->s);
+    if (grad) cudaMemcpyAsync(grad, m->d_g, sizeof(float) * m->np, cudaMemcpyDeviceToHost, m->s);
+    rc = status(cudaStreamSynchronize(m->s));
+    if (rc) return rc;
+    if (loss) {
+        double s = 0;
+        for (int b = 0; b < B; b++) s += lb[b];
+        *loss = s;
+    }
+    return GBFMM_OK;
+}
+
+// Adam on normalised data (the stored normalisation is applied to x and t).
+extern "C" int gbfmm_mlp_train(gbfmm_mlp* m, const float* x, const float* t, int n, int epochs, int batch, float lr,
+                               unsigned long long seed, double* final_loss)
+{
+    if (!m || !x || !t || n <= 0 || epochs <= 0 || batch <= 0) return GBFMM_ERR_ARG;
+    const int B = std::min(batch, n);
+    int rc = ensure_ws(m, B);
+    if (rc) return rc;
+    WS w = layout(m);
+    std::vector<float> xn = normalise(m, x, n, m->I, m->xm, m->xs);
+    std::vector<float> tn = normalise(m, t, n, m->O, m->ym, m->ys);
+    std::vector<int> perm(n);
+    for (int i = 0; i < n; i++) perm[i] = i;
+    std::mt19937_64 rng(seed);
+    std::vector<float> bx((size_t)B * m->I), bt((size_t)B * m->O), lb(B);
+    double last = 0;
+    for (int ep = 0; ep < epochs; ep++) {
+        std::shuffle(perm.begin(), perm.end(), rng);
+        double eloss = 0;
+        int nb = 0;
+        for (int s0 = 0; s0 + B <= n; s0 += B) {
+            for (int b = 0; b < B; b++) {
+                std::memcpy(&bx[(size_t)b * m->I], &xn[(size_t)perm[s0 + b] * m->I], sizeof(float) * m->I);
+                std::memcpy(&bt[(size_t)b * m->O], &tn[(size_t)perm[s0 + b] * m->O], sizeof(float) * m->O);
+            }
+            cudaMemcpyAsync(w.x, bx.data(), sizeof(float) * B * m->I, cudaMemcpyHostToDevice, m->s);
+            cudaMemcpyAsync(w.t, bt.data(), sizeof(float) * B * m->O, cudaMemcpyHostToDevice, m->s);
+            forward(m, w, B);
+            backward(m, w, B);
+            m->adam_t++;
+            const float b1 = 0.9f, b2 = 0.999f;
+            const float c1 = 1.f - std::pow(b1, (float)m->adam_t), c2 = 1.f - std::pow(b2, (float)m->adam_t);
+            g_kernel_launches.fetch_add(1);
+            k_adam<<<blocks(m->np, 256), 256, 0, m->s>>>(m->d_p, m->d_g, m->d_m, m->d_v, m->np, lr, b1, b2, 1e-8f, c1,
+                                                         c2);
+            cudaMemcpyAsync(lb.data(), w.lossb, sizeof(float) * B, cudaMemcpyDeviceToHost, m->s);
+            rc = status(cudaStreamSynchronize(m->s));
+            if (rc) return rc;
+            for (int b = 0; b < B; b++) eloss += lb[b];
+            nb++;
+        }
+        last = nb ? eloss / nb : 0;
+    }
+    if (final_loss) *final_loss = last;
+    return GBFMM_OK;
+}
+
+// Prediction in physical units (normalisation applied both ways).
+extern "C" int gbfmm_mlp_predict(gbfmm_mlp* m, const float* x, int B, float* y)
+{
+    if (!m || !x || !y || B <= 0) return GBFMM_ERR_ARG;
+    std::vector<float> xn = normalise(m, x, B, m->I, m->xm, m->xs);
+    int rc = gbfmm_mlp_forward(m, xn.data(), B, y);
+    if (rc) return rc;
+    for (int b = 0; b < B; b++)
+        for (int j = 0; j < m->O; j++) {
+            float s = m->ys.empty() ? 1.f : m->ys[j], u = m->ym.empty() ? 0.f : m->ym[j];
+            y[(size_t)b * m->O + j] = y[(size_t)b * m->O + j] * s + u;
+        }
+    return GBFMM_OK;
+}
+
+// Candidate encoding appended to the statistics.  The precision enters as the
+// mantissa bits its M2L operands carry, over 24: FP32 1, BF16X3 (hi+lo split)
+// 16/24, BF16X1 8/24.
+static void candidate_input(const float* feat, int P, int D, int prec, float* row)
+{
+    std::memcpy(row, feat, sizeof(float) * GBFMM_NFEAT);
+    const double N = std::pow(10.0, feat[0]);
+    row[GBFMM_NFEAT + 0] = P / 10.f;
+    row[GBFMM_NFEAT + 1] = D / 6.f;
+    row[GBFMM_NFEAT + 2] = prec == GBFMM_PREC_BF16X1 ? 8.f / 24.f : (prec == GBFMM_PREC_BF16X3 ? 16.f / 24.f : 1.f);
+    row[GBFMM_NFEAT + 3] = (float)(std::log2(N / std::pow(8.0, D)) / 5.0);
+}
+
+extern "C" int gbfmm_tuner_input(const float* feat, int order, int depth, int precision, float* row)
+{
+    if (!feat || !row || precision < GBFMM_PREC_FP32 || precision > GBFMM_PREC_BF16X1) return GBFMM_ERR_ARG;
+    candidate_input(feat, order, depth, precision, row);
+    return GBFMM_OK;
+}
+
+// Proposes the candidate with the smallest predicted time whose predicted error,
+// inflated by 'margin' (>= 1), stays within tol.  Candidates: orders 4..10,
+// depths 1..7 with 2 to 200 bodies per leaf, precisions BF16X1 and BF16X3.
+extern "C" int gbfmm_tuner_propose(gbfmm_mlp* m, const float* feat, double tol, double margin, int* order, int* depth,
+                                   int* precision, float* pred_err, float* pred_ms)
+{
+    if (!m || !feat || !order || !depth || !precision || tol <= 0) return GBFMM_ERR_ARG;
+    if (m->I != GBFMM_NFEAT + 4 || m->O != 2) return GBFMM_ERR_ARG;
+    const double N = std::pow(10.0, feat[0]);
+    std::vector<float> rows;
+    std::vector<int> cand;
+    for (int D = 1; D <= 7; D++) {
+        const double per = N / std::pow(8.0, D);
+        if (per < 2 || per > 200) continue;
+        for (int P = 4; P <= 10; P++)
+            for (int prec = GBFMM_PREC_BF16X3; prec <= GBFMM_PREC_BF16X1; prec++) {
+                std::vector<float> r(m->I);
+                candidate_input(feat, P, D, prec, r.data());
+                rows.insert(rows.end(), r.begin(), r.end());
+                cand.push_back(P | (D << 8) | (prec << 16));
+            }
+    }
+    if (cand.empty()) return GBFMM_ERR_ARG;
+    std::vector<float> y(cand.size() * 2);
+    int rc = gbfmm_mlp_predict(m, rows.data(), (int)cand.size(), y.data());
+    if (rc) return rc;
+    int best = -1;
+    const double lt = std::log10(tol / std::max(margin, 1.0));
+    for (size_t c = 0; c < cand.size(); c++)
+        if (y[2 * c] <= lt && (best < 0 || y[2 * c + 1] < y[2 * best + 1])) best = (int)c;
+    if (best < 0) return GBFMM_ERR_UNSUPPORTED;  // nothing predicted to meet the tolerance
+    *order = cand[best] & 0xff;
+    *depth = (cand[best] >> 8) & 0xff;
+    *precision = (cand[best] >> 16) & 0xff;
+    if (pred_err) *pred_err = (float)std::pow(10.0, y[2 * best]);
+    if (pred_ms) *pred_ms = (float)std::pow(10.0, y[2 * best + 1]);
+    return GBFMM_OK;
+}
+
+// Weights file: "GBFMMMLP", version, I, H, O, params, normalisation, FNV-1a 64 checksum.
+static uint64_t fnv1a(const void* p, size_t n, uint64_t h = 1469598103934665603ull)
+{
+    const unsigned char* c = (const unsigned char*)p;
+    for (size_t i = 0; i < n; i++) {
+        h ^= c[i];
+        h *= 1099511628211ull;
+    }
+    return h;
+}
+
+extern "C" int gbfmm_mlp_save(gbfmm_mlp* m, const char* path)
+{
+    if (!m || !path) return GBFMM_ERR_ARG;
+    std::vector<float> p(m->np);
+    int rc = gbfmm_mlp_get_params(m, p.data());
+    if (rc) return rc;
+    // normalisation: x mean, x std, y mean, y std (identity where unset)
+    std::vector<float> nrm;
+    auto put = [&](const std::vector<float>& v, int n, float unset) {
+        for (int i = 0; i < n; i++) nrm.push_back(v.empty() ? unset : v[i]);
+    };
+    put(m->xm, m->I, 0.f);
+    put(m->xs, m->I, 1.f);
+    put(m->ym, m->O, 0.f);
+    put(m->ys, m->O, 1.f);
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return GBFMM_ERR_ARG;
+    const char magic[8] = {'G', 'B', 'F', 'M', 'M', 'M', 'L', 'P'};
+    const int32_t hdr[4] = {1, m->I, m->H, m->O};
+    uint64_t h = fnv1a(hdr, sizeof(hdr));
+    h = fnv1a(p.data(), sizeof(float) * p.size(), h);
+    h = fnv1a(nrm.data(), sizeof(float) * nrm.size(), h);
+    bool ok = std::fwrite(magic, 1, 8, f) == 8 && std::fwrite(hdr, sizeof(hdr), 1, f) == 1 &&
+              std::fwrite(p.data(), sizeof(float), p.size(), f) == p.size() &&
+              std::fwrite(nrm.data(), sizeof(float), nrm.size(), f) == nrm.size() && std::fwrite(&h, 8, 1, f) == 1;
+    std::fclose(f);
+    return ok ? GBFMM_OK : GBFMM_ERR_ARG;
+}
+
+extern "C" int gbfmm_mlp_load(const char* path, gbfmm_mlp** out)
+{
+    if (!path || !out) return GBFMM_ERR_ARG;
+    *out = nullptr;
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return GBFMM_ERR_ARG;
+    char magic[8];
+    int32_t hdr[4];
+    bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, "GBFMMMLP", 8) == 0 &&
+              std::fread(hdr, sizeof(hdr), 1, f) == 1 && hdr[0] == 1 && hdr[1] > 0 && hdr[2] > 0 && hdr[3] > 0 &&
+              hdr[1] <= 4096 && hdr[2] <= 4096 && hdr[3] <= 64;
+    if (!ok) {
+        std::fclose(f);
+        return GBFMM_ERR_ARG;
+    }
+    gbfmm_mlp* m = nullptr;
+    int rc = gbfmm_mlp_create(hdr[1], hdr[2], hdr[3], 0, &m);
+    if (rc) {
+        std::fclose(f);
+        return rc;
+    }
+    std::vector<float> p(m->np), nrm(2 * (size_t)m->I + 2 * (size_t)m->O);
+    uint64_t h_file = 0;
+    ok = std::fread(p.data(), sizeof(float), p.size(), f) == p.size() &&
+         std::fread(nrm.data(), sizeof(float), nrm.size(), f) == nrm.size() && std::fread(&h_file, 8, 1, f) == 1;
+    std::fclose(f);
+    uint64_t h = fnv1a(hdr, sizeof(hdr));
+    h = fnv1a(p.data(), sizeof(float) * p.size(), h);
+    h = fnv1a(nrm.data(), sizeof(float) * nrm.size(), h);
+    if (!ok || h != h_file) {
+        gbfmm_mlp_destroy(m);
+        return GBFMM_ERR_ARG;  // truncated or corrupted file
+    }
+    gbfmm_mlp_set_params(m, p.data());
+    const float* q = nrm.data();
+    gbfmm_mlp_set_normalization(m, q, q + m->I, q + 2 * m->I, q + 2 * m->I + m->O);
+    *out = m;
+    return GBFMM_OK;
+}

@@ -135,6 +135,48 @@ int gbfmm_get_lists(gbfmm_handle* h, int which, long* count, int* target, int* s
 /* The same lists without a handle (host only): tree depth and image levels. */
 int gbfmm_lists(int max_depth, int images, int which, long* count, int* target, int* source, int* offset3);
 
+/* ---- learned parameter selection ---- */
+
+/* Per-step statistics of a system (no counterpart in the reference, which fixes
+ * P=10 and depth 3, zeta_fmm_solver.cpp:10-11): GBFMM_NFEAT floats -- log N,
+ * log density, log L, mean q^2, net-charge and dipole ratios, and the body
+ * occupancy histograms of octree levels 2..6 -- computed on the GPU from device
+ * coordinates and charges.  Written to host memory 'features'. */
+#define GBFMM_NFEAT 56
+int gbfmm_features(const void* coords, const void* charges, int natoms, const float* box, float* features,
+                   void* stream);
+
+/* A small MLP (n_in -> n_hidden -> n_hidden -> n_out, tanh) whose forward,
+ * backward and Adam kernels are this library's own.  Parameters are laid out as
+ * W1 b1 W2 b2 W3 b3 (row-major W[out][in]). */
+typedef struct gbfmm_mlp gbfmm_mlp;
+int gbfmm_mlp_create(int n_in, int n_hidden, int n_out, unsigned long long seed, gbfmm_mlp** out);
+int gbfmm_mlp_destroy(gbfmm_mlp* m);
+int gbfmm_mlp_num_params(gbfmm_mlp* m, int* n);
+int gbfmm_mlp_get_params(gbfmm_mlp* m, float* params);
+int gbfmm_mlp_set_params(gbfmm_mlp* m, const float* params);
+int gbfmm_mlp_set_normalization(gbfmm_mlp* m, const float* x_mean, const float* x_std, const float* y_mean,
+                                const float* y_std);
+/* Raw network on host rows x[B][n_in] -> y[B][n_out]. */
+int gbfmm_mlp_forward(gbfmm_mlp* m, const float* x, int batch, float* y);
+/* Raw network: loss = mean_b sum_j (y - t)^2 and its gradient (grad may be NULL). */
+int gbfmm_mlp_loss_grad(gbfmm_mlp* m, const float* x, const float* t, int batch, double* loss, float* grad);
+/* Adam training on normalised data (the stored normalisation is applied). */
+int gbfmm_mlp_train(gbfmm_mlp* m, const float* x, const float* t, int n, int epochs, int batch, float lr,
+                    unsigned long long seed, double* final_loss);
+/* Prediction in physical units (normalisation applied to inputs and outputs). */
+int gbfmm_mlp_predict(gbfmm_mlp* m, const float* x, int batch, float* y);
+/* Versioned weights file with an FNV-1a checksum; load rejects corrupted files. */
+int gbfmm_mlp_save(gbfmm_mlp* m, const char* path);
+int gbfmm_mlp_load(const char* path, gbfmm_mlp** out);
+/* Input row of the tuner network: statistics ++ encoding of (order, depth, precision). */
+int gbfmm_tuner_input(const float* features, int order, int depth, int precision, float* row);
+/* Proposes (order, depth, precision) with the smallest predicted time whose predicted
+ * relative force error times 'margin' is within 'tol'.  GBFMM_ERR_UNSUPPORTED if no
+ * candidate is predicted to meet it (the caller then keeps the plain FMM). */
+int gbfmm_tuner_propose(gbfmm_mlp* m, const float* features, double tol, double margin, int* order, int* depth,
+                        int* precision, float* pred_err, float* pred_ms);
+
 /* ---- tree build without allocation ---- */
 
 /* No counterpart in the reference.  For callers that cannot allocate device
@@ -170,10 +212,12 @@ int gbfmm_debug_harmonics(int order, int kind, const double* d, double* out);
 /* Many independent cubic systems solved as one batch through one captured
  * CUDA graph.  Host inputs: offsets[n_sys+1] into the concatenated coords
  * (3 floats per atom) and charges, boxes[n_sys] (cubic edge, nm), per-system
- * order and depth.  Outputs (host): forces, potentials, energies[n_sys]. */
+ * order and depth; flags as gbfmm_params.flags (GBFMM_FLAG_NO_GRAPH is
+ * ignored: a batch always replays its graph).  Outputs (host): forces,
+ * potentials, energies[n_sys]. */
 typedef struct gbfmm_batch gbfmm_batch;
 int gbfmm_batch_create(int n_sys, const int* atom_offsets, const int* orders, const int* depths, int images,
-                       int precision, gbfmm_batch** out);
+                       int precision, int flags, gbfmm_batch** out);
 int gbfmm_batch_execute(gbfmm_batch* b, const float* coords, const float* charges, const float* box_edges,
                         float* forces, float* potentials, double* energies);
 int gbfmm_batch_execute_device(gbfmm_batch* b, const void* d_coords, const void* d_charges,

@@ -1,0 +1,78 @@
+"""Batched solves: independent systems of uneven sizes, each with its own order
+and depth, through one CUDA graph.  With GBFMM_FLAG_DETERMINISTIC each system's
+result must equal a separate deterministic single-system solve bit for bit
+(same kernels, same summation order); without it the split-entry M2L adds with
+atomics, so the comparison is at FP32 rounding level.  Both are checked against
+the FP64 oracle."""
+import numpy as np
+import pytest
+
+from conftest import rel_rms
+
+pytestmark = pytest.mark.gpu
+
+
+def _systems(systems):
+    specs = [(1200, 2.5, 6, 2, 3), (400, 1.7, 8, 2, 1), (3000, 3.3, 5, 3, 6), (150, 1.2, 4, 1, 0),
+             (2200, 2.9, 7, 3, 4)]
+    out = []
+    for k, (nsite, L, P, D, ions) in enumerate(specs):
+        xyz, q, box = systems.water_ion_box(nsite, L, n_na=ions, n_cl=ions, seed=100 + k)
+        out.append((xyz, q, float(box[0]), P, D))
+    return out
+
+
+@pytest.mark.parametrize("precision,det", [(0, True), (1, True), (0, False)])
+def test_batch_matches_single_solves_and_oracle(pkg, oracle, systems, precision, det):
+    sy = _systems(systems)
+    flags = pkg.FLAG_DETERMINISTIC if det else 0
+    b = pkg.BatchSolver([len(s[1]) for s in sy], [s[3] for s in sy], [s[4] for s in sy], images=4,
+                        precision=precision, flags=flags)
+    X = np.concatenate([s[0] for s in sy])
+    Q = np.concatenate([s[1] for s in sy])
+    B = np.array([s[2] for s in sy], np.float32)
+    for _ in range(2):  # the second call replays the captured graph
+        f, p, e = b.execute(X, Q, B)
+    off = b.offsets
+    tol = 1e-5 if precision == 0 else 1e-4
+    for i, (xyz, q, L, P, D) in enumerate(sy):
+        s = pkg.ZetaFmmSolver(len(q), q, order=P, max_depth=D, images=4, precision=precision, flags=flags)
+        s.execute(xyz, L)
+        fi, pi = f[off[i]:off[i + 1]], p[off[i]:off[i + 1]]
+        if det:
+            assert np.array_equal(fi, s.forces())
+            assert np.array_equal(pi, s.potentials())
+            assert e[i] == s.get_energy()
+        else:
+            assert rel_rms(fi, s.forces()) < 2e-6
+            assert rel_rms(pi, s.potentials()) < 2e-6
+            assert abs(e[i] - s.get_energy()) <= 2e-6 * abs(e[i])
+        po, fo, eo = oracle.zeta_solve(xyz.astype(np.float64), q.astype(np.float64), L, P, D, 4)
+        assert rel_rms(fi, fo) < tol
+        assert abs(e[i] - eo) / abs(eo) < tol
+        s.close()
+    b.close()
+
+
+def test_batch_device_path_follows_new_coordinates(pkg, systems):
+    torch = pytest.importorskip("torch")
+    sy = _systems(systems)[:3]
+    b = pkg.BatchSolver([len(s[1]) for s in sy], [s[3] for s in sy], [s[4] for s in sy])
+    X = np.concatenate([s[0] for s in sy])
+    Q = np.concatenate([s[1] for s in sy])
+    B = np.array([s[2] for s in sy], np.float32)
+    f1, _, _ = b.execute(X, Q, B)
+    X2 = (X * np.float32(1.03)).astype(np.float32)
+    B2 = (B * np.float32(1.03)).astype(np.float32)
+    xd = torch.from_numpy(X2).cuda()
+    qd = torch.from_numpy(Q).cuda()
+    st = torch.cuda.current_stream()
+    b.execute_device(xd.data_ptr(), qd.data_ptr(), B2, st.cuda_stream)
+    st.synchronize()
+    f2, _, _ = b.execute(X2, Q, B2)
+    s = pkg.ZetaFmmSolver(len(sy[0][1]), sy[0][1], order=sy[0][3], max_depth=sy[0][4])
+    s.execute(X2[:len(sy[0][1])], float(B2[0]))
+    assert rel_rms(f2[:len(sy[0][1])], s.forces()) < 2e-6
+    assert rel_rms(f1, f2) > 1e-3  # the new coordinates were used
+    s.close()
+    b.close()
