@@ -7,6 +7,7 @@
 //              rows indexed by Morton code
 //   root       M~_0, L~_0 in FP64 (plus an FP32 copy of M~_0 for level-1 M2L)
 //   field      float4 (phi, grad) per body in tree order, scaled units
+#include <algorithm>
 #include <cuda_runtime.h>
 
 #include <atomic>
@@ -420,60 +421,129 @@ __device__ __forceinline__ float rsqrt_approx(float x)
     return y;
 }
 
+// Packed FP32 pairs (PTX .f32x2, sm_100 and later): two lanes of FP32 work per
+// instruction.  A b64 register holds (a, b).
+typedef unsigned long long f2_t;
+__device__ __forceinline__ f2_t f2_pack(float a, float b)
+{
+    f2_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void f2_unpack(f2_t v, float& a, float& b)
+{
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ f2_t f2_sub(f2_t a, f2_t b)
+{
+    f2_t d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2_t f2_add(f2_t a, f2_t b)
+{
+    f2_t d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2_t f2_mul(f2_t a, f2_t b)
+{
+    f2_t d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2_t f2_fma(f2_t a, f2_t b, f2_t c)
+{
+    f2_t d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+
+// Staged sources, two per record: {x_a, x_b, y_a, y_b}, {z_a, z_b, q_a, q_b}.
+// Padding sources sit far away (1e15, scaled units) with zero charge, so that
+// they add exact zeros without a test.
+constexpr float P2P_FAR = 1e15f;
+
 // K targets per thread (i, i+8, ..., i+8(K-1) of the cluster) against this
-// warp's source steps [sb, se); lane jj takes source 4 st + jj of each step.
-// Pair term as kernel.cu:480-490: phi += q/r, grad += q (x_j - x_i)/r^3,
-// skipped when r = 0 (a body with itself or a coincident body).
-template <int K>
-__device__ __forceinline__ void p2p_sweep(const float4* __restrict__ src, int sb, int se, int jj, const float4 (&xi)[K],
-                                          float (&acc)[K][4])
+// warp's source steps [sb, se); lane jj takes source pair 4 st + jj of each
+// step, two sources per packed instruction.  Pair term as kernel.cu:480-490:
+// phi += q/r, grad += q (x_j - x_i)/r^3, skipped when r = 0 (a body with itself
+// or a coincident body) where MASK is set.  Accumulates +q (x_i - x_j)/r^3; the
+// caller negates.
+template <int K, bool MASK>
+__device__ __forceinline__ void p2p_sweep(const float4* __restrict__ src, int sb, int se, int jj, const f2_t (&X)[K][3],
+                                          f2_t (&acc)[K][4])
 {
 #pragma unroll 2
     for (int st = sb; st < se; st++) {
-        const float4 s = src[4 * st + jj];
+        const float4 xy = src[2 * (4 * st + jj)];
+        const float4 zq = src[2 * (4 * st + jj) + 1];
+        const f2_t sx = f2_pack(xy.x, xy.y), sy = f2_pack(xy.z, xy.w), sz = f2_pack(zq.x, zq.y);
+        const f2_t sq = f2_pack(zq.z, zq.w);
 #pragma unroll
         for (int k = 0; k < K; k++) {
-            const float dx = xi[k].x - s.x, dy = xi[k].y - s.y, dz = xi[k].z - s.z;
-            const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            const float ri = r2 > 0.f ? rsqrt_approx(r2) : 0.f;
-            const float qr = s.w * ri;
-            acc[k][0] += qr;
-            const float q3 = qr * ri * ri;
-            acc[k][1] = fmaf(-q3, dx, acc[k][1]);
-            acc[k][2] = fmaf(-q3, dy, acc[k][2]);
-            acc[k][3] = fmaf(-q3, dz, acc[k][3]);
+            const f2_t dx = f2_sub(X[k][0], sx), dy = f2_sub(X[k][1], sy), dz = f2_sub(X[k][2], sz);
+            const f2_t r2 = f2_fma(dx, dx, f2_fma(dy, dy, f2_mul(dz, dz)));
+            float ra, rb;
+            f2_unpack(r2, ra, rb);
+            float ia = rsqrt_approx(ra), ib = rsqrt_approx(rb);
+            if (MASK) {
+                ia = ra > 0.f ? ia : 0.f;
+                ib = rb > 0.f ? ib : 0.f;
+            }
+            const f2_t ri = f2_pack(ia, ib);
+            const f2_t qr = f2_mul(sq, ri);
+            acc[k][0] = f2_add(acc[k][0], qr);
+            const f2_t q3 = f2_mul(qr, f2_mul(ri, ri));
+            acc[k][1] = f2_fma(q3, dx, acc[k][1]);
+            acc[k][2] = f2_fma(q3, dy, acc[k][2]);
+            acc[k][3] = f2_fma(q3, dz, acc[k][3]);
         }
     }
 }
 
-// One cluster of up to 8K targets starting at c0 (of this pass's ntc).
+// One cluster of up to 8K targets starting at c0 (of this pass's ntc); steps
+// below msteps need the r = 0 test.
 template <int K>
 __device__ __forceinline__ void p2p_cluster(const float4* __restrict__ src, const float4* __restrict__ tgt, int c0,
-                                            int ntc, int sb, int se, int lane, float4* part)
+                                            int ntc, int sb, int se, int msteps, int lane, float4* part)
 {
     const int ii = lane >> 2, jj = lane & 3;
-    float4 xi[K];
-    float acc[K][4];
+    f2_t X[K][3];
+    f2_t acc[K][4];
+    const f2_t zero = f2_pack(0.f, 0.f);
 #pragma unroll
     for (int k = 0; k < K; k++) {
-        xi[k] = tgt[min(c0 + ii + 8 * k, ntc - 1)];
-        acc[k][0] = acc[k][1] = acc[k][2] = acc[k][3] = 0.f;
+        const float4 a = tgt[min(c0 + ii + 8 * k, ntc - 1)];
+        X[k][0] = f2_pack(a.x, a.x);
+        X[k][1] = f2_pack(a.y, a.y);
+        X[k][2] = f2_pack(a.z, a.z);
+        acc[k][0] = acc[k][1] = acc[k][2] = acc[k][3] = zero;
     }
-    p2p_sweep<K>(src, sb, se, jj, xi, acc);
+    const int mid = min(max(msteps, sb), se);
+    p2p_sweep<K, true>(src, sb, mid, jj, X, acc);
+    p2p_sweep<K, false>(src, mid, se, jj, X, acc);
 #pragma unroll
     for (int k = 0; k < K; k++) {
+        float v[4];
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            float a, b;
+            f2_unpack(acc[k][c], a, b);
+            v[c] = a + b;
+        }
         // fixed butterfly over the 4 source lanes of each target
 #pragma unroll
         for (int o = 1; o < 4; o <<= 1)
 #pragma unroll
-            for (int c = 0; c < 4; c++) acc[k][c] += __shfl_xor_sync(0xffffffffu, acc[k][c], o);
+            for (int c = 0; c < 4; c++) v[c] += __shfl_xor_sync(0xffffffffu, v[c], o);
         const int t = c0 + ii + 8 * k;
         if (jj == 0 && t < ntc) {
             float4 pp = part[t];
-            pp.x += acc[k][0];
-            pp.y += acc[k][1];
-            pp.z += acc[k][2];
-            pp.w += acc[k][3];
+            pp.x += v[0];
+            pp.y -= v[1];
+            pp.z -= v[2];
+            pp.w -= v[3];
             part[t] = pp;
         }
     }
@@ -481,16 +551,23 @@ __device__ __forceinline__ void p2p_cluster(const float4* __restrict__ src, cons
 
 // One CTA per target leaf.  The source bodies of the 81 near leaves are staged in
 // shared memory, shifted into the target leaf's frame (scaled units, integer
-// offsets of the stencil, so the periodic shift is exact) and padded with zero
-// charges to a multiple of 4.  Lane = (target i = lane/4, source j = lane%4); a
-// thread carries up to 3 targets (clusters of 24), so every staged source it
-// loads serves 3 pairs.  Warp w sweeps a quarter of the sources; the 4 source
-// lanes of a target are reduced by shuffles and the per-warp partial sums are
-// added in warp order (deterministic).
+// offsets of the stencil, so the periodic shift is exact), two per record; the
+// target leaf itself is staged first (stencil entry 0).  Lane = (target i =
+// lane/4, source pair j = lane%4); a thread carries up to 3 targets (clusters of
+// 24).  Warp w sweeps a quarter of the sources; the 4 source lanes of a target
+// are reduced by shuffles and the per-warp partial sums are added in warp order
+// (deterministic).
+//
+// The r = 0 test is applied to the target leaf's own bodies only.  Bodies of two
+// different leaves cannot coincide when every staged body lies strictly inside
+// its leaf (|u| < 1/2 - 2^-20 in scaled units: the rounding of u and of the
+// integer shift is far below that margin); a CTA that stages any body outside
+// that range (bodies on or near a leaf face, or outside the box) applies the
+// test to every source.
 __global__ void __launch_bounds__(P2P_THREADS) k_p2p(const int* off, int depth, int periodic, const float4* atoms,
                                                      const int* stencil, int nst, float4* field)
 {
-    __shared__ float4 src[P2P_MAXS];
+    __shared__ float4 src[P2P_MAXS];      // P2P_MAXS sources in P2P_MAXS/2 records of two float4
     __shared__ float4 part[4][P2P_MAXT];  // per-warp partial sums, reduced in warp order
     __shared__ int e_off[128];
     __shared__ int e_beg[128];
@@ -538,37 +615,60 @@ __global__ void __launch_bounds__(P2P_THREADS) k_p2p(const int* off, int depth, 
         if (tid == 0) e_off[nst] = ws[0] + ws[1] + ws[2] + ws[3];
     }
     __syncthreads();
-    const int total = e_off[nst];
+    const int total = e_off[nst], nself = e_off[1];
+    float* srcf = reinterpret_cast<float*>(src);
+    // a target outside its leaf (outside the box) can meet the image of a body
+    // that lies well inside another leaf: then every pass takes the r = 0 test
+    bool tedge = false;
+    for (int i = tid; i < nt; i += P2P_THREADS) {
+        const float4 a = atoms[tb + i];
+        tedge |= fmaxf(fabsf(a.x), fmaxf(fabsf(a.y), fabsf(a.z))) >= 0.5f - 0x1p-20f;
+    }
+    const bool target_edge = __syncthreads_or(tedge) != 0;
     for (int t0 = 0; t0 < nt; t0 += P2P_MAXT) {
         const int ntc = min(P2P_MAXT, nt - t0);
         const float4* tgt = atoms + tb + t0;
         for (int i = tid; i < 4 * P2P_MAXT; i += P2P_THREADS) part[i / P2P_MAXT][i % P2P_MAXT] = make_float4(0.f, 0.f, 0.f, 0.f);
         for (int s0 = 0; s0 < total; s0 += P2P_MAXS) {
             const int ns = min(P2P_MAXS, total - s0);
-            const int ns4 = (ns + 3) & ~3;
+            const int ns8 = (ns + 7) & ~7;
             __syncthreads();
             // warp w copies whole source leaves w, w+4, ...: lane = body of the leaf,
-            // clipped to this pass's window [s0, s0+ns); zero-charge padding to ns4
+            // clipped to this pass's window [s0, s0+ns); far zero-charge padding to ns8
+            bool edge = false;
             for (int e = warp; e < nst; e += 4) {
                 const int b0 = max(e_off[e], s0), b1 = min(e_off[e + 1], s0 + ns);
                 const float4 d = e_d[e];
                 const int gb = e_beg[e] - e_off[e];
                 for (int g = b0 + lane; g < b1; g += 32) {
                     const float4 a = atoms[gb + g];
-                    src[g - s0] = make_float4(a.x + d.x, a.y + d.y, a.z + d.z, a.w);
+                    edge |= fmaxf(fabsf(a.x), fmaxf(fabsf(a.y), fabsf(a.z))) >= 0.5f - 0x1p-20f;
+                    const int r = g - s0;
+                    float* rec = srcf + 8 * (r >> 1) + (r & 1);
+                    rec[0] = a.x + d.x;
+                    rec[2] = a.y + d.y;
+                    rec[4] = a.z + d.z;
+                    rec[6] = a.w;
                 }
             }
-            if (tid < ns4 - ns) src[ns + tid] = make_float4(0.f, 0.f, 0.f, 0.f);
-            __syncthreads();
-            // this warp's quarter of the sources, in steps of 4
-            const int nsteps = ns4 >> 2;
+            if (tid < ns8 - ns) {
+                const int r = ns + tid;
+                float* rec = srcf + 8 * (r >> 1) + (r & 1);
+                rec[0] = rec[2] = rec[4] = P2P_FAR;
+                rec[6] = 0.f;
+            }
+            const bool any_edge = (__syncthreads_or(edge) != 0) || target_edge;
+            // this warp's quarter of the source steps (8 sources per step); the
+            // steps holding the target leaf's own bodies need the r = 0 test
+            const int nsteps = ns8 >> 3;
             const int per = (nsteps + 3) >> 2;
             const int sb = warp * per, se = min(nsteps, sb + per);
+            const int msteps = any_edge ? nsteps : max(0, (min(nself, s0 + ns) - s0 + 7) >> 3);
             for (int c0 = 0; c0 < ntc; c0 += 24) {
                 const int rem = ntc - c0;
-                if (rem > 16) p2p_cluster<3>(src, tgt, c0, ntc, sb, se, lane, part[warp]);
-                else if (rem > 8) p2p_cluster<2>(src, tgt, c0, ntc, sb, se, lane, part[warp]);
-                else p2p_cluster<1>(src, tgt, c0, ntc, sb, se, lane, part[warp]);
+                if (rem > 16) p2p_cluster<3>(src, tgt, c0, ntc, sb, se, msteps, lane, part[warp]);
+                else if (rem > 8) p2p_cluster<2>(src, tgt, c0, ntc, sb, se, msteps, lane, part[warp]);
+                else p2p_cluster<1>(src, tgt, c0, ntc, sb, se, msteps, lane, part[warp]);
             }
         }
         __syncthreads();
@@ -592,6 +692,74 @@ void launch_p2p(const int* offsets, int depth, int periodic, const float4* atoms
     int nleaf = 1 << (3 * depth);
     COUNT_LAUNCH();
     k_p2p<<<nleaf, P2P_THREADS, 0, s>>>(offsets, depth, periodic, atoms, stencil, nst, field);
+}
+
+// ------------------------------------------------------------------ M2M and L2L (one level per launch)
+
+// Scaled M2M and L2L operators are the same at every level (cell size of the
+// target level = 1): 8 dense R x R FP32 matrices, one per child octant, stored
+// transposed ([octant][column][row]) so that a warp, 32 consecutive output rows,
+// reads one line per column.  CTA = (32 rows) x (8 octants) of one parent cell:
+// every thread runs a short chain (one octant, at most R columns) and the work of
+// a level spreads over parents x ceil(R/32) CTAs.  Degree structure: an M2M output
+// row of degree j reads inputs of degree <= j, an L2L output row of degree j
+// inputs of degree >= j (kernel.cu:310-354, :408-454); both loops skip the zero
+// blocks.
+
+__device__ __forceinline__ int real_degree(int r) { return (int)sqrtf((float)r + 0.5f); }
+
+// M2M: M~_parent[r] = sum_oct sum_{c < (deg r + 1)^2} A_oct[r][c] M~_child(oct)[c];
+// the 8 children of a parent are Morton-consecutive.  The octant sum is taken in
+// octant order (deterministic).  grid = (nparent, ceil(R/32)), block = (32, 8).
+__global__ void __launch_bounds__(256) k_m2m(const float* __restrict__ Mc, float* __restrict__ Mp,
+                                             const float* __restrict__ At, int R, int Rpad)
+{
+    __shared__ float red[8][32];
+    const int o = threadIdx.y, r = blockIdx.y * 32 + threadIdx.x, p = blockIdx.x;
+    float acc = 0.f;
+    if (r < R) {
+        const int j = real_degree(r), cend = (j + 1) * (j + 1);
+        const float* a = At + (size_t)o * R * R + r;
+        const float* m = Mc + (size_t)(8 * p + o) * Rpad;
+#pragma unroll 4
+        for (int c = 0; c < cend; c++) acc = fmaf(a[(size_t)c * R], m[c], acc);
+    }
+    red[o][threadIdx.x] = acc;
+    __syncthreads();
+    if (o == 0 && r < R) {
+        float t = red[0][threadIdx.x];
+#pragma unroll
+        for (int k = 1; k < 8; k++) t += red[k][threadIdx.x];
+        Mp[(size_t)p * Rpad + r] = t;
+    }
+}
+
+// L2L: L~_child[r] += sum_{c >= (deg r)^2} A_oct[r][c] L~_parent[c], oct = the
+// child's octant.  grid = (nparent, ceil(R/32)), block = (32, 8 children).
+__global__ void __launch_bounds__(256) k_l2l(const float* __restrict__ Lp, float* __restrict__ Lc,
+                                             const float* __restrict__ At, int R, int Rpad)
+{
+    const int o = threadIdx.y, r = blockIdx.y * 32 + threadIdx.x, p = blockIdx.x;
+    if (r >= R) return;
+    const int j = real_degree(r);
+    const float* a = At + (size_t)o * R * R + r;
+    const float* l = Lp + (size_t)p * Rpad;
+    float acc = 0.f;
+#pragma unroll 4
+    for (int c = j * j; c < R; c++) acc = fmaf(a[(size_t)c * R], l[c], acc);
+    Lc[(size_t)(8 * p + o) * Rpad + r] += acc;
+}
+
+void launch_m2m(const float* M_child, float* M_parent, const float* At, int nparent, int R, int Rpad, cudaStream_t s)
+{
+    COUNT_LAUNCH();
+    k_m2m<<<dim3(nparent, (R + 31) / 32), dim3(32, 8), 0, s>>>(M_child, M_parent, At, R, Rpad);
+}
+
+void launch_l2l(const float* L_parent, float* L_child, const float* At, int nparent, int R, int Rpad, cudaStream_t s)
+{
+    COUNT_LAUNCH();
+    k_l2l<<<dim3(nparent, (R + 31) / 32), dim3(32, 8), 0, s>>>(L_parent, L_child, At, R, Rpad);
 }
 
 // ------------------------------------------------------------------ batched contraction (M2M, M2L, L2L)

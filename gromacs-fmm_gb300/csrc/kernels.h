@@ -95,6 +95,10 @@ void launch_l2p(int P, const int* offsets, int nleaf, const float4* atoms, const
 void launch_p2p(const int* offsets, int depth, int periodic, const float4* atoms, const int* stencil, int nst,
                 float4* field, cudaStream_t s);
 void launch_contract(const ContractArgs& a, int ntasks, cudaStream_t s);
+// One level of M2M (nparent parents from their 8 children each) or L2L (the 8
+// children of each of nparent parents); At = 8 transposed R x R scaled operators.
+void launch_m2m(const float* M_child, float* M_parent, const float* At, int nparent, int R, int Rpad, cudaStream_t s);
+void launch_l2l(const float* L_parent, float* L_child, const float* At, int nparent, int R, int Rpad, cudaStream_t s);
 
 struct RootArgs {
     int R, Rpad;

@@ -57,6 +57,7 @@ struct OpTables {
     int off_m2m[8], off_l2l[8];
     std::vector<int> off_cls;            // per M2L class
     std::vector<double> root_m2m, root_l2l, lattice;  // dense FP64 for the root
+    std::vector<float> m2m_t, l2l_t;     // dense FP32, [octant][column][row], levels >= 1
     WorkPartition part[3];
     // tensor-core M2L (orders <= TC_MAX_ORDER): chunk plan and class images
     TcPlan tc;
@@ -96,12 +97,20 @@ const OpTables* get_tables(int P, int images)
     };
     t->root_m2m.resize((size_t)8 * R * R);
     t->root_l2l.resize((size_t)8 * R * R);
+    t->m2m_t.assign((size_t)8 * R * R, 0.f);
+    t->l2l_t.assign((size_t)8 * R * R, 0.f);
+    auto transpose = [&](std::vector<float>& dst, int o) {
+        for (int r = 0; r < R; r++)
+            for (int c = 0; c < R; c++) dst[(size_t)o * R * R + (size_t)c * R + r] = (float)A[(size_t)r * R + c];
+    };
     for (int o = 0; o < 8; o++) {
         scaled_m2m(P, o, A.data());
         std::copy(A.begin(), A.end(), t->root_m2m.begin() + (size_t)o * R * R);
+        transpose(t->m2m_t, o);
         t->off_m2m[o] = append(t->plan[OP_M2M]);
         scaled_l2l(P, o, A.data());
         std::copy(A.begin(), A.end(), t->root_l2l.begin() + (size_t)o * R * R);
+        transpose(t->l2l_t, o);
         t->off_l2l[o] = append(t->plan[OP_L2L]);
     }
     t->off_cls.resize(t->st.classes.size());
@@ -151,6 +160,7 @@ struct gbfmm_handle {
     int* d_wb[3] = {};
     BlockInfo* d_blocks[3] = {};
     double *d_root_m2m = nullptr, *d_root_l2l = nullptr, *d_lattice = nullptr;
+    float *d_m2m_t = nullptr, *d_l2l_t = nullptr;
     int* d_p2p_st = nullptr;
     int n_p2p_st = 0;
     float *d_forces = nullptr, *d_pots = nullptr;
@@ -296,6 +306,8 @@ static int layout(gbfmm_handle* h, Arena& a)
     h->d_root_m2m = a.take<double>(t->root_m2m.size());
     h->d_root_l2l = a.take<double>(t->root_l2l.size());
     h->d_lattice = a.take<double>(t->lattice.size());
+    h->d_m2m_t = a.take<float>(t->m2m_t.size());
+    h->d_l2l_t = a.take<float>(t->l2l_t.size());
     h->d_p2p_st = a.take<int>(t->st.p2p.size());
     for (int k = 0; k < 3; k++) {
         h->d_items[k] = a.take<int4>(t->part[k].items.size() + 1);
@@ -563,10 +575,7 @@ static void enqueue_step(gbfmm_handle* h)
     mark(h, 1);
     launch_p2m(h->P, h->d_off, h->nleaf, h->d_atoms, h->Mlev[D], h->Rpad, s);
     mark(h, 2);
-    for (int k = D - 1; k >= 1; k--) {
-        ContractArgs a = contract_args(h, OP_M2M, 0, false, h->m2m_task0[k]);
-        launch_contract(a, h->m2m_ntask[k], s);
-    }
+    for (int k = D - 1; k >= 1; k--) launch_m2m(h->Mlev[k + 1], h->Mlev[k], h->d_m2m_t, 1 << (3 * k), h->R, h->Rpad, s);
     mark(h, 3);
     RootArgs ra;
     ra.R = h->R;
@@ -594,10 +603,7 @@ static void enqueue_step(gbfmm_handle* h)
     }
     mark(h, 5);
     launch_root_l2l(ra, s);
-    for (int k = 2; k <= D; k++) {
-        ContractArgs a = contract_args(h, OP_L2L, 1, true, h->l2l_task0[k]);
-        launch_contract(a, h->l2l_ntask[k], s);
-    }
+    for (int k = 2; k <= D; k++) launch_l2l(h->Llev[k - 1], h->Llev[k], h->d_l2l_t, 1 << (3 * (k - 1)), h->R, h->Rpad, s);
     mark(h, 6);
     launch_l2p(h->P, h->d_off, h->nleaf, h->d_atoms, h->Llev[D], h->Rpad, h->d_far, s);
     mark(h, 7);
@@ -686,9 +692,21 @@ extern "C" int gbfmm_create(const gbfmm_params* prm, int natoms, gbfmm_handle** 
     up(h->d_root_m2m, t->root_m2m.data(), sizeof(double) * t->root_m2m.size());
     up(h->d_root_l2l, t->root_l2l.data(), sizeof(double) * t->root_l2l.size());
     up(h->d_lattice, t->lattice.data(), sizeof(double) * t->lattice.size());
+    up(h->d_m2m_t, t->m2m_t.data(), sizeof(float) * t->m2m_t.size());
+    up(h->d_l2l_t, t->l2l_t.data(), sizeof(float) * t->l2l_t.size());
     if (h->tc) up(h->d_img, t->tc_img.data(), t->tc_img.size());
-    up(h->d_p2p_st, t->st.p2p.data(), sizeof(int) * t->st.p2p.size());
-    h->n_p2p_st = (int)t->st.p2p.size() / 3;
+    {
+        // the P2P kernel stages the target leaf itself first (entry 0): only its
+        // bodies can coincide with a target, so only they need the r = 0 test
+        std::vector<int> st = t->st.p2p;
+        for (size_t e = 0; e < st.size() / 3; e++)
+            if (st[3 * e] == 0 && st[3 * e + 1] == 0 && st[3 * e + 2] == 0) {
+                std::rotate(st.begin(), st.begin() + 3 * e, st.begin() + 3 * e + 3);
+                break;
+            }
+        up(h->d_p2p_st, st.data(), sizeof(int) * st.size());
+        h->n_p2p_st = (int)st.size() / 3;
+    }
     for (int k = 0; k < 3; k++) {
         std::vector<int4> it;
         for (const WorkItem& w : t->part[k].items) it.push_back(make_int4(w.blk, w.ca, w.cb, 0));

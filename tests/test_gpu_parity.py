@@ -84,6 +84,38 @@ def test_crowded_leaves(pkg, oracle, systems):
     s.close()
 
 
+@pytest.mark.parametrize("depth,images", [(3, 4), (1, 4), (2, 0)])
+def test_faces_outside_box_and_coincident_bodies(pkg, oracle, systems, depth, images):
+    """Bodies exactly on leaf faces, outside the box, coincident with another body
+    (r = 0: skipped), and two bodies that coincide only through the periodic
+    shift (exact in float and double: a 4 nm box).  Every r = 0 pair must be
+    skipped, as kernel.cu:480-490 does, wherever the two bodies are staged."""
+    xyz, q, box = systems.water_ion_box(2100, 4.0, n_na=5, n_cl=5, seed=21)
+    L = 4.0
+    h = L / 2 ** depth
+    rng = np.random.default_rng(3)
+    x = xyz.copy()
+    idx = rng.choice(len(q), 200, replace=False)
+    for k, i in enumerate(idx[:60]):           # on leaf faces, the box faces included
+        x[i, k % 3] = np.float32(h * rng.integers(0, 2 ** depth + 1))
+    for k, i in enumerate(idx[60:100]):        # just outside the box
+        x[i, k % 3] = np.float32(-0.0625 if k % 2 else L + 0.0625)
+    for k in range(10):                        # coincident pairs
+        x[idx[100 + k]] = x[idx[110 + k]]
+    for k in range(6):                         # coincident through the periodic shift
+        a, b = idx[120 + 2 * k], idx[121 + 2 * k]
+        d = k % 3
+        x[b] = x[a]
+        x[a, d] = np.float32(-0.125)
+        x[b, d] = np.float32(L - 0.125)
+    f, p, e, s = _solve(pkg, x, q, L, order=6, max_depth=depth, images=images)
+    assert np.isfinite(f).all() and np.isfinite(p).all()
+    po, fo, eo = oracle.zeta_solve(x.astype(np.float64), q.astype(np.float64), L, 6, depth, images)
+    assert rel_rms(f, fo) < TOL_F
+    assert rel_rms(p, po) < TOL_F
+    s.close()
+
+
 def test_device_execute_matches_host_execute(pkg, systems):
     torch = pytest.importorskip("torch")
     xyz, q, box = systems.water_ion_box(1200, 2.5, seed=12)
