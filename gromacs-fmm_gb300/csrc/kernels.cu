@@ -34,6 +34,20 @@ __global__ void __launch_bounds__(256) k_tree_keys(TreeArgs a)
     for (int i = threadIdx.x; i < 3 * nd; i += blockDim.x) ce[i] = sc->centre[i / nd][i % nd];
     const float inv_h = sc->inv_h;
     const float* coords = sc->coords;
+    if (threadIdx.x == 0) {
+        // L2 prefetch of the small operators and lists that the later stages
+        // read: 4 KB chunks, spread over the blocks (one chunk list per array)
+        for (int k = 0; k < TreeArgs::MAX_PREFETCH; k++) {
+            const char* base = static_cast<const char*>(a.pf[k]);
+            const unsigned long long bytes = a.pf_bytes[k] & ~15ull;
+            const unsigned long long chunks = (bytes + 4095) >> 12;
+            for (unsigned long long c = blockIdx.x; c < chunks; c += gridDim.x) {
+                const unsigned long long o = c << 12;
+                const unsigned sz = (unsigned)min(4096ull, bytes - o);
+                asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(base + o), "r"(sz) : "memory");
+            }
+        }
+    }
     __syncthreads();
     double s0 = 0, s1 = 0, s2 = 0, s3 = 0;
     int bad = 0;
@@ -84,6 +98,67 @@ __global__ void __launch_bounds__(256) k_tree_keys(TreeArgs a)
         a.partials[4 * blockIdx.x + threadIdx.x] = t;
     }
     if (bad) atomicOr(&a.flags[0], 1);
+    if (!a.done) return;
+    // last block: FP64 sums of the partials (fixed order) and the leaf scan
+    __shared__ int s_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(a.done, 1) == (int)gridDim.x - 1;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    if (warp < 4) {
+        // all loads issued before the fixed-order sum (one round trip)
+        constexpr int K = (TREE_MAX_BLOCKS + 31) / 32;
+        double v[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const int b = lane + 32 * k;
+            v[k] = b < (int)gridDim.x ? __ldcg(&a.partials[4 * b + warp]) : 0.0;
+        }
+        double t = 0;
+#pragma unroll
+        for (int k = 0; k < K; k++) t += v[k];
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (lane == 0) a.sums[warp] = t;
+    }
+    if (a.off) {
+        // exclusive scan of counts in tiles of 4096: thread t owns 16 consecutive
+        // leaves of a tile, loaded together
+        __shared__ int wsum[8];
+        __shared__ int carry_s;
+        const int n = a.nleaf;
+        int carry = 0;
+        for (int base = 0; base < n; base += 4096) {
+            const int b0 = base + 16 * threadIdx.x;
+            int c[16];
+#pragma unroll
+            for (int k = 0; k < 16; k++) c[k] = b0 + k < n ? __ldcg(&a.counts[b0 + k]) : 0;
+            int t = 0;
+#pragma unroll
+            for (int k = 0; k < 16; k++) t += c[k];
+            int x = t;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            if (lane == 31) wsum[warp] = x;
+            __syncthreads();
+            int run = carry + x - t;
+            for (int w = 0; w < warp; w++) run += wsum[w];
+#pragma unroll
+            for (int k = 0; k < 16; k++)
+                if (b0 + k < n) {
+                    a.off[b0 + k] = run;
+                    a.cursor[b0 + k] = run;
+                    run += c[k];
+                }
+            if (threadIdx.x == 255) carry_s = run;
+            __syncthreads();
+            carry = carry_s;
+        }
+        if (threadIdx.x == 0) a.off[n] = carry;
+    }
 }
 
 int tree_blocks(int n) { return n <= 0 ? 1 : (n + 255) / 256 < TREE_MAX_BLOCKS ? (n + 255) / 256 : TREE_MAX_BLOCKS; }
@@ -714,13 +789,20 @@ __device__ __forceinline__ int real_degree(int r) { return (int)sqrtf((float)r +
 __global__ void __launch_bounds__(256) k_m2m(const float* __restrict__ Mc, float* __restrict__ Mp,
                                              const float* __restrict__ At, int R, int Rpad)
 {
+    extern __shared__ float ms[];  // the 8 children, 8 x R
     __shared__ float red[8][32];
     const int o = threadIdx.y, r = blockIdx.y * 32 + threadIdx.x, p = blockIdx.x;
+    const int tid = threadIdx.y * 32 + threadIdx.x;
+    for (int i = tid; i < 8 * R; i += 256) {
+        const int oo = i / R;
+        ms[i] = Mc[(size_t)(8 * p + oo) * Rpad + (i - oo * R)];
+    }
+    __syncthreads();
     float acc = 0.f;
     if (r < R) {
         const int j = real_degree(r), cend = (j + 1) * (j + 1);
         const float* a = At + (size_t)o * R * R + r;
-        const float* m = Mc + (size_t)(8 * p + o) * Rpad;
+        const float* m = ms + o * R;
 #pragma unroll 4
         for (int c = 0; c < cend; c++) acc = fmaf(a[(size_t)c * R], m[c], acc);
     }
@@ -739,11 +821,15 @@ __global__ void __launch_bounds__(256) k_m2m(const float* __restrict__ Mc, float
 __global__ void __launch_bounds__(256) k_l2l(const float* __restrict__ Lp, float* __restrict__ Lc,
                                              const float* __restrict__ At, int R, int Rpad)
 {
+    extern __shared__ float ls[];  // the parent, R
     const int o = threadIdx.y, r = blockIdx.y * 32 + threadIdx.x, p = blockIdx.x;
+    const int tid = threadIdx.y * 32 + threadIdx.x;
+    for (int i = tid; i < R; i += 256) ls[i] = Lp[(size_t)p * Rpad + i];
+    __syncthreads();
     if (r >= R) return;
     const int j = real_degree(r);
     const float* a = At + (size_t)o * R * R + r;
-    const float* l = Lp + (size_t)p * Rpad;
+    const float* l = ls;
     float acc = 0.f;
 #pragma unroll 4
     for (int c = j * j; c < R; c++) acc = fmaf(a[(size_t)c * R], l[c], acc);
@@ -753,13 +839,13 @@ __global__ void __launch_bounds__(256) k_l2l(const float* __restrict__ Lp, float
 void launch_m2m(const float* M_child, float* M_parent, const float* At, int nparent, int R, int Rpad, cudaStream_t s)
 {
     COUNT_LAUNCH();
-    k_m2m<<<dim3(nparent, (R + 31) / 32), dim3(32, 8), 0, s>>>(M_child, M_parent, At, R, Rpad);
+    k_m2m<<<dim3(nparent, (R + 31) / 32), dim3(32, 8), sizeof(float) * 8 * R, s>>>(M_child, M_parent, At, R, Rpad);
 }
 
 void launch_l2l(const float* L_parent, float* L_child, const float* At, int nparent, int R, int Rpad, cudaStream_t s)
 {
     COUNT_LAUNCH();
-    k_l2l<<<dim3(nparent, (R + 31) / 32), dim3(32, 8), 0, s>>>(L_parent, L_child, At, R, Rpad);
+    k_l2l<<<dim3(nparent, (R + 31) / 32), dim3(32, 8), sizeof(float) * R, s>>>(L_parent, L_child, At, R, Rpad);
 }
 
 // ------------------------------------------------------------------ batched contraction (M2M, M2L, L2L)
@@ -1064,6 +1150,27 @@ __global__ void __launch_bounds__(256) k_finalize(FinalArgs a)
         for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w];
         a.partials[blockIdx.x] = t;
     }
+    if (!a.done) return;
+    // last block: the energy, partials summed in a fixed order
+    __shared__ int s_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(a.done, 1) == (int)gridDim.x - 1;
+    __syncthreads();
+    if (!s_last || threadIdx.x >= 32) return;
+    __threadfence();
+    constexpr int K = (FINAL_MAX_BLOCKS + 31) / 32;
+    double v[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        const int b = threadIdx.x + 32 * k;
+        v[k] = b < (int)gridDim.x ? __ldcg(&a.partials[b]) : 0.0;
+    }
+    double t = 0;
+#pragma unroll
+    for (int k = 0; k < K; k++) t += v[k];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (threadIdx.x == 0) *a.energy = t;
 }
 
 void launch_finalize(const FinalArgs& a, cudaStream_t s)

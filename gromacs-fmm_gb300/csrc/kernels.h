@@ -75,7 +75,23 @@ struct TreeArgs {
     int* counts;            // 8^D
     double* partials;       // per block: dipole (3) and total charge, FP64
     int* flags;             // [0] non-finite input seen
+    // Last-block epilogue (all NULL: none).  The last block to finish sums the
+    // partials into sums[4] (fixed order) and, when off != NULL, writes the
+    // exclusive scan of counts into off[0..nleaf] and cursor[0..nleaf).  done is
+    // a counter that is zero when the kernel starts.
+    int* done = nullptr;
+    double* sums = nullptr;
+    int* off = nullptr;
+    int* cursor = nullptr;
+    int nleaf = 0;
+    // Read-only data of the later stages, prefetched into L2 by block 0 at the
+    // start of the step (addresses 16-byte aligned, sizes rounded down to 16).
+    static constexpr int MAX_PREFETCH = 8;
+    const void* pf[MAX_PREFETCH] = {};
+    unsigned long long pf_bytes[MAX_PREFETCH] = {};
 };
+// Leaf counts up to this size are scanned by the tree-key kernel's last block.
+constexpr int TREE_EPILOGUE_MAX_LEAVES = 1 << 15;
 constexpr int TREE_MAX_BLOCKS = 4 * 152;
 constexpr int FINAL_MAX_BLOCKS = 4 * 152;
 void launch_sum_partials(const double* part, int nblocks, int width, double* out, cudaStream_t s);
@@ -129,6 +145,8 @@ struct FinalArgs {
     float* forces;           // 3N input order
     float* pots;             // N input order
     double* partials;        // per block: 0.5 * sum q * pot (FP64)
+    int* done = nullptr;     // zero at start: the last block sums the partials into *energy
+    double* energy = nullptr;
 };
 void launch_finalize(const FinalArgs& a, cudaStream_t s);
 

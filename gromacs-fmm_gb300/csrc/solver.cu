@@ -155,6 +155,7 @@ struct gbfmm_handle {
     double *d_M0 = nullptr, *d_L0 = nullptr;
     float* d_ops = nullptr;
     CEntry* d_entries = nullptr;
+    size_t tasks_bytes = 0;  // entries + tasks allocation
     CTask* d_tasks = nullptr;
     int4* d_items[3] = {};
     int* d_wb[3] = {};
@@ -275,7 +276,7 @@ static int layout(gbfmm_handle* h, Arena& a)
     h->d_q = a.take<float>(n);
     h->d_code = a.take<uint32_t>(n);
     h->d_uq = a.take<float4>(n);
-    h->d_counts = a.take<int>(h->nleaf + 1);
+    h->d_counts = a.take<int>(h->nleaf + 1 + 4);  // + the epilogue counters (zeroed per step)
     h->d_off = a.take<int>(h->nleaf + 1);
     h->d_cursor = a.take<int>(h->nleaf + 1);
     h->d_scan = a.take<int>((h->nleaf + 2047) / 2048 + 1);
@@ -473,7 +474,8 @@ static int build_tasks(gbfmm_handle* h)
         h->tc_ntask = (int)tasks.size() - tc_task0;
     }
     void* p = nullptr;
-    CK(cudaMalloc(&p, sizeof(CEntry) * ent.size() + sizeof(CTask) * tasks.size() + 512));
+    h->tasks_bytes = sizeof(CEntry) * ent.size() + sizeof(CTask) * tasks.size() + 512;
+    CK(cudaMalloc(&p, h->tasks_bytes));
     h->d_entries = (CEntry*)p;
     h->d_tasks = (CTask*)((char*)p + ((sizeof(CEntry) * ent.size() + 255) & ~(size_t)255));
     h->d_tc_tasks = h->d_tasks + tc_task0;
@@ -550,11 +552,10 @@ static void enqueue_step(gbfmm_handle* h)
     const int D = h->D, n = h->n;
     const long launches0 = g_kernel_launches.load();
     mark(h, 0);
-    cudaMemsetAsync(h->d_counts, 0, sizeof(int) * (h->nleaf + 1), s);
-    cudaMemsetAsync(h->d_sums, 0, sizeof(double) * 4, s);
-    cudaMemsetAsync(h->d_energy, 0, sizeof(double), s);
+    int* sync = h->d_counts + h->nleaf + 1;  // [0] tree keys, [1] finalize
+    cudaMemsetAsync(h->d_counts, 0, sizeof(int) * (h->nleaf + 1 + 4), s);
     cudaMemsetAsync(h->d_L, 0, sizeof(float) * h->lev_floats, s);
-    if (n > 0) {
+    {
         TreeArgs ta;
         ta.sc = h->d_sc;
         ta.charges = h->d_q;
@@ -565,11 +566,34 @@ static void enqueue_step(gbfmm_handle* h)
         ta.counts = h->d_counts;
         ta.partials = h->d_partials;
         ta.flags = h->d_flags;
+        ta.done = sync;
+        ta.sums = h->d_sums;
+        if (h->nleaf <= TREE_EPILOGUE_MAX_LEAVES) {
+            ta.off = h->d_off;
+            ta.cursor = h->d_cursor;
+            ta.nleaf = h->nleaf;
+        }
+        // the small operators and lists of the later stages (the application's
+        // other kernels evict them between steps)
+        int k = 0;
+        auto pf = [&](const void* p, size_t bytes) {
+            if (p && bytes >= 16 && k < TreeArgs::MAX_PREFETCH) {
+                ta.pf[k] = p;
+                ta.pf_bytes[k++] = bytes;
+            }
+        };
+        const OpTables* t = h->tab;
+        pf(h->d_m2m_t, sizeof(float) * t->m2m_t.size());
+        pf(h->d_root_m2m, sizeof(double) * (t->root_m2m.size() + t->root_l2l.size() + t->lattice.size()));
+        pf(h->d_l2l_t, sizeof(float) * t->l2l_t.size());
+        pf(h->d_entries, h->tasks_bytes);
+        pf(h->d_p2p_st, sizeof(int) * 3 * h->n_p2p_st);
         launch_tree_keys(ta, s);
-        launch_sum_partials(h->d_partials, tree_blocks(n), 4, h->d_sums, s);
+        if (!ta.off) {
+            launch_exclusive_scan(h->d_counts, h->d_off, h->nleaf, h->d_scan, s);
+            cudaMemcpyAsync(h->d_cursor, h->d_off, sizeof(int) * h->nleaf, cudaMemcpyDeviceToDevice, s);
+        }
     }
-    launch_exclusive_scan(h->d_counts, h->d_off, h->nleaf, h->d_scan, s);
-    cudaMemcpyAsync(h->d_cursor, h->d_off, sizeof(int) * h->nleaf, cudaMemcpyDeviceToDevice, s);
     launch_scatter(h->d_code, n, h->d_cursor, h->d_tmp, s);
     launch_leaf_sort(h->d_off, h->nleaf, h->d_tmp, h->d_uq, h->d_code, h->d_order, h->d_atoms, h->d_atom_leaf, s);
     mark(h, 1);
@@ -621,8 +645,11 @@ static void enqueue_step(gbfmm_handle* h)
         fa.forces = h->d_forces;
         fa.pots = h->d_pots;
         fa.partials = h->d_partials;
+        fa.done = sync + 1;
+        fa.energy = h->d_energy;
         launch_finalize(fa, s);
-        launch_sum_partials(h->d_partials, final_blocks(n), 1, h->d_energy, s);
+    } else {
+        cudaMemsetAsync(h->d_energy, 0, sizeof(double), s);
     }
     mark(h, 9);
     h->step_launches = (int)(g_kernel_launches.load() - launches0);
