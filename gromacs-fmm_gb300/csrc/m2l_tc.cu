@@ -1,8 +1,9 @@
 // Tensor-core M2L for sm_103a: tcgen05.mma (kind::f16, bf16 operands, FP32
 // accumulation in TMEM) with split-precision operands.
 //
-// One CTA owns 128 targets of one (level, octant) stencil (M = 128 rows of the
-// MMA = targets).  For each stencil entry e the CTA computes
+// One CTA owns a tile of up to 128 targets of one (level, octant): a box of
+// bx x by x bz parent cells (M = 128 rows of the MMA, one per target).  For each
+// stencil entry e of its range the CTA computes
 //     D[t][:] += M~_src(t,e)[:] . T~_class(e)^T
 // where the operator is split by output degree into "chunks": rows of degrees
 // j0..j1 only see input degrees n <= P - j0 (the j+n<=P truncation of
@@ -11,13 +12,17 @@
 // three products (hi*hi + hi*lo + lo*hi) keep ~16 bits (BF16X3), one product
 // (hi*hi) ~8 bits (BF16X1).
 //
-// Data movement per entry and stage (two stages):
-//   A (gathered source multipoles, 128 rows x K bf16, hi and lo): cp.async 16 B
-//     copies into the canonical 128B-swizzled K-major layout;
-//   B (operator chunk images, pre-swizzled on the host, hi and lo): one
-//     cp.async.bulk (TMA engine) completing on an mbarrier.
-// One thread issues the MMAs and commits them to the stage's "empty" mbarrier.
-// Every wait is bounded; on timeout the kernel records an error and finishes.
+// Data movement per entry and pipeline stage:
+//   A (source multipoles of the tile): the sources of a tile for one entry are a
+//     rectangular box of a halo-padded source grid (parity-split for same-level
+//     sources, natural for parent-level sources), loaded by ONE TMA tile copy per
+//     64-coefficient atom straight into the 128B-swizzled K-major layout;
+//   B (operator chunk images, pre-swizzled on the host): one cp.async.bulk.
+// One thread issues the copies, one thread the MMAs (committed to the stage's
+// "empty" mbarrier); four warps read TMEM and add to the target locals.  Every
+// wait is bounded; on timeout the kernel records an error and finishes.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -75,31 +80,27 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
                  : "memory");
 }
 
-__device__ __forceinline__ void cp_async16(void* dst, const void* src, bool valid)
+// TMA tile loads of the source grids, completing on an mbarrier (tx bytes).
+__device__ __forceinline__ void tma_load_5d(void* dst, const CUtensorMap* map, int c0, int c1, int c2, int c3, int c4,
+                                            uint64_t* bar)
 {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(valid ? 16 : 0)
-                 : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, "
+        "%6}], [%7];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(smem_u32(bar))
+        : "memory");
 }
 
-// Arrives on the mbarrier once all of this thread's earlier cp.async copies have
-// landed (the barrier's expected count includes this arrival).
-__device__ __forceinline__ void cp_async_arrive_noinc(uint64_t* bar)
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                            uint64_t* bar)
 {
-    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+        "%5}], [%6];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+        : "memory");
 }
 
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-// Waits until at most n of this thread's most recent cp.async groups are pending.
-__device__ __forceinline__ void cp_async_wait_pending(int n)
-{
-    switch (n) {
-        case 0: asm volatile("cp.async.wait_group 0;" ::: "memory"); break;
-        case 1: asm volatile("cp.async.wait_group 1;" ::: "memory"); break;
-        case 2: asm volatile("cp.async.wait_group 2;" ::: "memory"); break;
-        default: asm volatile("cp.async.wait_group 3;" ::: "memory"); break;
-    }
-}
-__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
@@ -150,41 +151,91 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v)
     for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
+// Target tile of level k: bx x by x bz parent cells (at most 8 x 4 x 4 = 128).
+__host__ __device__ __forceinline__ void tc_tile_shape_dev(int level, int& bx, int& by, int& bz)
+{
+    const int m = 1 << (level - 1);
+    bx = m < 8 ? m : 8;
+    by = m < 4 ? m : 4;
+    bz = m < 4 ? m : 4;
+}
+
 }  // namespace
 
-// FP32 multipole rows -> bf16 hi/lo rows of TC_K elements (zero padded).
-__global__ void k_split_bf16(const float* M, int Rpad, int R, long nrows, __nv_bfloat16* hi, __nv_bfloat16* lo)
+// ------------------------------------------------------------------ source grids
+
+// One thread per (grid row, 8 coefficients): the FP32 multipole of the row's
+// cell (periodic image in the halo, zero outside a non-periodic box) split into
+// bf16 hi and lo.
+__global__ void __launch_bounds__(256) k_tc_grids(const TcGridArgs g)
 {
-    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    long row = i / TC_KMAX, c = i % TC_KMAX;
-    if (row >= nrows) return;
-    float x = c < R ? M[row * Rpad + c] : 0.f;
-    __nv_bfloat16 h = __float2bfloat16_rn(x);
-    __nv_bfloat16 l = __float2bfloat16_rn(x - __bfloat162float(h));
-    hi[row * TC_KMAX + c] = h;
-    lo[row * TC_KMAX + c] = l;
+    const int groups = g.KP / 8;
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.rows * groups) return;
+    const long row = i / groups;
+    const int c0 = (int)(i - row * groups) * 8;
+    int q = 0;
+    while (q + 1 < g.ngrid && g.row0[q + 1] <= row) q++;
+    long r = row - g.row0[q];
+    const int W = g.W[q], n = 1 << g.level[q];
+    const int xh = (int)(r % W);
+    r /= W;
+    const int yh = (int)(r % W);
+    r /= W;
+    const int zh = (int)(r % W);
+    r /= W;
+    int x, y, z;
+    if (g.parity[q]) {
+        const int par = (int)r;
+        x = 2 * (xh - TC_HALO) + (par & 1);
+        y = 2 * (yh - TC_HALO) + ((par >> 1) & 1);
+        z = 2 * (zh - TC_HALO) + (par >> 2);
+    } else {
+        x = xh - TC_HALO;
+        y = yh - TC_HALO;
+        z = zh - TC_HALO;
+    }
+    bool valid = true;
+    if (g.periodic) {
+        x = ((x % n) + n) % n;
+        y = ((y % n) + n) % n;
+        z = ((z % n) + n) % n;
+    } else {
+        valid = x >= 0 && y >= 0 && z >= 0 && x < n && y < n && z < n;
+    }
+    const float* src = g.src[q] + (size_t)(valid ? morton_encode(x, y, z) : 0u) * g.Rpad;
+    alignas(16) __nv_bfloat16 h[8], l[8];
+#pragma unroll
+    for (int e = 0; e < 8; e++) {
+        const int c = c0 + e;
+        const float v = valid && c < g.R ? src[c] : 0.f;
+        h[e] = __float2bfloat16_rn(v);
+        l[e] = __float2bfloat16_rn(v - __bfloat162float(h[e]));
+    }
+    *reinterpret_cast<uint4*>(g.hi + row * g.KP + c0) = *reinterpret_cast<const uint4*>(h);
+    if (g.lo) *reinterpret_cast<uint4*>(g.lo + row * g.KP + c0) = *reinterpret_cast<const uint4*>(l);
 }
 
-void launch_split_bf16(const float* M, int Rpad, int R, long nrows, void* hi, void* lo, cudaStream_t s)
+void launch_tc_grids(const TcGridArgs& g, cudaStream_t s)
 {
-    long n = nrows * TC_KMAX;
+    const long n = g.rows * (g.KP / 8);
     if (n <= 0) return;
     g_kernel_launches.fetch_add(1, std::memory_order_relaxed);
-    k_split_bf16<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(M, Rpad, R, nrows, (__nv_bfloat16*)hi,
-                                                               (__nv_bfloat16*)lo);
+    k_tc_grids<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(g);
 }
 
+// ------------------------------------------------------------------ M2L
+
 // Warp-specialised pipeline, no block-wide barrier in the main loop:
-//   warps 0-3 (producers): thread t owns target row t; for entry i it waits until
-//     stage i%NS is free (the MMAs of entry i-NS committed), gathers its source
-//     row (cp.async, hi and lo bf16) into the 128B-swizzled A tile and arrives on
-//     the stage's full barrier when its copies land (cp.async.mbarrier.arrive);
-//     thread 0 also loads the operator images with one cp.async.bulk;
-//   warp 4 (MMA issuer, one lane): waits for the full barrier, issues the chunked
+//   warp 0, lane 0 (producer): for entry i it waits until stage i%NS is free (the
+//     MMAs of entry i-NS committed), then issues the TMA tile loads of the source
+//     box (one per K atom, hi and lo) and the bulk copy of the operator images,
+//     all completing on the stage's full barrier;
+//   warp 1, lane 0 (MMA issuer): waits for the full barrier, issues the chunked
 //     tcgen05.mma sequence into TMEM and commits to the stage's empty barrier.
 // After the last commit, warps 0-3 read their 32 TMEM lanes (tcgen05.ld) and add
 // the results to the target locals.
-__global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(TcArgs a)
+__global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(const __grid_constant__ TcArgs a)
 {
     extern __shared__ uint8_t smraw[];
     uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~(uintptr_t)1023);
@@ -196,17 +247,27 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(TcArgs a)
     const int NS = a.nstage;
     uint64_t* bar_full = reinterpret_cast<uint64_t*>(sm + NS * stage_bytes);
     uint64_t* bar_empty = bar_full + TC_MAXSTAGE;
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar_empty + TC_MAXSTAGE);
+    uint64_t* bar_done = bar_empty + TC_MAXSTAGE;  // one phase: every MMA of the CTA has completed
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar_done + 1);
 
     const CTask task = a.tasks[blockIdx.x];
+    const int k = task.level, s = task.octant;
+    int bx, by, bz;
+    tc_tile_shape_dev(k, bx, by, bz);
+    const int m = 1 << (k - 1), tx = m / bx, ty = m / by;
+    const int i0 = (task.q0 % tx) * bx, j0 = ((task.q0 / tx) % ty) * by, l0 = (task.q0 / (tx * ty)) * bz;
+    const int rows = bx * by * bz;
+    const int ox = (s >> 2) & 1, oy = (s >> 1) & 1, oz = s & 1;
+
     if (tid == 0) {
-        for (int k = 0; k < NS; k++) {
-            mbar_init(&bar_full[k], 128 + 1);  // 128 producer copy arrivals + the bulk-copy expect_tx
-            mbar_init(&bar_empty[k], 1);
+        for (int q = 0; q < NS; q++) {
+            mbar_init(&bar_full[q], 1);
+            mbar_init(&bar_empty[q], 1);
         }
+        mbar_init(bar_done, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == 4) {
+    if (warp == 2) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
                      "r"(a.tmem_cols)
                      : "memory");
@@ -219,59 +280,41 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(TcArgs a)
     const int ne = task.e_end - task.e_begin;
     bool ok = true;
 
-    if (warp < 4) {
-        // ---------------------------------------------------------------- producers
-        const int t = tid;
-        const bool tvalid = t < task.ntgt;
-        int vt[3], va[3];
-        const uint32_t q = (uint32_t)(task.q0 + t);
-        const uint32_t tcode = (q << 3) | (uint32_t)task.octant;
-        morton_decode(q, va[0], va[1], va[2]);
-        morton_decode(tcode, vt[0], vt[1], vt[2]);
-        const int chunks = a.k_atoms * 8;  // 16-byte chunks per row
+    if (warp == 0 && lane == 0) {
+        // ---------------------------------------------------------------- producer
+        const uint32_t tx_bytes = (split ? 2u : 1u) * (uint32_t)(a.k_atoms * rows * 128 + b_bytes);
         for (int i = 0; i < ne; i++) {
             const int st = i % NS, u = i / NS;
             if (i >= NS) ok = mbar_wait(&bar_empty[st], (u - 1) & 1, a.err) && ok;
             const CEntry en = a.entries[task.e_begin + i];
             uint8_t* A_hi = sm + st * stage_bytes;
             uint8_t* A_lo = A_hi + a_bytes;
-            if (t == 0) {
-                uint8_t* B = A_hi + (split ? 2 : 1) * a_bytes;
-                const uint32_t nb = (split ? 2u : 1u) * b_bytes;
-                mbar_expect_tx(&bar_full[st], nb);
-                bulk_g2s(B, a.bimg + (size_t)en.op * 2 * b_bytes, nb, &bar_full[st]);
-            }
-            const int slev = en.mode == 0 ? task.level : task.level - 1;
-            int row = -1;
-            if (tvalid) {
-                const int* base = en.mode == 0 ? vt : va;
-                int sx = base[0] + en.dx, sy = base[1] + en.dy, sz = base[2] + en.dz;
-                const int ns = 1 << slev;
-                bool in = true;
-                if (a.periodic) {
-                    sx &= ns - 1; sy &= ns - 1; sz &= ns - 1;
-                } else {
-                    in = sx >= 0 && sy >= 0 && sz >= 0 && sx < ns && sy < ns && sz < ns;
+            uint8_t* B = A_hi + (split ? 2 : 1) * a_bytes;
+            mbar_expect_tx(&bar_full[st], tx_bytes);
+            if (en.mode == 0) {
+                // same-level source: parity grid of level k
+                const int fx = (ox + en.dx) >> 1, fy = (oy + en.dy) >> 1, fz = (oz + en.dz) >> 1;
+                const int par = ((ox + en.dx) & 1) | (((oy + en.dy) & 1) << 1) | (((oz + en.dz) & 1) << 2);
+                const int cx = i0 + fx + TC_HALO, cy = j0 + fy + TC_HALO, cz = l0 + fz + TC_HALO;
+                for (int at = 0; at < a.k_atoms; at++) {
+                    tma_load_5d(A_hi + at * 128 * 128, &a.p_hi[k], 64 * at, cx, cy, cz, par, &bar_full[st]);
+                    if (split) tma_load_5d(A_lo + at * 128 * 128, &a.p_lo[k], 64 * at, cx, cy, cz, par, &bar_full[st]);
                 }
-                if (in) row = (int)morton_encode(sx, sy, sz);
+            } else {
+                // parent-level source: natural grid of level k-1
+                const int cx = i0 + en.dx + TC_HALO, cy = j0 + en.dy + TC_HALO, cz = l0 + en.dz + TC_HALO;
+                for (int at = 0; at < a.k_atoms; at++) {
+                    tma_load_4d(A_hi + at * 128 * 128, &a.n_hi[k - 1], 64 * at, cx, cy, cz, &bar_full[st]);
+                    if (split) tma_load_4d(A_lo + at * 128 * 128, &a.n_lo[k - 1], 64 * at, cx, cy, cz, &bar_full[st]);
+                }
             }
-            const bool valid = row >= 0;
-            const size_t g0 = (size_t)(valid ? row : 0) * TC_KMAX;
-            const __nv_bfloat16* gh = a.mh[slev] + g0;
-            const __nv_bfloat16* gl = a.ml[slev] + g0;
-            for (int kc = 0; kc < chunks; kc++) {
-                const int soff = (kc >> 3) * (128 * 128) + t * 128 + (((kc & 7) ^ (t & 7)) << 4);
-                cp_async16(A_hi + soff, gh + kc * 8, valid);
-                if (split) cp_async16(A_lo + soff, gl + kc * 8, valid);
-            }
-            cp_async_arrive_noinc(&bar_full[st]);
+            bulk_g2s(B, a.bimg + (size_t)en.op * 2 * b_bytes, (split ? 2u : 1u) * b_bytes, &bar_full[st]);
         }
-    } else if (lane == 0) {
+    } else if (warp == 1 && lane == 0) {
         // ---------------------------------------------------------------- MMA issuer
         for (int i = 0; i < ne; i++) {
             const int st = i % NS, u = i / NS;
             ok = mbar_wait(&bar_full[st], u & 1, a.err) && ok;
-            fence_proxy_async();
             tc_fence_after();
             const uint32_t a_hi = smem_u32(sm + st * stage_bytes), a_lo = a_hi + (uint32_t)a_bytes,
                            b_hi = a_hi + (uint32_t)((split ? 2 : 1) * a_bytes), b_lo = b_hi + (uint32_t)b_bytes;
@@ -293,26 +336,31 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(TcArgs a)
             }
             mma_commit(&bar_empty[st]);
         }
+        // completes when every MMA issued above has completed
+        if (ne > 0) mma_commit(bar_done);
     }
-    // all MMAs complete (the last commit covers every earlier MMA of this thread)
-    if (warp < 4 && ne > 0) ok = mbar_wait(&bar_empty[(ne - 1) % NS], ((ne - 1) / NS) & 1, a.err) && ok;
-    __syncthreads();
+    // The epilogue waits on the single-phase done barrier: a parity wait on a
+    // stage barrier could pass before its first phase completes.
+    __syncwarp();
+    if (ne > 0) ok = mbar_wait(bar_done, 0, a.err) && ok;
     tc_fence_after();
-    if (warp < 4 && ne > 0) {
-        float* dst = a.dst_lvl[task.level];
+    if (ne > 0) {
+        float* dst = a.dst_lvl[k];
         const int t = 32 * warp + lane;
-        const bool wv = t < task.ntgt;
-        const size_t trow = (size_t)(((uint32_t)(task.q0 + t) << 3) | (uint32_t)task.octant) * a.Rpad;
+        const bool wv = t < rows;
+        const int bi = t % bx, bj = (t / bx) % by, bl = t / (bx * by);
+        const uint32_t q = wv ? morton_encode(i0 + bi, j0 + bj, l0 + bl) : 0u;
+        const size_t trow = (size_t)((q << 3) | (uint32_t)s) * a.Rpad;
         for (int c = 0; c < a.nchunk; c++) {
             for (int b = 0; b < a.chunk_n[c]; b += 16) {
                 float v[16];
                 tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(a.chunk_col[c] + b), v);
 #pragma unroll
-                for (int k = 0; k < 16; k++) {
-                    const int r = a.chunk_row0[c] + b + k;
-                    if (wv && b + k < a.chunk_rows[c]) {
-                        if (a.atomic) atomicAdd(&dst[trow + r], v[k]);
-                        else dst[trow + r] += v[k];
+                for (int e = 0; e < 16; e++) {
+                    const int r = a.chunk_row0[c] + b + e;
+                    if (wv && b + e < a.chunk_rows[c]) {
+                        if (a.atomic) atomicAdd(&dst[trow + r], v[e]);
+                        else dst[trow + r] += v[e];
                     }
                 }
             }
@@ -320,9 +368,94 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(TcArgs a)
     }
     tc_fence_before();
     __syncthreads();
-    if (warp == 4)
+    if (warp == 2)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(a.tmem_cols) : "memory");
     (void)ok;
+}
+
+// ------------------------------------------------------------------ host side
+
+void tc_tile_shape(int level, int& bx, int& by, int& bz) { tc_tile_shape_dev(level, bx, by, bz); }
+
+int tc_tiles(int level)
+{
+    int bx, by, bz;
+    tc_tile_shape(level, bx, by, bz);
+    const int m = 1 << (level - 1);
+    return (m / bx) * (m / by) * (m / bz);
+}
+
+TcGrids tc_grid_layout(int D, int k_atoms)
+{
+    TcGrids g;
+    g.KP = 64 * k_atoms;
+    long rows = 0;
+    for (int k = 0; k <= D; k++) {
+        if (k < D) {  // natural grid: parent-level sources of level k+1
+            g.n_w[k] = (1 << k) + 2 * TC_HALO;
+            g.n_row0[k] = rows;
+            rows += (long)g.n_w[k] * g.n_w[k] * g.n_w[k];
+        }
+        if (k >= 1) {  // parity grid: same-level sources of level k
+            g.p_w[k] = (1 << (k - 1)) + 2 * TC_HALO;
+            g.p_row0[k] = rows;
+            rows += 8L * g.p_w[k] * g.p_w[k] * g.p_w[k];
+        }
+    }
+    g.rows = rows;
+    return g;
+}
+
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        else
+            cudaGetLastError();
+    }
+    return fn;
+}
+
+// rank-4 (natural) or rank-5 (parity) map of one grid: dims (KP, W, W, W[, 8]),
+// box (64, bx, by, bz[, 1]) of the target level's tile, 128-byte swizzle
+static bool encode_grid(CUtensorMap* map, void* base, int KP, int W, bool parity, int bx, int by, int bz)
+{
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc) return false;
+    const cuuint32_t rank = parity ? 5 : 4;
+    cuuint64_t dims[5] = {(cuuint64_t)KP, (cuuint64_t)W, (cuuint64_t)W, (cuuint64_t)W, 8};
+    const cuuint64_t row = (cuuint64_t)KP * 2;
+    cuuint64_t strides[4] = {row, row * W, row * W * W, row * W * W * W};
+    cuuint32_t box[5] = {64, (cuuint32_t)bx, (cuuint32_t)by, (cuuint32_t)bz, 1};
+    cuuint32_t es[5] = {1, 1, 1, 1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, rank, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+bool tc_encode_maps(TcArgs& a, int D, const TcGrids& g, void* hi, void* lo)
+{
+    __nv_bfloat16* h = static_cast<__nv_bfloat16*>(hi);
+    __nv_bfloat16* l = static_cast<__nv_bfloat16*>(lo);
+    for (int k = 1; k <= D; k++) {
+        int bx, by, bz;
+        tc_tile_shape(k, bx, by, bz);
+        if (!encode_grid(&a.p_hi[k], h + g.p_row0[k] * g.KP, g.KP, g.p_w[k], true, bx, by, bz)) return false;
+        if (!encode_grid(&a.n_hi[k - 1], h + g.n_row0[k - 1] * g.KP, g.KP, g.n_w[k - 1], false, bx, by, bz))
+            return false;
+        if (l) {
+            if (!encode_grid(&a.p_lo[k], l + g.p_row0[k] * g.KP, g.KP, g.p_w[k], true, bx, by, bz)) return false;
+            if (!encode_grid(&a.n_lo[k - 1], l + g.n_row0[k - 1] * g.KP, g.KP, g.n_w[k - 1], false, bx, by, bz))
+                return false;
+        }
+    }
+    return true;
 }
 
 size_t tc_stage_bytes(int k_atoms, int img_bytes, int nprod)
@@ -333,17 +466,17 @@ size_t tc_stage_bytes(int k_atoms, int img_bytes, int nprod)
 size_t tc_smem_bytes(const TcArgs& a)
 {
     return 1024 + (size_t)a.nstage * tc_stage_bytes(a.k_atoms, a.img_bytes, a.nprod) +
-           2 * TC_MAXSTAGE * sizeof(uint64_t) + 16;
+           (2 * TC_MAXSTAGE + 1) * sizeof(uint64_t) + 16;
 }
 
-// Stages per CTA: aim at two CTAs per SM (about 110 KB each), at least 2 stages.
+// Stages per CTA: about 110 KB each (two CTAs per SM), at least 2 where they fit.
 int tc_pick_stages(int k_atoms, int img_bytes, int nprod)
 {
     const size_t st = tc_stage_bytes(k_atoms, img_bytes, nprod);
     int ns = (int)((110 * 1024) / st);
     if (ns < 2) ns = 2;
     if (ns > TC_MAXSTAGE) ns = TC_MAXSTAGE;
-    if (1024 + ns * st + 2 * TC_MAXSTAGE * sizeof(uint64_t) + 16 > 227 * 1024) ns = 1;
+    while (ns > 1 && 1024 + ns * st + (2 * TC_MAXSTAGE + 1) * sizeof(uint64_t) + 16 > 227 * 1024) ns--;
     return ns;
 }
 

@@ -1,6 +1,8 @@
-// Tensor-core (tcgen05) M2L: launch interface and the host-side chunk plan.
+// Tensor-core (tcgen05) M2L: launch interface, the host-side chunk plan and the
+// layout of the bf16 source grids that the TMA engine reads.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -11,12 +13,14 @@
 
 namespace gbfmm {
 
-constexpr int TC_KMAX = 128;     // length of a split (bf16) multipole row; orders P <= 10
+constexpr int TC_KMAX = 128;     // longest split (bf16) multipole row; orders P <= 10
 constexpr int TC_MAX_ORDER = 10;
 constexpr int TC_MAXCHUNK = 8;
-constexpr int TC_TILE = 128;     // targets per CTA (MMA M)
-constexpr int TC_MAXSTAGE = 4;   // pipeline stages (operands of one entry each)
-constexpr int TC_THREADS = 160;  // 4 producer warps + 1 MMA warp
+constexpr int TC_TILE = 128;     // MMA M: rows of the target tile
+constexpr int TC_MAXSTAGE = 8;   // pipeline stages (operands of one entry each)
+constexpr int TC_THREADS = 128;  // producer lane, MMA lane, 4 epilogue warps
+constexpr int TC_HALO = 2;       // halo of the source grids (cells of the grid)
+constexpr int TC_MAXLEV = 8;
 
 // Degree chunks of the M2L operator: chunk c covers output rows [row0, row0+rows)
 // (whole degrees j0..j1), MMA N = n (rows padded to 16), K = k (inputs of degree
@@ -34,28 +38,61 @@ TcPlan make_tc_plan(int P);
 // Appends the hi and lo images of one R x R operator (row-major FP64) to 'out'.
 void append_tc_image(const TcPlan& pl, int R, const double* A, std::vector<uint8_t>& out);
 
-struct TcArgs {
-    const __nv_bfloat16* mh[8];  // per level: split multipole rows (hi), TC_KMAX bf16 each
-    const __nv_bfloat16* ml[8];  // (lo)
+// Source grids.  Every grid row holds KP = 64 * k_atoms bf16 coefficients of one
+// cell (zero past R), hi and lo splits in two arrays of the same layout.
+//   parity grid of level k >= 1 (same-level sources): [par][zh][yh][xh][KP] with
+//     W = 2^(k-1) + 2 TC_HALO, cell x = 2 (xh - TC_HALO) + px, par = px + 2 py + 4 pz;
+//   natural grid of level k >= 0 (parent-level sources): [z][y][x][KP] with
+//     W = 2^k + 2 TC_HALO, cell x = x' - TC_HALO.
+// Halo cells hold the periodic images (or zeros without periodicity), so the
+// sources of a tile of same-octant targets for one stencil entry form one
+// rectangular box: a single TMA tile load.
+struct TcGrids {
+    int KP = 0;
+    long rows = 0;
+    long p_row0[TC_MAXLEV] = {}, n_row0[TC_MAXLEV] = {};
+    int p_w[TC_MAXLEV] = {}, n_w[TC_MAXLEV] = {};
+};
+TcGrids tc_grid_layout(int D, int k_atoms);
+
+// Target tile of level k: a box of bx x by x bz parent cells (one octant).
+void tc_tile_shape(int level, int& bx, int& by, int& bz);
+int tc_tiles(int level);
+
+struct TcGridArgs {
+    int ngrid = 0;
+    long row0[2 * TC_MAXLEV];
+    int level[2 * TC_MAXLEV], parity[2 * TC_MAXLEV], W[2 * TC_MAXLEV];
+    const float* src[2 * TC_MAXLEV];  // FP32 rows of that level (Morton order)
+    int R, Rpad, KP, periodic;
+    long rows;
+    __nv_bfloat16 *hi, *lo;           // lo may be NULL (one product)
+};
+void launch_tc_grids(const TcGridArgs& g, cudaStream_t s);
+
+struct alignas(64) TcArgs {
+    CUtensorMap p_hi[TC_MAXLEV], p_lo[TC_MAXLEV];  // parity grids (level k)
+    CUtensorMap n_hi[TC_MAXLEV], n_lo[TC_MAXLEV];  // natural grids (level k)
     const uint8_t* bimg;         // class images: [class][hi | lo]
     const CEntry* entries;       // op = class index
-    const CTask* tasks;
-    float* dst_lvl[8];
+    const CTask* tasks;          // level, octant, q0 = tile index, entry range
+    float* dst_lvl[TC_MAXLEV];
     int* err;                    // bit 1: a bounded wait gave up
     int Rpad;
     int k_atoms, img_bytes, tmem_cols, nchunk;
     int nprod;                   // 3: hi*hi + hi*lo + lo*hi, 1: hi*hi
     int nstage;                  // pipeline stages, 2..TC_MAXSTAGE (tc_pick_stages)
-    int periodic;
     int atomic;                  // 1: atomicAdd into L (split entry ranges), 0: plain add
     int chunk_n[TC_MAXCHUNK], chunk_k[TC_MAXCHUNK], chunk_col[TC_MAXCHUNK], chunk_row0[TC_MAXCHUNK],
         chunk_rows[TC_MAXCHUNK], chunk_img[TC_MAXCHUNK];
 };
 
+// Encodes the tensor maps of the grids (hi, and lo when lo != NULL) into a.
+// Returns false when the driver's encoder is unavailable or refuses a map.
+bool tc_encode_maps(TcArgs& a, int D, const TcGrids& g, void* hi, void* lo);
 size_t tc_smem_bytes(const TcArgs& a);
 size_t tc_stage_bytes(int k_atoms, int img_bytes, int nprod);
 int tc_pick_stages(int k_atoms, int img_bytes, int nprod);
 void launch_m2l_tc(const TcArgs& a, int ntasks, cudaStream_t s);
-void launch_split_bf16(const float* M, int Rpad, int R, long nrows, void* hi, void* lo, cudaStream_t s);
 
 }  // namespace gbfmm

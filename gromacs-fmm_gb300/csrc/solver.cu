@@ -9,6 +9,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
+#include <new>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -171,10 +173,10 @@ struct gbfmm_handle {
     int* d_flags = nullptr;
     // tensor-core M2L
     bool tc = false;
-    __nv_bfloat16 *d_mh = nullptr, *d_ml = nullptr;
+    __nv_bfloat16 *d_gh = nullptr, *d_gl = nullptr;  // tensor-core source grids (hi, lo)
+    TcGrids tcg;
+    TcArgs* tca = nullptr;  // tensor maps and launch arguments (host, 64-byte aligned)
     uint8_t* d_img = nullptr;
-    long total_rows = 0;
-    long row_off[9] = {};
     CEntry* d_tc_entries = nullptr;
     CTask* d_tc_tasks = nullptr;
     int tc_ntask = 0, tc_split = 1;
@@ -241,6 +243,10 @@ const char* gbfmm_stage_name(int s) { return (s >= 0 && s < 9) ? k_stage_names[s
 static void free_handle(gbfmm_handle* h)
 {
     if (!h) return;
+    if (h->tca) {
+        h->tca->~TcArgs();
+        free(h->tca);
+    }
     if (h->gexec) cudaGraphExecDestroy(h->gexec);
     for (int i = 0; i < 16; i++)
         if (h->ev[i]) cudaEventDestroy(h->ev[i]);
@@ -291,14 +297,10 @@ static int layout(gbfmm_handle* h, Arena& a)
     h->lev_floats = lev;
     h->d_M = a.take<float>(lev);
     h->d_L = a.take<float>(lev);
-    h->total_rows = 0;
-    for (int k = 0; k <= D; k++) {
-        h->row_off[k] = h->total_rows;
-        h->total_rows += 1L << (3 * k);
-    }
     if (h->tc) {
-        h->d_mh = a.take<__nv_bfloat16>((size_t)h->total_rows * TC_KMAX);
-        h->d_ml = a.take<__nv_bfloat16>((size_t)h->total_rows * TC_KMAX);
+        h->tcg = tc_grid_layout(D, t->tc.k_atoms);
+        h->d_gh = a.take<__nv_bfloat16>((size_t)h->tcg.rows * h->tcg.KP);
+        if (h->prm.precision != GBFMM_PREC_BF16X1) h->d_gl = a.take<__nv_bfloat16>((size_t)h->tcg.rows * h->tcg.KP);
         h->d_img = a.take<uint8_t>(t->tc_img.size());
     }
     h->d_M0 = a.take<double>(R);
@@ -449,7 +451,7 @@ static int build_tasks(gbfmm_handle* h)
                 }
             }
         long tiles = 0;
-        for (int k = 1; k <= D; k++) tiles += 8 * std::max<long>(1, ((1L << (3 * (k - 1))) + TC_TILE - 1) / TC_TILE);
+        for (int k = 1; k <= D; k++) tiles += 8L * tc_tiles(k);
         int sp = h->prm.m2l_split > 0 ? h->prm.m2l_split : 1;
         if (h->prm.m2l_split <= 0)
             while (tiles * sp < 152 && sp < 8) sp *= 2;
@@ -457,14 +459,15 @@ static int build_tasks(gbfmm_handle* h)
         h->tc_split = sp;
         for (int k = 1; k <= D; k++) {
             const int lt = k == 1 ? 0 : 1;
-            long npar = 1L << (3 * (k - 1));
+            int bx, by, bz;
+            tc_tile_shape(k, bx, by, bz);
             for (int s = 0; s < 8; s++) {
                 int eb = e_tc[lt][s], ne = (int)t->st.m2l[lt][s].size();
                 int ch = (ne + sp - 1) / sp;
-                for (long q0 = 0; q0 < npar; q0 += TC_TILE)
+                for (int q = 0; q < tc_tiles(k); q++)
                     for (int e0 = 0; e0 < ne; e0 += ch) {
                         CTask c;
-                        c.level = k; c.octant = s; c.q0 = (int)q0; c.ntgt = (int)std::min<long>(TC_TILE, npar - q0);
+                        c.level = k; c.octant = s; c.q0 = q; c.ntgt = bx * by * bz;
                         c.e_begin = eb + e0; c.e_end = eb + std::min(ne, e0 + ch);
                         c.group = 0; c.r0 = 0; c.r1 = h->R;
                         tasks.push_back(c);
@@ -484,38 +487,70 @@ static int build_tasks(gbfmm_handle* h)
     return GBFMM_OK;
 }
 
-static TcArgs tc_args(gbfmm_handle* h)
+// Launch arguments of the tensor-core M2L, tensor maps included (encoded once:
+// the grids do not move).
+static int make_tc_args(gbfmm_handle* h)
 {
-    TcArgs a;
-    std::memset(&a, 0, sizeof(a));
+    void* mem = nullptr;
+    if (posix_memalign(&mem, 64, sizeof(TcArgs)) != 0) return fail(GBFMM_ERR_NOMEM, "host memory");
+    TcArgs* a = new (mem) TcArgs();
+    std::memset(a, 0, sizeof(TcArgs));
+    h->tca = a;
     const TcPlan& pl = h->tab->tc;
-    for (int k = 0; k <= h->D; k++) {
-        a.mh[k] = h->d_mh + (size_t)h->row_off[k] * TC_KMAX;
-        a.ml[k] = h->d_ml + (size_t)h->row_off[k] * TC_KMAX;
-        a.dst_lvl[k] = h->Llev[k];
-    }
-    a.bimg = h->d_img;
-    a.entries = h->d_entries;
-    a.tasks = h->d_tc_tasks;
-    a.err = h->d_flags + 1;
-    a.Rpad = h->Rpad;
-    a.k_atoms = pl.k_atoms;
-    a.img_bytes = pl.img_bytes;
-    a.tmem_cols = pl.tmem_cols;
-    a.nchunk = pl.nchunk;
-    a.nprod = h->prm.precision == GBFMM_PREC_BF16X1 ? 1 : 3;
-    a.nstage = tc_pick_stages(pl.k_atoms, pl.img_bytes, a.nprod);
-    a.periodic = h->periodic ? 1 : 0;
-    a.atomic = h->tc_split > 1 ? 1 : 0;
+    if (!tc_encode_maps(*a, h->D, h->tcg, h->d_gh, h->d_gl))
+        return fail(GBFMM_ERR_CUDA, "tensor map encoding of the M2L source grids failed");
+    for (int k = 0; k <= h->D; k++) a->dst_lvl[k] = h->Llev[k];
+    a->bimg = h->d_img;
+    a->entries = h->d_entries;
+    a->tasks = h->d_tc_tasks;
+    a->err = h->d_flags + 1;
+    a->Rpad = h->Rpad;
+    a->k_atoms = pl.k_atoms;
+    a->img_bytes = pl.img_bytes;
+    a->tmem_cols = pl.tmem_cols;
+    a->nchunk = pl.nchunk;
+    a->nprod = h->prm.precision == GBFMM_PREC_BF16X1 ? 1 : 3;
+    a->nstage = tc_pick_stages(pl.k_atoms, pl.img_bytes, a->nprod);
+    a->atomic = h->tc_split > 1 ? 1 : 0;
     for (int c = 0; c < pl.nchunk; c++) {
-        a.chunk_n[c] = pl.n[c];
-        a.chunk_k[c] = pl.k[c];
-        a.chunk_col[c] = pl.col[c];
-        a.chunk_row0[c] = pl.row0[c];
-        a.chunk_rows[c] = pl.rows[c];
-        a.chunk_img[c] = pl.img[c];
+        a->chunk_n[c] = pl.n[c];
+        a->chunk_k[c] = pl.k[c];
+        a->chunk_col[c] = pl.col[c];
+        a->chunk_row0[c] = pl.row0[c];
+        a->chunk_rows[c] = pl.rows[c];
+        a->chunk_img[c] = pl.img[c];
     }
-    return a;
+    return GBFMM_OK;
+}
+
+static TcGridArgs tc_grid_args(gbfmm_handle* h)
+{
+    TcGridArgs g;
+    const TcGrids& l = h->tcg;
+    for (int k = 0; k <= h->D; k++) {
+        if (k < h->D) {
+            g.row0[g.ngrid] = l.n_row0[k];
+            g.level[g.ngrid] = k;
+            g.parity[g.ngrid] = 0;
+            g.W[g.ngrid] = l.n_w[k];
+            g.src[g.ngrid++] = h->Mlev[k];
+        }
+        if (k >= 1) {
+            g.row0[g.ngrid] = l.p_row0[k];
+            g.level[g.ngrid] = k;
+            g.parity[g.ngrid] = 1;
+            g.W[g.ngrid] = l.p_w[k];
+            g.src[g.ngrid++] = h->Mlev[k];
+        }
+    }
+    g.R = h->R;
+    g.Rpad = h->Rpad;
+    g.KP = l.KP;
+    g.periodic = h->periodic ? 1 : 0;
+    g.rows = l.rows;
+    g.hi = h->d_gh;
+    g.lo = h->d_gl;
+    return g;
 }
 
 static ContractArgs contract_args(gbfmm_handle* h, int optype, int write_mode, bool src_is_L, int task0)
@@ -619,8 +654,8 @@ static void enqueue_step(gbfmm_handle* h)
     launch_root_lattice(ra, s);
     mark(h, 4);
     if (h->tc) {
-        launch_split_bf16(h->d_M, h->Rpad, h->R, h->total_rows, h->d_mh, h->d_ml, s);
-        launch_m2l_tc(tc_args(h), h->tc_ntask, s);
+        launch_tc_grids(tc_grid_args(h), s);
+        launch_m2l_tc(*h->tca, h->tc_ntask, s);
     } else {
         ContractArgs a = contract_args(h, OP_M2L, 2, false, h->m2l_task0);
         launch_contract(a, h->m2l_ntask, s);
@@ -752,6 +787,10 @@ extern "C" int gbfmm_create(const gbfmm_params* prm, int natoms, gbfmm_handle** 
     cudaMemset(h->d_M, 0, sizeof(float) * h->lev_floats);
     rc = build_tasks(h);
     if (rc != GBFMM_OK) return bail(rc);
+    if (h->tc) {
+        rc = make_tc_args(h);
+        if (rc != GBFMM_OK) return bail(rc);
+    }
     if (cudaMallocHost(&h->h_sc, sizeof(StepConst)) != cudaSuccess ||
         cudaMallocHost(&h->h_flags, sizeof(int) * 4) != cudaSuccess ||
         cudaMallocHost(&h->h_forces, sizeof(float) * 3 * std::max(natoms, 1)) != cudaSuccess ||
