@@ -259,6 +259,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(const __grid_constant_
     const int rows = bx * by * bz;
     const int ox = (s >> 2) & 1, oy = (s >> 1) & 1, oz = s & 1;
 
+    // the task's stencil entries, read once (the producer must not wait on
+    // global loads between its copies)
+    __shared__ CEntry ent[TC_MAXENT];
+    const int ne = min(task.e_end - task.e_begin, TC_MAXENT);
+    for (int i = tid; i < ne; i += TC_THREADS) ent[i] = a.entries[task.e_begin + i];
     if (tid == 0) {
         for (int q = 0; q < NS; q++) {
             mbar_init(&bar_full[q], 1);
@@ -277,7 +282,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(const __grid_constant_
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-    const int ne = task.e_end - task.e_begin;
     bool ok = true;
 
     if (warp == 0 && lane == 0) {
@@ -286,7 +290,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(const __grid_constant_
         for (int i = 0; i < ne; i++) {
             const int st = i % NS, u = i / NS;
             if (i >= NS) ok = mbar_wait(&bar_empty[st], (u - 1) & 1, a.err) && ok;
-            const CEntry en = a.entries[task.e_begin + i];
+            const CEntry en = ent[i];
             uint8_t* A_hi = sm + st * stage_bytes;
             uint8_t* A_lo = A_hi + a_bytes;
             uint8_t* B = A_hi + (split ? 2 : 1) * a_bytes;
@@ -336,13 +340,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(const __grid_constant_
             }
             mma_commit(&bar_empty[st]);
         }
-        // completes when every MMA issued above has completed
-        if (ne > 0) mma_commit(bar_done);
+        // completes when every MMA issued above has completed; only this thread
+        // polls it (a parity wait on a stage barrier could pass before that
+        // barrier's first phase completes), the others wait at the CTA barrier
+        if (ne > 0) {
+            mma_commit(bar_done);
+            ok = mbar_wait(bar_done, 0, a.err) && ok;
+        }
     }
-    // The epilogue waits on the single-phase done barrier: a parity wait on a
-    // stage barrier could pass before its first phase completes.
-    __syncwarp();
-    if (ne > 0) ok = mbar_wait(bar_done, 0, a.err) && ok;
+    tc_fence_before();
+    __syncthreads();
     tc_fence_after();
     if (ne > 0) {
         float* dst = a.dst_lvl[k];
@@ -469,11 +476,13 @@ size_t tc_smem_bytes(const TcArgs& a)
            (2 * TC_MAXSTAGE + 1) * sizeof(uint64_t) + 16;
 }
 
-// Stages per CTA: about 110 KB each (two CTAs per SM), at least 2 where they fit.
+// Stages per CTA: at most about 100 KB of dynamic shared memory, so that two CTAs
+// (with their static entry list and the per-CTA reserve) share an SM; at least 2
+// where they fit.
 int tc_pick_stages(int k_atoms, int img_bytes, int nprod)
 {
     const size_t st = tc_stage_bytes(k_atoms, img_bytes, nprod);
-    int ns = (int)((110 * 1024) / st);
+    int ns = (int)((100 * 1024 - 1200) / st);
     if (ns < 2) ns = 2;
     if (ns > TC_MAXSTAGE) ns = TC_MAXSTAGE;
     while (ns > 1 && 1024 + ns * st + (2 * TC_MAXSTAGE + 1) * sizeof(uint64_t) + 16 > 227 * 1024) ns--;

@@ -21,6 +21,7 @@ constexpr int TC_MAXSTAGE = 8;   // pipeline stages (operands of one entry each)
 constexpr int TC_THREADS = 128;  // producer lane, MMA lane, 4 epilogue warps
 constexpr int TC_HALO = 2;       // halo of the source grids (cells of the grid)
 constexpr int TC_MAXLEV = 8;
+constexpr int TC_MAXENT = 256;   // stencil entries of one task (the stencils have at most 182)
 
 // Degree chunks of the M2L operator: chunk c covers output rows [row0, row0+rows)
 // (whole degrees j0..j1), MMA N = n (rows padded to 16), K = k (inputs of degree
