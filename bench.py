@@ -28,6 +28,7 @@ FP64 restatement of zeta_fmm, OpenMP on all host cores) on a bounded sample.
 import argparse
 import json
 import os
+import re
 import subprocess
 import sys
 import threading
@@ -170,6 +171,20 @@ class Clocks:
         reasons = sorted({names[i] for r in rows for i in range(4) if "Active" in r[5 + i]})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(rows), "source": "nvidia-smi"}
+
+
+def ncu_traffic(kernel):
+    """DRAM bytes per launch of a kernel from its committed ncu summary
+    (profiles/<kernel>_water95600_*.md, line 'traffic_bytes_per_launch: N'), or None."""
+    d = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(d):
+        return None, None
+    for f in sorted(os.listdir(d)):
+        if f.startswith(kernel + "_water95600") and f.endswith(".md"):
+            m = re.search(r"traffic_bytes_per_launch:\s*(\d+)", open(os.path.join(d, f)).read())
+            if m:
+                return int(m.group(1)), "profiles/" + f
+    return None, None
 
 
 def dist_env():
@@ -433,8 +448,9 @@ def main():
     roof = None
     if dom:
         k = kern[dom]
+        tb, tsrc = ncu_traffic("k_" + dom + ("_tc" if dom == "m2l" and tuned["prec"] else ""))
         roof = {"kernel": dom, "bound": k["bound"], "achieved": k["achieved"], "peak": k["peak"], "unit": k["unit"],
-                "frac": k["frac"], "traffic": None,
+                "frac": k["frac"], "traffic": tb, "traffic_source": tsrc,
                 "peak_source": (f"bf16 dense, MEASURED_PEAKS.json ({src})" if k["bound"] == "tensor" else
                                 "nominal 152 SMs x 128 FP32 lanes x 2 x sm_max_mhz (no FP32 entry in "
                                 "MEASURED_PEAKS.json)")}
