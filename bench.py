@@ -408,6 +408,7 @@ def main():
     results = {}
     for name, (prec, P, D) in (("plain", PLAIN), ("tuned", best)):
         s = run.solver(prec, P, D)
+        tiles = s.autotune(xyz, box, reps=5)  # tile shapes of this configuration (gbfmm_autotune)
         if ws > 1:
             dist.barrier()
         clk = Clocks(local)
@@ -418,6 +419,7 @@ def main():
         r["e2e"] = n * ws * args.steps / run.time_e2e(s, args.steps)
         r["stages"] = run.stages(s, args.steps)
         r["launches"] = s.step_launches()
+        r["tiles"] = tiles
         _, _, ln = s.tree()
         r["p2p_pairs"] = p2p_pair_count(ln, D)
         results[name] = r
@@ -466,7 +468,8 @@ def main():
                            "depth": plain["D"], "rel_force_err_vs_ewald": plain["err"], "e2e": plain["e2e"],
                            "stage_ms": plain["stages"]},
             "speedup_tuned_vs_plain": tuned["value"] / plain["value"],
-            "tuner": tuner_info, "sweep": tune, "stage_ms": st, "kernels": kern, "roofline": roof, "clocks": tuned["clocks"],
+            "tuner": tuner_info, "tile_autotune": {"tuned": tuned["tiles"], "plain": plain["tiles"]},
+            "sweep": tune, "stage_ms": st, "kernels": kern, "roofline": roof, "clocks": tuned["clocks"],
             "gpu_launches": tuned["launches"] * args.steps}
     if rank == 0:
         v, cores, sec = cpu_reference(xyz, q, box, PLAIN[1], PLAIN[2], args.cpu_steps, 1)

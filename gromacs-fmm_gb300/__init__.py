@@ -77,6 +77,9 @@ def lib():
             "gbfmm_compare_forces": (ctypes.c_int, [vp, fp, dp]),
             "gbfmm_set_timing": (ctypes.c_int, [vp, ctypes.c_int]),
             "gbfmm_stage_times": (ctypes.c_int, [vp, fp, ctypes.c_int, ip]),
+            "gbfmm_autotune": (ctypes.c_int, [vp, fp, fp, ctypes.c_int, fp]),
+            "gbfmm_get_tuning": (ctypes.c_int, [vp, ip, ip, ip]),
+            "gbfmm_set_tuning": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
             "gbfmm_stage_name": (ctypes.c_char_p, [ctypes.c_int]),
             "gbfmm_step_launches": (ctypes.c_int, [vp, ip]),
             "gbfmm_get_tree": (ctypes.c_int, [vp, ip, ip, ip]),
@@ -216,6 +219,26 @@ class ZetaFmmSolver:
         n = ctypes.c_int()
         _check(lib().gbfmm_step_launches(self._h, ctypes.byref(n)))
         return n.value
+
+    def autotune(self, coords, box, reps=5):
+        """Times the P2P and tensor-core M2L tile shapes on this configuration and
+        keeps the fastest (gbfmm_autotune); returns the tuning and its step time."""
+        L = lib()
+        x = _f32(coords).reshape(-1)
+        m = box_matrix(box)
+        ms = ctypes.c_float()
+        _check(L.gbfmm_autotune(self._h, _fp(x), _fp(m), int(reps), ctypes.byref(ms)))
+        t = self.tuning()
+        t["ms"] = ms.value
+        return t
+
+    def tuning(self):
+        a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _check(lib().gbfmm_get_tuning(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return {"p2p_variant": a.value, "m2l_split": b.value, "m2l_stages": c.value}
+
+    def set_tuning(self, p2p_variant=0, m2l_split=1, m2l_stages=2):
+        _check(lib().gbfmm_set_tuning(self._h, int(p2p_variant), int(m2l_split), int(m2l_stages)))
 
     def stage_times(self):
         ms = np.zeros(16, np.float32)

@@ -539,20 +539,20 @@ __device__ __forceinline__ f2_t f2_fma(f2_t a, f2_t b, f2_t c)
 // they add exact zeros without a test.
 constexpr float P2P_FAR = 1e15f;
 
-// K targets per thread (i, i+8, ..., i+8(K-1) of the cluster) against this
-// warp's source steps [sb, se); lane jj takes source pair 4 st + jj of each
-// step, two sources per packed instruction.  Pair term as kernel.cu:480-490:
+// K targets per thread against this warp's source steps [sb, se); a step holds
+// SL source records (two sources each) and lane jj < SL takes record SL st + jj,
+// two sources per packed instruction.  Pair term as kernel.cu:480-490:
 // phi += q/r, grad += q (x_j - x_i)/r^3, skipped when r = 0 (a body with itself
 // or a coincident body) where MASK is set.  Accumulates +q (x_i - x_j)/r^3; the
 // caller negates.
-template <int K, bool MASK>
+template <int K, bool MASK, int SL>
 __device__ __forceinline__ void p2p_sweep(const float4* __restrict__ src, int sb, int se, int jj, const f2_t (&X)[K][3],
                                           f2_t (&acc)[K][4])
 {
 #pragma unroll 2
     for (int st = sb; st < se; st++) {
-        const float4 xy = src[2 * (4 * st + jj)];
-        const float4 zq = src[2 * (4 * st + jj) + 1];
+        const float4 xy = src[2 * (SL * st + jj)];
+        const float4 zq = src[2 * (SL * st + jj) + 1];
         const f2_t sx = f2_pack(xy.x, xy.y), sy = f2_pack(xy.z, xy.w), sz = f2_pack(zq.x, zq.y);
         const f2_t sq = f2_pack(zq.z, zq.w);
 #pragma unroll
@@ -577,27 +577,29 @@ __device__ __forceinline__ void p2p_sweep(const float4* __restrict__ src, int sb
     }
 }
 
-// One cluster of up to 8K targets starting at c0 (of this pass's ntc); steps
-// below msteps need the r = 0 test.
-template <int K>
+// One cluster of up to LT K targets starting at c0 (of this pass's ntc): lane =
+// (target row ii = lane / SL, source lane jj = lane % SL), SL = 32 / LT; thread
+// targets c0 + ii + LT k.  Steps below msteps need the r = 0 test.
+template <int K, int LT>
 __device__ __forceinline__ void p2p_cluster(const float4* __restrict__ src, const float4* __restrict__ tgt, int c0,
                                             int ntc, int sb, int se, int msteps, int lane, float4* part)
 {
-    const int ii = lane >> 2, jj = lane & 3;
+    constexpr int SL = 32 / LT;
+    const int ii = lane / SL, jj = lane % SL;
     f2_t X[K][3];
     f2_t acc[K][4];
     const f2_t zero = f2_pack(0.f, 0.f);
 #pragma unroll
     for (int k = 0; k < K; k++) {
-        const float4 a = tgt[min(c0 + ii + 8 * k, ntc - 1)];
+        const float4 a = tgt[min(c0 + ii + LT * k, ntc - 1)];
         X[k][0] = f2_pack(a.x, a.x);
         X[k][1] = f2_pack(a.y, a.y);
         X[k][2] = f2_pack(a.z, a.z);
         acc[k][0] = acc[k][1] = acc[k][2] = acc[k][3] = zero;
     }
     const int mid = min(max(msteps, sb), se);
-    p2p_sweep<K, true>(src, sb, mid, jj, X, acc);
-    p2p_sweep<K, false>(src, mid, se, jj, X, acc);
+    p2p_sweep<K, true, SL>(src, sb, mid, jj, X, acc);
+    p2p_sweep<K, false, SL>(src, mid, se, jj, X, acc);
 #pragma unroll
     for (int k = 0; k < K; k++) {
         float v[4];
@@ -607,12 +609,12 @@ __device__ __forceinline__ void p2p_cluster(const float4* __restrict__ src, cons
             f2_unpack(acc[k][c], a, b);
             v[c] = a + b;
         }
-        // fixed butterfly over the 4 source lanes of each target
+        // fixed butterfly over the SL source lanes of each target
 #pragma unroll
-        for (int o = 1; o < 4; o <<= 1)
+        for (int o = 1; o < SL; o <<= 1)
 #pragma unroll
             for (int c = 0; c < 4; c++) v[c] += __shfl_xor_sync(0xffffffffu, v[c], o);
-        const int t = c0 + ii + 8 * k;
+        const int t = c0 + ii + LT * k;
         if (jj == 0 && t < ntc) {
             float4 pp = part[t];
             pp.x += v[0];
@@ -624,14 +626,23 @@ __device__ __forceinline__ void p2p_cluster(const float4* __restrict__ src, cons
     }
 }
 
-// One CTA per target leaf.  The source bodies of the 81 near leaves are staged in
-// shared memory, shifted into the target leaf's frame (scaled units, integer
-// offsets of the stencil, so the periodic shift is exact), two per record; the
-// target leaf itself is staged first (stencil entry 0).  Lane = (target i =
-// lane/4, source pair j = lane%4); a thread carries up to 3 targets (clusters of
-// 24).  Warp w sweeps a quarter of the sources; the 4 source lanes of a target
-// are reduced by shuffles and the per-warp partial sums are added in warp order
-// (deterministic).
+struct P2PShared {
+    float4 src[P2P_MAXS];      // P2P_MAXS sources in P2P_MAXS/2 records of two float4
+    float4 part[4][P2P_MAXT];  // per-warp partial sums, reduced in warp order
+    int e_off[128];
+    int e_beg[128];
+    float4 e_d[128];
+    int ws[4];
+};
+
+// The near field of one target leaf (the CTA's 128 threads).  The source bodies
+// of the 81 near leaves are staged in shared memory, shifted into the target
+// leaf's frame (scaled units, integer offsets of the stencil, so the periodic
+// shift is exact), two per record; the target leaf itself is staged first
+// (stencil entry 0).  A warp step covers LT targets x SL = 32/LT source records;
+// a thread carries up to 3 targets (clusters of 3 LT).  Warp w sweeps a quarter of
+// the sources; the SL source lanes of a target are reduced by shuffles and the
+// per-warp partial sums are added in warp order (deterministic).
 //
 // The r = 0 test is applied to the target leaf's own bodies only.  Bodies of two
 // different leaves cannot coincide when every staged body lies strictly inside
@@ -639,134 +650,141 @@ __device__ __forceinline__ void p2p_cluster(const float4* __restrict__ src, cons
 // integer shift is far below that margin); a CTA that stages any body outside
 // that range (bodies on or near a leaf face, or outside the box) applies the
 // test to every source.
-__global__ void __launch_bounds__(P2P_THREADS) k_p2p(const int* off, int depth, int periodic, const float4* atoms,
-                                                     const int* stencil, int nst, float4* field)
+template <int LT>
+__device__ __forceinline__ void p2p_leaf(const P2PArgs& a, uint32_t tcode, P2PShared& sh)
 {
-    __shared__ float4 src[P2P_MAXS];      // P2P_MAXS sources in P2P_MAXS/2 records of two float4
-    __shared__ float4 part[4][P2P_MAXT];  // per-warp partial sums, reduced in warp order
-    __shared__ int e_off[128];
-    __shared__ int e_beg[128];
-    __shared__ float4 e_d[128];
+    constexpr int SL = 32 / LT, SPS = 2 * SL;  // sources per step
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int nd = 1 << depth;
-    const uint32_t tcode = blockIdx.x;
+    const int nd = 1 << a.depth;
     int tx, ty, tz;
     morton_decode(tcode, tx, ty, tz);
-    const int tb = off[tcode], nt = off[tcode + 1] - tb;
-    if (nt == 0) return;
+    const int tb = a.off[tcode], nt = a.off[tcode + 1] - tb;
+    if (nt == 0) return;  // uniform over the CTA
     // source leaves of the stencil
     int cnt = 0;
-    if (tid < nst) {
-        int vx = tx + stencil[3 * tid], vy = ty + stencil[3 * tid + 1], vz = tz + stencil[3 * tid + 2];
+    if (tid < a.nst) {
+        int vx = tx + a.stencil[3 * tid], vy = ty + a.stencil[3 * tid + 1], vz = tz + a.stencil[3 * tid + 2];
         bool ok = true;
-        if (periodic) {
+        if (a.periodic) {
             vx &= nd - 1; vy &= nd - 1; vz &= nd - 1;
         } else {
             ok = vx >= 0 && vy >= 0 && vz >= 0 && vx < nd && vy < nd && vz < nd;
         }
         if (ok) {
             uint32_t sc = morton_encode(vx, vy, vz);
-            e_beg[tid] = off[sc];
-            cnt = off[sc + 1] - off[sc];
+            sh.e_beg[tid] = a.off[sc];
+            cnt = a.off[sc + 1] - a.off[sc];
         } else {
-            e_beg[tid] = 0;
+            sh.e_beg[tid] = 0;
         }
-        e_d[tid] = make_float4((float)stencil[3 * tid], (float)stencil[3 * tid + 1], (float)stencil[3 * tid + 2], 0.f);
+        sh.e_d[tid] = make_float4((float)a.stencil[3 * tid], (float)a.stencil[3 * tid + 1],
+                                  (float)a.stencil[3 * tid + 2], 0.f);
     }
     // exclusive prefix over the stencil entries (nst <= 128)
     {
-        __shared__ int ws[4];
         int x = cnt;
         for (int o = 1; o < 32; o <<= 1) {
             int y = __shfl_up_sync(0xffffffffu, x, o);
             if (lane >= o) x += y;
         }
-        if (lane == 31) ws[warp] = x;
+        if (lane == 31) sh.ws[warp] = x;
         __syncthreads();
         int add = 0;
-        for (int w = 0; w < warp; w++) add += ws[w];
-        e_off[tid] = x - cnt + add;
+        for (int w = 0; w < warp; w++) add += sh.ws[w];
+        sh.e_off[tid] = x - cnt + add;
         __syncthreads();
-        if (tid == 0) e_off[nst] = ws[0] + ws[1] + ws[2] + ws[3];
+        if (tid == 0) sh.e_off[a.nst] = sh.ws[0] + sh.ws[1] + sh.ws[2] + sh.ws[3];
     }
     __syncthreads();
-    const int total = e_off[nst], nself = e_off[1];
-    float* srcf = reinterpret_cast<float*>(src);
+    const int total = sh.e_off[a.nst], nself = sh.e_off[1];
+    float* srcf = reinterpret_cast<float*>(sh.src);
     // a target outside its leaf (outside the box) can meet the image of a body
     // that lies well inside another leaf: then every pass takes the r = 0 test
     bool tedge = false;
     for (int i = tid; i < nt; i += P2P_THREADS) {
-        const float4 a = atoms[tb + i];
-        tedge |= fmaxf(fabsf(a.x), fmaxf(fabsf(a.y), fabsf(a.z))) >= 0.5f - 0x1p-20f;
+        const float4 b = a.atoms[tb + i];
+        tedge |= fmaxf(fabsf(b.x), fmaxf(fabsf(b.y), fabsf(b.z))) >= 0.5f - 0x1p-20f;
     }
     const bool target_edge = __syncthreads_or(tedge) != 0;
     for (int t0 = 0; t0 < nt; t0 += P2P_MAXT) {
         const int ntc = min(P2P_MAXT, nt - t0);
-        const float4* tgt = atoms + tb + t0;
-        for (int i = tid; i < 4 * P2P_MAXT; i += P2P_THREADS) part[i / P2P_MAXT][i % P2P_MAXT] = make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4* tgt = a.atoms + tb + t0;
+        for (int i = tid; i < 4 * P2P_MAXT; i += P2P_THREADS)
+            sh.part[i / P2P_MAXT][i % P2P_MAXT] = make_float4(0.f, 0.f, 0.f, 0.f);
         for (int s0 = 0; s0 < total; s0 += P2P_MAXS) {
             const int ns = min(P2P_MAXS, total - s0);
-            const int ns8 = (ns + 7) & ~7;
+            const int nsp = (ns + SPS - 1) / SPS * SPS;
             __syncthreads();
             // warp w copies whole source leaves w, w+4, ...: lane = body of the leaf,
-            // clipped to this pass's window [s0, s0+ns); far zero-charge padding to ns8
+            // clipped to this pass's window [s0, s0+ns); far zero-charge padding to nsp
             bool edge = false;
-            for (int e = warp; e < nst; e += 4) {
-                const int b0 = max(e_off[e], s0), b1 = min(e_off[e + 1], s0 + ns);
-                const float4 d = e_d[e];
-                const int gb = e_beg[e] - e_off[e];
+            for (int e = warp; e < a.nst; e += 4) {
+                const int b0 = max(sh.e_off[e], s0), b1 = min(sh.e_off[e + 1], s0 + ns);
+                const float4 d = sh.e_d[e];
+                const int gb = sh.e_beg[e] - sh.e_off[e];
                 for (int g = b0 + lane; g < b1; g += 32) {
-                    const float4 a = atoms[gb + g];
-                    edge |= fmaxf(fabsf(a.x), fmaxf(fabsf(a.y), fabsf(a.z))) >= 0.5f - 0x1p-20f;
+                    const float4 b = a.atoms[gb + g];
+                    edge |= fmaxf(fabsf(b.x), fmaxf(fabsf(b.y), fabsf(b.z))) >= 0.5f - 0x1p-20f;
                     const int r = g - s0;
                     float* rec = srcf + 8 * (r >> 1) + (r & 1);
-                    rec[0] = a.x + d.x;
-                    rec[2] = a.y + d.y;
-                    rec[4] = a.z + d.z;
-                    rec[6] = a.w;
+                    rec[0] = b.x + d.x;
+                    rec[2] = b.y + d.y;
+                    rec[4] = b.z + d.z;
+                    rec[6] = b.w;
                 }
             }
-            if (tid < ns8 - ns) {
+            if (tid < nsp - ns) {
                 const int r = ns + tid;
                 float* rec = srcf + 8 * (r >> 1) + (r & 1);
                 rec[0] = rec[2] = rec[4] = P2P_FAR;
                 rec[6] = 0.f;
             }
             const bool any_edge = (__syncthreads_or(edge) != 0) || target_edge;
-            // this warp's quarter of the source steps (8 sources per step); the
-            // steps holding the target leaf's own bodies need the r = 0 test
-            const int nsteps = ns8 >> 3;
+            // this warp's quarter of the source steps; the steps holding the
+            // target leaf's own bodies need the r = 0 test
+            const int nsteps = nsp / SPS;
             const int per = (nsteps + 3) >> 2;
             const int sb = warp * per, se = min(nsteps, sb + per);
-            const int msteps = any_edge ? nsteps : max(0, (min(nself, s0 + ns) - s0 + 7) >> 3);
-            for (int c0 = 0; c0 < ntc; c0 += 24) {
+            const int msteps = any_edge ? nsteps : max(0, (min(nself, s0 + ns) - s0 + SPS - 1) / SPS);
+            for (int c0 = 0; c0 < ntc; c0 += 3 * LT) {
                 const int rem = ntc - c0;
-                if (rem > 16) p2p_cluster<3>(src, tgt, c0, ntc, sb, se, msteps, lane, part[warp]);
-                else if (rem > 8) p2p_cluster<2>(src, tgt, c0, ntc, sb, se, msteps, lane, part[warp]);
-                else p2p_cluster<1>(src, tgt, c0, ntc, sb, se, msteps, lane, part[warp]);
+                if (rem > 2 * LT) p2p_cluster<3, LT>(sh.src, tgt, c0, ntc, sb, se, msteps, lane, sh.part[warp]);
+                else if (rem > LT) p2p_cluster<2, LT>(sh.src, tgt, c0, ntc, sb, se, msteps, lane, sh.part[warp]);
+                else p2p_cluster<1, LT>(sh.src, tgt, c0, ntc, sb, se, msteps, lane, sh.part[warp]);
             }
         }
         __syncthreads();
         for (int i = tid; i < ntc; i += P2P_THREADS) {
-            float4 r = part[0][i];
+            float4 r = sh.part[0][i];
             for (int w = 1; w < 4; w++) {
-                r.x += part[w][i].x;
-                r.y += part[w][i].y;
-                r.z += part[w][i].z;
-                r.w += part[w][i].w;
+                r.x += sh.part[w][i].x;
+                r.y += sh.part[w][i].y;
+                r.z += sh.part[w][i].z;
+                r.w += sh.part[w][i].w;
             }
-            field[tb + t0 + i] = r;
+            a.field[tb + t0 + i] = r;
         }
         __syncthreads();
     }
 }
 
-void launch_p2p(const int* offsets, int depth, int periodic, const float4* atoms, const int* stencil, int nst,
-                float4* field, cudaStream_t s)
+// One CTA per target leaf.
+template <int LT>
+__global__ void __launch_bounds__(P2P_THREADS) k_p2p(const P2PArgs a)
 {
-    int nleaf = 1 << (3 * depth);
+    __shared__ P2PShared sh;
+    p2p_leaf<LT>(a, blockIdx.x, sh);
+}
+
+int p2p_variants() { return 3; }
+
+void launch_p2p(const P2PArgs& a, int variant, cudaStream_t s)
+{
+    const int nleaf = 1 << (3 * a.depth);
     COUNT_LAUNCH();
-    k_p2p<<<nleaf, P2P_THREADS, 0, s>>>(offsets, depth, periodic, atoms, stencil, nst, field);
+    if (variant == 1) k_p2p<4><<<nleaf, P2P_THREADS, 0, s>>>(a);
+    else if (variant == 2) k_p2p<16><<<nleaf, P2P_THREADS, 0, s>>>(a);
+    else k_p2p<8><<<nleaf, P2P_THREADS, 0, s>>>(a);
 }
 
 // ------------------------------------------------------------------ M2M and L2L (one level per launch)

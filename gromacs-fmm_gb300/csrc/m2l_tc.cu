@@ -489,6 +489,14 @@ int tc_pick_stages(int k_atoms, int img_bytes, int nprod)
     return ns;
 }
 
+int tc_max_stages(int k_atoms, int img_bytes, int nprod)
+{
+    const size_t st = tc_stage_bytes(k_atoms, img_bytes, nprod);
+    int ns = TC_MAXSTAGE;
+    while (ns > 1 && 1024 + ns * st + (2 * TC_MAXSTAGE + 1) * sizeof(uint64_t) + 16 > 227 * 1024) ns--;
+    return ns;
+}
+
 void launch_m2l_tc(const TcArgs& a, int ntasks, cudaStream_t s)
 {
     if (ntasks <= 0) return;

@@ -21,7 +21,8 @@ constexpr int TC_MAXSTAGE = 8;   // pipeline stages (operands of one entry each)
 constexpr int TC_THREADS = 128;  // producer lane, MMA lane, 4 epilogue warps
 constexpr int TC_HALO = 2;       // halo of the source grids (cells of the grid)
 constexpr int TC_MAXLEV = 8;
-constexpr int TC_MAXENT = 256;   // stencil entries of one task (the stencils have at most 182)
+constexpr int TC_MAXENT = 256;
+constexpr int TC_NSPLIT = 4;     // entry splits 1, 2, 4, 8 of a tile's stencil (autotuned)   // stencil entries of one task (the stencils have at most 182)
 
 // Degree chunks of the M2L operator: chunk c covers output rows [row0, row0+rows)
 // (whole degrees j0..j1), MMA N = n (rows padded to 16), K = k (inputs of degree
@@ -94,6 +95,7 @@ bool tc_encode_maps(TcArgs& a, int D, const TcGrids& g, void* hi, void* lo);
 size_t tc_smem_bytes(const TcArgs& a);
 size_t tc_stage_bytes(int k_atoms, int img_bytes, int nprod);
 int tc_pick_stages(int k_atoms, int img_bytes, int nprod);
+int tc_max_stages(int k_atoms, int img_bytes, int nprod);  // most that fit one CTA's shared memory
 void launch_m2l_tc(const TcArgs& a, int ntasks, cudaStream_t s);
 
 }  // namespace gbfmm

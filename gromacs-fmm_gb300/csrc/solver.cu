@@ -178,8 +178,12 @@ struct gbfmm_handle {
     TcArgs* tca = nullptr;  // tensor maps and launch arguments (host, 64-byte aligned)
     uint8_t* d_img = nullptr;
     CEntry* d_tc_entries = nullptr;
-    CTask* d_tc_tasks = nullptr;
-    int tc_ntask = 0, tc_split = 1;
+    // tensor-core M2L task lists, one per entry split 2^v (v < TC_NSPLIT)
+    CTask* d_tc_tasks_v[TC_NSPLIT] = {};
+    int tc_task0_v[TC_NSPLIT] = {}, tc_ntask_v[TC_NSPLIT] = {};
+    int tc_split_v = 0;
+    int tc_nstage = 2;
+    int p2p_variant = 0;  // P2P warp-step shape (autotuned)
     StepConst* d_sc = nullptr;
     StepConst* h_sc = nullptr;  // pinned
     int* h_flags = nullptr;     // pinned
@@ -436,7 +440,6 @@ static int build_tasks(gbfmm_handle* h)
         h->l2l_ntask[k] = (int)tasks.size() - h->l2l_task0[k];
     }
     // tensor-core M2L: entries carry the class index, tiles of TC_TILE targets
-    int tc_task0 = (int)tasks.size();
     if (h->tc) {
         int e_tc[2][8];
         for (int lt = 0; lt < 2; lt++)
@@ -450,38 +453,53 @@ static int build_tasks(gbfmm_handle* h)
                     ent.push_back(e);
                 }
             }
+        // task lists for the entry splits 1, 2, 4, 8 (a tile's stencil entries
+        // cut into that many ranges; split > 1 adds into L with atomics); the
+        // autotuner picks one, the default fills the GPU with CTAs
         long tiles = 0;
         for (int k = 1; k <= D; k++) tiles += 8L * tc_tiles(k);
-        int sp = h->prm.m2l_split > 0 ? h->prm.m2l_split : 1;
-        if (h->prm.m2l_split <= 0)
-            while (tiles * sp < 152 && sp < 8) sp *= 2;
-        if (h->prm.flags & GBFMM_FLAG_DETERMINISTIC) sp = 1;
-        h->tc_split = sp;
-        for (int k = 1; k <= D; k++) {
-            const int lt = k == 1 ? 0 : 1;
-            int bx, by, bz;
-            tc_tile_shape(k, bx, by, bz);
-            for (int s = 0; s < 8; s++) {
-                int eb = e_tc[lt][s], ne = (int)t->st.m2l[lt][s].size();
-                int ch = (ne + sp - 1) / sp;
-                for (int q = 0; q < tc_tiles(k); q++)
-                    for (int e0 = 0; e0 < ne; e0 += ch) {
-                        CTask c;
-                        c.level = k; c.octant = s; c.q0 = q; c.ntgt = bx * by * bz;
-                        c.e_begin = eb + e0; c.e_end = eb + std::min(ne, e0 + ch);
-                        c.group = 0; c.r0 = 0; c.r1 = h->R;
-                        tasks.push_back(c);
-                    }
-            }
+        int def = 0;
+        if (h->prm.m2l_split > 0) {
+            while (def < 3 && (1 << def) < h->prm.m2l_split) def++;
+        } else {
+            while (tiles * (1L << def) < 152 && def < 3) def++;
         }
-        h->tc_ntask = (int)tasks.size() - tc_task0;
+        const bool det = (h->prm.flags & GBFMM_FLAG_DETERMINISTIC) != 0;
+        if (det) def = 0;
+        for (int v = 0; v < TC_NSPLIT; v++) {
+            const int sp = 1 << v;
+            h->tc_task0_v[v] = (int)tasks.size();
+            if (det && v > 0) {
+                h->tc_ntask_v[v] = 0;
+                continue;
+            }
+            for (int k = 1; k <= D; k++) {
+                const int lt = k == 1 ? 0 : 1;
+                int bx, by, bz;
+                tc_tile_shape(k, bx, by, bz);
+                for (int s = 0; s < 8; s++) {
+                    int eb = e_tc[lt][s], ne = (int)t->st.m2l[lt][s].size();
+                    int ch = (ne + sp - 1) / sp;
+                    for (int q = 0; q < tc_tiles(k); q++)
+                        for (int e0 = 0; e0 < ne; e0 += ch) {
+                            CTask c;
+                            c.level = k; c.octant = s; c.q0 = q; c.ntgt = bx * by * bz;
+                            c.e_begin = eb + e0; c.e_end = eb + std::min(ne, e0 + ch);
+                            c.group = 0; c.r0 = 0; c.r1 = h->R;
+                            tasks.push_back(c);
+                        }
+                }
+            }
+            h->tc_ntask_v[v] = (int)tasks.size() - h->tc_task0_v[v];
+        }
+        h->tc_split_v = def;
     }
     void* p = nullptr;
     h->tasks_bytes = sizeof(CEntry) * ent.size() + sizeof(CTask) * tasks.size() + 512;
     CK(cudaMalloc(&p, h->tasks_bytes));
     h->d_entries = (CEntry*)p;
     h->d_tasks = (CTask*)((char*)p + ((sizeof(CEntry) * ent.size() + 255) & ~(size_t)255));
-    h->d_tc_tasks = h->d_tasks + tc_task0;
+    for (int v = 0; v < TC_NSPLIT; v++) h->d_tc_tasks_v[v] = h->d_tasks + h->tc_task0_v[v];
     CK(cudaMemcpy(h->d_entries, ent.data(), sizeof(CEntry) * ent.size(), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(h->d_tasks, tasks.data(), sizeof(CTask) * tasks.size(), cudaMemcpyHostToDevice));
     return GBFMM_OK;
@@ -502,7 +520,7 @@ static int make_tc_args(gbfmm_handle* h)
     for (int k = 0; k <= h->D; k++) a->dst_lvl[k] = h->Llev[k];
     a->bimg = h->d_img;
     a->entries = h->d_entries;
-    a->tasks = h->d_tc_tasks;
+    a->tasks = h->d_tc_tasks_v[h->tc_split_v];
     a->err = h->d_flags + 1;
     a->Rpad = h->Rpad;
     a->k_atoms = pl.k_atoms;
@@ -511,7 +529,8 @@ static int make_tc_args(gbfmm_handle* h)
     a->nchunk = pl.nchunk;
     a->nprod = h->prm.precision == GBFMM_PREC_BF16X1 ? 1 : 3;
     a->nstage = tc_pick_stages(pl.k_atoms, pl.img_bytes, a->nprod);
-    a->atomic = h->tc_split > 1 ? 1 : 0;
+    h->tc_nstage = a->nstage;
+    a->atomic = h->tc_split_v > 0 ? 1 : 0;
     for (int c = 0; c < pl.nchunk; c++) {
         a->chunk_n[c] = pl.n[c];
         a->chunk_k[c] = pl.k[c];
@@ -655,7 +674,11 @@ static void enqueue_step(gbfmm_handle* h)
     mark(h, 4);
     if (h->tc) {
         launch_tc_grids(tc_grid_args(h), s);
-        launch_m2l_tc(*h->tca, h->tc_ntask, s);
+        TcArgs& ta = *h->tca;  // the current tuning: entry split and pipeline depth
+        ta.tasks = h->d_tc_tasks_v[h->tc_split_v];
+        ta.atomic = h->tc_split_v > 0 ? 1 : 0;
+        ta.nstage = h->tc_nstage;
+        launch_m2l_tc(ta, h->tc_ntask_v[h->tc_split_v], s);
     } else {
         ContractArgs a = contract_args(h, OP_M2L, 2, false, h->m2l_task0);
         launch_contract(a, h->m2l_ntask, s);
@@ -666,7 +689,17 @@ static void enqueue_step(gbfmm_handle* h)
     mark(h, 6);
     launch_l2p(h->P, h->d_off, h->nleaf, h->d_atoms, h->Llev[D], h->Rpad, h->d_far, s);
     mark(h, 7);
-    launch_p2p(h->d_off, D, h->periodic ? 1 : 0, h->d_atoms, h->d_p2p_st, h->n_p2p_st, h->d_near, s);
+    {
+        P2PArgs pa;
+        pa.off = h->d_off;
+        pa.depth = D;
+        pa.periodic = h->periodic ? 1 : 0;
+        pa.atoms = h->d_atoms;
+        pa.stencil = h->d_p2p_st;
+        pa.nst = h->n_p2p_st;
+        pa.field = h->d_near;
+        launch_p2p(pa, h->p2p_variant, s);
+    }
     mark(h, 8);
     if (n > 0) {
         FinalArgs fa;
@@ -957,6 +990,110 @@ extern "C" int gbfmm_execute(gbfmm_handle* h, const float* coords, const float* 
         std::printf("[gbfmm] natoms=%d P=%d depth=%d images=%d energy=%.8f\n", h->n, h->P, h->D, h->prm.images,
                     *h->h_energy);
     return rc;
+}
+
+// ---- autotuner: warp-step shape of P2P, entry split and pipeline depth of the
+// tensor-core M2L, chosen by timing whole steps (CUDA-graph replays) of the
+// caller's own configuration.
+
+static void apply_tuning(gbfmm_handle* h, int p2p_variant, int split_v, int nstage)
+{
+    h->p2p_variant = p2p_variant;
+    h->tc_split_v = split_v;
+    h->tc_nstage = nstage;
+    if (h->gexec) {
+        cudaGraphExecDestroy(h->gexec);
+        h->gexec = nullptr;
+    }
+}
+
+extern "C" int gbfmm_set_tuning(gbfmm_handle* h, int p2p_variant, int m2l_split, int m2l_stages)
+{
+    if (!h) return fail(GBFMM_ERR_ARG, "handle is NULL");
+    if (p2p_variant < 0 || p2p_variant >= p2p_variants()) return fail(GBFMM_ERR_ARG, "p2p variant %d", p2p_variant);
+    int v = 0;
+    while (v < TC_NSPLIT - 1 && (1 << v) < m2l_split) v++;
+    if (m2l_split < 1 || (1 << v) != m2l_split) return fail(GBFMM_ERR_ARG, "m2l split %d is not 1, 2, 4 or 8", m2l_split);
+    int ns = h->tc_nstage;
+    if (h->tc) {
+        if (h->tc_ntask_v[v] == 0) return fail(GBFMM_ERR_ARG, "m2l split %d unavailable (deterministic handle)", m2l_split);
+        const TcPlan& pl = h->tab->tc;
+        const int mx = tc_max_stages(pl.k_atoms, pl.img_bytes, h->tca->nprod);
+        if (m2l_stages < 1 || m2l_stages > mx) return fail(GBFMM_ERR_ARG, "m2l stages %d outside [1,%d]", m2l_stages, mx);
+        ns = m2l_stages;
+    }
+    CK(cudaStreamSynchronize(h->stream));
+    apply_tuning(h, p2p_variant, v, ns);
+    return GBFMM_OK;
+}
+
+extern "C" int gbfmm_get_tuning(gbfmm_handle* h, int* p2p_variant, int* m2l_split, int* m2l_stages)
+{
+    if (!h) return fail(GBFMM_ERR_ARG, "handle is NULL");
+    if (p2p_variant) *p2p_variant = h->p2p_variant;
+    if (m2l_split) *m2l_split = 1 << h->tc_split_v;
+    if (m2l_stages) *m2l_stages = h->tc_nstage;
+    return GBFMM_OK;
+}
+
+extern "C" int gbfmm_autotune(gbfmm_handle* h, const float* coords, const float* box, int reps, float* best_ms)
+{
+    if (!h) return fail(GBFMM_ERR_ARG, "handle is NULL");
+    if (!h->have_charges) return fail(GBFMM_ERR_STATE, "charges not set");
+    if (h->n > 0 && !coords) return fail(GBFMM_ERR_ARG, "coordinates are NULL");
+    if (reps <= 0) reps = 5;
+    int rc = set_box(h, box, h->d_coords);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(h->d_coords, coords, sizeof(float) * 3 * h->n, cudaMemcpyHostToDevice, h->stream));
+    const bool timing = h->timing;
+    h->timing = false;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    int err = GBFMM_OK;
+    auto measure = [&](int pv, int sv, int ns) -> float {
+        apply_tuning(h, pv, sv, ns);
+        for (int i = 0; i < 2 && err == GBFMM_OK; i++) err = run_step(h);
+        if (err) return 1e30f;
+        cudaEventRecord(e0, h->stream);
+        for (int i = 0; i < reps && err == GBFMM_OK; i++) err = run_step(h);
+        cudaEventRecord(e1, h->stream);
+        if (cudaEventSynchronize(e1) != cudaSuccess) err = GBFMM_ERR_CUDA;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        return err ? 1e30f : ms / reps;
+    };
+    int bp = h->p2p_variant, bs = h->tc_split_v, bn = h->tc_nstage;
+    float bt = measure(bp, bs, bn);
+    // coordinate search: P2P shape, then M2L split, then M2L pipeline depth
+    for (int pv = 0; pv < p2p_variants() && !err; pv++) {
+        if (pv == bp) continue;
+        const float t = measure(pv, bs, bn);
+        if (t < bt) { bt = t; bp = pv; }
+    }
+    if (h->tc) {
+        for (int sv = 0; sv < TC_NSPLIT && !err; sv++) {
+            if (sv == bs || h->tc_ntask_v[sv] == 0) continue;
+            const float t = measure(bp, sv, bn);
+            if (t < bt) { bt = t; bs = sv; }
+        }
+        const TcPlan& pl = h->tab->tc;
+        const int cand[3] = {2, tc_pick_stages(pl.k_atoms, pl.img_bytes, h->tca->nprod),
+                             tc_max_stages(pl.k_atoms, pl.img_bytes, h->tca->nprod)};
+        for (int c = 0; c < 3 && !err; c++) {
+            const int ns = std::min(cand[c], cand[2]);
+            if (ns == bn || ns < 1) continue;
+            const float t = measure(bp, bs, ns);
+            if (t < bt) { bt = t; bn = ns; }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    apply_tuning(h, bp, bs, bn);
+    h->timing = timing;
+    if (err) return err;
+    if (best_ms) *best_ms = bt;
+    return GBFMM_OK;
 }
 
 extern "C" int gbfmm_device_outputs(gbfmm_handle* h, void** f, void** p, void** e)

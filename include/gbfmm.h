@@ -207,6 +207,18 @@ int gbfmm_tree_build_noalloc(const void* coords, const void* charges, int natoms
 int gbfmm_debug_operator(int order, int images, int kind, int index, double* mat, int* dim, double* class_vec);
 int gbfmm_debug_harmonics(int order, int kind, const double* d, double* out);
 
+/* ---- autotuner (tile shapes) ----
+ * gbfmm_autotune times whole steps (CUDA-graph replays, reps per candidate) of
+ * the given configuration for the P2P warp-step shapes and, on the tensor-core
+ * path, the M2L entry split (1, 2, 4, 8; 1 only on a deterministic handle) and
+ * pipeline depth, and keeps the fastest (best_ms: its step time; may be NULL).
+ * Results are the same up to the order of floating-point additions.  No
+ * reference counterpart: the reference's launch shapes are fixed
+ * (gpu_solver.cu:221-248). */
+int gbfmm_autotune(gbfmm_handle* h, const float* coords, const float* box, int reps, float* best_ms);
+int gbfmm_get_tuning(gbfmm_handle* h, int* p2p_variant, int* m2l_split, int* m2l_stages);
+int gbfmm_set_tuning(gbfmm_handle* h, int p2p_variant, int m2l_split, int m2l_stages);
+
 /* ---- batched solves ---- */
 
 /* Many independent cubic systems solved as one batch through one captured

@@ -1,0 +1,69 @@
+"""The tile-shape autotuner: every P2P warp-step shape and every tensor-core M2L
+entry split and pipeline depth gives the same forces (up to the order of the
+floating-point additions) and the FP64 oracle's to the path's tolerance; the
+autotuner keeps one of them and reports its step time."""
+import numpy as np
+import pytest
+
+from conftest import rel_rms
+
+pytestmark = pytest.mark.gpu
+
+
+def _system(systems):
+    xyz, q, box = systems.water_ion_box(6000, 5.6, n_na=8, n_cl=8, seed=71)
+    return xyz, q, float(box[0])
+
+
+@pytest.mark.parametrize("precision,tol", [(0, 1e-5), (1, 1e-4), (2, 3e-3)])
+def test_every_shape_matches(pkg, oracle, systems, precision, tol):
+    xyz, q, L = _system(systems)
+    s = pkg.ZetaFmmSolver(len(q), q, order=6, max_depth=3, images=4, precision=precision)
+    s.execute(xyz, L)
+    f0 = s.forces()
+    _, fo, _ = oracle.zeta_solve(xyz.astype(np.float64), q.astype(np.float64), L, 6, 3, 4)
+    assert rel_rms(f0, fo) < tol
+    splits = (1, 2, 4, 8) if precision else (1,)
+    stages = (1, 2) if precision else (2,)
+    for pv in range(3):
+        for sp in splits:
+            for ns in stages:
+                if precision:
+                    s.set_tuning(pv, sp, ns)
+                else:
+                    s.set_tuning(pv, 1, s.tuning()["m2l_stages"])
+                s.execute(xyz, L)
+                assert rel_rms(s.forces(), f0) < 1e-5, (pv, sp, ns)
+    s.close()
+
+
+def test_autotune_keeps_a_valid_tuning(pkg, systems):
+    xyz, q, L = _system(systems)
+    s = pkg.ZetaFmmSolver(len(q), q, order=5, max_depth=3, images=4, precision=2)
+    s.execute(xyz, L)
+    f0 = s.forces()
+    t = s.autotune(xyz, L, reps=3)
+    assert t["ms"] > 0 and t["p2p_variant"] in (0, 1, 2) and t["m2l_split"] in (1, 2, 4, 8)
+    s.execute(xyz, L)
+    assert rel_rms(s.forces(), f0) < 1e-5
+    s.close()
+
+
+def test_deterministic_handle_keeps_whole_tiles(pkg, systems):
+    xyz, q, L = _system(systems)
+    s = pkg.ZetaFmmSolver(len(q), q, order=5, max_depth=3, images=4, precision=1, flags=pkg.FLAG_DETERMINISTIC)
+    assert s.tuning()["m2l_split"] == 1
+    with pytest.raises(pkg.FmmError):
+        s.set_tuning(0, 2, 2)
+    s.execute(xyz, L)
+    f1 = s.forces()
+    s.autotune(xyz, L, reps=2)
+    assert s.tuning()["m2l_split"] == 1
+    s.execute(xyz, L)
+    f2 = s.forces()
+    s.set_tuning(s.tuning()["p2p_variant"], 1, s.tuning()["m2l_stages"])
+    # the same shapes give bit-identical results on a deterministic handle
+    s.execute(xyz, L)
+    assert np.array_equal(s.forces(), f2)
+    assert rel_rms(f2, f1) < 1e-5
+    s.close()
