@@ -136,6 +136,10 @@ struct gbfmm_handle {
     bool periodic = true;
     const OpTables* tab = nullptr;
     cudaStream_t stream = nullptr;
+    // P2P runs on its own low-priority stream, concurrently with the far field
+    // (captured as a fork/join of the step graph)
+    cudaStream_t stream_nf = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     // host state
     std::vector<float> h_q;
     bool have_charges = false, have_result = false, results_on_host = false;
@@ -261,6 +265,9 @@ static void free_handle(gbfmm_handle* h)
     if (h->h_pots) cudaFreeHost(h->h_pots);
     if (h->h_energy) cudaFreeHost(h->h_energy);
     if (h->stream) cudaStreamDestroy(h->stream);
+    if (h->stream_nf) cudaStreamDestroy(h->stream_nf);
+    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    if (h->ev_join) cudaEventDestroy(h->ev_join);
     delete h;
 }
 
@@ -651,6 +658,24 @@ static void enqueue_step(gbfmm_handle* h)
     launch_scatter(h->d_code, n, h->d_cursor, h->d_tmp, s);
     launch_leaf_sort(h->d_off, h->nleaf, h->d_tmp, h->d_uq, h->d_code, h->d_order, h->d_atoms, h->d_atom_leaf, s);
     mark(h, 1);
+    // The near field needs only the tree: in graph mode it forks onto its own
+    // stream and overlaps the far-field chain below (joined before finalize);
+    // the stage-timing pass runs it in line, after L2P.
+    P2PArgs pa;
+    pa.off = h->d_off;
+    pa.depth = D;
+    pa.periodic = h->periodic ? 1 : 0;
+    pa.atoms = h->d_atoms;
+    pa.stencil = h->d_p2p_st;
+    pa.nst = h->n_p2p_st;
+    pa.field = h->d_near;
+    const bool fork = !h->timing;
+    if (fork) {
+        cudaEventRecord(h->ev_fork, s);
+        cudaStreamWaitEvent(h->stream_nf, h->ev_fork, 0);
+        launch_p2p(pa, h->p2p_variant, h->stream_nf);
+        cudaEventRecord(h->ev_join, h->stream_nf);
+    }
     launch_p2m(h->P, h->d_off, h->nleaf, h->d_atoms, h->Mlev[D], h->Rpad, s);
     mark(h, 2);
     for (int k = D - 1; k >= 1; k--) launch_m2m(h->Mlev[k + 1], h->Mlev[k], h->d_m2m_t, 1 << (3 * k), h->R, h->Rpad, s);
@@ -689,17 +714,8 @@ static void enqueue_step(gbfmm_handle* h)
     mark(h, 6);
     launch_l2p(h->P, h->d_off, h->nleaf, h->d_atoms, h->Llev[D], h->Rpad, h->d_far, s);
     mark(h, 7);
-    {
-        P2PArgs pa;
-        pa.off = h->d_off;
-        pa.depth = D;
-        pa.periodic = h->periodic ? 1 : 0;
-        pa.atoms = h->d_atoms;
-        pa.stencil = h->d_p2p_st;
-        pa.nst = h->n_p2p_st;
-        pa.field = h->d_near;
-        launch_p2p(pa, h->p2p_variant, s);
-    }
+    if (fork) cudaStreamWaitEvent(s, h->ev_join, 0);
+    else launch_p2p(pa, h->p2p_variant, s);
     mark(h, 8);
     if (n > 0) {
         FinalArgs fa;
@@ -766,7 +782,15 @@ extern "C" int gbfmm_create(const gbfmm_params* prm, int natoms, gbfmm_handle** 
         free_handle(h);
         return code;
     };
-    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(fail(GBFMM_ERR_CUDA, "stream create failed"));
+    {
+        int lo = 0, hi = 0;
+        cudaDeviceGetStreamPriorityRange(&lo, &hi);
+        if (cudaStreamCreateWithPriority(&h->stream, cudaStreamNonBlocking, hi) != cudaSuccess ||
+            cudaStreamCreateWithPriority(&h->stream_nf, cudaStreamNonBlocking, lo) != cudaSuccess ||
+            cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess)
+            return bail(fail(GBFMM_ERR_CUDA, "stream create failed"));
+    }
     Arena sz;
     layout(h, sz);
     h->arena_bytes = sz.off + 256;
@@ -913,7 +937,7 @@ static int run_step(gbfmm_handle* h)
             enqueue_step(h);
             cudaError_t e = cudaStreamEndCapture(h->stream, &g);
             if (e != cudaSuccess) return fail(GBFMM_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
-            e = cudaGraphInstantiate(&h->gexec, g, 0);
+            e = cudaGraphInstantiate(&h->gexec, g, cudaGraphInstantiateFlagUseNodePriority);
             cudaGraphDestroy(g);
             if (e != cudaSuccess) return fail(GBFMM_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
         }
@@ -1429,7 +1453,7 @@ static int batch_capture(gbfmm_batch* b)
     }
     cudaError_t e = cudaStreamEndCapture(b->master, &g);
     if (e != cudaSuccess) return fail(GBFMM_ERR_CUDA, "batch graph capture: %s", cudaGetErrorString(e));
-    e = cudaGraphInstantiate(&b->gexec, g, 0);
+    e = cudaGraphInstantiate(&b->gexec, g, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(GBFMM_ERR_CUDA, "batch graph instantiate: %s", cudaGetErrorString(e));
     return GBFMM_OK;
