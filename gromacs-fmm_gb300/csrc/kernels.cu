@@ -776,15 +776,47 @@ __global__ void __launch_bounds__(P2P_THREADS) k_p2p(const P2PArgs a)
     p2p_leaf<LT>(a, blockIdx.x, sh);
 }
 
-int p2p_variants() { return 3; }
+// Persistent form: a fixed number of CTAs per SM walk the queue of leaves
+// through an atomic counter (zero when the step starts), fetching the next leaf
+// while they work on the current one.  With fewer CTAs than the SM holds, the
+// concurrently running far-field kernels keep room to start.
+template <int LT>
+__global__ void __launch_bounds__(P2P_THREADS) k_p2p_queue(const P2PArgs a, int* counter, int nitems)
+{
+    __shared__ P2PShared sh;
+    __shared__ int next;
+    if (threadIdx.x == 0) next = atomicAdd(counter, 1);
+    __syncthreads();
+    int item = next;
+    while (item < nitems) {
+        __syncthreads();  // every thread has read 'next'
+        if (threadIdx.x == 0) next = atomicAdd(counter, 1);
+        p2p_leaf<LT>(a, (uint32_t)item, sh);
+        __syncthreads();
+        item = next;
+    }
+}
 
-void launch_p2p(const P2PArgs& a, int variant, cudaStream_t s)
+int p2p_variants() { return 3 * 5; }
+
+void launch_p2p(const P2PArgs& a, int variant, cudaStream_t s, int* counter)
 {
     const int nleaf = 1 << (3 * a.depth);
+    const int shape = variant % 3, per_sm = variant / 3;  // per_sm 0: one CTA per leaf
     COUNT_LAUNCH();
-    if (variant == 1) k_p2p<4><<<nleaf, P2P_THREADS, 0, s>>>(a);
-    else if (variant == 2) k_p2p<16><<<nleaf, P2P_THREADS, 0, s>>>(a);
-    else k_p2p<8><<<nleaf, P2P_THREADS, 0, s>>>(a);
+    if (per_sm == 0 || !counter) {
+        if (shape == 1) k_p2p<4><<<nleaf, P2P_THREADS, 0, s>>>(a);
+        else if (shape == 2) k_p2p<16><<<nleaf, P2P_THREADS, 0, s>>>(a);
+        else k_p2p<8><<<nleaf, P2P_THREADS, 0, s>>>(a);
+        return;
+    }
+    int sms = 152;
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int grid = std::min(nleaf, sms * (per_sm + 1));  // 2..5 CTAs per SM
+    if (shape == 1) k_p2p_queue<4><<<grid, P2P_THREADS, 0, s>>>(a, counter, nleaf);
+    else if (shape == 2) k_p2p_queue<16><<<grid, P2P_THREADS, 0, s>>>(a, counter, nleaf);
+    else k_p2p_queue<8><<<grid, P2P_THREADS, 0, s>>>(a, counter, nleaf);
 }
 
 // ------------------------------------------------------------------ M2M and L2L (one level per launch)

@@ -108,9 +108,11 @@ void launch_leaf_sort(const int* offsets, int nleaf, int* tmp_idx, const float4*
 void launch_p2m(int P, const int* offsets, int nleaf, const float4* atoms, float* M_leaf, int Rpad, cudaStream_t s);
 void launch_l2p(int P, const int* offsets, int nleaf, const float4* atoms, const float* L_leaf, int Rpad, float4* field,
                 cudaStream_t s);
-// Near field.  variant: the warp-step shape (0: 8 targets x 4 source lanes,
-// 1: 4 x 8, 2: 16 x 2), chosen by the autotuner; all give the same sums up to the
-// order of the additions.
+// Near field.  variant = shape + 3 * persistence: shape = the warp-step shape
+// (0: 8 targets x 4 source lanes, 1: 4 x 8, 2: 16 x 2); persistence 0 = one CTA
+// per leaf, 1..4 = (persistence + 1) CTAs per SM walking the leaves through
+// *counter (zero at launch).  Chosen by the autotuner; all give the same sums up
+// to the order of the additions.
 struct P2PArgs {
     const int* off;           // leaf offsets (8^depth + 1)
     int depth, periodic;
@@ -120,7 +122,7 @@ struct P2PArgs {
     float4* field;            // sorted near field (phi, grad), scaled units
 };
 int p2p_variants();
-void launch_p2p(const P2PArgs& a, int variant, cudaStream_t s);
+void launch_p2p(const P2PArgs& a, int variant, cudaStream_t s, int* counter);
 void launch_contract(const ContractArgs& a, int ntasks, cudaStream_t s);
 // One level of M2M (nparent parents from their 8 children each) or L2L (the 8
 // children of each of nparent parents); At = 8 transposed R x R scaled operators.

@@ -613,7 +613,7 @@ static void enqueue_step(gbfmm_handle* h)
     const int D = h->D, n = h->n;
     const long launches0 = g_kernel_launches.load();
     mark(h, 0);
-    int* sync = h->d_counts + h->nleaf + 1;  // [0] tree keys, [1] finalize
+    int* sync = h->d_counts + h->nleaf + 1;  // [0] tree keys, [1] finalize, [2] P2P queue
     cudaMemsetAsync(h->d_counts, 0, sizeof(int) * (h->nleaf + 1 + 4), s);
     cudaMemsetAsync(h->d_L, 0, sizeof(float) * h->lev_floats, s);
     {
@@ -673,7 +673,7 @@ static void enqueue_step(gbfmm_handle* h)
     if (fork) {
         cudaEventRecord(h->ev_fork, s);
         cudaStreamWaitEvent(h->stream_nf, h->ev_fork, 0);
-        launch_p2p(pa, h->p2p_variant, h->stream_nf);
+        launch_p2p(pa, h->p2p_variant, h->stream_nf, sync + 2);
         cudaEventRecord(h->ev_join, h->stream_nf);
     }
     launch_p2m(h->P, h->d_off, h->nleaf, h->d_atoms, h->Mlev[D], h->Rpad, s);
@@ -715,7 +715,7 @@ static void enqueue_step(gbfmm_handle* h)
     launch_l2p(h->P, h->d_off, h->nleaf, h->d_atoms, h->Llev[D], h->Rpad, h->d_far, s);
     mark(h, 7);
     if (fork) cudaStreamWaitEvent(s, h->ev_join, 0);
-    else launch_p2p(pa, h->p2p_variant, s);
+    else launch_p2p(pa, h->p2p_variant, s, sync + 2);
     mark(h, 8);
     if (n > 0) {
         FinalArgs fa;
