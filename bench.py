@@ -313,6 +313,67 @@ class Runner:
         return acc
 
 
+def batch_line(pkg, torch, dev, systems, steps, warmup):
+    """64 independent systems (atom counts log-uniform in [2,000, 200,000], water +
+    0.15 M NaCl, one cubic box each; order 6, BF16X3, depth for 16-128 bodies per
+    leaf): one batched CUDA graph (gbfmm_batch_*, near fields in one persistent
+    kernel) against the same systems solved one after another, device-resident,
+    L2 flushed before every step."""
+    tuner_mod = G.load_module("tuner")
+    sy = systems.batch_systems(n_sys=64)
+    nat = [len(s[1]) for s in sy]
+    P, prec = 6, 1
+    depths = [tuner_mod.plain_depth(n) for n in nat]
+    X = np.concatenate([s[0] for s in sy]).astype(np.float32)
+    Q = np.concatenate([s[1] for s in sy]).astype(np.float32)
+    B = np.array([float(s[2][0]) for s in sy], np.float32)
+    xd = torch.from_numpy(X).to(dev)
+    qd = torch.from_numpy(Q).to(dev)
+    st = torch.cuda.current_stream(dev)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+
+    def timed(fn):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        tot = 0.0
+        for _ in range(steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            fn()
+            e1.record(st)
+            e1.synchronize()
+            tot += e0.elapsed_time(e1)
+        return tot / steps
+
+    b = pkg.BatchSolver(nat, [P] * len(nat), depths, images=4, precision=prec)
+    b.execute(X, Q, B)  # captures the graph
+    ms_batch = timed(lambda: b.execute_device(xd.data_ptr(), qd.data_ptr(), B, st.cuda_stream))
+    b.close()
+    off = np.concatenate([[0], np.cumsum(nat)])
+    singles = []
+    for i, (xyz, q, box) in enumerate(sy):
+        s = pkg.ZetaFmmSolver(len(q), q, order=P, max_depth=depths[i], images=4, precision=prec)
+        s.execute(xyz, float(box[0]))
+        singles.append(s)
+
+    def seq():
+        for i, s in enumerate(singles):
+            s.execute_device(xd.data_ptr() + 12 * int(off[i]), float(B[i]), st.cuda_stream)
+
+    ms_seq = timed(seq)
+    for s in singles:
+        s.close()
+    n = int(off[-1])
+    return {"workload": f"64 systems, {n} atoms (log-uniform 2,000-200,000 per system), order {P}, "
+                        f"{PREC_NAME[prec]}, depth for 16-128 bodies per leaf",
+            "atoms": n, "value": n / (ms_batch * 1e-3), "unit": UNIT, "ms_per_step": ms_batch,
+            "sequential_single_solves": {"value": n / (ms_seq * 1e-3), "ms_per_step": ms_seq},
+            "speedup_vs_sequential": ms_seq / ms_batch}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -320,6 +381,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbfmm", choices=["gbfmm", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--no-batch", action="store_true", help="skip the 64-system batched line")
     ap.add_argument("--profile", default=None,
                     help="precision,order,depth: only run --steps host-API steps of that configuration "
                          "(a short, fixed launch sequence for ncu captures); prints no bench line")
@@ -471,6 +533,8 @@ def main():
             "tuner": tuner_info, "tile_autotune": {"tuned": tuned["tiles"], "plain": plain["tiles"]},
             "sweep": tune, "stage_ms": st, "kernels": kern, "roofline": roof, "clocks": tuned["clocks"],
             "gpu_launches": tuned["launches"] * args.steps}
+    if rank == 0 and not args.no_batch:
+        line["batch"] = batch_line(pkg, torch, dev, systems, max(3, min(args.steps, 10)), 2)
     if rank == 0:
         v, cores, sec = cpu_reference(xyz, q, box, PLAIN[1], PLAIN[2], args.cpu_steps, 1)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",

@@ -797,6 +797,50 @@ __global__ void __launch_bounds__(P2P_THREADS) k_p2p_queue(const P2PArgs a, int*
     }
 }
 
+// Batched form: the leaves of many systems in one queue.  Item i belongs to the
+// system s with first[s] <= i < first[s+1] (systems ordered by work per leaf,
+// heaviest first, so that the queue ends with the light leaves).
+template <int LT>
+__global__ void __launch_bounds__(P2P_THREADS) k_p2p_batch(const P2PBatchArgs b)
+{
+    __shared__ P2PShared sh;
+    __shared__ int next, leaf;
+    __shared__ P2PArgs cur;
+    if (threadIdx.x == 0) next = atomicAdd(b.counter, 1);
+    __syncthreads();
+    int item = next;
+    while (item < b.nitems) {
+        __syncthreads();  // every thread has read 'next' and finished with 'cur'
+        if (threadIdx.x == 0) {
+            next = atomicAdd(b.counter, 1);
+            int lo = 0, hi = b.nsys - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (b.first[mid] <= item) lo = mid;
+                else hi = mid - 1;
+            }
+            cur = b.sys[lo];
+            leaf = item - b.first[lo];
+        }
+        __syncthreads();
+        p2p_leaf<LT>(cur, (uint32_t)leaf, sh);
+        __syncthreads();
+        item = next;
+    }
+}
+
+void launch_p2p_batch(const P2PBatchArgs& b, int shape, int per_sm, cudaStream_t s)
+{
+    if (b.nitems <= 0) return;
+    int sms = 152, dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int grid = std::min(b.nitems, sms * std::max(1, std::min(per_sm, 5)));
+    COUNT_LAUNCH();
+    if (shape == 1) k_p2p_batch<4><<<grid, P2P_THREADS, 0, s>>>(b);
+    else if (shape == 2) k_p2p_batch<16><<<grid, P2P_THREADS, 0, s>>>(b);
+    else k_p2p_batch<8><<<grid, P2P_THREADS, 0, s>>>(b);
+}
+
 int p2p_variants() { return 3 * 5; }
 
 void launch_p2p(const P2PArgs& a, int variant, cudaStream_t s, int* counter)

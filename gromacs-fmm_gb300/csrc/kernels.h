@@ -122,6 +122,14 @@ struct P2PArgs {
     float4* field;            // sorted near field (phi, grad), scaled units
 };
 int p2p_variants();
+// Near fields of many systems in one persistent launch (per_sm CTAs per SM).
+struct P2PBatchArgs {
+    const P2PArgs* sys;  // nsys (device)
+    const int* first;    // nsys + 1 prefix sums of the systems' leaf counts (device)
+    int nsys, nitems;
+    int* counter;        // zero at launch
+};
+void launch_p2p_batch(const P2PBatchArgs& b, int shape, int per_sm, cudaStream_t s);
 void launch_p2p(const P2PArgs& a, int variant, cudaStream_t s, int* counter);
 void launch_contract(const ContractArgs& a, int ntasks, cudaStream_t s);
 // One level of M2M (nparent parents from their 8 children each) or L2L (the 8

@@ -606,8 +606,30 @@ static void mark(gbfmm_handle* h, int stage)
     if (h->timing) cudaEventRecord(h->ev[stage], h->stream);
 }
 
-// Enqueues one full step on h->stream (captured into the graph on first use).
-static void enqueue_step(gbfmm_handle* h)
+static P2PArgs p2p_args(const gbfmm_handle* h)
+{
+    P2PArgs pa;
+    pa.off = h->d_off;
+    pa.depth = h->D;
+    pa.periodic = h->periodic ? 1 : 0;
+    pa.atoms = h->d_atoms;
+    pa.stencil = h->d_p2p_st;
+    pa.nst = h->n_p2p_st;
+    pa.field = h->d_near;
+    return pa;
+}
+
+// Phases of a step on h->stream: STEP_NEAR includes the near field (P2P), forked
+// onto its own stream in graph mode; a batch leaves it out and runs all systems'
+// near fields in one persistent kernel between the tree and the finalize.
+enum { STEP_NEAR = 1, STEP_FINAL = 2 };
+
+static void enqueue_final(gbfmm_handle* h);
+
+// Enqueues one step on h->stream (captured into the graph on first use): the
+// tree (tree_done, if given, is recorded after it), the near field (STEP_NEAR),
+// the far field and the finalize (STEP_FINAL).
+static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cudaEvent_t tree_done = nullptr)
 {
     cudaStream_t s = h->stream;
     const int D = h->D, n = h->n;
@@ -661,15 +683,10 @@ static void enqueue_step(gbfmm_handle* h)
     // The near field needs only the tree: in graph mode it forks onto its own
     // stream and overlaps the far-field chain below (joined before finalize);
     // the stage-timing pass runs it in line, after L2P.
-    P2PArgs pa;
-    pa.off = h->d_off;
-    pa.depth = D;
-    pa.periodic = h->periodic ? 1 : 0;
-    pa.atoms = h->d_atoms;
-    pa.stencil = h->d_p2p_st;
-    pa.nst = h->n_p2p_st;
-    pa.field = h->d_near;
-    const bool fork = !h->timing;
+    const P2PArgs pa = p2p_args(h);
+    const bool near = (mode & STEP_NEAR) != 0;
+    const bool fork = near && !h->timing;
+    if (tree_done) cudaEventRecord(tree_done, s);
     if (fork) {
         cudaEventRecord(h->ev_fork, s);
         cudaStreamWaitEvent(h->stream_nf, h->ev_fork, 0);
@@ -715,8 +732,19 @@ static void enqueue_step(gbfmm_handle* h)
     launch_l2p(h->P, h->d_off, h->nleaf, h->d_atoms, h->Llev[D], h->Rpad, h->d_far, s);
     mark(h, 7);
     if (fork) cudaStreamWaitEvent(s, h->ev_join, 0);
-    else launch_p2p(pa, h->p2p_variant, s, sync + 2);
+    else if (near) launch_p2p(pa, h->p2p_variant, s, sync + 2);
     mark(h, 8);
+    if (mode & STEP_FINAL) enqueue_final(h);
+    mark(h, 9);
+    h->step_launches = (int)(g_kernel_launches.load() - launches0);
+}
+
+// Forces, potentials and energy from the near and far fields (on h->stream).
+static void enqueue_final(gbfmm_handle* h)
+{
+    cudaStream_t s = h->stream;
+    const int n = h->n;
+    int* sync = h->d_counts + h->nleaf + 1;
     if (n > 0) {
         FinalArgs fa;
         fa.sc = h->d_sc;
@@ -735,8 +763,6 @@ static void enqueue_step(gbfmm_handle* h)
     } else {
         cudaMemsetAsync(h->d_energy, 0, sizeof(double), s);
     }
-    mark(h, 9);
-    h->step_launches = (int)(g_kernel_launches.load() - launches0);
 }
 
 extern "C" int gbfmm_create(const gbfmm_params* prm, int natoms, gbfmm_handle** out)
@@ -1330,6 +1356,12 @@ struct gbfmm_batch {
     cudaEvent_t ein = nullptr, eout = nullptr;
     cudaGraphExec_t gexec = nullptr;
     bool have_result = false;
+    // the systems' near fields in one persistent kernel
+    void* p2p_buf = nullptr;  // P2PArgs[n_sys], first[n_sys+1], counter
+    P2PBatchArgs p2p{};
+    cudaStream_t near_stream = nullptr;
+    std::vector<cudaEvent_t> ev_tree;
+    cudaEvent_t ev_near = nullptr;
 };
 
 static void free_batch(gbfmm_batch* b)
@@ -1345,6 +1377,10 @@ static void free_batch(gbfmm_batch* b)
     if (b->master) cudaStreamDestroy(b->master);
     if (b->buf) cudaFree(b->buf);
     if (b->h_sc) cudaFreeHost(b->h_sc);
+    if (b->p2p_buf) cudaFree(b->p2p_buf);
+    if (b->near_stream) cudaStreamDestroy(b->near_stream);
+    for (cudaEvent_t e : b->ev_tree) cudaEventDestroy(e);
+    if (b->ev_near) cudaEventDestroy(b->ev_near);
     delete b;
 }
 
@@ -1421,8 +1457,49 @@ extern "C" int gbfmm_batch_create(int n_sys, const int* atom_offsets, const int*
         b->ev.push_back(e);
     }
     if (cudaEventCreateWithFlags(&b->ein, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&b->eout, cudaEventDisableTiming) != cudaSuccess)
+        cudaEventCreateWithFlags(&b->eout, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev_near, cudaEventDisableTiming) != cudaSuccess)
         return bail(fail(GBFMM_ERR_CUDA, "event create"));
+    {
+        int lo = 0, hi = 0;
+        cudaDeviceGetStreamPriorityRange(&lo, &hi);
+        if (cudaStreamCreateWithPriority(&b->near_stream, cudaStreamNonBlocking, lo) != cudaSuccess)
+            return bail(fail(GBFMM_ERR_CUDA, "stream create"));
+    }
+    for (int i = 0; i < n_sys; i++) {
+        cudaEvent_t e;
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+            return bail(fail(GBFMM_ERR_CUDA, "event create"));
+        b->ev_tree.push_back(e);
+    }
+    // near-field queue: systems ordered by bodies per leaf, heaviest first
+    {
+        std::vector<int> ord(n_sys);
+        for (int i = 0; i < n_sys; i++) ord[i] = i;
+        auto per_leaf = [&](int i) { return (double)b->hs[i]->n / (double)b->hs[i]->nleaf; };
+        std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return per_leaf(x) > per_leaf(y); });
+        std::vector<P2PArgs> args(n_sys);
+        std::vector<int> first(n_sys + 1, 0);
+        for (int k = 0; k < n_sys; k++) {
+            args[k] = p2p_args(b->hs[ord[k]]);
+            first[k + 1] = first[k] + b->hs[ord[k]]->nleaf;
+        }
+        const size_t a_b = (sizeof(P2PArgs) * n_sys + 255) & ~(size_t)255;
+        const size_t f_b = (sizeof(int) * (n_sys + 1) + 255) & ~(size_t)255;
+        if (cudaMalloc(&b->p2p_buf, a_b + f_b + 256) != cudaSuccess) {
+            cudaGetLastError();
+            return bail(fail(GBFMM_ERR_NOMEM, "batch queue"));
+        }
+        char* base = (char*)b->p2p_buf;
+        if (cudaMemcpy(base, args.data(), sizeof(P2PArgs) * n_sys, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(base + a_b, first.data(), sizeof(int) * (n_sys + 1), cudaMemcpyHostToDevice) != cudaSuccess)
+            return bail(fail(GBFMM_ERR_CUDA, "batch queue upload"));
+        b->p2p.sys = (const P2PArgs*)base;
+        b->p2p.first = (const int*)(base + a_b);
+        b->p2p.nsys = n_sys;
+        b->p2p.nitems = first[n_sys];
+        b->p2p.counter = (int*)(base + a_b + f_b);
+    }
     *out = b;
     return GBFMM_OK;
 }
@@ -1438,13 +1515,28 @@ static int batch_capture(gbfmm_batch* b)
     std::vector<int> ord(b->n_sys);
     for (int i = 0; i < b->n_sys; i++) ord[i] = i;
     std::sort(ord.begin(), ord.end(), [&](int x, int y) { return b->hs[x]->n > b->hs[y]->n; });
+    // 1) every system's tree and far field on the worker streams (the handles
+    //    keep, and later destroy, their own streams; only the capture moves)
     for (int k = 0; k < b->n_sys; k++) {
-        // the handle keeps (and later destroys) its own stream; only the capture
-        // goes to the worker stream
         gbfmm_handle* h = b->hs[ord[k]];
         cudaStream_t own = h->stream;
         h->stream = b->workers[k % nw];
-        enqueue_step(h);
+        enqueue_step(h, 0, b->ev_tree[k]);
+        h->stream = own;
+    }
+    // 2) all near fields: one persistent kernel over every system's leaves
+    CK(cudaStreamWaitEvent(b->near_stream, b->ein, 0));
+    CK(cudaMemsetAsync(b->p2p.counter, 0, sizeof(int), b->near_stream));
+    for (int k = 0; k < b->n_sys; k++) CK(cudaStreamWaitEvent(b->near_stream, b->ev_tree[k], 0));
+    launch_p2p_batch(b->p2p, 0, 4, b->near_stream);
+    CK(cudaEventRecord(b->ev_near, b->near_stream));
+    // 3) every system's forces, potentials and energy
+    for (int w = 0; w < nw; w++) CK(cudaStreamWaitEvent(b->workers[w], b->ev_near, 0));
+    for (int k = 0; k < b->n_sys; k++) {
+        gbfmm_handle* h = b->hs[ord[k]];
+        cudaStream_t own = h->stream;
+        h->stream = b->workers[k % nw];
+        enqueue_final(h);
         h->stream = own;
     }
     for (int w = 0; w < nw; w++) {
