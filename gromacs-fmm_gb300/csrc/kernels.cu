@@ -481,6 +481,93 @@ void launch_l2p(int P, const int* offsets, int nleaf, const float4* atoms, const
     GBFMM_ORDER_SWITCH(P, (k_l2p<PP, 4><<<(nleaf + 3) / 4, 128, 0, s>>>(offsets, nleaf, atoms, L_leaf, Rpad, field)));
 }
 
+// ------------------------------------------------------------------ fused downward pass
+
+__device__ __forceinline__ int real_degree(int r) { return (int)sqrtf((float)r + 0.5f); }
+
+// Downward pass in one launch.  CTA = one leaf-parent cell p (level D-1, D >= 2):
+// the locals of p's ancestors are rebuilt from level 1 down (L~_k = M2L part + L2L
+// of the parent, in the order of the one-level kernels: a few R^2 FMAs each, the
+// same for every CTA of the subtree), then p's 8 leaves, then L2P of their bodies
+// (one warp per leaf).
+template <int P>
+__global__ void __launch_bounds__(256) k_down(DownArgs a)
+{
+    constexpr int R = (P + 1) * (P + 1);
+    __shared__ float Lc[R], Ln[R];
+    __shared__ float Lleaf[8][R + 1];
+    const int D = a.depth;
+    const uint32_t p = blockIdx.x;
+    const uint32_t a1 = p >> (3 * (D - 2));  // level-1 ancestor
+    for (int r = threadIdx.x; r < R; r += blockDim.x) Lc[r] = a.L[1][(size_t)a1 * a.Rpad + r];
+    __syncthreads();
+    for (int k = 2; k <= D - 1; k++) {
+        const uint32_t anc = p >> (3 * (D - 1 - k));
+        const float* A0 = a.l2l_t + (size_t)(anc & 7) * R * R;
+        for (int r = threadIdx.x; r < R; r += blockDim.x) {
+            const int j = real_degree(r);
+            float acc = 0.f;
+            for (int c = j * j; c < R; c++) acc = fmaf(A0[(size_t)c * R + r], Lc[c], acc);
+            Ln[r] = a.L[k][(size_t)anc * a.Rpad + r] + acc;
+        }
+        __syncthreads();
+        for (int r = threadIdx.x; r < R; r += blockDim.x) Lc[r] = Ln[r];
+        __syncthreads();
+    }
+    for (int i = threadIdx.x; i < 8 * R; i += blockDim.x) {
+        const int o = i / R, r = i - o * R;
+        const float* A0 = a.l2l_t + (size_t)o * R * R;
+        const int j = real_degree(r);
+        float acc = 0.f;
+        for (int c = j * j; c < R; c++) acc = fmaf(A0[(size_t)c * R + r], Lc[c], acc);
+        Lleaf[o][r] = a.L[D][(size_t)((p << 3) | (uint32_t)o) * a.Rpad + r] + acc;
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, o = threadIdx.x >> 5;
+    const uint32_t leaf = (p << 3) | (uint32_t)o;
+    const float* Lw = Lleaf[o];
+    auto lre = [&](int nn, int mm) { return Lw[ridx_re(nn, mm)]; };
+    auto lim = [&](int nn, int mm) { return mm > 0 ? Lw[ridx_im(nn, mm)] : 0.f; };
+    const int b = a.off[leaf], n = a.off[leaf + 1] - b;
+    for (int c0 = 0; c0 < n; c0 += 32) {
+        if (c0 + lane >= n) break;
+        const float4 q = a.atoms[b + c0 + lane];
+        float phi = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
+        stream_regular<P>(q.x, q.y, q.z, [&](int np, int mp, float ya, float yb) {
+            const float wm = mp == 0 ? 1.f : 2.f;
+            phi += wm * (lre(np, mp) * ya - lim(np, mp) * yb);
+            if (np + 1 <= P) {
+                float Lr = lre(np + 1, mp), Li = lim(np + 1, mp);
+                gz -= wm * (Lr * ya - Li * yb);
+                if (mp >= 1) {
+                    const float w = (mp - 1) == 0 ? 1.f : 2.f;
+                    Lr = lre(np + 1, mp - 1);
+                    Li = lim(np + 1, mp - 1);
+                    gx -= 0.5f * w * (Lr * ya - Li * yb);
+                    gy -= 0.5f * w * (Lr * yb + Li * ya);
+                }
+                Lr = lre(np + 1, mp + 1);
+                Li = lim(np + 1, mp + 1);
+                gx += (Lr * ya - Li * yb);
+                gy -= (Lr * yb + Li * ya);
+                if (mp == 1) {
+                    Lr = lre(np + 1, 0);
+                    gx -= 0.5f * Lr * ya;
+                    gy -= 0.5f * Lr * yb;
+                }
+            }
+        });
+        a.field[b + c0 + lane] = make_float4(phi, gx, gy, gz);
+    }
+}
+
+void launch_down(int P, const DownArgs& a, cudaStream_t s)
+{
+    COUNT_LAUNCH();
+    GBFMM_ORDER_SWITCH(P, (k_down<PP><<<1u << (3 * (a.depth - 1)), 256, 0, s>>>(a)));
+}
+
+
 // ------------------------------------------------------------------ P2P
 
 constexpr int P2P_THREADS = 128;
@@ -875,7 +962,6 @@ void launch_p2p(const P2PArgs& a, int variant, cudaStream_t s, int* counter)
 // inputs of degree >= j (kernel.cu:310-354, :408-454); both loops skip the zero
 // blocks.
 
-__device__ __forceinline__ int real_degree(int r) { return (int)sqrtf((float)r + 0.5f); }
 
 // M2M: M~_parent[r] = sum_oct sum_{c < (deg r + 1)^2} A_oct[r][c] M~_child(oct)[c];
 // the 8 children of a parent are Morton-consecutive.  The octant sum is taken in
@@ -910,37 +996,12 @@ __global__ void __launch_bounds__(256) k_m2m(const float* __restrict__ Mc, float
     }
 }
 
-// L2L: L~_child[r] += sum_{c >= (deg r)^2} A_oct[r][c] L~_parent[c], oct = the
-// child's octant.  grid = (nparent, ceil(R/32)), block = (32, 8 children).
-__global__ void __launch_bounds__(256) k_l2l(const float* __restrict__ Lp, float* __restrict__ Lc,
-                                             const float* __restrict__ At, int R, int Rpad)
-{
-    extern __shared__ float ls[];  // the parent, R
-    const int o = threadIdx.y, r = blockIdx.y * 32 + threadIdx.x, p = blockIdx.x;
-    const int tid = threadIdx.y * 32 + threadIdx.x;
-    for (int i = tid; i < R; i += 256) ls[i] = Lp[(size_t)p * Rpad + i];
-    __syncthreads();
-    if (r >= R) return;
-    const int j = real_degree(r);
-    const float* a = At + (size_t)o * R * R + r;
-    const float* l = ls;
-    float acc = 0.f;
-#pragma unroll 4
-    for (int c = j * j; c < R; c++) acc = fmaf(a[(size_t)c * R], l[c], acc);
-    Lc[(size_t)(8 * p + o) * Rpad + r] += acc;
-}
-
 void launch_m2m(const float* M_child, float* M_parent, const float* At, int nparent, int R, int Rpad, cudaStream_t s)
 {
     COUNT_LAUNCH();
     k_m2m<<<dim3(nparent, (R + 31) / 32), dim3(32, 8), sizeof(float) * 8 * R, s>>>(M_child, M_parent, At, R, Rpad);
 }
 
-void launch_l2l(const float* L_parent, float* L_child, const float* At, int nparent, int R, int Rpad, cudaStream_t s)
-{
-    COUNT_LAUNCH();
-    k_l2l<<<dim3(nparent, (R + 31) / 32), dim3(32, 8), sizeof(float) * R, s>>>(L_parent, L_child, At, R, Rpad);
-}
 
 // ------------------------------------------------------------------ batched contraction (M2M, M2L, L2L)
 

@@ -132,10 +132,20 @@ struct P2PBatchArgs {
 void launch_p2p_batch(const P2PBatchArgs& b, int shape, int per_sm, cudaStream_t s);
 void launch_p2p(const P2PArgs& a, int variant, cudaStream_t s, int* counter);
 void launch_contract(const ContractArgs& a, int ntasks, cudaStream_t s);
-// One level of M2M (nparent parents from their 8 children each) or L2L (the 8
-// children of each of nparent parents); At = 8 transposed R x R scaled operators.
+// Fused downward pass (depth >= 2): L2L of levels 2..depth and L2P, one launch.
+struct DownArgs {
+    const int* off;
+    const float4* atoms;
+    const float* L[8];        // per level: L~ rows holding their M2L part (level 1: complete)
+    const float* l2l_t;       // 8 transposed R x R scaled L2L operators
+    float4* field;            // sorted far field (phi, grad), scaled units
+    int depth, Rpad;
+};
+void launch_down(int P, const DownArgs& a, cudaStream_t s);
+
+// One level of M2M (nparent parents from their 8 children each); At = 8
+// transposed R x R scaled operators.
 void launch_m2m(const float* M_child, float* M_parent, const float* At, int nparent, int R, int Rpad, cudaStream_t s);
-void launch_l2l(const float* L_parent, float* L_child, const float* At, int nparent, int R, int Rpad, cudaStream_t s);
 
 struct RootArgs {
     int R, Rpad;

@@ -56,7 +56,6 @@ struct OpTables {
     Stencils st;
     PackPlan plan[3];
     std::vector<float> packed;           // all packed FP32 operators
-    int off_m2m[8], off_l2l[8];
     std::vector<int> off_cls;            // per M2L class
     std::vector<double> root_m2m, root_l2l, lattice;  // dense FP64 for the root
     std::vector<float> m2m_t, l2l_t;     // dense FP32, [octant][column][row], levels >= 1
@@ -109,11 +108,9 @@ const OpTables* get_tables(int P, int images)
         scaled_m2m(P, o, A.data());
         std::copy(A.begin(), A.end(), t->root_m2m.begin() + (size_t)o * R * R);
         transpose(t->m2m_t, o);
-        t->off_m2m[o] = append(t->plan[OP_M2M]);
         scaled_l2l(P, o, A.data());
         std::copy(A.begin(), A.end(), t->root_l2l.begin() + (size_t)o * R * R);
         transpose(t->l2l_t, o);
-        t->off_l2l[o] = append(t->plan[OP_L2L]);
     }
     t->off_cls.resize(t->st.classes.size());
     if (P <= TC_MAX_ORDER) t->tc = make_tc_plan(P);
@@ -168,6 +165,7 @@ struct gbfmm_handle {
     BlockInfo* d_blocks[3] = {};
     double *d_root_m2m = nullptr, *d_root_l2l = nullptr, *d_lattice = nullptr;
     float *d_m2m_t = nullptr, *d_l2l_t = nullptr;
+
     int* d_p2p_st = nullptr;
     int n_p2p_st = 0;
     float *d_forces = nullptr, *d_pots = nullptr;
@@ -192,8 +190,6 @@ struct gbfmm_handle {
     StepConst* h_sc = nullptr;  // pinned
     int* h_flags = nullptr;     // pinned
     // task ranges
-    int m2m_task0[8] = {}, m2m_ntask[8] = {};
-    int l2l_task0[8] = {}, l2l_ntask[8] = {};
     int m2l_task0 = 0, m2l_ntask = 0;
     // graph
     cudaGraphExec_t gexec = nullptr;
@@ -321,6 +317,7 @@ static int layout(gbfmm_handle* h, Arena& a)
     h->d_root_l2l = a.take<double>(t->root_l2l.size());
     h->d_lattice = a.take<double>(t->lattice.size());
     h->d_m2m_t = a.take<float>(t->m2m_t.size());
+
     h->d_l2l_t = a.take<float>(t->l2l_t.size());
     h->d_p2p_st = a.take<int>(t->st.p2p.size());
     for (int k = 0; k < 3; k++) {
@@ -348,29 +345,13 @@ static void level_ptrs(gbfmm_handle* h)
     }
 }
 
-// Contraction task lists: M2M per level, M2L for all levels, L2L per level.
+// Task lists: the FP32 M2L contraction and the tensor-core M2L tiles.
 static int build_tasks(gbfmm_handle* h)
 {
     const OpTables* t = h->tab;
     const int D = h->D;
     std::vector<CEntry> ent;
     std::vector<CTask> tasks;
-    // M2M entries: 8 children
-    const int e_m2m = (int)ent.size();
-    for (int o = 0; o < 8; o++) {
-        CEntry e;
-        e.dx = (int8_t)((o >> 2) & 1); e.dy = (int8_t)((o >> 1) & 1); e.dz = (int8_t)(o & 1); e.mode = 2;
-        e.op = t->off_m2m[o];
-        ent.push_back(e);
-    }
-    // L2L entries: parent, one per target octant
-    const int e_l2l = (int)ent.size();
-    for (int o = 0; o < 8; o++) {
-        CEntry e;
-        e.dx = e.dy = e.dz = 0; e.mode = 1;
-        e.op = t->off_l2l[o];
-        ent.push_back(e);
-    }
     // M2L stencils
     int e_m2l[2][8];
     for (int lt = 0; lt < 2; lt++)
@@ -384,21 +365,6 @@ static int build_tasks(gbfmm_handle* h)
                 ent.push_back(e);
             }
         }
-    // M2M tasks: target level k = D-1 .. 1 (level 0 is the FP64 root)
-    for (int k = D - 1; k >= 1; k--) {
-        h->m2m_task0[k] = (int)tasks.size();
-        long ncell = 1L << (3 * k);
-        const WorkPartition& wp = t->part[OP_M2M];
-        for (long q0 = 0; q0 < ncell; q0 += CT_TILE)
-            for (int g = 0; g < wp.groups; g++) {
-                CTask c;
-                c.level = k; c.octant = -1; c.q0 = (int)q0; c.ntgt = (int)std::min<long>(CT_TILE, ncell - q0);
-                c.e_begin = e_m2m; c.e_end = e_m2m + 8;
-                c.group = g; c.r0 = wp.row0[g]; c.r1 = wp.row1[g];
-                tasks.push_back(c);
-            }
-        h->m2m_ntask[k] = (int)tasks.size() - h->m2m_task0[k];
-    }
     // M2L tasks
     long work = 0;
     for (int k = 1; k <= D; k++) work += (1L << (3 * k)) * (k == 1 ? 107 : 182);
@@ -431,21 +397,6 @@ static int build_tasks(gbfmm_handle* h)
     }
     h->m2l_ntask = (int)tasks.size() - h->m2l_task0;
     (void)work;
-    // L2L tasks: target level k = 2 .. D (level 1 comes from the FP64 root)
-    for (int k = 2; k <= D; k++) {
-        h->l2l_task0[k] = (int)tasks.size();
-        long npar = 1L << (3 * (k - 1));
-        for (int s = 0; s < 8; s++)
-            for (long q0 = 0; q0 < npar; q0 += CT_TILE)
-                for (int g = 0; g < t->part[OP_L2L].groups; g++) {
-                    CTask c;
-                    c.level = k; c.octant = s; c.q0 = (int)q0; c.ntgt = (int)std::min<long>(CT_TILE, npar - q0);
-                    c.e_begin = e_l2l + s; c.e_end = e_l2l + s + 1;
-                    c.group = g; c.r0 = t->part[OP_L2L].row0[g]; c.r1 = t->part[OP_L2L].row1[g];
-                    tasks.push_back(c);
-                }
-        h->l2l_ntask[k] = (int)tasks.size() - h->l2l_task0[k];
-    }
     // tensor-core M2L: entries carry the class index, tiles of TC_TILE targets
     if (h->tc) {
         int e_tc[2][8];
@@ -727,9 +678,22 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
     }
     mark(h, 5);
     launch_root_l2l(ra, s);
-    for (int k = 2; k <= D; k++) launch_l2l(h->Llev[k - 1], h->Llev[k], h->d_l2l_t, 1 << (3 * (k - 1)), h->R, h->Rpad, s);
-    mark(h, 6);
-    launch_l2p(h->P, h->d_off, h->nleaf, h->d_atoms, h->Llev[D], h->Rpad, h->d_far, s);
+    if (D >= 2) {
+        // L2L of levels 2..D and L2P in one launch
+        DownArgs da;
+        da.off = h->d_off;
+        da.atoms = h->d_atoms;
+        for (int k = 0; k <= D; k++) da.L[k] = h->Llev[k];
+        da.l2l_t = h->d_l2l_t;
+        da.field = h->d_far;
+        da.depth = D;
+        da.Rpad = h->Rpad;
+        launch_down(h->P, da, s);
+        mark(h, 6);
+    } else {
+        mark(h, 6);  // depth 1: the leaves are level 1, complete after the root L2L
+        launch_l2p(h->P, h->d_off, h->nleaf, h->d_atoms, h->Llev[D], h->Rpad, h->d_far, s);
+    }
     mark(h, 7);
     if (fork) cudaStreamWaitEvent(s, h->ev_join, 0);
     else if (near) launch_p2p(pa, h->p2p_variant, s, sync + 2);
