@@ -737,7 +737,7 @@ struct P2PShared {
 // integer shift is far below that margin); a CTA that stages any body outside
 // that range (bodies on or near a leaf face, or outside the box) applies the
 // test to every source.
-template <int LT>
+template <int LT, int KM = 3>
 __device__ __forceinline__ void p2p_leaf(const P2PArgs& a, uint32_t tcode, P2PShared& sh)
 {
     constexpr int SL = 32 / LT, SPS = 2 * SL;  // sources per step
@@ -833,9 +833,10 @@ __device__ __forceinline__ void p2p_leaf(const P2PArgs& a, uint32_t tcode, P2PSh
             const int per = (nsteps + 3) >> 2;
             const int sb = warp * per, se = min(nsteps, sb + per);
             const int msteps = any_edge ? nsteps : max(0, (min(nself, s0 + ns) - s0 + SPS - 1) / SPS);
-            for (int c0 = 0; c0 < ntc; c0 += 3 * LT) {
+            for (int c0 = 0; c0 < ntc; c0 += KM * LT) {
                 const int rem = ntc - c0;
-                if (rem > 2 * LT) p2p_cluster<3, LT>(sh.src, tgt, c0, ntc, sb, se, msteps, lane, sh.part[warp]);
+                if (KM >= 4 && rem > 3 * LT) p2p_cluster<(KM >= 4 ? 4 : 3), LT>(sh.src, tgt, c0, ntc, sb, se, msteps, lane, sh.part[warp]);
+                else if (rem > 2 * LT) p2p_cluster<3, LT>(sh.src, tgt, c0, ntc, sb, se, msteps, lane, sh.part[warp]);
                 else if (rem > LT) p2p_cluster<2, LT>(sh.src, tgt, c0, ntc, sb, se, msteps, lane, sh.part[warp]);
                 else p2p_cluster<1, LT>(sh.src, tgt, c0, ntc, sb, se, msteps, lane, sh.part[warp]);
             }
@@ -856,11 +857,11 @@ __device__ __forceinline__ void p2p_leaf(const P2PArgs& a, uint32_t tcode, P2PSh
 }
 
 // One CTA per target leaf.
-template <int LT>
+template <int LT, int KM = 3>
 __global__ void __launch_bounds__(P2P_THREADS) k_p2p(const P2PArgs a)
 {
     __shared__ P2PShared sh;
-    p2p_leaf<LT>(a, blockIdx.x, sh);
+    p2p_leaf<LT, KM>(a, blockIdx.x, sh);
 }
 
 // Persistent form: a fixed number of CTAs per SM walk the queue of leaves
@@ -928,13 +929,18 @@ void launch_p2p_batch(const P2PBatchArgs& b, int shape, int per_sm, cudaStream_t
     else k_p2p_batch<8><<<grid, P2P_THREADS, 0, s>>>(b);
 }
 
-int p2p_variants() { return 3 * 5; }
+int p2p_variants() { return 3 * 5 + 2; }
 
 void launch_p2p(const P2PArgs& a, int variant, cudaStream_t s, int* counter)
 {
     const int nleaf = 1 << (3 * a.depth);
-    const int shape = variant % 3, per_sm = variant / 3;  // per_sm 0: one CTA per leaf
     COUNT_LAUNCH();
+    if (variant >= 15) {  // one CTA per leaf, up to 4 targets per thread
+        if (variant == 15) k_p2p<8, 4><<<nleaf, P2P_THREADS, 0, s>>>(a);
+        else k_p2p<4, 4><<<nleaf, P2P_THREADS, 0, s>>>(a);
+        return;
+    }
+    const int shape = variant % 3, per_sm = variant / 3;  // per_sm 0: one CTA per leaf
     if (per_sm == 0 || !counter) {
         if (shape == 1) k_p2p<4><<<nleaf, P2P_THREADS, 0, s>>>(a);
         else if (shape == 2) k_p2p<16><<<nleaf, P2P_THREADS, 0, s>>>(a);

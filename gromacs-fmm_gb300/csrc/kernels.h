@@ -112,7 +112,8 @@ void launch_l2p(int P, const int* offsets, int nleaf, const float4* atoms, const
 // (0: 8 targets x 4 source lanes, 1: 4 x 8, 2: 16 x 2); persistence 0 = one CTA
 // per leaf, 1..4 = (persistence + 1) CTAs per SM walking the leaves through
 // *counter (zero at launch).  Chosen by the autotuner; all give the same sums up
-// to the order of the additions.
+// to the order of the additions.  Variants 15 and 16: one CTA per leaf, up to 4
+// targets per thread, shapes 8 x 4 and 4 x 8.
 struct P2PArgs {
     const int* off;           // leaf offsets (8^depth + 1)
     int depth, periodic;

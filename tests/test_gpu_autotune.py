@@ -24,8 +24,9 @@ def test_every_shape_matches(pkg, oracle, systems, precision, tol):
     _, fo, _ = oracle.zeta_solve(xyz.astype(np.float64), q.astype(np.float64), L, 6, 3, 4)
     assert rel_rms(f0, fo) < tol
     ns0 = s.tuning()["m2l_stages"]
-    # P2P: 3 warp-step shapes x (one CTA per leaf, or 2..5 persistent CTAs per SM)
-    for pv in range(15):
+    # P2P: 3 warp-step shapes x (one CTA per leaf, or 2..5 persistent CTAs per SM), and
+    # two shapes with up to 4 targets per thread
+    for pv in range(17):
         s.set_tuning(pv, 1, ns0)
         s.execute(xyz, L)
         assert rel_rms(s.forces(), f0) < 1e-5, pv
@@ -44,7 +45,7 @@ def test_autotune_keeps_a_valid_tuning(pkg, systems):
     s.execute(xyz, L)
     f0 = s.forces()
     t = s.autotune(xyz, L, reps=3)
-    assert t["ms"] > 0 and 0 <= t["p2p_variant"] < 15 and t["m2l_split"] in (1, 2, 4, 8)
+    assert t["ms"] > 0 and 0 <= t["p2p_variant"] < 17 and t["m2l_split"] in (1, 2, 4, 8)
     s.execute(xyz, L)
     assert rel_rms(s.forces(), f0) < 1e-5
     s.close()
