@@ -383,8 +383,9 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-system batched line")
     ap.add_argument("--profile", default=None,
-                    help="precision,order,depth: only run --steps host-API steps of that configuration "
-                         "(a short, fixed launch sequence for ncu captures); prints no bench line")
+                    help="precision,order,depth[,p2p_variant,m2l_split,m2l_stages]: only run --steps host-API "
+                         "steps of that configuration and tuning (a short, fixed launch sequence for ncu "
+                         "captures); prints no bench line")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_env()
@@ -392,9 +393,12 @@ def main():
     xyz, q, box = systems.cfg_96k()
     n = len(q)
     if args.profile:
-        prec, P, D = (int(v) for v in args.profile.split(","))
+        vals = [int(v) for v in args.profile.split(",")]
+        prec, P, D = vals[:3]
         pkg = G.load_package()
         s = pkg.ZetaFmmSolver(n, q, order=P, max_depth=D, images=4, precision=prec)
+        if len(vals) == 6:
+            s.set_tuning(*vals[3:])
         for _ in range(args.steps):
             s.execute(xyz, box)
         print(json.dumps({"profile": args.profile, "steps": args.steps, "energy": s.get_energy(),

@@ -56,4 +56,43 @@ GBFMM_HD void morton_decode(uint32_t c, int& ix, int& iy, int& iz) {
 // BFS index of the first cell of a level in the complete octree.
 GBFMM_HD long level_base(int k) { return ((1L << (3 * k)) - 1) / 7; }
 
+#ifdef __CUDACC__
+// Sums of FP32 products held as unevaluated FP32 pairs (hi + lo, about 48
+// significant bits) with error-free transformations: the exact product by FMA
+// (hi = a*b rounded, lo = fma(a, b, -hi)) and Knuth's two-sum.  On GB300 an FP64
+// add waits ~64 cycles for its predecessor and the SM retires 2 FP64 lanes per
+// clock, against 4 cycles and 128 lanes for FP32, so reductions run in this form
+// and only their final value is converted to FP64.
+struct f2sum {
+    float hi, lo;
+};
+__device__ __forceinline__ f2sum f2s_prod(float a, float b)
+{
+    const float p = __fmul_rn(a, b);
+    return {p, fmaf(a, b, -p)};
+}
+__device__ __forceinline__ f2sum f2s_add(f2sum a, f2sum b)
+{
+    const float s = __fadd_rn(a.hi, b.hi);
+    const float bb = __fsub_rn(s, a.hi);
+    float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+    e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+    const float h = __fadd_rn(s, e);
+    return {h, __fsub_rn(e, __fsub_rn(h, s))};
+}
+// Fixed butterfly over the warp: every lane ends with the same sum.
+__device__ __forceinline__ f2sum f2s_warp_sum(f2sum v)
+{
+    for (int o = 16; o > 0; o >>= 1) {
+        f2sum w;
+        w.hi = __shfl_xor_sync(0xffffffffu, v.hi, o);
+        w.lo = __shfl_xor_sync(0xffffffffu, v.lo, o);
+        // the same operand order on both lanes of a pair: lower lane first
+        v = (threadIdx.x & o) ? f2s_add(w, v) : f2s_add(v, w);
+    }
+    return v;
+}
+__device__ __forceinline__ double f2s_value(f2sum v) { return (double)v.hi + (double)v.lo; }
+#endif
+
 }  // namespace gbfmm

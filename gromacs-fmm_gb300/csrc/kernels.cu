@@ -12,6 +12,7 @@
 
 #include <atomic>
 
+#include "async.cuh"
 #include "common.cuh"
 #include "kernels.h"
 
@@ -49,7 +50,7 @@ __global__ void __launch_bounds__(256) k_tree_keys(TreeArgs a)
         }
     }
     __syncthreads();
-    double s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+    f2sum sd[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};  // dipole (3), total charge
     int bad = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) {
         float x[3] = {coords[3 * i], coords[3 * i + 1], coords[3 * i + 2]};
@@ -73,29 +74,24 @@ __global__ void __launch_bounds__(256) k_tree_keys(TreeArgs a)
         a.code[i] = code;
         a.uq[i] = make_float4(u[0], u[1], u[2], q);
         atomicAdd(&a.counts[code], 1);
-        double dq = (double)q;
-        s0 += dq * (double)x[0];
-        s1 += dq * (double)x[1];
-        s2 += dq * (double)x[2];
-        s3 += dq;
+#pragma unroll
+        for (int d = 0; d < 3; d++) sd[d] = f2s_add(sd[d], f2s_prod(q, x[d]));
+        sd[3] = f2s_add(sd[3], f2sum{q, 0.f});
     }
-    // block reduction of the dipole and total charge (FP64)
-    for (int o = 16; o > 0; o >>= 1) {
-        s0 += __shfl_xor_sync(0xffffffffu, s0, o);
-        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
-        s2 += __shfl_xor_sync(0xffffffffu, s2, o);
-        s3 += __shfl_xor_sync(0xffffffffu, s3, o);
-    }
-    __shared__ double red[8][4];
+    // block reduction of the dipole and total charge (exact products, FP32-pair
+    // sums in a fixed order)
+    __shared__ f2sum red[8][4];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) {
-        red[warp][0] = s0; red[warp][1] = s1; red[warp][2] = s2; red[warp][3] = s3;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const f2sum w = f2s_warp_sum(sd[k]);
+        if (lane == 0) red[warp][k] = w;
     }
     __syncthreads();
     if (threadIdx.x < 4) {
-        double t = 0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w][threadIdx.x];
-        a.partials[4 * blockIdx.x + threadIdx.x] = t;
+        f2sum t = red[0][threadIdx.x];
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) t = f2s_add(t, red[w][threadIdx.x]);
+        reinterpret_cast<f2sum*>(a.partials)[4 * blockIdx.x + threadIdx.x] = t;
     }
     if (bad) atomicOr(&a.flags[0], 1);
     if (!a.done) return;
@@ -110,17 +106,18 @@ __global__ void __launch_bounds__(256) k_tree_keys(TreeArgs a)
     if (warp < 4) {
         // all loads issued before the fixed-order sum (one round trip)
         constexpr int K = (TREE_MAX_BLOCKS + 31) / 32;
-        double v[K];
+        f2sum v[K];
+        const float2* part = reinterpret_cast<const float2*>(a.partials);
 #pragma unroll
         for (int k = 0; k < K; k++) {
             const int b = lane + 32 * k;
-            v[k] = b < (int)gridDim.x ? __ldcg(&a.partials[4 * b + warp]) : 0.0;
+            const float2 p = b < (int)gridDim.x ? __ldcg(&part[4 * b + warp]) : make_float2(0.f, 0.f);
+            v[k] = f2sum{p.x, p.y};
         }
-        double t = 0;
 #pragma unroll
-        for (int k = 0; k < K; k++) t += v[k];
-        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-        if (lane == 0) a.sums[warp] = t;
+        for (int k = 1; k < K; k++) v[0] = f2s_add(v[0], v[k]);
+        const f2sum t = f2s_warp_sum(v[0]);
+        if (lane == 0) a.sums[warp] = f2s_value(t);
     }
     if (a.off) {
         // exclusive scan of counts in tiles of 4096: thread t owns 16 consecutive
@@ -1008,6 +1005,88 @@ void launch_m2m(const float* M_child, float* M_parent, const float* At, int npar
     k_m2m<<<dim3(nparent, (R + 31) / 32), dim3(32, 8), sizeof(float) * 8 * R, s>>>(M_child, M_parent, At, R, Rpad);
 }
 
+// P2M of 8 sibling leaves (one warp each, the arithmetic of k_p2m) followed by
+// the M2M of their parent in the same CTA (the arithmetic of k_m2m: one thread
+// per (octant, row), the octant sum in octant order), so that the leaf level
+// and the level above it come out of one launch.  grid = nleaf / 8, block = 256.
+template <int P>
+__global__ void __launch_bounds__(256) k_p2m_m2m(const int* off, const float4* atoms, float* M, float* Mp,
+                                                 const float* __restrict__ At, int Rpad)
+{
+    constexpr int R = (P + 1) * (P + 1);
+    constexpr int LD = 33;
+    extern __shared__ float sm[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int leaf = blockIdx.x * 8 + warp;
+    float* S = sm + warp * R * LD;
+    float* ch = sm + 8 * R * LD;  // the 8 leaf multipoles
+    float* red = ch + 8 * R;      // per-octant partial sums of the parent
+    for (int r = 0; r < R; r++) S[r * LD + lane] = 0.f;
+    const int b = off[leaf], n = off[leaf + 1] - b;
+    for (int c0 = 0; c0 < n; c0 += 32) {
+        float4 a = c0 + lane < n ? atoms[b + c0 + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float q = a.w;
+        stream_regular<P>(a.x, a.y, a.z, [&](int nn, int mm, float yr, float yi) {
+            S[ridx_re(nn, mm) * LD + lane] += q * yr;
+            if (mm > 0) S[ridx_im(nn, mm) * LD + lane] -= q * yi;
+        });
+    }
+    __syncwarp();
+    float* out = M + (long)leaf * Rpad;
+    for (int r = lane; r < R; r += 32) {
+        float t = 0.f;
+#pragma unroll 8
+        for (int c = 0; c < 32; c++) t += S[r * LD + c];
+        out[r] = t;
+        ch[warp * R + r] = t;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 8 * R; i += 256) {
+        const int o = i / R, r = i - o * R;
+        const int j = real_degree(r), cend = (j + 1) * (j + 1);
+        const float* a = At + (size_t)o * R * R + r;
+        const float* m = ch + o * R;
+        float acc = 0.f;
+#pragma unroll 4
+        for (int c = 0; c < cend; c++) acc = fmaf(a[(size_t)c * R], m[c], acc);
+        red[i] = acc;
+    }
+    __syncthreads();
+    for (int r = threadIdx.x; r < R; r += 256) {
+        float t = red[r];
+#pragma unroll
+        for (int k = 1; k < 8; k++) t += red[k * R + r];
+        Mp[(size_t)blockIdx.x * Rpad + r] = t;
+    }
+}
+
+constexpr size_t P2M_M2M_MAX_SMEM = 200 * 1024;
+
+template <int P>
+static bool p2m_m2m_dispatch(const int* off, int nleaf, const float4* atoms, float* M, float* Mp, const float* At,
+                             int Rpad, cudaStream_t s)
+{
+    constexpr int R = (P + 1) * (P + 1);
+    const size_t shm = sizeof(float) * (8 * R * 33 + 16 * R);
+    if (shm > P2M_M2M_MAX_SMEM || nleaf % 8 != 0) return false;
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_p2m_m2m<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+        attr = true;
+    }
+    COUNT_LAUNCH();
+    k_p2m_m2m<P><<<nleaf / 8, 256, shm, s>>>(off, atoms, M, Mp, At, Rpad);
+    return true;
+}
+
+bool launch_p2m_m2m(int P, const int* offsets, int nleaf, const float4* atoms, float* M_leaf, float* M_parent,
+                    const float* At, int Rpad, cudaStream_t s)
+{
+    bool ok = false;
+    GBFMM_ORDER_SWITCH(P, ok = p2m_m2m_dispatch<PP>(offsets, nleaf, atoms, M_leaf, M_parent, At, Rpad, s));
+    return ok;
+}
+
 
 // ------------------------------------------------------------------ batched contraction (M2M, M2L, L2L)
 
@@ -1166,63 +1245,6 @@ void launch_contract(const ContractArgs& a, int ntasks, cudaStream_t s)
 
 // ------------------------------------------------------------------ root (FP64)
 
-// M~_0 = sum_o A_o M~_1[o] in FP64.  A CTA owns 8 output rows; its 256 threads
-// are (child o, row, quarter of the columns), reduced in a fixed order.  The
-// degree-0 and degree-1 moments (total charge and dipole about the box centre)
-// are then replaced by their exact FP64 sums over the bodies, which is what the
-// reference's FP64 P2M/M2M produces: the FP32 upward pass would otherwise leave
-// a monopole residual of ~1e-7 of sum|q| that the periodic lattice operator
-// (about 81 periods wide) turns into a constant shift of every potential.
-__global__ void __launch_bounds__(256) k_root_m2m(RootArgs a)
-{
-    __shared__ double part[8][8][4];
-    const int tid = threadIdx.x, p = tid & 3, rl = (tid >> 2) & 7, o = tid >> 5;
-    const int r = blockIdx.x * 8 + rl;
-    const int qc = (a.R + 3) / 4;
-    double t = 0;
-    if (r < a.R) {
-        const double* A = a.m2m + ((size_t)o * a.R + r) * a.R;
-        const float* m = a.M1 + (size_t)o * a.Rpad;
-        for (int c = p * qc; c < min(a.R, (p + 1) * qc); c++) t += A[c] * (double)m[c];
-    }
-    part[o][rl][p] = t;
-    __syncthreads();
-    if (tid < 8) {
-        const int rr = blockIdx.x * 8 + tid;
-        if (rr < a.R) {
-            double s = 0;
-            for (int oo = 0; oo < 8; oo++)
-                for (int pp = 0; pp < 4; pp++) s += part[oo][tid][pp];
-            if (rr < 4) {
-                const double Q = a.sums[3], L = a.sc->box_len, c = 0.5 * L;
-                if (rr == 0) s = Q;
-                else if (rr == 1) s = -(a.sums[2] - Q * c) / L;
-                else if (rr == 2) s = (a.sums[0] - Q * c) / (2.0 * L);
-                else s = -(a.sums[1] - Q * c) / (2.0 * L);
-            }
-            a.M0[rr] = s;
-        }
-    }
-}
-
-// Fixed-order sum of per-block partials: out[j] = sum_b part[b*width + j].  Warp
-// j reduces column j: lane l sums blocks l, l+32, ... then a fixed butterfly.
-__global__ void k_sum_partials(const double* part, int nblocks, int width, double* out)
-{
-    const int j = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (j >= width) return;
-    double s = 0;
-    for (int b = lane; b < nblocks; b += 32) s += part[(size_t)b * width + j];
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) out[j] = s;
-}
-
-void launch_sum_partials(const double* part, int nblocks, int width, double* out, cudaStream_t s)
-{
-    COUNT_LAUNCH();
-    k_sum_partials<<<1, 32 * width, 0, s>>>(part, nblocks, width, out);
-}
-
 // L~_0 = A_lattice M~_0 (images >= 2), and the FP32 copy of M~_0.  One warp per
 // output row; lanes split the FP64 dot product, reduced by a fixed butterfly.
 __global__ void __launch_bounds__(256) k_root_lattice(RootArgs a)
@@ -1256,11 +1278,6 @@ __global__ void __launch_bounds__(256) k_root_l2l(RootArgs a)
     if (lane == 0) a.L1[(size_t)o * a.Rpad + r] += (float)t;
 }
 
-void launch_root_m2m(const RootArgs& a, cudaStream_t s)
-{
-    COUNT_LAUNCH();
-    k_root_m2m<<<(a.R + 7) / 8, 256, 0, s>>>(a);
-}
 void launch_root_lattice(const RootArgs& a, cudaStream_t s)
 {
     COUNT_LAUNCH();
@@ -1272,6 +1289,210 @@ void launch_root_l2l(const RootArgs& a, cudaStream_t s)
     k_root_l2l<<<(8 * a.R + 7) / 8, 256, 0, s>>>(a);
 }
 
+// ------------------------------------------------------------------ upper tree in one launch
+
+constexpr int TOP_THREADS = 512;
+
+__host__ __device__ __forceinline__ bool top_staged(int R) { return R <= TOP_STAGE_MAX_R; }
+__host__ __device__ __forceinline__ int top_r2p(int R) { return (R * R + 1) & ~1; }  // FP64 block stride
+
+// Shared memory of k_top.  Staged: FP32 M2M operator (8 R^2) | FP64 root M2M
+// block of the CTA's octant (R2p) | FP64 lattice (R2p) | input cells (64 rows of
+// Rpad) | M~_0 (R, FP64) | level 1 as FP64 (R) | level 1 (Rpad) | level 2
+// (8 Rpad) | octant partials (64 R).  Unstaged: M~_0, level 1 (FP64, FP32).
+size_t top_smem_bytes(int R)
+{
+    const size_t r = (size_t)R, rp = (size_t)((R + 3) & ~3), r2p = (size_t)top_r2p(R);
+    if (!top_staged(R)) return sizeof(double) * 2 * r + sizeof(float) * rp;
+    return sizeof(float) * 8 * r * r + sizeof(double) * (2 * r2p + 2 * r) + sizeof(float) * (73 * rp + 64 * r);
+}
+
+// M2M of np parents whose 8 children sit in ch[(8p + o) Rpad + c], operator At
+// [octant][column][row], all in shared memory.  A thread owns (octant, row) of
+// up to four parents: one operator read feeds four independent chains.  Each
+// (parent, octant, row) sum runs over the columns in order and the octant sum is
+// taken in octant order: the arithmetic of k_m2m.  Parents go to par (shared,
+// stride Rpad) and dst (global, stride Rpad).
+__device__ __forceinline__ void top_m2m(const float* ch, float* red, float* par, float* dst, int np, const float* At,
+                                        int R, int Rpad)
+{
+    const int pq = np >= 4 ? 4 : 1, ng = np / pq;
+    for (int i = threadIdx.x; i < ng * 8 * R; i += TOP_THREADS) {
+        const int r = i % R, o = (i / R) & 7, p0 = (i / (8 * R)) * pq;
+        const int j = real_degree(r), cend = (j + 1) * (j + 1);
+        const float* a = At + o * R * R + r;
+        float acc[4] = {0.f, 0.f, 0.f, 0.f};
+        if (pq == 4) {
+            const float* m0 = ch + (8 * p0 + o) * Rpad;
+#pragma unroll 2
+            for (int c = 0; c < cend; c++) {
+                const float w = a[c * R];
+#pragma unroll
+                for (int k = 0; k < 4; k++) acc[k] = fmaf(w, m0[8 * k * Rpad + c], acc[k]);
+            }
+#pragma unroll
+            for (int k = 0; k < 4; k++) red[(8 * (p0 + k) + o) * R + r] = acc[k];
+        } else {
+            const float* m0 = ch + (8 * p0 + o) * Rpad;
+#pragma unroll 4
+            for (int c = 0; c < cend; c++) acc[0] = fmaf(a[c * R], m0[c], acc[0]);
+            red[(8 * p0 + o) * R + r] = acc[0];
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < np * R; i += TOP_THREADS) {
+        const int p = i / R, r = i - p * R;
+        float t = red[8 * p * R + r];
+#pragma unroll
+        for (int k = 1; k < 8; k++) t += red[(8 * p + k) * R + r];
+        par[p * Rpad + r] = t;
+        dst[(size_t)p * Rpad + r] = t;
+    }
+    __syncthreads();
+}
+
+// Fixed pairwise tree over the 4 x 8 shares of one root row ((octant, quarter)
+// index k = 4 o + q): five dependent FP64 additions instead of 31 (an FP64 add
+// waits ~64 cycles for its predecessor on GB300).
+__device__ __forceinline__ double tree_sum32(double (&v)[32])
+{
+#pragma unroll
+    for (int w = 16; w >= 1; w >>= 1)
+#pragma unroll
+        for (int k = 0; k < w; k++) v[k] = v[k] + v[k + w];
+    return v[0];
+}
+
+// CTA g owns the subtree of level-1 cell g.  Staged form (R <= TOP_STAGE_MAX_R):
+// the operators and the input cells arrive by bulk copies on one mbarrier (one
+// memory latency), then M2M from level 'from' (3 or 2) up to level 1 in shared
+// memory.  Both forms then take the CTA's share of the FP64 root M2M
+// M~_0 = sum_o A_o M~_1[o] (octant g; columns in four quarters, one thread per
+// (row, quarter)); the last CTA to finish adds the 32 shares of a row by a fixed
+// pairwise tree and applies the lattice operator (one thread per (row, column
+// quarter), quarters added pairwise), so that the upper tree takes one launch.
+// The degree-0 and degree-1 moments of M~_0 (total charge and dipole about the
+// box centre) are replaced by their exact FP64 sums over the bodies, which is
+// what the reference's FP64 P2M/M2M produces: the FP32 upward pass would otherwise
+// leave a monopole residual of ~1e-7 of sum|q| that the periodic lattice operator
+// (about 81 periods wide) turns into a constant shift of every potential.
+template <bool STAGED>
+__global__ void __launch_bounds__(TOP_THREADS) k_top(const TopArgs a)
+{
+    extern __shared__ float4 topsm[];
+    __shared__ uint64_t bar;
+    __shared__ double lq[4 * 256];  // lattice quarters (R <= 256 rows)
+    const int R = a.root.R, Rpad = a.root.Rpad, R2p = top_r2p(R), g = blockIdx.x, tid = threadIdx.x;
+    float* At = reinterpret_cast<float*>(topsm);
+    double* Ag = reinterpret_cast<double*>(At + (STAGED ? 8 * R * R : 0));
+    double* lat = Ag + (STAGED ? R2p : 0);
+    float* in = reinterpret_cast<float*>(lat + (STAGED ? R2p : 0));
+    double* M0s = reinterpret_cast<double*>(in + (STAGED ? 64 * Rpad : 0));
+    double* m1d = M0s + R;
+    float* m1 = reinterpret_cast<float*>(m1d + R);
+    float* mid = m1 + Rpad;
+    float* red = mid + 8 * Rpad;
+    if (STAGED) {
+        // bulk copies: 8 R^2 floats, R2p doubles and Rpad-float rows are all
+        // multiples of 16 bytes; the sources are 16-byte aligned allocations
+        const int rows = a.from == 3 ? 64 : a.from == 2 ? 8 : 1;
+        const float* src_in = a.from >= 2 ? a.Min + (size_t)rows * g * Rpad : a.M1 + (size_t)g * Rpad;
+        if (tid == 0) {
+            mbar_init(&bar, 1);
+            mbar_init_fence();
+            const uint32_t b_at = a.from >= 2 ? 32u * R * R : 0u, b_ag = 8u * R2p, b_lat = a.lattice ? 8u * R2p : 0u,
+                           b_in = 4u * rows * Rpad;
+            mbar_expect_tx(&bar, b_at + b_ag + b_lat + b_in);
+            if (b_at) bulk_g2s(At, a.m2m_t, b_at, &bar);
+            bulk_g2s(Ag, a.root.m2m + (size_t)g * R2p, b_ag, &bar);
+            if (b_lat) bulk_g2s(lat, a.root.lattice, b_lat, &bar);
+            bulk_g2s(a.from == 3 ? in : a.from == 2 ? mid : m1, src_in, b_in, &bar);
+        }
+        __syncthreads();
+        mbar_wait(&bar, 0, a.err, 1);
+        if (a.from == 3) top_m2m(in, red, mid, a.M2 + (size_t)8 * g * Rpad, 8, At, R, Rpad);
+        if (a.from >= 2) top_m2m(mid, red, m1, a.M1 + (size_t)g * Rpad, 1, At, R, Rpad);
+    } else {
+        for (int r = tid; r < R; r += TOP_THREADS) m1[r] = a.M1[(size_t)g * Rpad + r];
+        __syncthreads();
+    }
+    for (int r = tid; r < R; r += TOP_THREADS) m1d[r] = (double)m1[r];
+    __syncthreads();
+    const double* A0 = STAGED ? Ag : a.root.m2m + (size_t)g * R2p;
+    const int qc = (R + 3) / 4;
+    for (int i = tid; i < 4 * R; i += TOP_THREADS) {
+        const int r = i >> 2, p = i & 3;
+        const double* A = A0 + (size_t)r * R;
+        double t = 0;
+        for (int c = p * qc; c < min(R, (p + 1) * qc); c++) t = fma(A[c], m1d[c], t);
+        a.part[((size_t)g * R + r) * 4 + p] = t;
+    }
+    __shared__ int s_last;
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) s_last = atomicAdd(a.done, 1) == (int)gridDim.x - 1;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    for (int r = tid; r < R; r += TOP_THREADS) {
+        double v[32];
+#pragma unroll
+        for (int k = 0; k < 32; k++) v[k] = __ldcg(&a.part[((size_t)(k >> 2) * R + r) * 4 + (k & 3)]);
+        double s = tree_sum32(v);
+        if (r < 4) {
+            const double Q = a.root.sums[3], L = a.root.sc->box_len, c = 0.5 * L;
+            if (r == 0) s = Q;
+            else if (r == 1) s = -(a.root.sums[2] - Q * c) / L;
+            else if (r == 2) s = (a.root.sums[0] - Q * c) / (2.0 * L);
+            else s = -(a.root.sums[1] - Q * c) / (2.0 * L);
+        }
+        M0s[r] = s;
+        a.root.M0[r] = s;
+    }
+    if (tid == 0) {
+        // FP32 constants of the tin-foil dipole correction for the finalize
+        // (solver.cpp:30-49): q * ke * coef * M per body and ke * coef * |M|^2 / N
+        const double M0 = a.root.sums[0], M1 = a.root.sums[1], M2 = a.root.sums[2];
+        const double cK = a.root.sc->coef * KE;
+        a.fconst[0] = (float)(cK * M0);
+        a.fconst[1] = (float)(cK * M1);
+        a.fconst[2] = (float)(cK * M2);
+        a.fconst[3] = (float)(cK * (M0 * M0 + M1 * M1 + M2 * M2) / (double)max(a.natoms, 1));
+    }
+    __syncthreads();
+    if (!a.lattice) return;
+    const double* Alat = STAGED ? lat : a.root.lattice;
+    for (int i = tid; i < 4 * R; i += TOP_THREADS) {
+        const int r = i >> 2, p = i & 3;
+        const double* A = Alat + (size_t)r * R;
+        double t = 0;
+        if (a.root.images >= 2)
+            for (int c = p * qc; c < min(R, (p + 1) * qc); c++) t = fma(A[c], M0s[c], t);
+        lq[i] = t;
+    }
+    __syncthreads();
+    for (int r = tid; r < R; r += TOP_THREADS) {
+        a.root.L0[r] = (lq[4 * r] + lq[4 * r + 1]) + (lq[4 * r + 2] + lq[4 * r + 3]);
+        a.root.M0f[r] = (float)M0s[r];
+    }
+}
+
+void launch_top(const TopArgs& a, cudaStream_t s)
+{
+    const size_t shm = top_smem_bytes(a.root.R);
+    const bool staged = top_staged(a.root.R);
+    static size_t attr[2] = {0, 0};
+    if (shm > attr[staged]) {
+        if (staged) cudaFuncSetAttribute(k_top<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+        else cudaFuncSetAttribute(k_top<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+        attr[staged] = shm;
+    }
+    COUNT_LAUNCH();
+    if (staged) k_top<true><<<8, TOP_THREADS, shm, s>>>(a);
+    else k_top<false><<<8, TOP_THREADS, shm, s>>>(a);
+    if (!a.lattice) launch_root_lattice(a.root, s);
+}
+
 // ------------------------------------------------------------------ finalize
 
 // Unit conversion of gpu_solver.cu:250-256 (phi*ke, F = -q*ke*grad phi), the
@@ -1279,13 +1500,10 @@ void launch_root_l2l(const RootArgs& a, cudaStream_t s)
 // (solver.cpp:58-67) and the FP64 energy 0.5*sum(q*phi) (fmm.cpp:89-98).
 __global__ void __launch_bounds__(256) k_finalize(FinalArgs a)
 {
-    const double M0 = a.sums[0], M1 = a.sums[1], M2 = a.sums[2];
-    const double cK = a.sc->coef * KE;
+    // FP32 constants of the dipole correction, computed once in FP64 by k_top
+    const float fM0 = a.fconst[0], fM1 = a.fconst[1], fM2 = a.fconst[2], corr_f = a.fconst[3];
     const float inv_h = a.sc->inv_h, inv_h2 = a.sc->inv_h * a.sc->inv_h;
-    const double corr = cK * (M0 * M0 + M1 * M1 + M2 * M2) / (double)a.n;
-    const float fM0 = (float)(cK * M0), fM1 = (float)(cK * M1), fM2 = (float)(cK * M2);
-    const float corr_f = (float)corr;
-    double e = 0;
+    f2sum e = {0.f, 0.f};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) {
         const float4 nf = a.near[i], ff = a.far[i];
         const float q = a.atoms[i].w;
@@ -1300,16 +1518,16 @@ __global__ void __launch_bounds__(256) k_finalize(FinalArgs a)
         float pot = phi * (float)KE;
         if (q != 0.f) pot -= corr_f / q;
         a.pots[o] = pot;
-        e += (double)(0.5f * q) * (double)pot;
+        e = f2s_add(e, f2s_prod(0.5f * q, pot));  // the exact product, as FP64 would hold it
     }
-    for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
-    __shared__ double red[8];
+    e = f2s_warp_sum(e);
+    __shared__ f2sum red[8];
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = e;
     __syncthreads();
     if (threadIdx.x == 0) {
-        double t = 0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w];
-        a.partials[blockIdx.x] = t;
+        f2sum t = red[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) t = f2s_add(t, red[w]);
+        reinterpret_cast<f2sum*>(a.partials)[blockIdx.x] = t;
     }
     if (!a.done) return;
     // last block: the energy, partials summed in a fixed order
@@ -1321,17 +1539,18 @@ __global__ void __launch_bounds__(256) k_finalize(FinalArgs a)
     if (!s_last || threadIdx.x >= 32) return;
     __threadfence();
     constexpr int K = (FINAL_MAX_BLOCKS + 31) / 32;
-    double v[K];
+    f2sum v[K];
+    const float2* part = reinterpret_cast<const float2*>(a.partials);
 #pragma unroll
     for (int k = 0; k < K; k++) {
         const int b = threadIdx.x + 32 * k;
-        v[k] = b < (int)gridDim.x ? __ldcg(&a.partials[b]) : 0.0;
+        const float2 p = b < (int)gridDim.x ? __ldcg(&part[b]) : make_float2(0.f, 0.f);
+        v[k] = f2sum{p.x, p.y};
     }
-    double t = 0;
 #pragma unroll
-    for (int k = 0; k < K; k++) t += v[k];
-    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-    if (threadIdx.x == 0) *a.energy = t;
+    for (int k = 1; k < K; k++) v[0] = f2s_add(v[0], v[k]);
+    const f2sum t = f2s_warp_sum(v[0]);
+    if (threadIdx.x == 0) *a.energy = f2s_value(t);
 }
 
 void launch_finalize(const FinalArgs& a, cudaStream_t s)

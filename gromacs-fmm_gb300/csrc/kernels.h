@@ -73,7 +73,7 @@ struct TreeArgs {
     uint32_t* code;         // N leaf codes (input order)
     float4* uq;             // N scaled coords + charge (input order)
     int* counts;            // 8^D
-    double* partials;       // per block: dipole (3) and total charge, FP64
+    double* partials;       // per block: dipole (3) and total charge, FP32 pairs (hi, lo)
     int* flags;             // [0] non-finite input seen
     // Last-block epilogue (all NULL: none).  The last block to finish sums the
     // partials into sums[4] (fixed order) and, when off != NULL, writes the
@@ -94,7 +94,6 @@ struct TreeArgs {
 constexpr int TREE_EPILOGUE_MAX_LEAVES = 1 << 15;
 constexpr int TREE_MAX_BLOCKS = 4 * 152;
 constexpr int FINAL_MAX_BLOCKS = 4 * 152;
-void launch_sum_partials(const double* part, int nblocks, int width, double* out, cudaStream_t s);
 int tree_blocks(int n);
 int final_blocks(int n);
 
@@ -106,6 +105,11 @@ void launch_scatter(const uint32_t* code, int n, int* cursor, int* tmp_idx, cuda
 void launch_leaf_sort(const int* offsets, int nleaf, int* tmp_idx, const float4* uq, const uint32_t* code, int* order,
                       float4* atoms, int* atom_leaf, cudaStream_t s);
 void launch_p2m(int P, const int* offsets, int nleaf, const float4* atoms, float* M_leaf, int Rpad, cudaStream_t s);
+// P2M of the leaves and M2M of their parents in one launch (8 sibling leaves per
+// CTA).  Returns false, launching nothing, when the order's shared memory does
+// not fit or nleaf is not a multiple of 8.
+bool launch_p2m_m2m(int P, const int* offsets, int nleaf, const float4* atoms, float* M_leaf, float* M_parent,
+                    const float* At, int Rpad, cudaStream_t s);
 void launch_l2p(int P, const int* offsets, int nleaf, const float4* atoms, const float* L_leaf, int Rpad, float4* field,
                 cudaStream_t s);
 // Near field.  variant = shape + 3 * persistence: shape = the warp-step shape
@@ -150,9 +154,9 @@ void launch_m2m(const float* M_child, float* M_parent, const float* At, int npar
 
 struct RootArgs {
     int R, Rpad;
-    const double* m2m;      // 8 x R x R
+    const double* m2m;      // 8 blocks of R x R, block o at o * ((R^2 + 1) & ~1)
     const double* l2l;      // 8 x R x R
-    const double* lattice;  // R x R
+    const double* lattice;  // R x R (allocated to an even count)
     const float* M1;        // level-1 multipoles (8 rows)
     double* M0;             // root multipole (FP64)
     double* L0;             // root local (FP64)
@@ -162,9 +166,34 @@ struct RootArgs {
     const StepConst* sc;
     int images;
 };
-void launch_root_m2m(const RootArgs& a, cudaStream_t s);
 void launch_root_lattice(const RootArgs& a, cudaStream_t s);
 void launch_root_l2l(const RootArgs& a, cudaStream_t s);
+
+// The upper tree in one launch of 8 CTAs (one per level-1 cell).  For
+// R <= TOP_STAGE_MAX_R (orders up to 6) the operators are staged in shared memory
+// and the launch does the M2M from level 'from' (3, 2, or 1 = level 1 already
+// complete) up to level 1; for larger R only from = 1 is allowed (the M2M levels
+// take launch_m2m).  Then the FP64 root M2M and, when 'lattice' is set, the
+// lattice operator (else launch_top follows with launch_root_lattice).  Same
+// arithmetic as launch_m2m per level, the root M2M and launch_root_lattice.
+struct TopArgs {
+    RootArgs root;
+    int from;
+    int lattice;          // 1: the last CTA applies the lattice operator (R <= TOP_LATTICE_MAX_R)
+    const float* Min;     // multipoles of level 'from' (from >= 2)
+    float* M2;            // level-2 multipoles (written when from = 3)
+    float* M1;            // level-1 multipoles (written when from >= 2, read when from = 1)
+    const float* m2m_t;   // FP32 M2M operator, [octant][column][row]
+    double* part;         // 8 x R x 4 FP64 partial sums of the root M2M
+    float* fconst;        // out: FP32 dipole-correction constants of the finalize (4)
+    int natoms;
+    int* done;            // zero at launch
+    int* err;             // bit 1: the bounded wait for the staged copies gave up
+};
+constexpr int TOP_STAGE_MAX_R = 49;
+constexpr int TOP_LATTICE_MAX_R = 144;
+size_t top_smem_bytes(int R);
+void launch_top(const TopArgs& a, cudaStream_t s);
 
 struct FinalArgs {
     const StepConst* sc;
@@ -173,10 +202,10 @@ struct FinalArgs {
     const int* order;        // sorted -> input index
     const float4* near;      // sorted (phi, grad) near field, scaled units
     const float4* far;       // sorted far field, scaled units
-    const double* sums;      // dipole + total charge
+    const float* fconst;     // q*ke*coef*M (3) and ke*coef*|M|^2/N, FP32 (written by k_top)
     float* forces;           // 3N input order
     float* pots;             // N input order
-    double* partials;        // per block: 0.5 * sum q * pot (FP64)
+    double* partials;        // per block: 0.5 * sum q * pot as an FP32 pair (hi, lo)
     int* done = nullptr;     // zero at start: the last block sums the partials into *energy
     double* energy = nullptr;
 };

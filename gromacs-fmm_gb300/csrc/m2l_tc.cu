@@ -28,6 +28,7 @@
 
 #include <atomic>
 
+#include "async.cuh"
 #include "common.cuh"
 #include "kernels.h"
 #include "m2l_tc.h"
@@ -37,48 +38,6 @@ namespace gbfmm {
 extern std::atomic<long> g_kernel_launches;
 
 namespace {
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
-{
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-// Bounded wait: gives up after ~2^24 polls (well over a second) and flags the error.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err)
-{
-    for (uint32_t i = 0; i < (1u << 24); i++)
-        if (mbar_try_wait(bar, parity)) return true;
-    atomicOr(err, 2);
-    return false;
-}
-
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
-{
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_u32(dst)),
-                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
-                 : "memory");
-}
 
 // TMA tile loads of the source grids, completing on an mbarrier (tx bytes).
 __device__ __forceinline__ void tma_load_5d(void* dst, const CUtensorMap* map, int c0, int c1, int c2, int c3, int c4,
@@ -170,6 +129,19 @@ __host__ __device__ __forceinline__ void tc_tile_shape_dev(int level, int& bx, i
 __global__ void __launch_bounds__(256) k_tc_grids(const TcGridArgs g)
 {
     const int groups = g.KP / 8;
+    const long conv_blocks = (g.rows * groups + 255) / 256;
+    if (blockIdx.x >= conv_blocks) {
+        const int lane = threadIdx.x & 31, R = g.root_R;
+        const int w = (int)(blockIdx.x - conv_blocks) * 8 + (threadIdx.x >> 5);
+        const int o = w / R, r = w % R;
+        if (o >= 8) return;
+        const double* A = g.root_l2l + ((size_t)o * R + r) * R;
+        double t = 0;
+        for (int c = lane; c < R; c += 32) t += A[c] * g.L0[c];
+        for (int k = 16; k > 0; k >>= 1) t += __shfl_xor_sync(0xffffffffu, t, k);
+        if (lane == 0) g.L1[(size_t)o * g.Rpad + r] += (float)t;
+        return;
+    }
     const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= g.rows * groups) return;
     const long row = i / groups;
@@ -220,8 +192,9 @@ void launch_tc_grids(const TcGridArgs& g, cudaStream_t s)
 {
     const long n = g.rows * (g.KP / 8);
     if (n <= 0) return;
+    const long root_blocks = g.root_l2l ? (8L * g.root_R + 7) / 8 : 0;
     g_kernel_launches.fetch_add(1, std::memory_order_relaxed);
-    k_tc_grids<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(g);
+    k_tc_grids<<<(unsigned)((n + 255) / 256 + root_blocks), 256, 0, s>>>(g);
 }
 
 // ------------------------------------------------------------------ M2L
@@ -270,7 +243,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(const __grid_constant_
             mbar_init(&bar_empty[q], 1);
         }
         mbar_init(bar_done, 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        mbar_init_fence();
     }
     if (warp == 2) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),

@@ -69,6 +69,13 @@ struct TcGridArgs {
     int R, Rpad, KP, periodic;
     long rows;
     __nv_bfloat16 *hi, *lo;           // lo may be NULL (one product)
+    // Root L2L, run by extra blocks of the same launch (before the M2L adds to
+    // level 1): L1[o][r] += sum_c l2l[o][r][c] L0[c] in FP64, one warp per (o, r),
+    // the arithmetic of k_root_l2l.  Skipped when root_l2l is NULL.
+    const double* root_l2l = nullptr;
+    const double* L0 = nullptr;
+    float* L1 = nullptr;
+    int root_R = 0;
 };
 void launch_tc_grids(const TcGridArgs& g, cudaStream_t s);
 

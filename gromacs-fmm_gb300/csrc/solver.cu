@@ -96,7 +96,10 @@ const OpTables* get_tables(int P, int images)
         pack_operator(pl, A.data(), t->packed.data() + off);
         return off;
     };
-    t->root_m2m.resize((size_t)8 * R * R);
+    // FP64 root operators in blocks of an even number of doubles (16-byte aligned
+    // rows for bulk copies): M2M block o at o * R2p, the lattice padded to R2p
+    const size_t R2p = ((size_t)R * R + 1) & ~(size_t)1;
+    t->root_m2m.assign(8 * R2p, 0.0);
     t->root_l2l.resize((size_t)8 * R * R);
     t->m2m_t.assign((size_t)8 * R * R, 0.f);
     t->l2l_t.assign((size_t)8 * R * R, 0.f);
@@ -106,7 +109,7 @@ const OpTables* get_tables(int P, int images)
     };
     for (int o = 0; o < 8; o++) {
         scaled_m2m(P, o, A.data());
-        std::copy(A.begin(), A.end(), t->root_m2m.begin() + (size_t)o * R * R);
+        std::copy(A.begin(), A.end(), t->root_m2m.begin() + o * R2p);
         transpose(t->m2m_t, o);
         scaled_l2l(P, o, A.data());
         std::copy(A.begin(), A.end(), t->root_l2l.begin() + (size_t)o * R * R);
@@ -119,7 +122,7 @@ const OpTables* get_tables(int P, int images)
         t->off_cls[c] = append(t->plan[OP_M2L]);
         if (P <= TC_MAX_ORDER) append_tc_image(t->tc, R, A.data(), t->tc_img);
     }
-    t->lattice.resize((size_t)R * R);
+    t->lattice.assign(R2p, 0.0);
     lattice_operator(P, images, t->lattice.data());
     g_tabs.push_back(t);
     return t;
@@ -156,6 +159,8 @@ struct gbfmm_handle {
     float* Llev[8] = {};
     size_t lev_floats = 0;
     double *d_M0 = nullptr, *d_L0 = nullptr;
+    double* d_root_part = nullptr;  // 8 x R x 4 shares of the FP64 root M2M
+    float* d_fconst = nullptr;      // dipole-correction constants of the finalize
     float* d_ops = nullptr;
     CEntry* d_entries = nullptr;
     size_t tasks_bytes = 0;  // entries + tasks allocation
@@ -312,6 +317,8 @@ static int layout(gbfmm_handle* h, Arena& a)
     }
     h->d_M0 = a.take<double>(R);
     h->d_L0 = a.take<double>(R);
+    h->d_root_part = a.take<double>(32 * (size_t)R);
+    h->d_fconst = a.take<float>(4);
     h->d_ops = a.take<float>(t->packed.size());
     h->d_root_m2m = a.take<double>(t->root_m2m.size());
     h->d_root_l2l = a.take<double>(t->root_l2l.size());
@@ -586,7 +593,7 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
     const int D = h->D, n = h->n;
     const long launches0 = g_kernel_launches.load();
     mark(h, 0);
-    int* sync = h->d_counts + h->nleaf + 1;  // [0] tree keys, [1] finalize, [2] P2P queue
+    int* sync = h->d_counts + h->nleaf + 1;  // [0] tree keys, [1] finalize, [2] P2P queue, [3] upper tree
     cudaMemsetAsync(h->d_counts, 0, sizeof(int) * (h->nleaf + 1 + 4), s);
     cudaMemsetAsync(h->d_L, 0, sizeof(float) * h->lev_floats, s);
     {
@@ -618,7 +625,8 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
         };
         const OpTables* t = h->tab;
         pf(h->d_m2m_t, sizeof(float) * t->m2m_t.size());
-        pf(h->d_root_m2m, sizeof(double) * (t->root_m2m.size() + t->root_l2l.size() + t->lattice.size()));
+        pf(h->d_root_m2m, (size_t)(reinterpret_cast<const char*>(h->d_lattice + t->lattice.size()) -
+                                   reinterpret_cast<const char*>(h->d_root_m2m)));
         pf(h->d_l2l_t, sizeof(float) * t->l2l_t.size());
         pf(h->d_entries, h->tasks_bytes);
         pf(h->d_p2p_st, sizeof(int) * 3 * h->n_p2p_st);
@@ -644,9 +652,15 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
         launch_p2p(pa, h->p2p_variant, h->stream_nf, sync + 2);
         cudaEventRecord(h->ev_join, h->stream_nf);
     }
-    launch_p2m(h->P, h->d_off, h->nleaf, h->d_atoms, h->Mlev[D], h->Rpad, s);
+    // upward pass: P2M with the M2M of the leaf parents in one launch, M2M launches
+    // down to level 3, then levels 2 and 1 and the FP64 root in one launch (k_top)
+    const bool fused = D >= 2 && launch_p2m_m2m(h->P, h->d_off, h->nleaf, h->d_atoms, h->Mlev[D], h->Mlev[D - 1],
+                                                h->d_m2m_t, h->Rpad, s);
+    if (!fused) launch_p2m(h->P, h->d_off, h->nleaf, h->d_atoms, h->Mlev[D], h->Rpad, s);
     mark(h, 2);
-    for (int k = D - 1; k >= 1; k--) launch_m2m(h->Mlev[k + 1], h->Mlev[k], h->d_m2m_t, 1 << (3 * k), h->R, h->Rpad, s);
+    const int top_from = D == 1 || h->R > TOP_STAGE_MAX_R ? 1 : std::min(3, fused ? D - 1 : D);
+    for (int k = fused ? D - 2 : D - 1; k >= top_from; k--)
+        launch_m2m(h->Mlev[k + 1], h->Mlev[k], h->d_m2m_t, 1 << (3 * k), h->R, h->Rpad, s);
     mark(h, 3);
     RootArgs ra;
     ra.R = h->R;
@@ -662,11 +676,29 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
     ra.sums = h->d_sums;
     ra.sc = h->d_sc;
     ra.images = h->prm.images;
-    launch_root_m2m(ra, s);
-    launch_root_lattice(ra, s);
+    TopArgs top;
+    top.root = ra;
+    top.from = top_from;
+    top.lattice = h->R <= TOP_LATTICE_MAX_R ? 1 : 0;
+    top.Min = h->Mlev[top_from];
+    top.M2 = D >= 2 ? h->Mlev[2] : nullptr;
+    top.M1 = h->Mlev[1];
+    top.m2m_t = h->d_m2m_t;
+    top.part = h->d_root_part;
+    top.fconst = h->d_fconst;
+    top.natoms = h->n;
+    top.done = sync + 3;
+    top.err = h->d_flags + 2;
+    launch_top(top, s);
     mark(h, 4);
     if (h->tc) {
-        launch_tc_grids(tc_grid_args(h), s);
+        // the root L2L rides on the grid conversion, ahead of the M2L
+        TcGridArgs tg = tc_grid_args(h);
+        tg.root_l2l = h->d_root_l2l;
+        tg.L0 = h->d_L0;
+        tg.L1 = h->Llev[1];
+        tg.root_R = h->R;
+        launch_tc_grids(tg, s);
         TcArgs& ta = *h->tca;  // the current tuning: entry split and pipeline depth
         ta.tasks = h->d_tc_tasks_v[h->tc_split_v];
         ta.atomic = h->tc_split_v > 0 ? 1 : 0;
@@ -677,7 +709,7 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
         launch_contract(a, h->m2l_ntask, s);
     }
     mark(h, 5);
-    launch_root_l2l(ra, s);
+    if (!h->tc) launch_root_l2l(ra, s);
     if (D >= 2) {
         // L2L of levels 2..D and L2P in one launch
         DownArgs da;
@@ -717,7 +749,7 @@ static void enqueue_final(gbfmm_handle* h)
         fa.order = h->d_order;
         fa.near = h->d_near;
         fa.far = h->d_far;
-        fa.sums = h->d_sums;
+        fa.fconst = h->d_fconst;
         fa.forces = h->d_forces;
         fa.pots = h->d_pots;
         fa.partials = h->d_partials;
@@ -975,10 +1007,11 @@ static int fetch(gbfmm_handle* h)
         for (int s = 0; s < 9; s++) cudaEventElapsedTime(&h->stage_ms[s], h->ev[s], h->ev[s + 1]);
     }
     h->results_on_host = true;
-    if (h->h_flags[1]) {
+    if (h->h_flags[1] || h->h_flags[2]) {
         CK(cudaMemsetAsync(h->d_flags, 0, sizeof(int) * 4, h->stream));
         h->have_result = false;
-        return fail(GBFMM_ERR_TIMEOUT, "a bounded device wait in the tensor-core M2L gave up");
+        return fail(GBFMM_ERR_TIMEOUT, h->h_flags[1] ? "a bounded device wait in the tensor-core M2L gave up"
+                                                      : "a bounded device wait in the upper-tree kernel gave up");
     }
     if (h->h_flags[0]) {
         CK(cudaMemsetAsync(h->d_flags, 0, sizeof(int) * 4, h->stream));
