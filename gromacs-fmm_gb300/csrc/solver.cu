@@ -140,6 +140,7 @@ struct gbfmm_handle {
     // (captured as a fork/join of the step graph)
     cudaStream_t stream_nf = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaEvent_t ev_sc = nullptr;  // the step's copy of h_sc has been made (h_sc may be rewritten)
     // host state
     std::vector<float> h_q;
     bool have_charges = false, have_result = false, results_on_host = false;
@@ -268,6 +269,7 @@ static void free_handle(gbfmm_handle* h)
     if (h->stream) cudaStreamDestroy(h->stream);
     if (h->stream_nf) cudaStreamDestroy(h->stream_nf);
     if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    if (h->ev_sc) cudaEventDestroy(h->ev_sc);
     if (h->ev_join) cudaEventDestroy(h->ev_join);
     delete h;
 }
@@ -595,7 +597,6 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
     mark(h, 0);
     int* sync = h->d_counts + h->nleaf + 1;  // [0] tree keys, [1] finalize, [2] P2P queue, [3] upper tree
     cudaMemsetAsync(h->d_counts, 0, sizeof(int) * (h->nleaf + 1 + 4), s);
-    cudaMemsetAsync(h->d_L, 0, sizeof(float) * h->lev_floats, s);
     {
         TreeArgs ta;
         ta.sc = h->d_sc;
@@ -652,6 +653,7 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
         launch_p2p(pa, h->p2p_variant, h->stream_nf, sync + 2);
         cudaEventRecord(h->ev_join, h->stream_nf);
     }
+    cudaMemsetAsync(h->d_L, 0, sizeof(float) * h->lev_floats, s);  // the locals, after the fork
     // upward pass: P2M with the M2M of the leaf parents in one launch, M2M launches
     // down to level 3, then levels 2 and 1 and the FP64 root in one launch (k_top)
     const bool fused = D >= 2 && launch_p2m_m2m(h->P, h->d_off, h->nleaf, h->d_atoms, h->Mlev[D], h->Mlev[D - 1],
@@ -810,7 +812,8 @@ extern "C" int gbfmm_create(const gbfmm_params* prm, int natoms, gbfmm_handle** 
         if (cudaStreamCreateWithPriority(&h->stream, cudaStreamNonBlocking, hi) != cudaSuccess ||
             cudaStreamCreateWithPriority(&h->stream_nf, cudaStreamNonBlocking, lo) != cudaSuccess ||
             cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-            cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess)
+            cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&h->ev_sc, cudaEventDisableTiming) != cudaSuccess)
             return bail(fail(GBFMM_ERR_CUDA, "stream create failed"));
     }
     Arena sz;
@@ -920,6 +923,9 @@ static int set_box(gbfmm_handle* h, const float* box, const float* d_coords)
         return fail(GBFMM_ERR_BOX, "box must be cubic (got %g x %g x %g)", box[0], box[4], box[8]);
     const double L = (double)box[0];
     const int D = h->D, nd = 1 << D;
+    // the previous step's copy of the constants must have been made before they
+    // are rewritten (it runs first in that step, so this rarely waits)
+    if (h->ev_sc) cudaEventSynchronize(h->ev_sc);
     StepConst* sc = h->h_sc;
     sc->coords = d_coords;
     sc->inv_h = (float)(nd / L);
@@ -948,14 +954,24 @@ static int set_box(gbfmm_handle* h, const float* box, const float* d_coords)
     return GBFMM_OK;
 }
 
-static int run_step(gbfmm_handle* h)
+static bool graph_mode(const gbfmm_handle* h) { return !(h->prm.flags & GBFMM_FLAG_NO_GRAPH) && !h->timing; }
+
+// One step: the upload of the step constants (the first node of the graph, then
+// an event that set_box waits on) and enqueue_step.  In graph mode the graph is
+// launched on 'launch' (default: the handle's stream).
+static int run_step(gbfmm_handle* h, cudaStream_t launch = nullptr)
 {
-    CK(cudaMemcpyAsync(h->d_sc, h->h_sc, sizeof(StepConst), cudaMemcpyHostToDevice, h->stream));
-    const bool use_graph = !(h->prm.flags & GBFMM_FLAG_NO_GRAPH) && !h->timing;
+    const bool use_graph = graph_mode(h);
+    auto upload = [h, use_graph]() {
+        cudaMemcpyAsync(h->d_sc, h->h_sc, sizeof(StepConst), cudaMemcpyHostToDevice, h->stream);
+        // inside the capture: an event-record node of the graph
+        cudaEventRecordWithFlags(h->ev_sc, h->stream, use_graph ? cudaEventRecordExternal : cudaEventRecordDefault);
+    };
     if (use_graph) {
         if (!h->gexec) {
             cudaGraph_t g = nullptr;
             CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+            upload();
             enqueue_step(h);
             cudaError_t e = cudaStreamEndCapture(h->stream, &g);
             if (e != cudaSuccess) return fail(GBFMM_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
@@ -963,8 +979,9 @@ static int run_step(gbfmm_handle* h)
             cudaGraphDestroy(g);
             if (e != cudaSuccess) return fail(GBFMM_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
         }
-        CK(cudaGraphLaunch(h->gexec, h->stream));
+        CK(cudaGraphLaunch(h->gexec, launch ? launch : h->stream));
     } else {
+        upload();
         enqueue_step(h);
         CK(cudaGetLastError());
     }
@@ -982,6 +999,17 @@ extern "C" int gbfmm_execute_device(gbfmm_handle* h, const void* d_coords, const
     if (rc) return rc;
     cudaStream_t us = (cudaStream_t)stream;
     cudaEvent_t ein = h->ev[14], eout = h->ev[15];
+    if (graph_mode(h)) {
+        // the step graph runs on the caller's stream, after any earlier work on
+        // the handle's stream; later copies of the results follow it
+        CK(cudaEventRecord(ein, h->stream));
+        CK(cudaStreamWaitEvent(us, ein, 0));
+        rc = run_step(h, us);
+        if (rc) return rc;
+        CK(cudaEventRecord(eout, us));
+        CK(cudaStreamWaitEvent(h->stream, eout, 0));
+        return GBFMM_OK;
+    }
     // order the internal stream after the caller's stream, and the caller's after us
     CK(cudaEventRecord(ein, us));
     CK(cudaStreamWaitEvent(h->stream, ein, 0));
@@ -1351,6 +1379,7 @@ struct gbfmm_batch {
     std::vector<cudaStream_t> workers;
     std::vector<cudaEvent_t> ev;
     cudaEvent_t ein = nullptr, eout = nullptr;
+    cudaEvent_t ev_sc = nullptr;  // the copy of h_sc has been made
     cudaGraphExec_t gexec = nullptr;
     bool have_result = false;
     // the systems' near fields in one persistent kernel
@@ -1370,6 +1399,7 @@ static void free_batch(gbfmm_batch* b)
     for (cudaStream_t s : b->workers) cudaStreamDestroy(s);
     for (cudaEvent_t e : b->ev) cudaEventDestroy(e);
     if (b->ein) cudaEventDestroy(b->ein);
+    if (b->ev_sc) cudaEventDestroy(b->ev_sc);
     if (b->eout) cudaEventDestroy(b->eout);
     if (b->master) cudaStreamDestroy(b->master);
     if (b->buf) cudaFree(b->buf);
@@ -1454,6 +1484,7 @@ extern "C" int gbfmm_batch_create(int n_sys, const int* atom_offsets, const int*
         b->ev.push_back(e);
     }
     if (cudaEventCreateWithFlags(&b->ein, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev_sc, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&b->eout, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&b->ev_near, cudaEventDisableTiming) != cudaSuccess)
         return bail(fail(GBFMM_ERR_CUDA, "event create"));
@@ -1552,6 +1583,7 @@ extern "C" int gbfmm_batch_execute_device(gbfmm_batch* b, const void* d_coords, 
                                           const float* box_edges, void* stream)
 {
     if (!b || !box_edges || (b->natoms > 0 && (!d_coords || !d_charges))) return fail(GBFMM_ERR_ARG, "NULL argument");
+    if (b->ev_sc) cudaEventSynchronize(b->ev_sc);  // the previous batch's copy of h_sc has been made
     for (int i = 0; i < b->n_sys; i++) {
         gbfmm_handle* h = b->hs[i];
         float box[9] = {box_edges[i], 0, 0, 0, box_edges[i], 0, 0, 0, box_edges[i]};
@@ -1565,6 +1597,7 @@ extern "C" int gbfmm_batch_execute_device(gbfmm_batch* b, const void* d_coords, 
     if (d_charges != b->d_q)
         CK(cudaMemcpyAsync(b->d_q, d_charges, sizeof(float) * b->natoms, cudaMemcpyDeviceToDevice, b->master));
     CK(cudaMemcpyAsync(b->d_sc, b->h_sc, sizeof(StepConst) * b->n_sys, cudaMemcpyHostToDevice, b->master));
+    CK(cudaEventRecord(b->ev_sc, b->master));
     if (!b->gexec) {
         int rc = batch_capture(b);
         if (rc) return rc;
