@@ -103,6 +103,7 @@ __global__ void __launch_bounds__(256) k_tree_keys(TreeArgs a)
     __syncthreads();
     if (!s_last) return;
     __threadfence();
+    if (threadIdx.x == 0) *a.done = 0;  // every block has counted: ready for the next step
     if (warp < 4) {
         // all loads issued before the fixed-order sum (one round trip)
         constexpr int K = (TREE_MAX_BLOCKS + 31) / 32;
@@ -270,11 +271,12 @@ void launch_scatter(const uint32_t* code, int n, int* cursor, int* tmp_idx, cuda
 // Stable order inside each leaf (ascending input index), which makes the body
 // order identical to the per-level stable counting sort of tree.cpp:43-74.
 __global__ void __launch_bounds__(256) k_leaf_sort(const int* off, int nleaf, const int* tmp_idx, const float4* uq,
-                                                   int* order, float4* atoms, int* atom_leaf)
+                                                   int* order, float4* atoms, int* atom_leaf, int* counts)
 {
     const int lane = threadIdx.x & 31;
     const int leaf = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (leaf >= nleaf) return;
+    if (counts && lane == 0) counts[leaf] = 0;  // consumed by the scan: zero for the next step
     const int b = off[leaf], n = off[leaf + 1] - b;
     if (n <= 32) {
         int v = lane < n ? tmp_idx[b + lane] : 0x7fffffff;
@@ -301,12 +303,13 @@ __global__ void __launch_bounds__(256) k_leaf_sort(const int* off, int nleaf, co
 }
 
 void launch_leaf_sort(const int* offsets, int nleaf, int* tmp_idx, const float4* uq, const uint32_t* code, int* order,
-                      float4* atoms, int* atom_leaf, cudaStream_t s)
+                      float4* atoms, int* atom_leaf, int* counts, cudaStream_t s)
 {
     (void)code;
     long threads = (long)nleaf * 32;
     COUNT_LAUNCH();
-    k_leaf_sort<<<(int)((threads + 255) / 256), 256, 0, s>>>(offsets, nleaf, tmp_idx, uq, order, atoms, atom_leaf);
+    k_leaf_sort<<<(int)((threads + 255) / 256), 256, 0, s>>>(offsets, nleaf, tmp_idx, uq, order, atoms, atom_leaf,
+                                                            counts);
 }
 
 // ------------------------------------------------------------------ P2M
@@ -1434,6 +1437,7 @@ __global__ void __launch_bounds__(TOP_THREADS) k_top(const TopArgs a)
     __syncthreads();
     if (!s_last) return;
     __threadfence();
+    if (tid == 0) *a.done = 0;  // ready for the next step
     for (int r = tid; r < R; r += TOP_THREADS) {
         double v[32];
 #pragma unroll
@@ -1538,6 +1542,11 @@ __global__ void __launch_bounds__(256) k_finalize(FinalArgs a)
     __syncthreads();
     if (!s_last || threadIdx.x >= 32) return;
     __threadfence();
+    if (threadIdx.x == 0) {
+        // ready for the next step: this counter and the one after the near field
+        *a.done = 0;
+        if (a.zero_after) *a.zero_after = 0;
+    }
     constexpr int K = (FINAL_MAX_BLOCKS + 31) / 32;
     f2sum v[K];
     const float2* part = reinterpret_cast<const float2*>(a.partials);

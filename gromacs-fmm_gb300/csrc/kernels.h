@@ -102,8 +102,9 @@ extern std::atomic<long> g_kernel_launches;
 void launch_tree_keys(const TreeArgs& a, cudaStream_t s);
 void launch_exclusive_scan(const int* in, int* out, int n, int* scratch, cudaStream_t s);
 void launch_scatter(const uint32_t* code, int n, int* cursor, int* tmp_idx, cudaStream_t s);
+// Also zeroes counts[0..nleaf) (consumed by then) when counts != NULL.
 void launch_leaf_sort(const int* offsets, int nleaf, int* tmp_idx, const float4* uq, const uint32_t* code, int* order,
-                      float4* atoms, int* atom_leaf, cudaStream_t s);
+                      float4* atoms, int* atom_leaf, int* counts, cudaStream_t s);
 void launch_p2m(int P, const int* offsets, int nleaf, const float4* atoms, float* M_leaf, int Rpad, cudaStream_t s);
 // P2M of the leaves and M2M of their parents in one launch (8 sibling leaves per
 // CTA).  Returns false, launching nothing, when the order's shared memory does
@@ -206,7 +207,8 @@ struct FinalArgs {
     float* forces;           // 3N input order
     float* pots;             // N input order
     double* partials;        // per block: 0.5 * sum q * pot as an FP32 pair (hi, lo)
-    int* done = nullptr;     // zero at start: the last block sums the partials into *energy
+    int* done = nullptr;     // zero at start: the last block sums the partials into *energy and re-zeroes it
+    int* zero_after = nullptr;  // a counter of the step (the P2P queue) that the last block also re-zeroes
     double* energy = nullptr;
 };
 void launch_finalize(const FinalArgs& a, cudaStream_t s);

@@ -595,8 +595,10 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
     const int D = h->D, n = h->n;
     const long launches0 = g_kernel_launches.load();
     mark(h, 0);
+    // Leaf counts and the step's counters are zero when a step starts: zeroed at
+    // creation, then re-zeroed by their last users (leaf sort, the last blocks of
+    // the tree, upper-tree and finalize kernels) and after a reported device error.
     int* sync = h->d_counts + h->nleaf + 1;  // [0] tree keys, [1] finalize, [2] P2P queue, [3] upper tree
-    cudaMemsetAsync(h->d_counts, 0, sizeof(int) * (h->nleaf + 1 + 4), s);
     {
         TreeArgs ta;
         ta.sc = h->d_sc;
@@ -638,7 +640,8 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
         }
     }
     launch_scatter(h->d_code, n, h->d_cursor, h->d_tmp, s);
-    launch_leaf_sort(h->d_off, h->nleaf, h->d_tmp, h->d_uq, h->d_code, h->d_order, h->d_atoms, h->d_atom_leaf, s);
+    launch_leaf_sort(h->d_off, h->nleaf, h->d_tmp, h->d_uq, h->d_code, h->d_order, h->d_atoms, h->d_atom_leaf,
+                     h->d_counts, s);
     mark(h, 1);
     // The near field needs only the tree: in graph mode it forks onto its own
     // stream and overlaps the far-field chain below (joined before finalize);
@@ -756,6 +759,7 @@ static void enqueue_final(gbfmm_handle* h)
         fa.pots = h->d_pots;
         fa.partials = h->d_partials;
         fa.done = sync + 1;
+        fa.zero_after = sync + 2;
         fa.energy = h->d_energy;
         launch_finalize(fa, s);
     } else {
@@ -866,6 +870,7 @@ extern "C" int gbfmm_create(const gbfmm_params* prm, int natoms, gbfmm_handle** 
     }
     if (rc != GBFMM_OK) return bail(fail(rc, "operator upload failed"));
     cudaMemset(h->d_flags, 0, sizeof(int) * 4);
+    cudaMemset(h->d_counts, 0, sizeof(int) * (h->nleaf + 1 + 4));  // then kept zero between steps
     cudaMemset(h->d_M, 0, sizeof(float) * h->lev_floats);
     rc = build_tasks(h);
     if (rc != GBFMM_OK) return bail(rc);
@@ -1037,6 +1042,7 @@ static int fetch(gbfmm_handle* h)
     h->results_on_host = true;
     if (h->h_flags[1] || h->h_flags[2]) {
         CK(cudaMemsetAsync(h->d_flags, 0, sizeof(int) * 4, h->stream));
+        CK(cudaMemsetAsync(h->d_counts, 0, sizeof(int) * (h->nleaf + 1 + 4), h->stream));
         h->have_result = false;
         return fail(GBFMM_ERR_TIMEOUT, h->h_flags[1] ? "a bounded device wait in the tensor-core M2L gave up"
                                                       : "a bounded device wait in the upper-tree kernel gave up");

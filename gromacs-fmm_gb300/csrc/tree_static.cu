@@ -151,7 +151,7 @@ extern "C" int gbfmm_tree_build_noalloc(const void* d_coords, const void* d_char
     launch_scatter((const uint32_t*)(base + OFF_CODE), natoms, cursor, (int*)(base + OFF_TMP), s);
     launch_leaf_sort(off, nleaf, (int*)(base + OFF_TMP), (const float4*)(base + OFF_UQ),
                      (const uint32_t*)(base + OFF_CODE), (int*)d_order, (float4*)(base + OFF_ATOMS),
-                     (int*)(base + OFF_LEAF), s);
+                     (int*)(base + OFF_LEAF), nullptr, s);
     e = cudaGetLastError();
     if (e != cudaSuccess) return err(GBFMM_ERR_CUDA, cudaGetErrorString(e));
     return GBFMM_OK;
