@@ -49,6 +49,8 @@ __global__ void __launch_bounds__(256) k_tree_keys(TreeArgs a)
             }
         }
     }
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < a.zero_n4; i += (long)gridDim.x * blockDim.x)
+        a.zero[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     __syncthreads();
     f2sum sd[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};  // dipole (3), total charge
     int bad = 0;

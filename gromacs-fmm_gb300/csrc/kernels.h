@@ -89,6 +89,10 @@ struct TreeArgs {
     static constexpr int MAX_PREFETCH = 8;
     const void* pf[MAX_PREFETCH] = {};
     unsigned long long pf_bytes[MAX_PREFETCH] = {};
+    // Buffer of the step zeroed on the way (the local expansions, which the
+    // far field accumulates into): zero_n4 float4s, or none when NULL.
+    float4* zero = nullptr;
+    long zero_n4 = 0;
 };
 // Leaf counts up to this size are scanned by the tree-key kernel's last block.
 constexpr int TREE_EPILOGUE_MAX_LEAVES = 1 << 15;

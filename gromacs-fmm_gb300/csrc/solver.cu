@@ -608,6 +608,8 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
         ta.code = h->d_code;
         ta.uq = h->d_uq;
         ta.counts = h->d_counts;
+        ta.zero = reinterpret_cast<float4*>(h->d_L);  // lev_floats: levels of Rpad (a multiple of 4) floats
+        ta.zero_n4 = (long)(h->lev_floats / 4);
         ta.partials = h->d_partials;
         ta.flags = h->d_flags;
         ta.done = sync;
@@ -656,7 +658,6 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
         launch_p2p(pa, h->p2p_variant, h->stream_nf, sync + 2);
         cudaEventRecord(h->ev_join, h->stream_nf);
     }
-    cudaMemsetAsync(h->d_L, 0, sizeof(float) * h->lev_floats, s);  // the locals, after the fork
     // upward pass: P2M with the M2M of the leaf parents in one launch, M2M launches
     // down to level 3, then levels 2 and 1 and the FP64 root in one launch (k_top)
     const bool fused = D >= 2 && launch_p2m_m2m(h->P, h->d_off, h->nleaf, h->d_atoms, h->Mlev[D], h->Mlev[D - 1],
@@ -963,8 +964,9 @@ static bool graph_mode(const gbfmm_handle* h) { return !(h->prm.flags & GBFMM_FL
 
 // One step: the upload of the step constants (the first node of the graph, then
 // an event that set_box waits on) and enqueue_step.  In graph mode the graph is
-// launched on 'launch' (default: the handle's stream).
-static int run_step(gbfmm_handle* h, cudaStream_t launch = nullptr)
+// launched on 'launch' when on_launch is set (any stream, the legacy default
+// stream 0 included), else on the handle's stream.
+static int run_step(gbfmm_handle* h, cudaStream_t launch = nullptr, bool on_launch = false)
 {
     const bool use_graph = graph_mode(h);
     auto upload = [h, use_graph]() {
@@ -984,7 +986,7 @@ static int run_step(gbfmm_handle* h, cudaStream_t launch = nullptr)
             cudaGraphDestroy(g);
             if (e != cudaSuccess) return fail(GBFMM_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
         }
-        CK(cudaGraphLaunch(h->gexec, launch ? launch : h->stream));
+        CK(cudaGraphLaunch(h->gexec, on_launch ? launch : h->stream));
     } else {
         upload();
         enqueue_step(h);
@@ -1009,7 +1011,7 @@ extern "C" int gbfmm_execute_device(gbfmm_handle* h, const void* d_coords, const
         // the handle's stream; later copies of the results follow it
         CK(cudaEventRecord(ein, h->stream));
         CK(cudaStreamWaitEvent(us, ein, 0));
-        rc = run_step(h, us);
+        rc = run_step(h, us, true);
         if (rc) return rc;
         CK(cudaEventRecord(eout, us));
         CK(cudaStreamWaitEvent(h->stream, eout, 0));

@@ -133,6 +133,36 @@ def test_device_execute_matches_host_execute(pkg, systems):
     s.close()
 
 
+class _CudaView:
+    """Zero-copy view of a device buffer of float32 (no stream synchronisation)."""
+
+    def __init__(self, ptr, shape):
+        self.__cuda_array_interface__ = {"shape": shape, "typestr": "<f4", "data": (int(ptr), False), "version": 2}
+
+
+def test_device_execute_is_ordered_on_the_callers_stream(pkg, systems):
+    """Work enqueued on the caller's stream after gbfmm_execute_device sees the
+    step's results without any other synchronisation, on the legacy default
+    stream (handle 0) as on a created stream."""
+    torch = pytest.importorskip("torch")
+    xyz, q, box = systems.water_ion_box(3000, 3.0, seed=21)
+    xyz2 = np.mod(xyz + np.float32(0.37), np.float32(box[0])).astype(np.float32)
+    s = pkg.ZetaFmmSolver(len(q), q, order=6, max_depth=3, images=4, flags=pkg.FLAG_DETERMINISTIC)
+    s.execute(xyz2, box)
+    f_ref = s.forces().copy()
+    x2 = torch.from_numpy(xyz2).cuda()
+    torch.cuda.synchronize()
+    for stream in (torch.cuda.default_stream(), torch.cuda.Stream()):
+        s.execute(xyz, box)  # the output buffers now hold another configuration
+        with torch.cuda.stream(stream):
+            s.execute_device(x2.data_ptr(), box, stream.cuda_stream)
+            fp, _, _ = s.device_outputs()
+            f_dev = torch.as_tensor(_CudaView(fp, (len(q), 3)), device="cuda").clone()
+        stream.synchronize()
+        assert np.array_equal(f_dev.cpu().numpy(), f_ref)
+    s.close()
+
+
 def test_deterministic_flag_is_bitwise_repeatable(pkg, systems):
     xyz, q, box = systems.water_ion_box(2000, 2.8, seed=13)
     s = pkg.ZetaFmmSolver(len(q), q, order=8, max_depth=3, images=4, flags=pkg.FLAG_DETERMINISTIC)
