@@ -1065,7 +1065,9 @@ __global__ void __launch_bounds__(256) k_p2m_m2m(const int* off, const float4* a
     }
 }
 
-constexpr size_t P2M_M2M_MAX_SMEM = 200 * 1024;
+// Fused only while a CTA's shared memory allows several CTAs per SM (orders up
+// to 7): at higher orders the standalone P2M keeps more warps resident.
+constexpr size_t P2M_M2M_MAX_SMEM = 80 * 1024;
 
 template <int P>
 static bool p2m_m2m_dispatch(const int* off, int nleaf, const float4* atoms, float* M, float* Mp, const float* At,
@@ -1386,7 +1388,8 @@ __global__ void __launch_bounds__(TOP_THREADS) k_top(const TopArgs a)
 {
     extern __shared__ float4 topsm[];
     __shared__ uint64_t bar;
-    __shared__ double lq[4 * 256];  // lattice quarters (R <= 256 rows)
+    static_assert(TOP_LATTICE_MAX_R <= 64, "lattice quarters buffer");
+    __shared__ double lq[4 * 64];  // lattice quarters (R <= TOP_LATTICE_MAX_R rows)
     const int R = a.root.R, Rpad = a.root.Rpad, R2p = top_r2p(R), g = blockIdx.x, tid = threadIdx.x;
     float* At = reinterpret_cast<float*>(topsm);
     double* Ag = reinterpret_cast<double*>(At + (STAGED ? 8 * R * R : 0));

@@ -196,7 +196,7 @@ struct TopArgs {
     int* err;             // bit 1: the bounded wait for the staged copies gave up
 };
 constexpr int TOP_STAGE_MAX_R = 49;
-constexpr int TOP_LATTICE_MAX_R = 144;
+constexpr int TOP_LATTICE_MAX_R = TOP_STAGE_MAX_R;  // larger: the multi-CTA k_root_lattice
 size_t top_smem_bytes(int R);
 void launch_top(const TopArgs& a, cudaStream_t s);
 
