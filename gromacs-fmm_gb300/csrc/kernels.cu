@@ -24,6 +24,26 @@ std::atomic<long> g_kernel_launches{0};
 
 // ------------------------------------------------------------------ tree
 
+// Sum over the tree-key blocks of one of the four per-block partials (dipole x, y,
+// z, total charge; FP32 pairs) by one warp: every load issued first (one round
+// trip), the blocks added in a fixed order, then a fixed butterfly.
+__device__ __forceinline__ f2sum sum_tree_partials(const double* partials, int nblocks, int quantity)
+{
+    const int lane = threadIdx.x & 31;
+    constexpr int K = (TREE_MAX_BLOCKS + 31) / 32;
+    f2sum v[K];
+    const float2* part = reinterpret_cast<const float2*>(partials);
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        const int b = lane + 32 * k;
+        const float2 p = b < nblocks ? __ldcg(&part[4 * b + quantity]) : make_float2(0.f, 0.f);
+        v[k] = f2sum{p.x, p.y};
+    }
+#pragma unroll
+    for (int k = 1; k < K; k++) v[0] = f2s_add(v[0], v[k]);
+    return f2s_warp_sum(v[0]);
+}
+
 __global__ void __launch_bounds__(256) k_tree_keys(TreeArgs a)
 {
     extern __shared__ float sh[];
@@ -97,7 +117,8 @@ __global__ void __launch_bounds__(256) k_tree_keys(TreeArgs a)
     }
     if (bad) atomicOr(&a.flags[0], 1);
     if (!a.done) return;
-    // last block: FP64 sums of the partials (fixed order) and the leaf scan
+    // last block: the leaf scan, and (when sums != NULL) the sums of the partials;
+    // the solver leaves the sums to the upper-tree kernel, off this serial path
     __shared__ int s_last;
     __threadfence();
     __syncthreads();
@@ -106,34 +127,32 @@ __global__ void __launch_bounds__(256) k_tree_keys(TreeArgs a)
     if (!s_last) return;
     __threadfence();
     if (threadIdx.x == 0) *a.done = 0;  // every block has counted: ready for the next step
-    if (warp < 4) {
-        // all loads issued before the fixed-order sum (one round trip)
-        constexpr int K = (TREE_MAX_BLOCKS + 31) / 32;
-        f2sum v[K];
-        const float2* part = reinterpret_cast<const float2*>(a.partials);
-#pragma unroll
-        for (int k = 0; k < K; k++) {
-            const int b = lane + 32 * k;
-            const float2 p = b < (int)gridDim.x ? __ldcg(&part[4 * b + warp]) : make_float2(0.f, 0.f);
-            v[k] = f2sum{p.x, p.y};
-        }
-#pragma unroll
-        for (int k = 1; k < K; k++) v[0] = f2s_add(v[0], v[k]);
-        const f2sum t = f2s_warp_sum(v[0]);
+    if (a.sums && warp < 4) {
+        const f2sum t = sum_tree_partials(a.partials, (int)gridDim.x, warp);
         if (lane == 0) a.sums[warp] = f2s_value(t);
     }
     if (a.off) {
-        // exclusive scan of counts in tiles of 4096: thread t owns 16 consecutive
-        // leaves of a tile, loaded together
+        // exclusive scan of counts in tiles of 4096 staged in shared memory
+        // (coalesced loads and stores); thread t scans 16 consecutive leaves
+        __shared__ int4 tile4[1024];
+        int* tile = reinterpret_cast<int*>(tile4);
         __shared__ int wsum[8];
         __shared__ int carry_s;
         const int n = a.nleaf;
         int carry = 0;
         for (int base = 0; base < n; base += 4096) {
-            const int b0 = base + 16 * threadIdx.x;
+            const int m = min(4096, n - base);
+            for (int i = threadIdx.x; i < 4096; i += 256) tile[i] = i < m ? __ldcg(&a.counts[base + i]) : 0;
+            __syncthreads();
             int c[16];
 #pragma unroll
-            for (int k = 0; k < 16; k++) c[k] = b0 + k < n ? __ldcg(&a.counts[b0 + k]) : 0;
+            for (int k = 0; k < 4; k++) {
+                const int4 v = tile4[4 * threadIdx.x + k];
+                c[4 * k] = v.x;
+                c[4 * k + 1] = v.y;
+                c[4 * k + 2] = v.z;
+                c[4 * k + 3] = v.w;
+            }
             int t = 0;
 #pragma unroll
             for (int k = 0; k < 16; k++) t += c[k];
@@ -147,15 +166,22 @@ __global__ void __launch_bounds__(256) k_tree_keys(TreeArgs a)
             int run = carry + x - t;
             for (int w = 0; w < warp; w++) run += wsum[w];
 #pragma unroll
-            for (int k = 0; k < 16; k++)
-                if (b0 + k < n) {
-                    a.off[b0 + k] = run;
-                    a.cursor[b0 + k] = run;
-                    run += c[k];
-                }
+            for (int k = 0; k < 16; k++) {
+                const int v = run;
+                run += c[k];
+                c[k] = v;
+            }
+#pragma unroll
+            for (int k = 0; k < 4; k++) tile4[4 * threadIdx.x + k] = make_int4(c[4 * k], c[4 * k + 1], c[4 * k + 2], c[4 * k + 3]);
             if (threadIdx.x == 255) carry_s = run;
             __syncthreads();
+            for (int i = threadIdx.x; i < m; i += 256) {
+                const int v = tile[i];
+                a.off[base + i] = v;
+                a.cursor[base + i] = v;
+            }
             carry = carry_s;
+            __syncthreads();  // the tile is reused by the next 4096 leaves
         }
         if (threadIdx.x == 0) a.off[n] = carry;
     }
@@ -1443,17 +1469,28 @@ __global__ void __launch_bounds__(TOP_THREADS) k_top(const TopArgs a)
     if (!s_last) return;
     __threadfence();
     if (tid == 0) *a.done = 0;  // ready for the next step
+    // dipole (3) and total charge of the bodies: the tree-key kernel's per-block
+    // partials, one warp per quantity
+    __shared__ double sums[4];
+    if (tid < 128) {
+        const f2sum t = sum_tree_partials(a.tree_part, a.tree_nblocks, tid >> 5);
+        if ((tid & 31) == 0) {
+            sums[tid >> 5] = f2s_value(t);
+            a.sums[tid >> 5] = f2s_value(t);
+        }
+    }
+    __syncthreads();
     for (int r = tid; r < R; r += TOP_THREADS) {
         double v[32];
 #pragma unroll
         for (int k = 0; k < 32; k++) v[k] = __ldcg(&a.part[((size_t)(k >> 2) * R + r) * 4 + (k & 3)]);
         double s = tree_sum32(v);
         if (r < 4) {
-            const double Q = a.root.sums[3], L = a.root.sc->box_len, c = 0.5 * L;
+            const double Q = sums[3], L = a.root.sc->box_len, c = 0.5 * L;
             if (r == 0) s = Q;
-            else if (r == 1) s = -(a.root.sums[2] - Q * c) / L;
-            else if (r == 2) s = (a.root.sums[0] - Q * c) / (2.0 * L);
-            else s = -(a.root.sums[1] - Q * c) / (2.0 * L);
+            else if (r == 1) s = -(sums[2] - Q * c) / L;
+            else if (r == 2) s = (sums[0] - Q * c) / (2.0 * L);
+            else s = -(sums[1] - Q * c) / (2.0 * L);
         }
         M0s[r] = s;
         a.root.M0[r] = s;
@@ -1461,7 +1498,7 @@ __global__ void __launch_bounds__(TOP_THREADS) k_top(const TopArgs a)
     if (tid == 0) {
         // FP32 constants of the tin-foil dipole correction for the finalize
         // (solver.cpp:30-49): q * ke * coef * M per body and ke * coef * |M|^2 / N
-        const double M0 = a.root.sums[0], M1 = a.root.sums[1], M2 = a.root.sums[2];
+        const double M0 = sums[0], M1 = sums[1], M2 = sums[2];
         const double cK = a.root.sc->coef * KE;
         a.fconst[0] = (float)(cK * M0);
         a.fconst[1] = (float)(cK * M1);

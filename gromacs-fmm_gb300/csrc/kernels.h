@@ -75,10 +75,10 @@ struct TreeArgs {
     int* counts;            // 8^D
     double* partials;       // per block: dipole (3) and total charge, FP32 pairs (hi, lo)
     int* flags;             // [0] non-finite input seen
-    // Last-block epilogue (all NULL: none).  The last block to finish sums the
-    // partials into sums[4] (fixed order) and, when off != NULL, writes the
-    // exclusive scan of counts into off[0..nleaf] and cursor[0..nleaf).  done is
-    // a counter that is zero when the kernel starts.
+    // Last-block epilogue (done NULL: none).  The last block to finish sums the
+    // partials into sums[4] (fixed order) when sums != NULL and, when off != NULL,
+    // writes the exclusive scan of counts into off[0..nleaf] and cursor[0..nleaf).
+    // done is a counter that is zero when the kernel starts (and again at its end).
     int* done = nullptr;
     double* sums = nullptr;
     int* off = nullptr;
@@ -167,7 +167,6 @@ struct RootArgs {
     double* L0;             // root local (FP64)
     float* M0f;             // FP32 copy of the root multipole (level-0 row)
     float* L1;              // level-1 locals (8 rows)
-    const double* sums;     // dipole (3) and total charge of the bodies, FP64
     const StepConst* sc;
     int images;
 };
@@ -190,6 +189,9 @@ struct TopArgs {
     float* M1;            // level-1 multipoles (written when from >= 2, read when from = 1)
     const float* m2m_t;   // FP32 M2M operator, [octant][column][row]
     double* part;         // 8 x R x 4 FP64 partial sums of the root M2M
+    const double* tree_part;  // the tree-key kernel's per-block dipole/charge partials (FP32 pairs)
+    int tree_nblocks;
+    double* sums;         // out: dipole (3) and total charge, FP64
     float* fconst;        // out: FP32 dipole-correction constants of the finalize (4)
     int natoms;
     int* done;            // zero at launch

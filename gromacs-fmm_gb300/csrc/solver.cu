@@ -613,7 +613,7 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
         ta.partials = h->d_partials;
         ta.flags = h->d_flags;
         ta.done = sync;
-        ta.sums = h->d_sums;
+        ta.sums = nullptr;  // summed by the upper-tree kernel, off the serial path
         if (h->nleaf <= TREE_EPILOGUE_MAX_LEAVES) {
             ta.off = h->d_off;
             ta.cursor = h->d_cursor;
@@ -679,7 +679,6 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
     ra.L0 = h->d_L0;
     ra.M0f = h->Mlev[0];
     ra.L1 = h->Llev[1];
-    ra.sums = h->d_sums;
     ra.sc = h->d_sc;
     ra.images = h->prm.images;
     TopArgs top;
@@ -691,6 +690,9 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
     top.M1 = h->Mlev[1];
     top.m2m_t = h->d_m2m_t;
     top.part = h->d_root_part;
+    top.tree_part = h->d_partials;
+    top.tree_nblocks = tree_blocks(h->n);
+    top.sums = h->d_sums;
     top.fconst = h->d_fconst;
     top.natoms = h->n;
     top.done = sync + 3;
