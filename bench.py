@@ -313,6 +313,89 @@ class Runner:
         return acc
 
 
+def rel_diff(f, g):
+    return float(np.sqrt(np.sum((f - g) ** 2) / np.sum(g ** 2)))
+
+
+def large_line(pkg, torch, dev, systems, tuner_mod, steps):
+    """The 1,002,002-atom water cube (21.5 nm, the period the reference gives the
+    21.5 x 21.5 x 43 nm slab): the learned tuner's checked proposal against the
+    plain order-10 FP32 FMM at its depth, device-resident steps, L2 flushed.  The
+    accuracy judge is the plain FMM (1e-5 of Ewald where Ewald is affordable)."""
+    xyz, q, box = systems.cfg_1m()
+    n = len(q)
+    mlp = tuner_mod.Mlp.load()
+    ts = tuner_mod.TunedSolver(q, mlp, tol=TOL)
+    P, D, prec = ts.propose(xyz, float(box[0]))
+    checks = [{"order": c["proposal"][0], "diff_vs_plain": c["diff_vs_plain"], "accepted": c["accepted"]}
+              for c in ts.checks if c["proposal"] is not None]
+    ts.solver.close()
+    mlp.close()
+    run = Runner(pkg, torch, dev, xyz, q, box)
+    out = {"workload": "water+ion 1,002,002 atoms, 21.5 nm cubic periodic box (333,402 SPC/E waters + "
+                       "898 Na+ + 898 Cl-)", "atoms": n}
+    for name, (pr, PP, DD) in (("tuned", (prec, P, D)), ("plain_fp32", (0, 10, tuner_mod.plain_depth(n)))):
+        s = run.solver(pr, PP, DD)
+        ms = run.time_device(s, steps, 3) / steps
+        out[name] = {"order": PP, "depth": DD, "precision": PREC_NAME[pr], "ms_per_step": ms,
+                     "value": n / (ms * 1e-3)}
+        s.close()
+    out["tuner_checks"] = checks
+    out["speedup_tuned_vs_plain"] = out["tuned"]["value"] / out["plain_fp32"]["value"]
+    return out
+
+
+def frames_line(pkg, torch, dev, systems, tuner_mod, n_frames):
+    """The 250,002-atom box over a trajectory of kicked frames (sigma 0.01 nm per
+    frame): per tolerance, the tuner proposes and checks once on the first frame,
+    and the choice then serves every frame; against the plain order-10, depth-5
+    FP32 FMM on every frame: the largest relative force difference and the mean
+    device time per frame (L2 flushed before each)."""
+    xyz, q, box = systems.cfg_250k()
+    n = len(q)
+    L = float(box[0])
+    frames = list(systems.kicked_frames(xyz, box, n_frames))
+    base = pkg.ZetaFmmSolver(n, q, order=10, max_depth=5, images=4)
+    fb, tb = [], []
+    st = torch.cuda.current_stream(dev)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+
+    def dev_time(s, x):
+        xd = torch.from_numpy(x).to(dev)
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        s.execute_device(xd.data_ptr(), L, st.cuda_stream)
+        e1.record(st)
+        e1.synchronize()
+        return e0.elapsed_time(e1)
+
+    base.execute(frames[0], L)
+    for x in frames:
+        tb.append(dev_time(base, x))
+        fb.append(base.forces().copy())
+    base.close()
+    out = {"workload": f"water+ion 250,002 atoms, 13.6 nm cube, {n_frames} frames with 0.01 nm Gaussian kicks",
+           "baseline": {"order": 10, "depth": 5, "precision": "fp32", "ms_per_frame": float(np.mean(tb))}}
+    for tol in (1e-3, 5e-4):
+        mlp = tuner_mod.Mlp.load()
+        ts = tuner_mod.TunedSolver(q, mlp, tol=tol)
+        P, D, prec = ts.propose(frames[0], L)
+        s = ts.solver
+        diffs, tt = [], []
+        for x, f0 in zip(frames, fb):
+            tt.append(dev_time(s, x))
+            diffs.append(rel_diff(s.forces(), f0))
+        s.close()
+        mlp.close()
+        out[f"tol_{tol:g}"] = {"order": P, "depth": D, "precision": PREC_NAME[prec],
+                               "max_rel_force_diff_vs_baseline": max(diffs), "ms_per_frame": float(np.mean(tt)),
+                               "speedup_vs_baseline": float(np.mean(tb)) / float(np.mean(tt))}
+    return out
+
+
 def batch_line(pkg, torch, dev, systems, steps, warmup):
     """64 independent systems (atom counts log-uniform in [2,000, 200,000], water +
     0.15 M NaCl, one cubic box each; order 6, BF16X3, depth for 16-128 bodies per
@@ -382,6 +465,9 @@ def main():
     ap.add_argument("--impl", default="gbfmm", choices=["gbfmm", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-system batched line")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the 1,002,002-atom line and the 250,002-atom trajectory line")
+    ap.add_argument("--frames", type=int, default=20, help="frames of the trajectory line")
     ap.add_argument("--profile", default=None,
                     help="precision,order,depth[,p2p_variant,m2l_split,m2l_stages]: only run --steps host-API "
                          "steps of that configuration and tuning (a short, fixed launch sequence for ncu "
@@ -539,6 +625,9 @@ def main():
             "gpu_launches": tuned["launches"] * args.steps}
     if rank == 0 and not args.no_batch:
         line["batch"] = batch_line(pkg, torch, dev, systems, max(3, min(args.steps, 10)), 2)
+    if rank == 0 and not args.no_extra:
+        line["large"] = large_line(pkg, torch, dev, systems, tuner_mod, 5)
+        line["frames"] = frames_line(pkg, torch, dev, systems, tuner_mod, args.frames)
     if rank == 0:
         v, cores, sec = cpu_reference(xyz, q, box, PLAIN[1], PLAIN[2], args.cpu_steps, 1)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",

@@ -108,6 +108,29 @@ def cfg_250k():
     return water_ion_box(83182 + 456, 13.6, n_na=228, n_cl=228, seed=5)
 
 
+def cfg_1m():
+    """The large water slab: 333,402 waters + 898 Na+ + 898 Cl- (0.15 M) = 1,002,002
+    atoms filling a 21.5 nm cube, depth 5 (30.6 bodies per leaf).  The slab is
+    described on a 21.5 x 21.5 x 43 nm box with the upper half empty; the reference's
+    solver takes box[XX][XX] as the period of a cube (zeta_fmm_solver.cpp:38-40), so
+    the system it solves is this cube, and so does this library (cubic boxes only)."""
+    return water_ion_box(333402 + 1796, 21.5, n_na=898, n_cl=898, seed=3)
+
+
+def kicked_frames(xyz, box, n_frames, sigma=0.01, seed=7):
+    """Frames of a trajectory: each frame adds Gaussian kicks of sigma nm to the
+    previous one (wrapped into the box).  Yields float32 coordinates."""
+    rng = np.random.default_rng(seed)
+    L = np.broadcast_to(np.asarray(box, dtype=np.float64), (3,))
+    x = xyz.astype(np.float64)
+    for _ in range(n_frames):
+        x = np.mod(x + rng.normal(0.0, sigma, size=x.shape), L)
+        x32 = x.astype(np.float32)
+        for d in range(3):
+            x32[x32[:, d] >= np.float32(L[d]), d] = np.float32(0.0)
+        yield x32
+
+
 def batch_systems(n_sys=64, seed=4, nmin=2000, nmax=200000, density=100.2):
     """Independent cubic water+ion boxes, atom counts log-uniform in [nmin, nmax],
     L = (N/density)^(1/3), 0.15 M NaCl.  Returns a list of (xyz, q, box)."""

@@ -1,0 +1,64 @@
+"""Full-size systems of the benchmark configurations: the 1,002,002-atom water cube
+at depth 5 and the 250,002-atom box over a kicked trajectory.  The FP64 oracle is
+too slow at these sizes, so the checks are size-independent properties: the
+mixed-precision path against the plain FP32 path (which the parity tests pin to
+the oracle at smaller sizes and at 95,600 atoms), energy agreement, finiteness,
+and the tuner's checked choice holding over the frames."""
+import time
+
+import numpy as np
+import pytest
+
+from conftest import G, rel_rms
+
+pytestmark = pytest.mark.gpu
+
+
+def test_million_atoms_depth5_tensor_core_vs_fp32(pkg, systems):
+    xyz, q, box = systems.cfg_1m()
+    L = float(box[0])
+    assert len(q) == 1002002
+    plain = pkg.ZetaFmmSolver(len(q), q, order=10, max_depth=5, images=4)
+    plain.execute(xyz, L)
+    f0, p0, e0 = plain.forces(), plain.potentials(), plain.get_energy()
+    plain.close()
+    assert np.isfinite(f0).all() and np.isfinite(p0).all()
+    tc = pkg.ZetaFmmSolver(len(q), q, order=8, max_depth=5, images=4, precision=pkg.PREC_BF16X3)
+    tc.execute(xyz, L)
+    f1, p1, e1 = tc.forces(), tc.potentials(), tc.get_energy()
+    tc.close()
+    assert rel_rms(f1, f0) < 5e-4
+    assert rel_rms(p1, p0) < 5e-4
+    assert abs(e1 - e0) < 2e-5 * abs(e0)
+
+
+def test_trajectory_frames_keep_the_checked_choice(pkg, systems):
+    """The tuner's choice, checked once on the first frame at 5e-4, stays within
+    5e-4 (+20 %: the tuner's own judge is the order-10 FMM at depth 4, about 1e-5
+    from the depth-5 one) of the order-10, depth-5 FP32 baseline on later frames
+    of a trajectory (0.01 nm kicks per frame), and is faster than it."""
+    pytest.importorskip("torch")
+    tuner = G.load_module("tuner")
+    xyz, q, box = systems.cfg_250k()
+    L = float(box[0])
+    frames = list(systems.kicked_frames(xyz, box, 3))
+    mlp = tuner.Mlp.load()
+    ts = tuner.TunedSolver(q, mlp, tol=5e-4)
+    ts.propose(frames[0], L)
+    base = pkg.ZetaFmmSolver(len(q), q, order=10, max_depth=5, images=4)
+    t_base = t_tuned = 0.0
+    for x in frames:
+        base.execute(x, L)
+        fb = base.forces()
+        ts.solver.execute(x, L)
+        assert rel_rms(ts.solver.forces(), fb) < 6e-4
+        t0 = time.perf_counter()
+        base.execute(x, L)
+        t_base += time.perf_counter() - t0
+        t0 = time.perf_counter()
+        ts.solver.execute(x, L)
+        t_tuned += time.perf_counter() - t0
+    base.close()
+    ts.solver.close()
+    mlp.close()
+    assert t_tuned * 2 < t_base
