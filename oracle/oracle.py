@@ -180,6 +180,9 @@ def ref_lib():
         R.zref_nlist.argtypes = [ctypes.c_int]
         R.zref_list.restype = None
         R.zref_list.argtypes = [ctypes.c_int, _ip, _ip, _dp]
+        R.zref_solve.restype = ctypes.c_int
+        R.zref_solve.argtypes = [ctypes.c_int, _dp, _dp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                 _dp, _dp]
         _ref = R
     return _ref
 
@@ -211,3 +214,21 @@ def ref_run(xyz, cycle, depth, images, theta=0.4):
         R.zref_list(which, _i(t), _i(s), _d(o))
         out[name] = (t[:cnt], s[:cnt], o[:cnt])
     return out
+
+
+def ref_solve(xyz, q, cycle, P, depth, images=4):
+    """The reference's own FP64 kernels (kernel.cu p2m ... l2p, run on the host by
+    oracle/ref_kernels_driver.cpp) on its own tree and lists.  Returns potentials
+    (kJ/mol/e) and forces (kJ/mol/nm) in input order, before the dipole correction:
+    the quantities of zeta_solve(..., stages=3)."""
+    R = ref_lib()
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    n = len(q)
+    pot = np.zeros(n)
+    force = np.zeros((n, 3))
+    rc = R.zref_solve(n, _d(xyz), _d(q), float(cycle), int(P), int(depth), int(images), _d(pot), _d(force))
+    if rc != 0:
+        raise ValueError("zref_solve rejected its arguments")
+    return pot, force
+

@@ -1,6 +1,9 @@
 #!/usr/bin/env bash
 # Builds oracle/_ref/libzetaref.so from the reference's own, unmodified zeta_fmm
-# tree and traverser sources plus oracle/ref_driver.cpp.  Runs only where the
+# sources: tree.cpp and traverser.cpp, and the FP64 kernels of kernel.cu (the part
+# before GPUKernel::GPUKernel(), piped to the compiler as host code through
+# oracle/ref_cuda_shim.h, so that no copy of the source is written), plus
+# oracle/ref_driver.cpp and oracle/ref_kernels_driver.cpp.  Runs only where the
 # reference checkout is present; the outputs stay out of git (oracle/_ref/).
 set -euo pipefail
 REF=${GB_FMM_REFERENCE:-/root/reference}
@@ -12,7 +15,11 @@ if [ ! -f "$SRC/tree.cpp" ]; then
 fi
 CUDA_INC=${CUDA_HOME:-/usr/local/cuda}/include
 mkdir -p "$HERE/_ref"
-g++ -std=c++17 -O2 -fPIC -shared -w -I"$CUDA_INC" -I"$SRC" \
-    "$SRC/tree.cpp" "$SRC/traverser.cpp" "$HERE/ref_driver.cpp" \
-    -o "$HERE/_ref/libzetaref.so"
+FLAGS=(-std=c++17 -O2 -fPIC -w -I"$CUDA_INC" -I"$SRC")
+last=$(grep -n "zeta_fmm::GPUKernel::GPUKernel()" "$SRC/kernel.cu" | cut -d: -f1)
+sed -n "1,$((last - 1))p" "$SRC/kernel.cu" |
+    g++ "${FLAGS[@]}" -x c++ -include "$HERE/ref_cuda_shim.h" -c - -o "$HERE/_ref/ref_kernels.o"
+g++ "${FLAGS[@]}" -shared \
+    "$SRC/tree.cpp" "$SRC/traverser.cpp" "$HERE/ref_driver.cpp" "$HERE/ref_kernels_driver.cpp" \
+    "$HERE/_ref/ref_kernels.o" -o "$HERE/_ref/libzetaref.so"
 echo "built $HERE/_ref/libzetaref.so"

@@ -22,6 +22,12 @@
  *   - energy 0.5*sum(q*phi)    fmm.cpp:89-98
  * Per-cell loops are OpenMP-parallel where the reference's kernels are
  * parallel over cells (each cell writes only its own expansion or bodies).
+ *
+ * Pinning: the tree and lists equal fixtures made by the reference's own
+ * tree.cpp/traverser.cpp bit for bit, and the potentials and forces (before the
+ * dipole correction) equal those of the reference's own FP64 kernels, run on the
+ * host by oracle/ref_kernels_driver.cpp, to 1e-12 relative (5e-16 measured) on
+ * the configurations of tests/golden/ref_outputs.npz.
  */
 #include "zeta64.h"
 

@@ -8,7 +8,12 @@ oracle/_ref/libzetaref.so by oracle/ref_build.sh) and records:
                   bodies exactly on cell boundaries and outside the box;
 * lists_small.npz -- complete P2P/M2L lists (target, source, offset in periods)
                   for depth 1-2 and images 0, 1, 2, 4;
-* lists_hash.json -- counts and SHA-256 of the complete lists for depth 3-4.
+* lists_hash.json -- counts and SHA-256 of the complete lists for depth 3-4;
+* ref_outputs.npz -- FP64 potentials and forces of the reference's own kernels
+                  (kernel.cu p2m ... l2p, run on the host by
+                  oracle/ref_kernels_driver.cpp; before the dipole correction) on
+                  every 5th atom of seeded water/ion boxes (REF_CASES), with the
+                  SHA-256 of the generated coordinates.
 
 Needs the reference checkout (only present where fixtures are generated):
     python tests/golden/make_golden.py
@@ -40,6 +45,17 @@ def digest(t, s, o):
     for a in (t, s, o):
         h.update(np.ascontiguousarray(a, dtype="<i4").tobytes())
     return h.hexdigest()
+
+
+# (lattice sites, box edge, ion pairs, order, depth, images); inputs are
+# systems.water_ion_box(sites, edge, ions, ions, seed=sites + order)
+REF_CASES = [(300, 2.0, 2, 4, 2, 4), (800, 2.0, 4, 5, 1, 4), (1000, 2.2, 4, 8, 2, 4), (1500, 3.0, 6, 10, 3, 0),
+             (1500, 3.0, 6, 6, 3, 2)]
+
+
+def ref_case_inputs(systems, case):
+    ns, L, ions, P, D, im = case
+    return systems.water_ion_box(ns, L, n_na=ions, n_cl=ions, seed=ns + P)
 
 
 def tree_case(xyz, cycle, depth):
@@ -91,6 +107,19 @@ def main():
     with open(os.path.join(HERE, "lists_hash.json"), "w") as f:
         json.dump(hashes, f, indent=1, sort_keys=True)
     out.update(hashes)
+    # 5. outputs of the reference's own FP64 kernels
+    ref = {}
+    for k, case in enumerate(REF_CASES):
+        xyz, q, box = ref_case_inputs(systems, case)
+        pot, force = O.ref_solve(xyz.astype(np.float64), q.astype(np.float64), float(case[1]), case[3], case[4],
+                                 case[5])
+        sample = np.arange(0, len(q), 5, dtype=np.int32)
+        ref[f"case{k}_params"] = np.array(case, np.float64)
+        ref[f"case{k}_xyz_sha256"] = np.frombuffer(hashlib.sha256(xyz.tobytes()).digest(), np.uint8)
+        ref[f"case{k}_idx"] = sample
+        ref[f"case{k}_pot"] = pot[sample]
+        ref[f"case{k}_force"] = force[sample]
+    np.savez_compressed(os.path.join(HERE, "ref_outputs.npz"), **ref)
     print(json.dumps(out, indent=1))
 
 

@@ -1,6 +1,7 @@
-"""GPU parity: the sm_103a FP32 path against the FP64 oracle (relative RMS force
-and potential error <= 1e-5, relative energy error <= 1e-6) and the tree against
-fixtures made by the reference's own tree.cpp (bit-exact)."""
+"""GPU parity: the sm_103a FP32 path against the FP64 oracle and against the
+outputs of the reference's own FP64 kernels (relative RMS force and potential
+error <= 1e-5, relative energy error <= 1e-6), and the tree against fixtures made
+by the reference's own tree.cpp (bit-exact)."""
 import numpy as np
 import pytest
 
@@ -36,6 +37,28 @@ def test_parity_vs_oracle(pkg, oracle, systems, n_sites, L, ions, P, depth, imag
     assert rel_rms(p, po) < TOL_F
     assert abs(e - eo) / abs(eo) < TOL_E
     s.close()
+
+
+def test_parity_vs_reference_kernel_outputs(pkg, oracle, systems):
+    """The FP32 path against the outputs of the reference's own FP64 kernels
+    (kernel.cu, committed fixture): the dipole correction, which the reference
+    applies on the host after its kernels, is taken off the GPU results with the
+    oracle's correction term."""
+    g = golden("ref_outputs.npz")
+    k = 0
+    while f"case{k}_params" in g:
+        ns, L, ions, P, D, im = g[f"case{k}_params"]
+        xyz, q, box = systems.water_ion_box(int(ns), float(L), n_na=int(ions), n_cl=int(ions), seed=int(ns) + int(P))
+        f, p, e, s = _solve(pkg, xyz, q, box, order=int(P), max_depth=int(D), images=int(im))
+        s.close()
+        x64, q64 = xyz.astype(np.float64), q.astype(np.float64)
+        p1, f1, _ = oracle.zeta_solve(x64, q64, float(L), int(P), int(D), int(im))
+        p0, f0, _ = oracle.zeta_solve(x64, q64, float(L), int(P), int(D), int(im), stages=3)
+        idx = g[f"case{k}_idx"]
+        assert rel_rms(f[idx] - (f1 - f0)[idx], g[f"case{k}_force"]) < TOL_F
+        assert rel_rms(p[idx] - (p1 - p0)[idx], g[f"case{k}_pot"]) < TOL_F
+        k += 1
+    assert k == 5
 
 
 def test_parity_water_96k(pkg, oracle, systems):

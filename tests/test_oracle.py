@@ -1,6 +1,7 @@
 """The oracle pinned against the reference: tree and lists against fixtures made
-by the reference's own tree.cpp/traverser.cpp, operators against physics (FP64
-Ewald and direct lattice sums)."""
+by the reference's own tree.cpp/traverser.cpp, potentials and forces against the
+outputs of the reference's own FP64 kernels (kernel.cu, run on the host), and the
+operators against physics (FP64 Ewald and direct lattice sums)."""
 import hashlib
 import json
 import os
@@ -96,3 +97,46 @@ def test_zeta_oracle_near_and_far_split(oracle, systems):
     p2, f2, _ = oracle.zeta_solve(x, q, float(box[0]), 6, 2, 4, stages=2)
     p4, f4, _ = oracle.zeta_solve(x, q, float(box[0]), 6, 2, 4, stages=4)
     assert np.allclose(f1 + f2 + f4, f_all, rtol=1e-12, atol=1e-9)
+
+
+def ref_cases():
+    g = golden("ref_outputs.npz")
+    k = 0
+    while f"case{k}_params" in g:
+        yield k, g
+        k += 1
+
+
+def ref_case_inputs(systems, g, k):
+    ns, L, ions, P, D, im = g[f"case{k}_params"]
+    xyz, q, box = systems.water_ion_box(int(ns), float(L), n_na=int(ions), n_cl=int(ions), seed=int(ns) + int(P))
+    assert hashlib.sha256(xyz.tobytes()).digest() == g[f"case{k}_xyz_sha256"].tobytes(), "input generator drifted"
+    return xyz, q, float(L), int(P), int(D), int(im)
+
+
+def test_oracle_equals_reference_kernels(oracle, systems):
+    """FP64 potentials and forces of the oracle's restatement equal those of the
+    reference's own kernels (before the dipole correction) to rounding."""
+    n_cases = 0
+    for k, g in ref_cases():
+        xyz, q, L, P, D, im = ref_case_inputs(systems, g, k)
+        pot, force, _ = oracle.zeta_solve(xyz.astype(np.float64), q.astype(np.float64), L, P, D, im, stages=3)
+        idx = g[f"case{k}_idx"]
+        assert rel_rms(pot[idx], g[f"case{k}_pot"]) < 1e-12
+        assert rel_rms(force[idx], g[f"case{k}_force"]) < 1e-12
+        n_cases += 1
+    assert n_cases == 5
+
+
+def test_reference_kernels_reproduce_their_fixture(oracle, systems):
+    """Where the reference is built, its kernels reproduce the committed fixture."""
+    if not oracle.ref_available():
+        pytest.skip("reference library not built")
+    for k, g in ref_cases():
+        xyz, q, L, P, D, im = ref_case_inputs(systems, g, k)
+        pot, force = oracle.ref_solve(xyz.astype(np.float64), q.astype(np.float64), L, P, D, im)
+        idx = g[f"case{k}_idx"]
+        assert np.array_equal(pot[idx], g[f"case{k}_pot"])
+        assert np.array_equal(force[idx], g[f"case{k}_force"])
+        break
+
