@@ -449,6 +449,10 @@ size_t tc_smem_bytes(const TcArgs& a)
            (2 * TC_MAXSTAGE + 1) * sizeof(uint64_t) + 16;
 }
 
+// Dynamic shared memory a CTA may take: 227 KB less the kernel's static entry
+// list (TC_MAXENT entries) and a reserve.
+constexpr size_t TC_DYN_SMEM_MAX = 227 * 1024 - TC_MAXENT * sizeof(CEntry) - 512;
+
 // Stages per CTA: at most about 100 KB of dynamic shared memory, so that two CTAs
 // (with their static entry list and the per-CTA reserve) share an SM; at least 2
 // where they fit.
@@ -458,7 +462,7 @@ int tc_pick_stages(int k_atoms, int img_bytes, int nprod)
     int ns = (int)((100 * 1024 - 1200) / st);
     if (ns < 2) ns = 2;
     if (ns > TC_MAXSTAGE) ns = TC_MAXSTAGE;
-    while (ns > 1 && 1024 + ns * st + (2 * TC_MAXSTAGE + 1) * sizeof(uint64_t) + 16 > 227 * 1024) ns--;
+    while (ns > 1 && 1024 + ns * st + (2 * TC_MAXSTAGE + 1) * sizeof(uint64_t) + 16 > TC_DYN_SMEM_MAX) ns--;
     return ns;
 }
 
@@ -466,7 +470,7 @@ int tc_max_stages(int k_atoms, int img_bytes, int nprod)
 {
     const size_t st = tc_stage_bytes(k_atoms, img_bytes, nprod);
     int ns = TC_MAXSTAGE;
-    while (ns > 1 && 1024 + ns * st + (2 * TC_MAXSTAGE + 1) * sizeof(uint64_t) + 16 > 227 * 1024) ns--;
+    while (ns > 1 && 1024 + ns * st + (2 * TC_MAXSTAGE + 1) * sizeof(uint64_t) + 16 > TC_DYN_SMEM_MAX) ns--;
     return ns;
 }
 

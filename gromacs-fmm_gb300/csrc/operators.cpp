@@ -580,9 +580,17 @@ namespace gbfmm {
 
 static inline int round16(int x) { return (x + 15) & ~15; }
 
-// Degree chunks by dynamic programming: minimise sum(N*K) over contiguous degree
-// ranges, with N = rows padded to 16 (<= 256) and K = (P-j0+1)^2 padded to 16.
-TcPlan make_tc_plan(int P)
+// Degree chunks by dynamic programming over contiguous degree ranges j0..j1
+// (N = rows padded to 16, <= 256; K = (P-j0+1)^2 padded to 16).  The cost of a
+// chunk per entry and product is its MMA issue, about 128 cycles per tcgen05.mma
+// (M = 128, K = 16) whatever N is, plus the copy of its operator image (N rows of
+// 128-byte K atoms at about 64 B/cycle).  The operator is zero where j + n > P
+// (m2l_matrix), so a chunk may span more degrees than the truncation needs: at
+// low orders one chunk is cheapest.  Where the images would keep two pipeline
+// stages of the split-precision form from fitting a CTA's shared memory, the image
+// bytes weigh more (make_tc_plan); the plan of fewest multiply-adds is the last
+// resort.
+static TcPlan tc_plan_dp(int P, int byte_weight)  // byte_weight 0: fewest multiply-adds
 {
     TcPlan pl;
     pl.P = P;
@@ -595,7 +603,7 @@ TcPlan make_tc_plan(int P)
             int N = round16(rows);
             if (N > 256) break;
             int K = round16((P - j0 + 1) * (P - j0 + 1));
-            int cost = N * K + 256;  // small per-chunk overhead favours fewer MMAs
+            int cost = byte_weight ? (K / 16) * 128 + N * ((K + 63) / 64) * byte_weight : N * K + 256;
             if (best[j1 + 1] < INF && cost + best[j1 + 1] < best[j0]) {
                 best[j0] = cost + best[j1 + 1];
                 nxt[j0] = j1 + 1;
@@ -622,6 +630,19 @@ TcPlan make_tc_plan(int P)
     while (t < col) t <<= 1;
     pl.tmem_cols = t;
     return pl;
+}
+
+TcPlan make_tc_plan(int P)
+{
+    // two stages of hi and lo tiles (A: 128 rows per K atom, B: the images) within
+    // 220 KB of shared memory (the kernel's static entry list and barriers take
+    // the rest of the 227 KB): the image bytes weigh more until they fit
+    for (int w = 2; w <= 64; w *= 2) {
+        TcPlan pl = tc_plan_dp(P, w);
+        const size_t stage = 2 * ((size_t)128 * pl.k_atoms * 128 + (size_t)pl.img_bytes);
+        if (2 * stage <= 220 * 1024) return pl;
+    }
+    return tc_plan_dp(P, 0);
 }
 
 static uint16_t f2bf(float f)
