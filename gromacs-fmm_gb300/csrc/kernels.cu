@@ -1405,10 +1405,12 @@ __device__ __forceinline__ double tree_sum32(double (&v)[32])
 // pairwise tree and applies the lattice operator (one thread per (row, column
 // quarter), quarters added pairwise), so that the upper tree takes one launch.
 // The degree-0 and degree-1 moments of M~_0 (total charge and dipole about the
-// box centre) are replaced by their exact FP64 sums over the bodies, which is
-// what the reference's FP64 P2M/M2M produces: the FP32 upward pass would otherwise
-// leave a monopole residual of ~1e-7 of sum|q| that the periodic lattice operator
-// (about 81 periods wide) turns into a constant shift of every potential.
+// box centre) are replaced by sums over the bodies of exact products in FP32
+// pairs (about 48 bits; the tree-key kernel's per-block partials, summed here),
+// which is what the reference's FP64 P2M/M2M produces to that accuracy: the FP32
+// upward pass would otherwise leave a monopole residual of ~1e-7 of sum|q| that
+// the periodic lattice operator (about 81 periods wide) turns into a constant
+// shift of every potential.
 template <bool STAGED>
 __global__ void __launch_bounds__(TOP_THREADS) k_top(const TopArgs a)
 {
