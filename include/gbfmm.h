@@ -111,7 +111,12 @@ int gbfmm_get_energy(gbfmm_handle* h, double* coulomb_energy);
 int gbfmm_compare_forces(gbfmm_handle* h, const float* ref_forces, double* l2f);
 
 /* Per-stage device times of the last execute (ms, CUDA events), when built with
- * timing enabled by gbfmm_set_timing(h, 1). */
+ * timing enabled by gbfmm_set_timing(h, 1); the stages then run one after
+ * another (no near/far overlap).  Stages: tree; p2m (with the M2M of the leaf
+ * parents where fused); m2m (the remaining per-level M2M launches); root (upper
+ * tree, FP64 root and lattice); m2l (bf16 source grids and root L2L, M2L); l2l
+ * (the fused downward pass of L2L and L2P at depth >= 2); l2p (depth 1 only);
+ * p2p; finalize. */
 int gbfmm_set_timing(gbfmm_handle* h, int enable);
 int gbfmm_stage_times(gbfmm_handle* h, float* ms, int n_max, int* n_out);
 const char* gbfmm_stage_name(int stage);
