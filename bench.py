@@ -17,8 +17,10 @@ metric: atoms*steps/s at <= 1e-3 relative RMS force error against FP64 Ewald.
   value  device-resident: one CUDA-graph replay per step through
          gbfmm_execute_device, CUDA events on the caller's stream, L2 flushed
          (256 MB write) before every timed step.
-  e2e    the reference-facing call gbfmm_execute: host coordinates in (H2D),
-         host forces + potentials + energy out (D2H), synchronous.
+  e2e    the reference-facing call gbfmm_execute: host coordinates in, host
+         forces + potentials + energy out, synchronous.  On GB300 the step
+         reads and writes that host memory in place over NVLink-C2C; the same
+         call with staging copies is reported beside it (value_with_copies).
 Multi-GPU (torchrun): independent replicas per rank ("replicas only": a single
 system does not shard), value = sum over ranks of atoms / max time.
 
@@ -187,6 +189,22 @@ def ncu_traffic(kernel):
     return None, None
 
 
+def pageable_access(device=0):
+    """True where the device reads pageable host memory coherently (the driver's
+    CU_DEVICE_ATTRIBUTE_PAGEABLE_MEMORY_ACCESS, a read-only query)."""
+    import ctypes
+    try:
+        cu = ctypes.CDLL("libcuda.so.1")
+        if cu.cuInit(0) != 0:
+            return False
+        d, v = ctypes.c_int(), ctypes.c_int(0)
+        if cu.cuDeviceGet(ctypes.byref(d), int(device)) != 0:
+            return False
+        return cu.cuDeviceGetAttribute(ctypes.byref(v), 88, d) == 0 and v.value != 0
+    except OSError:
+        return False
+
+
 def dist_env():
     return int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0"))
 
@@ -259,8 +277,8 @@ class Runner:
         self.stream = torch.cuda.current_stream(dev)
         self.flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > L2
 
-    def solver(self, prec, P, D):
-        return self.pkg.ZetaFmmSolver(self.n, self.q, order=P, max_depth=D, images=4, precision=prec)
+    def solver(self, prec, P, D, flags=0):
+        return self.pkg.ZetaFmmSolver(self.n, self.q, order=P, max_depth=D, images=4, precision=prec, flags=flags)
 
     def step(self, s):
         s.execute_device(self.x_dev.data_ptr(), self.box, self.stream.cuda_stream)
@@ -569,6 +587,12 @@ def main():
         r = {"prec": prec, "P": P, "D": D, "ms": ms / args.steps, "value": value,
              "err": err_of(s), "clocks": clk.summary()}
         r["e2e"] = n * ws * args.steps / run.time_e2e(s, args.steps)
+        # the same call with staging copies (GBFMM_FLAG_HOST_COPY), for comparison
+        sc = run.solver(prec, P, D, flags=pkg.FLAG_HOST_COPY)
+        t = s.tuning()
+        sc.set_tuning(t["p2p_variant"], t["m2l_split"], t["m2l_stages"])
+        r["e2e_copies"] = n * ws * args.steps / run.time_e2e(sc, args.steps)
+        sc.close()
         r["stages"] = run.stages(s, args.steps)
         r["launches"] = s.step_launches()
         r["tiles"] = tiles
@@ -615,7 +639,11 @@ def main():
             "config": dict(config, order=P, depth=D, precision=PREC_NAME[tuned["prec"]]),
             "rel_force_err_vs_ewald": tuned["err"],
             "e2e": {"value": tuned["e2e"], "unit": UNIT, "h2d_bytes_per_step": 12 * n,
-                    "d2h_bytes_per_step": 12 * n + 4 * n + 8},
+                    "d2h_bytes_per_step": 12 * n + 4 * n + 8,
+                    "host_io": ("in place: the step reads the host coordinates and writes the host results "
+                                "over NVLink-C2C (pageable-memory access), no staging copies")
+                    if pageable_access(local) else "staging copies (cudaMemcpyAsync)",
+                    "value_with_copies": tuned["e2e_copies"]},
             "plain_fp32": {"value": plain["value"], "ms_per_step": plain["ms"], "order": plain["P"],
                            "depth": plain["D"], "rel_force_err_vs_ewald": plain["err"], "e2e": plain["e2e"],
                            "stage_ms": plain["stages"]},

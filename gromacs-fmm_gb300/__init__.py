@@ -22,6 +22,7 @@ PREC_BF16X3 = 1
 PREC_BF16X1 = 2
 FLAG_NO_GRAPH = 1
 FLAG_DETERMINISTIC = 2
+FLAG_HOST_COPY = 4
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "invalid box", 3: "non-finite coordinate or charge", 4: "CUDA error",
           5: "out of memory", 6: "unsupported", 7: "call out of order", 8: "device wait timed out",

@@ -1551,6 +1551,8 @@ __global__ void __launch_bounds__(256) k_finalize(FinalArgs a)
     // FP32 constants of the dipole correction, computed once in FP64 by k_top
     const float fM0 = a.fconst[0], fM1 = a.fconst[1], fM2 = a.fconst[2], corr_f = a.fconst[3];
     const float inv_h = a.sc->inv_h, inv_h2 = a.sc->inv_h * a.sc->inv_h;
+    float* __restrict__ forces = a.sc->out_forces;
+    float* __restrict__ pots = a.sc->out_pots;
     f2sum e = {0.f, 0.f};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) {
         const float4 nf = a.near[i], ff = a.far[i];
@@ -1559,13 +1561,13 @@ __global__ void __launch_bounds__(256) k_finalize(FinalArgs a)
         const float gx = (nf.y + ff.y) * inv_h2, gy = (nf.z + ff.z) * inv_h2, gz = (nf.w + ff.w) * inv_h2;
         const int o = a.order[i];
         const float qk = -q * (float)KE;
-        a.forces[3 * o] = qk * gx + q * fM0;
-        a.forces[3 * o + 1] = qk * gy + q * fM1;
-        a.forces[3 * o + 2] = qk * gz + q * fM2;
+        forces[3 * o] = qk * gx + q * fM0;
+        forces[3 * o + 1] = qk * gy + q * fM1;
+        forces[3 * o + 2] = qk * gz + q * fM2;
         // FP32 per body (no FP64 division), FP64 accumulation of the energy
         float pot = phi * (float)KE;
         if (q != 0.f) pot -= corr_f / q;
-        a.pots[o] = pot;
+        pots[o] = pot;
         e = f2s_add(e, f2s_prod(0.5f * q, pot));  // the exact product, as FP64 would hold it
     }
     e = f2s_warp_sum(e);
@@ -1603,7 +1605,12 @@ __global__ void __launch_bounds__(256) k_finalize(FinalArgs a)
 #pragma unroll
     for (int k = 1; k < K; k++) v[0] = f2s_add(v[0], v[k]);
     const f2sum t = f2s_warp_sum(v[0]);
-    if (threadIdx.x == 0) *a.energy = f2s_value(t);
+    if (threadIdx.x == 0) {
+        *a.sc->out_energy = f2s_value(t);
+        int* fl = a.sc->out_flags;
+        if (fl)
+            for (int k = 0; k < 4; k++) fl[k] = __ldcg(&a.flags[k]);
+    }
 }
 
 void launch_finalize(const FinalArgs& a, cudaStream_t s)

@@ -56,7 +56,14 @@ struct ContractArgs {
 // memory so that a captured graph can be replayed for a new box and new
 // coordinate pointer without re-capture.
 struct StepConst {
-    const float* coords;                 // 3N device coordinates of this step
+    const float* coords;                 // 3N coordinates of this step (device, or host memory the device reads in place)
+    // where the finalize writes this step's results: the handle's device buffers,
+    // or (a host call on a device that reaches pageable memory) its pinned host
+    // buffers, written in place with no copy afterwards
+    float* out_forces;                   // 3N, input order
+    float* out_pots;                     // N
+    double* out_energy;
+    int* out_flags;                      // non-NULL: the finalize's last block copies the step's 4 flags here
     float inv_h;                         // 2^D / L
     float pad_;
     double coef;                         // 4 pi / (3 V), dipole correction
@@ -210,12 +217,10 @@ struct FinalArgs {
     const float4* near;      // sorted (phi, grad) near field, scaled units
     const float4* far;       // sorted far field, scaled units
     const float* fconst;     // q*ke*coef*M (3) and ke*coef*|M|^2/N, FP32 (written by k_top)
-    float* forces;           // 3N input order
-    float* pots;             // N input order
+    const int* flags;        // the step's 4 flags (device), copied to sc->out_flags when that is set
     double* partials;        // per block: 0.5 * sum q * pot as an FP32 pair (hi, lo)
-    int* done = nullptr;     // zero at start: the last block sums the partials into *energy and re-zeroes it
+    int* done = nullptr;     // zero at start: the last block sums the partials into *sc->out_energy and re-zeroes it
     int* zero_after = nullptr;  // a counter of the step (the P2P queue) that the last block also re-zeroes
-    double* energy = nullptr;
 };
 void launch_finalize(const FinalArgs& a, cudaStream_t s);
 

@@ -144,6 +144,8 @@ struct gbfmm_handle {
     // host state
     std::vector<float> h_q;
     bool have_charges = false, have_result = false, results_on_host = false;
+    bool host_direct = false;       // the device reads pageable host memory: host calls work in place
+    bool results_in_place = false;  // the last step wrote its results into the pinned host buffers
     int verbose = 0;
     // device arena
     void* arena = nullptr;
@@ -758,12 +760,10 @@ static void enqueue_final(gbfmm_handle* h)
         fa.near = h->d_near;
         fa.far = h->d_far;
         fa.fconst = h->d_fconst;
-        fa.forces = h->d_forces;
-        fa.pots = h->d_pots;
+        fa.flags = h->d_flags;
         fa.partials = h->d_partials;
         fa.done = sync + 1;
         fa.zero_after = sync + 2;
-        fa.energy = h->d_energy;
         launch_finalize(fa, s);
     } else {
         cudaMemsetAsync(h->d_energy, 0, sizeof(double), s);
@@ -798,6 +798,14 @@ extern "C" int gbfmm_create(const gbfmm_params* prm, int natoms, gbfmm_handle** 
     }
     gbfmm_handle* h = new gbfmm_handle();
     h->prm = p;
+    {
+        int pageable = 0;
+        if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) {
+            cudaGetLastError();
+            pageable = 0;
+        }
+        h->host_direct = pageable != 0 && !(p.flags & GBFMM_FLAG_HOST_COPY);
+    }
     h->n = natoms;
     h->P = p.order;
     h->R = nreal(p.order);
@@ -920,7 +928,9 @@ extern "C" int gbfmm_set_charges(gbfmm_handle* h, int natoms, const float* q)
 // Fills the box-dependent step constants.  Cubic boxes only: the reference takes
 // the period from box[XX][XX] and the root half-width as its half
 // (zeta_fmm_solver.cpp:38-40).
-static int set_box(gbfmm_handle* h, const float* box, const float* d_coords)
+// host_out: the finalize writes the results into the handle's pinned host
+// buffers (a host call whose coordinates the device reads in place).
+static int set_box(gbfmm_handle* h, const float* box, const float* d_coords, bool host_out = false)
 {
     if (!box) return fail(GBFMM_ERR_ARG, "box is NULL");
     for (int i = 0; i < 9; i++)
@@ -936,6 +946,10 @@ static int set_box(gbfmm_handle* h, const float* box, const float* d_coords)
     if (h->ev_sc) cudaEventSynchronize(h->ev_sc);
     StepConst* sc = h->h_sc;
     sc->coords = d_coords;
+    sc->out_forces = host_out ? h->h_forces : h->d_forces;
+    sc->out_pots = host_out ? h->h_pots : h->d_pots;
+    sc->out_energy = host_out ? h->h_energy : h->d_energy;
+    sc->out_flags = host_out ? h->h_flags : nullptr;
     sc->inv_h = (float)(nd / L);
     sc->coef = 4.0 * M_PI / (3.0 * L * L * L);
     sc->box_len = L;
@@ -996,6 +1010,7 @@ static int run_step(gbfmm_handle* h, cudaStream_t launch = nullptr, bool on_laun
     }
     h->have_result = true;
     h->results_on_host = false;
+    h->results_in_place = false;
     return GBFMM_OK;
 }
 
@@ -1034,10 +1049,12 @@ static int fetch(gbfmm_handle* h)
     if (!h->have_result) return fail(GBFMM_ERR_STATE, "no result: call gbfmm_execute first");
     if (h->results_on_host) return GBFMM_OK;
     const int n = h->n;
-    CK(cudaMemcpyAsync(h->h_forces, h->d_forces, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, h->stream));
-    CK(cudaMemcpyAsync(h->h_pots, h->d_pots, sizeof(float) * n, cudaMemcpyDeviceToHost, h->stream));
-    CK(cudaMemcpyAsync(h->h_energy, h->d_energy, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-    CK(cudaMemcpyAsync(h->h_flags, h->d_flags, sizeof(int) * 4, cudaMemcpyDeviceToHost, h->stream));
+    if (!h->results_in_place) {
+        CK(cudaMemcpyAsync(h->h_forces, h->d_forces, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaMemcpyAsync(h->h_pots, h->d_pots, sizeof(float) * n, cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaMemcpyAsync(h->h_energy, h->d_energy, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaMemcpyAsync(h->h_flags, h->d_flags, sizeof(int) * 4, cudaMemcpyDeviceToHost, h->stream));
+    }
     CK(cudaStreamSynchronize(h->stream));
     if (h->timing) {
         h->n_stage = 9;
@@ -1065,11 +1082,17 @@ extern "C" int gbfmm_execute(gbfmm_handle* h, const float* coords, const float* 
     if (!h->have_charges) return fail(GBFMM_ERR_STATE, "charges not set");
     if (h->n > 0 && !coords) return fail(GBFMM_ERR_ARG, "coordinates are NULL");
     h->verbose = verbose;
-    int rc = set_box(h, box, h->d_coords);
+    // Where the device reaches pageable host memory (NVLink-C2C on GB300), the
+    // step reads the caller's coordinates in place and the finalize writes the
+    // results into the pinned host buffers: no staging copies either way.
+    const bool in_place = h->host_direct && h->n > 0;
+    int rc = set_box(h, box, in_place ? coords : h->d_coords, in_place);
     if (rc) return rc;
-    CK(cudaMemcpyAsync(h->d_coords, coords, sizeof(float) * 3 * h->n, cudaMemcpyHostToDevice, h->stream));
+    if (!in_place)
+        CK(cudaMemcpyAsync(h->d_coords, coords, sizeof(float) * 3 * h->n, cudaMemcpyHostToDevice, h->stream));
     rc = run_step(h);
     if (rc) return rc;
+    h->results_in_place = in_place;
     rc = fetch(h);
     if (rc == GBFMM_OK && verbose)
         std::printf("[gbfmm] natoms=%d P=%d depth=%d images=%d energy=%.8f\n", h->n, h->P, h->D, h->prm.images,

@@ -60,6 +60,8 @@ typedef struct gbfmm_params {
 
 #define GBFMM_FLAG_NO_GRAPH 1        /* launch the step kernel by kernel instead of replaying a CUDA graph */
 #define GBFMM_FLAG_DETERMINISTIC 2   /* no floating-point atomics in M2L (m2l_split forced to 1) */
+#define GBFMM_FLAG_HOST_COPY 4       /* gbfmm_execute copies through device buffers even where the device
+                                        reads pageable host memory (default there: in place, no copies) */
 
 typedef struct gbfmm_handle gbfmm_handle;
 
@@ -81,7 +83,11 @@ int gbfmm_set_charges(gbfmm_handle* h, int natoms, const float* charges);
 /* BaseSolver::execute (basesolver.h:67; zeta_fmm_solver.cpp:16-64): host
  * coordinates (float[3*natoms], nm) and the box (float[9], row-major 3x3, nm;
  * must be cubic: the reference uses box[XX][XX] as the period).  Synchronous,
- * like the reference: results are on the host when it returns. */
+ * like the reference: results are on the host when it returns.  On a device
+ * that reads pageable host memory coherently (GB300 over NVLink-C2C) the step
+ * reads 'coords' in place and writes the results straight into the handle's
+ * pinned host buffers, with no staging copies (GBFMM_FLAG_HOST_COPY turns this
+ * off); elsewhere the coordinates and results are copied. */
 int gbfmm_execute(gbfmm_handle* h, const float* coords, const float* box, int verbose);
 
 /* Device-resident execute: d_coords float[3*natoms] on the device, results left
@@ -89,7 +95,8 @@ int gbfmm_execute(gbfmm_handle* h, const float* coords, const float* box, int ve
  * (cudaStream_t, NULL = default stream). */
 int gbfmm_execute_device(gbfmm_handle* h, const void* d_coords, const float* box, void* stream);
 
-/* Device pointers of the last results, in input atom order: forces float[3*natoms]
+/* Device pointers of the results of the last gbfmm_execute_device (and of a
+ * gbfmm_execute that copied), in input atom order: forces float[3*natoms]
  * (kJ/mol/nm), potentials float[natoms] (kJ/mol/e), energy double[1] (kJ/mol). */
 int gbfmm_device_outputs(gbfmm_handle* h, void** d_forces, void** d_potentials, void** d_energy);
 

@@ -186,6 +186,25 @@ def test_device_execute_is_ordered_on_the_callers_stream(pkg, systems):
     s.close()
 
 
+def test_host_call_in_place_matches_copies(pkg, systems):
+    """gbfmm_execute reads the host coordinates and writes the host results in
+    place where the device reaches pageable memory (GB300 over NVLink-C2C), and
+    copies through device buffers with GBFMM_FLAG_HOST_COPY: the results are
+    the same bit for bit, on repeated calls."""
+    xyz, q, box = systems.water_ion_box(3000, 3.0, n_na=4, n_cl=4, seed=31)
+    out = []
+    for flags in (pkg.FLAG_DETERMINISTIC, pkg.FLAG_DETERMINISTIC | pkg.FLAG_HOST_COPY):
+        s = pkg.ZetaFmmSolver(len(q), q, order=6, max_depth=3, images=4, flags=flags)
+        res = []
+        for k in range(2):
+            s.execute(xyz if k else xyz * np.float32(1.01), box)
+            res.append((s.forces(), s.potentials(), s.get_energy()))
+        out.append(res[1])
+        s.close()
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    assert out[0][2] == out[1][2]
+
+
 def test_deterministic_flag_is_bitwise_repeatable(pkg, systems):
     xyz, q, box = systems.water_ion_box(2000, 2.8, seed=13)
     s = pkg.ZetaFmmSolver(len(q), q, order=8, max_depth=3, images=4, flags=pkg.FLAG_DETERMINISTIC)
