@@ -293,6 +293,12 @@ class BatchSolver:
         L.gbfmm_batch_device_outputs.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp)]
         L.gbfmm_batch_destroy.restype = ctypes.c_int
         L.gbfmm_batch_destroy.argtypes = [vp]
+        L.gbfmm_batch_autotune.restype = ctypes.c_int
+        L.gbfmm_batch_autotune.argtypes = [vp, vp, vp, fp, ctypes.c_int, fp]
+        L.gbfmm_batch_get_tuning.restype = ctypes.c_int
+        L.gbfmm_batch_get_tuning.argtypes = [vp, ip, ip, ip, ip]
+        L.gbfmm_batch_set_tuning.restype = ctypes.c_int
+        L.gbfmm_batch_set_tuning.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         self.n_sys = len(natoms_list)
         self.offsets = np.concatenate([[0], np.cumsum(natoms_list)]).astype(np.int32)
         o = np.ascontiguousarray(orders, dtype=np.int32)
@@ -331,6 +337,25 @@ class BatchSolver:
         _check(lib().gbfmm_batch_execute_device(self._b, ctypes.c_void_p(int(coords_ptr)),
                                                 ctypes.c_void_p(int(charges_ptr)), _fp(b),
                                                 ctypes.c_void_p(int(stream_ptr))))
+
+    def tuning(self):
+        v = [ctypes.c_int() for _ in range(4)]
+        _check(lib().gbfmm_batch_get_tuning(self._b, *[ctypes.byref(x) for x in v]))
+        return {"p2p_shape": v[0].value, "p2p_per_sm": v[1].value, "m2l_split": v[2].value,
+                "m2l_stages": v[3].value}
+
+    def set_tuning(self, p2p_shape=0, p2p_per_sm=4, m2l_split=0, m2l_stages=0):
+        _check(lib().gbfmm_batch_set_tuning(self._b, int(p2p_shape), int(p2p_per_sm), int(m2l_split),
+                                            int(m2l_stages)))
+
+    def autotune(self, coords_ptr, charges_ptr, box_edges, reps=3):
+        """Device inputs (as execute_device); keeps the fastest batch tuning and
+        returns it with its step time."""
+        b = _f32(box_edges)
+        ms = ctypes.c_float()
+        _check(lib().gbfmm_batch_autotune(self._b, ctypes.c_void_p(int(coords_ptr)), ctypes.c_void_p(int(charges_ptr)),
+                                          _fp(b), int(reps), ctypes.byref(ms)))
+        return dict(self.tuning(), ms=ms.value)
 
 
 def lists(max_depth, images, which):

@@ -916,7 +916,7 @@ __global__ void __launch_bounds__(P2P_THREADS) k_p2p_queue(const P2PArgs a, int*
 // Batched form: the leaves of many systems in one queue.  Item i belongs to the
 // system s with first[s] <= i < first[s+1] (systems ordered by work per leaf,
 // heaviest first, so that the queue ends with the light leaves).
-template <int LT>
+template <int LT, int KM = 3>
 __global__ void __launch_bounds__(P2P_THREADS) k_p2p_batch(const P2PBatchArgs b)
 {
     __shared__ P2PShared sh;
@@ -939,11 +939,13 @@ __global__ void __launch_bounds__(P2P_THREADS) k_p2p_batch(const P2PBatchArgs b)
             leaf = item - b.first[lo];
         }
         __syncthreads();
-        p2p_leaf<LT>(cur, (uint32_t)leaf, sh);
+        p2p_leaf<LT, KM>(cur, (uint32_t)leaf, sh);
         __syncthreads();
         item = next;
     }
 }
+
+int p2p_batch_shapes() { return 5; }
 
 void launch_p2p_batch(const P2PBatchArgs& b, int shape, int per_sm, cudaStream_t s)
 {
@@ -954,6 +956,8 @@ void launch_p2p_batch(const P2PBatchArgs& b, int shape, int per_sm, cudaStream_t
     COUNT_LAUNCH();
     if (shape == 1) k_p2p_batch<4><<<grid, P2P_THREADS, 0, s>>>(b);
     else if (shape == 2) k_p2p_batch<16><<<grid, P2P_THREADS, 0, s>>>(b);
+    else if (shape == 3) k_p2p_batch<8, 4><<<grid, P2P_THREADS, 0, s>>>(b);
+    else if (shape == 4) k_p2p_batch<4, 4><<<grid, P2P_THREADS, 0, s>>>(b);
     else k_p2p_batch<8><<<grid, P2P_THREADS, 0, s>>>(b);
 }
 

@@ -1418,6 +1418,8 @@ struct gbfmm_batch {
     // the systems' near fields in one persistent kernel
     void* p2p_buf = nullptr;  // P2PArgs[n_sys], first[n_sys+1], counter
     P2PBatchArgs p2p{};
+    int p2p_shape = 0, p2p_per_sm = 4;  // near-field kernel shape and CTAs per SM (batch autotuner)
+    int m2l_split_v = -1, m2l_stages = 0;  // batch-wide M2L tuning of the tensor-core systems (-1 / 0: their own)
     cudaStream_t near_stream = nullptr;
     std::vector<cudaEvent_t> ev_tree;
     cudaEvent_t ev_near = nullptr;
@@ -1589,7 +1591,7 @@ static int batch_capture(gbfmm_batch* b)
     CK(cudaStreamWaitEvent(b->near_stream, b->ein, 0));
     CK(cudaMemsetAsync(b->p2p.counter, 0, sizeof(int), b->near_stream));
     for (int k = 0; k < b->n_sys; k++) CK(cudaStreamWaitEvent(b->near_stream, b->ev_tree[k], 0));
-    launch_p2p_batch(b->p2p, 0, 4, b->near_stream);
+    launch_p2p_batch(b->p2p, b->p2p_shape, b->p2p_per_sm, b->near_stream);
     CK(cudaEventRecord(b->ev_near, b->near_stream));
     // 3) every system's forces, potentials and energy
     for (int w = 0; w < nw; w++) CK(cudaStreamWaitEvent(b->workers[w], b->ev_near, 0));
@@ -1639,6 +1641,118 @@ extern "C" int gbfmm_batch_execute_device(gbfmm_batch* b, const void* d_coords, 
     CK(cudaEventRecord(b->eout, b->master));
     CK(cudaStreamWaitEvent(us, b->eout, 0));
     b->have_result = true;
+    return GBFMM_OK;
+}
+
+// ---- batch autotuner: the near-field kernel's warp-step shape and CTAs per SM
+// and, for the tensor-core systems, a batch-wide M2L entry split and pipeline
+// depth, chosen by timing replays of the batch graph on the caller's inputs.
+
+static int apply_batch_tuning(gbfmm_batch* b, int shape, int per_sm, int split_v, int nstage)
+{
+    if (shape < 0 || shape >= p2p_batch_shapes()) return fail(GBFMM_ERR_ARG, "batch p2p shape %d", shape);
+    if (per_sm < 1 || per_sm > 5) return fail(GBFMM_ERR_ARG, "batch p2p CTAs per SM %d outside [1,5]", per_sm);
+    if (split_v >= TC_NSPLIT) return fail(GBFMM_ERR_ARG, "m2l split");
+    for (gbfmm_handle* h : b->hs)
+        if (h->tc && split_v >= 0 && h->tc_ntask_v[split_v] == 0)
+            return fail(GBFMM_ERR_ARG, "m2l split %d unavailable (deterministic batch)", 1 << split_v);
+    if (nstage < 0) return fail(GBFMM_ERR_ARG, "m2l stages %d", nstage);
+    if (b->gexec) CK(cudaStreamSynchronize(b->master));
+    b->p2p_shape = shape;
+    b->p2p_per_sm = per_sm;
+    b->m2l_split_v = split_v;
+    b->m2l_stages = nstage;
+    for (gbfmm_handle* h : b->hs) {
+        if (!h->tc) continue;
+        if (split_v >= 0) h->tc_split_v = split_v;
+        if (nstage > 0) {
+            const TcPlan& pl = h->tab->tc;
+            h->tc_nstage = std::max(1, std::min(nstage, tc_max_stages(pl.k_atoms, pl.img_bytes, h->tca->nprod)));
+        }
+    }
+    if (b->gexec) {
+        cudaGraphExecDestroy(b->gexec);
+        b->gexec = nullptr;
+    }
+    return GBFMM_OK;
+}
+
+extern "C" int gbfmm_batch_set_tuning(gbfmm_batch* b, int p2p_shape, int p2p_per_sm, int m2l_split, int m2l_stages)
+{
+    if (!b) return fail(GBFMM_ERR_ARG, "batch is NULL");
+    int v = -1;
+    if (m2l_split != 0) {
+        v = 0;
+        while (v < TC_NSPLIT - 1 && (1 << v) < m2l_split) v++;
+        if (m2l_split < 1 || (1 << v) != m2l_split) return fail(GBFMM_ERR_ARG, "m2l split %d is not 0, 1, 2, 4 or 8", m2l_split);
+    }
+    return apply_batch_tuning(b, p2p_shape, p2p_per_sm, v, m2l_stages);
+}
+
+extern "C" int gbfmm_batch_get_tuning(gbfmm_batch* b, int* p2p_shape, int* p2p_per_sm, int* m2l_split, int* m2l_stages)
+{
+    if (!b) return fail(GBFMM_ERR_ARG, "batch is NULL");
+    if (p2p_shape) *p2p_shape = b->p2p_shape;
+    if (p2p_per_sm) *p2p_per_sm = b->p2p_per_sm;
+    if (m2l_split) *m2l_split = b->m2l_split_v >= 0 ? 1 << b->m2l_split_v : 0;
+    if (m2l_stages) *m2l_stages = b->m2l_stages;
+    return GBFMM_OK;
+}
+
+extern "C" int gbfmm_batch_autotune(gbfmm_batch* b, const void* d_coords, const void* d_charges,
+                                    const float* box_edges, int reps, float* best_ms)
+{
+    if (!b || !box_edges || (b->natoms > 0 && (!d_coords || !d_charges))) return fail(GBFMM_ERR_ARG, "NULL argument");
+    if (reps <= 0) reps = 3;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    int err = GBFMM_OK;
+    auto measure = [&](int sh, int ps, int sv, int ns) -> float {
+        if (apply_batch_tuning(b, sh, ps, sv, ns) != GBFMM_OK) return 1e30f;
+        for (int i = 0; i < 2 && err == GBFMM_OK; i++)
+            err = gbfmm_batch_execute_device(b, d_coords, d_charges, box_edges, b->master);
+        if (err) return 1e30f;
+        cudaEventRecord(e0, b->master);
+        for (int i = 0; i < reps && err == GBFMM_OK; i++)
+            err = gbfmm_batch_execute_device(b, d_coords, d_charges, box_edges, b->master);
+        cudaEventRecord(e1, b->master);
+        if (cudaEventSynchronize(e1) != cudaSuccess) err = GBFMM_ERR_CUDA;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        return err ? 1e30f : ms / reps;
+    };
+    int bs = b->p2p_shape, bp = b->p2p_per_sm, bv = b->m2l_split_v, bn = b->m2l_stages;
+    float bt = measure(bs, bp, bv, bn);
+    // coordinate search: near-field shape and CTAs per SM, then M2L split, then M2L depth
+    for (int sh = 0; sh < p2p_batch_shapes() && !err; sh++)
+        for (int ps = 2; ps <= 5 && !err; ps++) {
+            if (sh == bs && ps == bp) continue;
+            const float t = measure(sh, ps, bv, bn);
+            if (t < bt) { bt = t; bs = sh; bp = ps; }
+        }
+    bool any_tc = false;
+    for (gbfmm_handle* h : b->hs) any_tc |= h->tc;
+    if (any_tc) {
+        for (int sv = 0; sv < TC_NSPLIT && !err; sv++) {
+            bool ok = sv != bv;
+            for (gbfmm_handle* h : b->hs) ok &= !h->tc || h->tc_ntask_v[sv] > 0;
+            if (!ok) continue;
+            const float t = measure(bs, bp, sv, bn);
+            if (t < bt) { bt = t; bv = sv; }
+        }
+        for (int ns = 1; ns <= 4 && !err; ns++) {
+            if (ns == bn) continue;
+            const float t = measure(bs, bp, bv, ns);
+            if (t < bt) { bt = t; bn = ns; }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (err) return err;
+    const int rc = apply_batch_tuning(b, bs, bp, bv, bn);
+    if (rc) return rc;
+    if (best_ms) *best_ms = bt;
     return GBFMM_OK;
 }
 

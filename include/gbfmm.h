@@ -249,6 +249,21 @@ int gbfmm_batch_execute_device(gbfmm_batch* b, const void* d_coords, const void*
 int gbfmm_batch_device_outputs(gbfmm_batch* b, void** d_forces, void** d_potentials, void** d_energies);
 int gbfmm_batch_destroy(gbfmm_batch* b);
 
+/* Batch autotuner: times replays of the batch graph on the caller's device
+ * inputs (as gbfmm_batch_execute_device) for the near-field kernel's warp-step
+ * shape (0: 8 targets x 4 source lanes, 1: 4 x 8, 2: 16 x 2, 3 and 4: 8 x 4 and
+ * 4 x 8 with up to 4 targets per thread) and CTAs per SM (2..5), then, when
+ * any system uses the tensor-core M2L, a batch-wide M2L entry split (1, 2, 4,
+ * 8) and pipeline depth, and keeps the fastest (best_ms: its step time).
+ * m2l_split / m2l_stages 0 in get/set mean each system's own.  Results are the
+ * same up to the order of floating-point additions.  No reference counterpart:
+ * the reference solves one system per call with fixed launch shapes
+ * (gpu_solver.cu:221-248). */
+int gbfmm_batch_autotune(gbfmm_batch* b, const void* d_coords, const void* d_charges, const float* box_edges,
+                         int reps, float* best_ms);
+int gbfmm_batch_get_tuning(gbfmm_batch* b, int* p2p_shape, int* p2p_per_sm, int* m2l_split, int* m2l_stages);
+int gbfmm_batch_set_tuning(gbfmm_batch* b, int p2p_shape, int p2p_per_sm, int m2l_split, int m2l_stages);
+
 #ifdef __cplusplus
 }
 #endif

@@ -76,3 +76,64 @@ def test_batch_device_path_follows_new_coordinates(pkg, systems):
     assert rel_rms(f1, f2) > 1e-3  # the new coordinates were used
     s.close()
     b.close()
+
+
+def _batch_inputs(pkg, systems, precision, flags=0):
+    sy = _systems(systems)
+    b = pkg.BatchSolver([len(s[1]) for s in sy], [s[3] for s in sy], [s[4] for s in sy], images=4,
+                        precision=precision, flags=flags)
+    X = np.concatenate([s[0] for s in sy])
+    Q = np.concatenate([s[1] for s in sy])
+    B = np.array([s[2] for s in sy], np.float32)
+    return b, X, Q, B
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_batch_every_tuning_matches(pkg, systems, precision):
+    """Every near-field shape and CTA count of the batch kernel, and every M2L
+    split and depth, give the same forces up to the order of the additions."""
+    b, X, Q, B = _batch_inputs(pkg, systems, precision)
+    f0, p0, _ = b.execute(X, Q, B)
+    for shape in range(5):
+        for per_sm in (2, 5):
+            b.set_tuning(shape, per_sm, 0, 0)
+            f, p, _ = b.execute(X, Q, B)
+            assert rel_rms(f, f0) < 1e-5, (shape, per_sm)
+            assert rel_rms(p, p0) < 1e-5, (shape, per_sm)
+    if precision:
+        for split in (1, 2, 4, 8):
+            for stages in (1, 2):
+                b.set_tuning(0, 4, split, stages)
+                f, _, _ = b.execute(X, Q, B)
+                assert rel_rms(f, f0) < 1e-5, (split, stages)
+    with pytest.raises(pkg.FmmError):
+        b.set_tuning(5, 4, 0, 0)
+    b.close()
+
+
+def test_batch_autotune_keeps_a_valid_tuning(pkg, systems):
+    torch = pytest.importorskip("torch")
+    b, X, Q, B = _batch_inputs(pkg, systems, 1)
+    f0, _, e0 = b.execute(X, Q, B)
+    xd = torch.from_numpy(X).cuda()
+    qd = torch.from_numpy(Q).cuda()
+    t = b.autotune(xd.data_ptr(), qd.data_ptr(), B, reps=2)
+    assert t["ms"] > 0 and 0 <= t["p2p_shape"] < 5 and 1 <= t["p2p_per_sm"] <= 5
+    assert t["m2l_split"] in (0, 1, 2, 4, 8)
+    f1, _, e1 = b.execute(X, Q, B)
+    assert rel_rms(f1, f0) < 1e-5
+    assert np.allclose(e1, e0, rtol=1e-5, atol=0)
+    b.close()
+
+
+def test_deterministic_batch_keeps_whole_m2l_tiles(pkg, systems):
+    b, X, Q, B = _batch_inputs(pkg, systems, 1, flags=pkg.FLAG_DETERMINISTIC)
+    with pytest.raises(pkg.FmmError):
+        b.set_tuning(0, 4, 2, 0)
+    f1, _, _ = b.execute(X, Q, B)
+    b.set_tuning(3, 3, 1, 2)
+    f2, _, _ = b.execute(X, Q, B)
+    f3, _, _ = b.execute(X, Q, B)
+    assert np.array_equal(f2, f3)
+    assert rel_rms(f2, f1) < 1e-5
+    b.close()
