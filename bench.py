@@ -416,15 +416,23 @@ def frames_line(pkg, torch, dev, systems, tuner_mod, n_frames):
 
 def batch_line(pkg, torch, dev, systems, steps, warmup):
     """64 independent systems (atom counts log-uniform in [2,000, 200,000], water +
-    0.15 M NaCl, one cubic box each; order 6, BF16X3, depth for 16-128 bodies per
-    leaf): one batched CUDA graph (gbfmm_batch_*, near fields in one persistent
-    kernel) against the same systems solved one after another, device-resident,
-    L2 flushed before every step."""
+    0.15 M NaCl, one cubic box each), solved in one batched CUDA graph
+    (gbfmm_batch_*, near fields in one persistent kernel, tiles from
+    gbfmm_batch_autotune), device-resident, L2 flushed before every step:
+      value  each system's own order drawn (seeded) from 6..10 and its depth in
+             3..5 (16-128 bodies per leaf where that range allows), BF16X3;
+      tuned  each system's order and depth proposed by the learned tuner for the
+             1e-3 tolerance (each proposal checked against the plain order-10
+             FMM), one batch-wide precision (BF16X3 if any system asks for more
+             than BF16X1); every system's batched forces are checked against its
+             plain FMM again.
+    Each is compared with the same systems solved one after another (one graph
+    per system), and each system's own step time is reported (tuned)."""
     tuner_mod = G.load_module("tuner")
     sy = systems.batch_systems(n_sys=64)
     nat = [len(s[1]) for s in sy]
-    P, prec = 6, 1
-    depths = [tuner_mod.plain_depth(n) for n in nat]
+    off = np.concatenate([[0], np.cumsum(nat)])
+    n = int(off[-1])
     X = np.concatenate([s[0] for s in sy]).astype(np.float32)
     Q = np.concatenate([s[1] for s in sy]).astype(np.float32)
     B = np.array([float(s[2][0]) for s in sy], np.float32)
@@ -433,12 +441,12 @@ def batch_line(pkg, torch, dev, systems, steps, warmup):
     st = torch.cuda.current_stream(dev)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
 
-    def timed(fn):
+    def timed(fn, nsteps=steps):
         for _ in range(warmup):
             fn()
         torch.cuda.synchronize()
         tot = 0.0
-        for _ in range(steps):
+        for _ in range(nsteps):
             flush.zero_()
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
@@ -447,36 +455,69 @@ def batch_line(pkg, torch, dev, systems, steps, warmup):
             e1.record(st)
             e1.synchronize()
             tot += e0.elapsed_time(e1)
-        return tot / steps
+        return tot / nsteps
 
-    b = pkg.BatchSolver(nat, [P] * len(nat), depths, images=4, precision=prec)
-    b.execute(X, Q, B)  # captures the graph
-    ms_default = timed(lambda: b.execute_device(xd.data_ptr(), qd.data_ptr(), B, st.cuda_stream))
-    tiles = b.autotune(xd.data_ptr(), qd.data_ptr(), B, reps=2)  # gbfmm_batch_autotune
-    b.execute(X, Q, B)  # captures the tuned graph
-    ms_batch = timed(lambda: b.execute_device(xd.data_ptr(), qd.data_ptr(), B, st.cuda_stream))
-    b.close()
-    off = np.concatenate([[0], np.cumsum(nat)])
-    singles = []
+    def run_batch(orders, depths, prec):
+        b = pkg.BatchSolver(nat, orders, depths, images=4, precision=prec)
+        f, _, _ = b.execute(X, Q, B)  # captures the graph
+        ms_default = timed(lambda: b.execute_device(xd.data_ptr(), qd.data_ptr(), B, st.cuda_stream))
+        tiles = b.autotune(xd.data_ptr(), qd.data_ptr(), B, reps=2)  # gbfmm_batch_autotune
+        b.execute(X, Q, B)  # captures the tuned graph
+        ms = timed(lambda: b.execute_device(xd.data_ptr(), qd.data_ptr(), B, st.cuda_stream))
+        b.close()
+        singles = []
+        for i, (xyz, q, box) in enumerate(sy):
+            s = pkg.ZetaFmmSolver(len(q), q, order=orders[i], max_depth=depths[i], images=4, precision=prec)
+            s.execute(xyz, float(box[0]))
+            singles.append(s)
+
+        def seq():
+            for i, s in enumerate(singles):
+                s.execute_device(xd.data_ptr() + 12 * int(off[i]), float(B[i]), st.cuda_stream)
+
+        ms_seq = timed(seq)
+        per = [timed(lambda s=s, i=i: s.execute_device(xd.data_ptr() + 12 * int(off[i]), float(B[i]),
+                                                       st.cuda_stream), 3) for i, s in enumerate(singles)]
+        for s in singles:
+            s.close()
+        return f, {"value": n / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "tile_autotune": tiles,
+                   "ms_per_step_default_tiles": ms_default, "precision": PREC_NAME[prec],
+                   "sequential_single_solves": {"value": n / (ms_seq * 1e-3), "ms_per_step": ms_seq},
+                   "speedup_vs_sequential": ms_seq / ms}, per
+
+    rng = np.random.default_rng(64)
+    spec_orders = [int(v) for v in rng.integers(6, 11, size=len(nat))]
+    spec_depths = [min(5, max(3, tuner_mod.plain_depth(k))) for k in nat]
+    _, spec, spec_per = run_batch(spec_orders, spec_depths, 1)
+    spec.update(orders=sorted(set(spec_orders)), depths=sorted(set(spec_depths)),
+                per_system_ms={"min": min(spec_per), "median": float(np.median(spec_per)), "max": max(spec_per)})
+    # the tuner's proposal per system (statistics and MLP on the device, checked)
+    mlp = tuner_mod.Mlp.load()
+    props = []
+    for xyz, q, box in sy:
+        ts = tuner_mod.TunedSolver(q, mlp, tol=TOL)
+        props.append(ts.propose(xyz, float(box[0])))
+        ts.solver.close()
+    mlp.close()
+    orders = [p[0] for p in props]
+    depths = [p[1] for p in props]
+    prec = 2 if all(p[2] == 2 for p in props) else 1
+    f, tuned, per = run_batch(orders, depths, prec)
+    diffs = []
     for i, (xyz, q, box) in enumerate(sy):
-        s = pkg.ZetaFmmSolver(len(q), q, order=P, max_depth=depths[i], images=4, precision=prec)
-        s.execute(xyz, float(box[0]))
-        singles.append(s)
-
-    def seq():
-        for i, s in enumerate(singles):
-            s.execute_device(xd.data_ptr() + 12 * int(off[i]), float(B[i]), st.cuda_stream)
-
-    ms_seq = timed(seq)
-    for s in singles:
-        s.close()
-    n = int(off[-1])
-    return {"workload": f"64 systems, {n} atoms (log-uniform 2,000-200,000 per system), order {P}, "
-                        f"{PREC_NAME[prec]}, depth for 16-128 bodies per leaf",
-            "atoms": n, "value": n / (ms_batch * 1e-3), "unit": UNIT, "ms_per_step": ms_batch,
-            "tile_autotune": tiles, "ms_per_step_default_tiles": ms_default,
-            "sequential_single_solves": {"value": n / (ms_seq * 1e-3), "ms_per_step": ms_seq},
-            "speedup_vs_sequential": ms_seq / ms_batch}
+        pl = pkg.ZetaFmmSolver(len(q), q, order=10, max_depth=tuner_mod.plain_depth(len(q)), images=4)
+        pl.execute(xyz, float(box[0]))
+        diffs.append(rel_diff(f[off[i]:off[i + 1]], pl.forces()))
+        pl.close()
+    tuned.update(orders=sorted(set(orders)), depths=sorted(set(depths)),
+                 max_rel_force_diff_vs_plain=max(diffs), systems_over_tolerance=int(sum(d > TOL for d in diffs)),
+                 per_system_ms={"min": min(per), "median": float(np.median(per)), "max": max(per)},
+                 per_system=[{"atoms": nat[i], "order": orders[i], "depth": depths[i], "ms": per[i],
+                              "rel_force_diff_vs_plain": diffs[i]} for i in range(len(sy))])
+    return {"workload": f"64 systems, {n} atoms (log-uniform 2,000-200,000 per system), 0.15 M NaCl, "
+                        "order 6-10 and depth 3-5 per system, bf16x3",
+            "atoms": n, "value": spec["value"], "unit": UNIT, "ms_per_step": spec["ms_per_step"],
+            "spec": spec, "tuned": tuned}
 
 
 def main():
@@ -543,15 +584,21 @@ def main():
     pkg.lib()
     run = Runner(pkg, torch, dev, xyz, q, box)
 
-    # FP64 Ewald forces on sampled atoms: the accuracy judge of every candidate
+    # FP64 Ewald forces on sampled atoms and the total energy: the accuracy judge
+    # of every candidate (OpenMP on the host cores)
     from oracle import oracle as O
+    O.set_threads(os.cpu_count() or 1)
     tg = np.arange(0, n, 191)
     _, fe, _ = O.ewald(xyz.astype(np.float64), q.astype(np.float64), box[0], eps=1e-9, targets=tg)
+    _, _, ee = O.ewald(xyz.astype(np.float64), q.astype(np.float64), box[0], eps=1e-7, energy=True)
 
     def err_of(s):
         s.execute(xyz, box)
         f = s.forces()
         return float(np.sqrt(np.sum((f[tg] - fe) ** 2) / np.sum(fe ** 2)))
+
+    def energy_err(s):
+        return abs(s.get_energy() - ee) / abs(ee)  # after err_of's execute
 
     # tuned parameters: the learned tuner's proposal for this system (statistics
     # on the device, MLP forward on the device), checked against the plain
@@ -575,8 +622,10 @@ def main():
     for prec, P, D in CANDIDATES:
         s = run.solver(prec, P, D)
         e = err_of(s)
+        ee_rel = energy_err(s)
         ms = run.time_device(s, 5, 3) / 5
-        tune.append({"precision": PREC_NAME[prec], "order": P, "depth": D, "rel_force_err": e, "ms": ms})
+        tune.append({"precision": PREC_NAME[prec], "order": P, "depth": D, "rel_force_err": e,
+                     "rel_energy_err": ee_rel, "ms": ms})
         s.close()
 
     results = {}
@@ -590,6 +639,7 @@ def main():
         value, ms = replica_throughput(n, args.steps, ms, dist if ws > 1 else None, dev)
         r = {"prec": prec, "P": P, "D": D, "ms": ms / args.steps, "value": value,
              "err": err_of(s), "clocks": clk.summary()}
+        r["eerr"] = energy_err(s)
         r["e2e"] = n * ws * args.steps / run.time_e2e(s, args.steps)
         # the same call with staging copies (GBFMM_FLAG_HOST_COPY), for comparison
         sc = run.solver(prec, P, D, flags=pkg.FLAG_HOST_COPY)
@@ -641,7 +691,9 @@ def main():
             "vs_baseline": None, "dtype": "f32+bf16x3" if tuned["prec"] == 1 else (
                 "f32+bf16" if tuned["prec"] == 2 else "f32"), "data": "synthetic",
             "config": dict(config, order=P, depth=D, precision=PREC_NAME[tuned["prec"]]),
-            "rel_force_err_vs_ewald": tuned["err"],
+            "rel_force_err_vs_ewald": tuned["err"], "rel_energy_err_vs_ewald": tuned["eerr"],
+            "ewald": "FP64 Ewald (oracle/ewald64.c): forces on every 191st atom (eps 1e-9), total energy "
+                     "(eps 1e-7)",
             "e2e": {"value": tuned["e2e"], "unit": UNIT, "h2d_bytes_per_step": 12 * n,
                     "d2h_bytes_per_step": 12 * n + 4 * n + 8,
                     "host_io": ("in place: the step reads the host coordinates and writes the host results "
@@ -649,7 +701,8 @@ def main():
                     if pageable_access(local) else "staging copies (cudaMemcpyAsync)",
                     "value_with_copies": tuned["e2e_copies"]},
             "plain_fp32": {"value": plain["value"], "ms_per_step": plain["ms"], "order": plain["P"],
-                           "depth": plain["D"], "rel_force_err_vs_ewald": plain["err"], "e2e": plain["e2e"],
+                           "depth": plain["D"], "rel_force_err_vs_ewald": plain["err"],
+                           "rel_energy_err_vs_ewald": plain["eerr"], "e2e": plain["e2e"],
                            "stage_ms": plain["stages"]},
             "speedup_tuned_vs_plain": tuned["value"] / plain["value"],
             "tuner": tuner_info, "tile_autotune": {"tuned": tuned["tiles"], "plain": plain["tiles"]},
