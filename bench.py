@@ -307,15 +307,24 @@ class Runner:
         return float(sum(a.elapsed_time(b) for a, b in zip(ev0, ev1)))
 
     def time_e2e(self, s, steps):
+        """Host wall time of `steps` calls of the C ABI's gbfmm_execute, as the
+        mdrun adapter makes them (host coordinates in; forces, potentials and
+        energy on the host when it returns), L2 flushed before each call."""
         for _ in range(2):
             s.execute(self.xyz, self.box)
+        x = np.ascontiguousarray(self.xyz, dtype=np.float32)
+        m = self.pkg.box_matrix(self.box)
+        fn, h = self.pkg.lib().gbfmm_execute, s._h
+        xp, mp = self.pkg._fp(x), self.pkg._fp(m)
         tot = 0.0
         for _ in range(steps):
             self.flush.zero_()
             self.torch.cuda.synchronize()
             t0 = time.perf_counter()
-            s.execute(self.xyz, self.box)
+            rc = fn(h, xp, mp, 0)
             tot += time.perf_counter() - t0
+            if rc != 0:
+                raise RuntimeError(f"gbfmm_execute returned {rc}")
         return tot
 
     def stages(self, s, steps):
@@ -423,9 +432,9 @@ def batch_line(pkg, torch, dev, systems, steps, warmup):
              3..5 (16-128 bodies per leaf where that range allows), BF16X3;
       tuned  each system's order and depth proposed by the learned tuner for the
              1e-3 tolerance (each proposal checked against the plain order-10
-             FMM), one batch-wide precision (BF16X3 if any system asks for more
-             than BF16X1); every system's batched forces are checked against its
-             plain FMM again.
+             FMM), each with its own precision (gbfmm_batch_create_mixed);
+             every system's batched forces are checked against its plain FMM
+             again.
     Each is compared with the same systems solved one after another (one graph
     per system), and each system's own step time is reported (tuned)."""
     tuner_mod = G.load_module("tuner")
@@ -467,7 +476,8 @@ def batch_line(pkg, torch, dev, systems, steps, warmup):
         b.close()
         singles = []
         for i, (xyz, q, box) in enumerate(sy):
-            s = pkg.ZetaFmmSolver(len(q), q, order=orders[i], max_depth=depths[i], images=4, precision=prec)
+            s = pkg.ZetaFmmSolver(len(q), q, order=orders[i], max_depth=depths[i], images=4,
+                                  precision=prec[i] if isinstance(prec, list) else prec)
             s.execute(xyz, float(box[0]))
             singles.append(s)
 
@@ -480,8 +490,9 @@ def batch_line(pkg, torch, dev, systems, steps, warmup):
                                                        st.cuda_stream), 3) for i, s in enumerate(singles)]
         for s in singles:
             s.close()
+        pn = sorted({PREC_NAME[v] for v in prec}) if isinstance(prec, list) else PREC_NAME[prec]
         return f, {"value": n / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "tile_autotune": tiles,
-                   "ms_per_step_default_tiles": ms_default, "precision": PREC_NAME[prec],
+                   "ms_per_step_default_tiles": ms_default, "precision": pn,
                    "sequential_single_solves": {"value": n / (ms_seq * 1e-3), "ms_per_step": ms_seq},
                    "speedup_vs_sequential": ms_seq / ms}, per
 
@@ -501,8 +512,8 @@ def batch_line(pkg, torch, dev, systems, steps, warmup):
     mlp.close()
     orders = [p[0] for p in props]
     depths = [p[1] for p in props]
-    prec = 2 if all(p[2] == 2 for p in props) else 1
-    f, tuned, per = run_batch(orders, depths, prec)
+    precs = [p[2] for p in props]
+    f, tuned, per = run_batch(orders, depths, precs)
     diffs = []
     for i, (xyz, q, box) in enumerate(sy):
         pl = pkg.ZetaFmmSolver(len(q), q, order=10, max_depth=tuner_mod.plain_depth(len(q)), images=4)
@@ -512,7 +523,8 @@ def batch_line(pkg, torch, dev, systems, steps, warmup):
     tuned.update(orders=sorted(set(orders)), depths=sorted(set(depths)),
                  max_rel_force_diff_vs_plain=max(diffs), systems_over_tolerance=int(sum(d > TOL for d in diffs)),
                  per_system_ms={"min": min(per), "median": float(np.median(per)), "max": max(per)},
-                 per_system=[{"atoms": nat[i], "order": orders[i], "depth": depths[i], "ms": per[i],
+                 per_system=[{"atoms": nat[i], "order": orders[i], "depth": depths[i],
+                              "precision": PREC_NAME[precs[i]], "ms": per[i],
                               "rel_force_diff_vs_plain": diffs[i]} for i in range(len(sy))])
     return {"workload": f"64 systems, {n} atoms (log-uniform 2,000-200,000 per system), 0.15 M NaCl, "
                         "order 6-10 and depth 3-5 per system, bf16x3",
@@ -530,7 +542,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-system batched line")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the 1,002,002-atom line and the 250,002-atom trajectory line")
-    ap.add_argument("--frames", type=int, default=20, help="frames of the trajectory line")
+    ap.add_argument("--frames", type=int, default=200, help="frames of the trajectory line")
     ap.add_argument("--profile", default=None,
                     help="precision,order,depth[,p2p_variant,m2l_split,m2l_stages]: only run --steps host-API "
                          "steps of that configuration and tuning (a short, fixed launch sequence for ncu "

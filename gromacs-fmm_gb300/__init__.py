@@ -274,7 +274,8 @@ class ZetaFmmSolver:
 class BatchSolver:
     """Many independent cubic systems solved together through one CUDA graph
     (gbfmm_batch_*).  systems: list of (coords (n,3), charges (n,), box edge);
-    orders/depths: one per system."""
+    orders/depths: one per system; precision: one for every system, or a list
+    with each system's own (gbfmm_batch_create_mixed)."""
 
     def __init__(self, natoms_list, orders, depths, images=4, precision=PREC_FP32, flags=0):
         L = lib()
@@ -285,6 +286,9 @@ class BatchSolver:
         L.gbfmm_batch_create.restype = ctypes.c_int
         L.gbfmm_batch_create.argtypes = [ctypes.c_int, ip, ip, ip, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                          ctypes.POINTER(vp)]
+        L.gbfmm_batch_create_mixed.restype = ctypes.c_int
+        L.gbfmm_batch_create_mixed.argtypes = [ctypes.c_int, ip, ip, ip, ip, ctypes.c_int, ctypes.c_int,
+                                               ctypes.POINTER(vp)]
         L.gbfmm_batch_execute.restype = ctypes.c_int
         L.gbfmm_batch_execute.argtypes = [vp, fp, fp, fp, fp, fp, dp]
         L.gbfmm_batch_execute_device.restype = ctypes.c_int
@@ -304,8 +308,14 @@ class BatchSolver:
         o = np.ascontiguousarray(orders, dtype=np.int32)
         d = np.ascontiguousarray(depths, dtype=np.int32)
         h = ctypes.c_void_p()
-        _check(L.gbfmm_batch_create(self.n_sys, self.offsets.ctypes.data_as(ip), o.ctypes.data_as(ip),
-                                    d.ctypes.data_as(ip), images, precision, flags, ctypes.byref(h)))
+        if np.ndim(precision) == 0:
+            _check(L.gbfmm_batch_create(self.n_sys, self.offsets.ctypes.data_as(ip), o.ctypes.data_as(ip),
+                                        d.ctypes.data_as(ip), images, int(precision), flags, ctypes.byref(h)))
+        else:  # each system's own precision
+            pr = np.ascontiguousarray(precision, dtype=np.int32)
+            _check(L.gbfmm_batch_create_mixed(self.n_sys, self.offsets.ctypes.data_as(ip), o.ctypes.data_as(ip),
+                                              d.ctypes.data_as(ip), pr.ctypes.data_as(ip), images, flags,
+                                              ctypes.byref(h)))
         self._b = h
 
     def close(self):

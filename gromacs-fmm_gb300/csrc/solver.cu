@@ -1446,8 +1446,24 @@ static void free_batch(gbfmm_batch* b)
     delete b;
 }
 
+static int batch_create(int n_sys, const int* atom_offsets, const int* orders, const int* depths,
+                        const int* precisions, int precision, int images, int flags, gbfmm_batch** out);
+
 extern "C" int gbfmm_batch_create(int n_sys, const int* atom_offsets, const int* orders, const int* depths, int images,
                                   int precision, int flags, gbfmm_batch** out)
+{
+    return batch_create(n_sys, atom_offsets, orders, depths, nullptr, precision, images, flags, out);
+}
+
+extern "C" int gbfmm_batch_create_mixed(int n_sys, const int* atom_offsets, const int* orders, const int* depths,
+                                        const int* precisions, int images, int flags, gbfmm_batch** out)
+{
+    if (!precisions) return fail(GBFMM_ERR_ARG, "precisions is NULL");
+    return batch_create(n_sys, atom_offsets, orders, depths, precisions, 0, images, flags, out);
+}
+
+static int batch_create(int n_sys, const int* atom_offsets, const int* orders, const int* depths,
+                        const int* precisions, int precision, int images, int flags, gbfmm_batch** out)
 {
     if (!out) return fail(GBFMM_ERR_ARG, "out is NULL");
     *out = nullptr;
@@ -1491,7 +1507,7 @@ extern "C" int gbfmm_batch_create(int n_sys, const int* atom_offsets, const int*
         p.order = orders[i];
         p.max_depth = depths[i];
         p.images = images;
-        p.precision = precision;
+        p.precision = precisions ? precisions[i] : precision;
         p.flags = flags & ~GBFMM_FLAG_NO_GRAPH;
         gbfmm_handle* h = nullptr;
         int rc = gbfmm_create(&p, atom_offsets[i + 1] - atom_offsets[i], &h);

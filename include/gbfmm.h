@@ -242,6 +242,10 @@ int gbfmm_set_tuning(gbfmm_handle* h, int p2p_variant, int m2l_split, int m2l_st
 typedef struct gbfmm_batch gbfmm_batch;
 int gbfmm_batch_create(int n_sys, const int* atom_offsets, const int* orders, const int* depths, int images,
                        int precision, int flags, gbfmm_batch** out);
+/* As gbfmm_batch_create, with each system's own M2L precision (precisions[n_sys],
+ * GBFMM_PREC_*).  No reference counterpart (the reference solves one system). */
+int gbfmm_batch_create_mixed(int n_sys, const int* atom_offsets, const int* orders, const int* depths,
+                             const int* precisions, int images, int flags, gbfmm_batch** out);
 int gbfmm_batch_execute(gbfmm_batch* b, const float* coords, const float* charges, const float* box_edges,
                         float* forces, float* potentials, double* energies);
 int gbfmm_batch_execute_device(gbfmm_batch* b, const void* d_coords, const void* d_charges,

@@ -137,3 +137,26 @@ def test_deterministic_batch_keeps_whole_m2l_tiles(pkg, systems):
     assert np.array_equal(f2, f3)
     assert rel_rms(f2, f1) < 1e-5
     b.close()
+
+
+def test_batch_mixed_precisions_match_single_solves(pkg, systems):
+    """Each system with its own M2L precision (gbfmm_batch_create_mixed): bit for
+    bit the deterministic single-system solve at that precision."""
+    sy = _systems(systems)
+    precs = [0, 1, 2, 1, 0]
+    b = pkg.BatchSolver([len(s[1]) for s in sy], [s[3] for s in sy], [s[4] for s in sy], images=4,
+                        precision=precs, flags=pkg.FLAG_DETERMINISTIC)
+    X = np.concatenate([s[0] for s in sy])
+    Q = np.concatenate([s[1] for s in sy])
+    B = np.array([s[2] for s in sy], np.float32)
+    for _ in range(2):
+        f, p, e = b.execute(X, Q, B)
+    off = b.offsets
+    for i, (xyz, q, L, P, D) in enumerate(sy):
+        s = pkg.ZetaFmmSolver(len(q), q, order=P, max_depth=D, images=4, precision=precs[i],
+                              flags=pkg.FLAG_DETERMINISTIC)
+        s.execute(xyz, L)
+        assert np.array_equal(f[off[i]:off[i + 1]], s.forces()), i
+        assert e[i] == s.get_energy(), i
+        s.close()
+    b.close()
