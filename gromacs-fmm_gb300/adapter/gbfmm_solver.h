@@ -1,0 +1,79 @@
+// The GROMACS-side drop-in: a coulomb_solver::BaseSolver that forwards to the
+// C ABI of libgbfmm (include/gbfmm.h).  A maintainer copies this file to
+// src/gromacs/coulomb_solvers/gbfmm_solver.h of the fork, adds GBFMM to
+// SolverExecuter::SolverType (executer.h:30-35) with a branch in set_solver
+// (executer.h:37-60), and passes SolverType::GBFMM in md.cpp:852.
+//
+// Mirrors zeta_fmm::ZetaFmmSolver (src/gromacs/zeta_fmm/zeta_fmm_solver.cpp),
+// with these differences: the device state lives for the solver's lifetime
+// (the reference allocates and frees it inside every execute); get_energy
+// returns 0.5 * sum(q * phi) (the reference's is a stub, :109-115); errors
+// throw instead of exit().
+#pragma once
+
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+
+#include "gbfmm.h"
+#include "gromacs/coulomb_solvers/basesolver.h"
+
+namespace coulomb_solver
+{
+class GbFmmSolver : public BaseSolver
+{
+public:
+    // The reference's constants (zeta_fmm_solver.cpp:6-14): order 10, depth 3,
+    // 4 images; params may override them (gbfmm_params_default fills the rest).
+    GbFmmSolver(FILE* f, const t_mdatoms& md, const gbfmm_params* params = nullptr) : BaseSolver(f, md)
+    {
+        gbfmm_params p;
+        if (params) p = *params;
+        else gbfmm_params_default(&p);
+        check(gbfmm_create(&p, natoms, &h_));
+        check(gbfmm_set_charges(h_, natoms, chargeA_.data()));
+    }
+    ~GbFmmSolver() override { gbfmm_destroy(h_); }
+
+    // basesolver.h:56-61.  The library copies the charges; mdrun calls this
+    // every step (md.cpp:1252), so they are re-sent.
+    void set_parameter(const t_mdatoms& md) override
+    {
+        BaseSolver::set_parameter(md);
+        if (h_) check(gbfmm_set_charges(h_, natoms, chargeA_.data()));
+    }
+
+    // zeta_fmm_solver.cpp:16-64: RVec is float[3] and matrix float[3][3], so the
+    // pointers pass straight through.
+    void execute(gmx::ArrayRef<const gmx::RVec> coord, const matrix box, int verbose = 0, int = 0) override
+    {
+        check(gbfmm_execute(h_, coord.data()[0].as_vec(), &box[0][0], verbose));
+    }
+
+    // zeta_fmm_solver.cpp:66-76: accumulates into the force buffer (no virial).
+    void add_force(gmx::ForceWithVirial* fv) override { check(gbfmm_add_forces(h_, fv->force_.data()[0].as_vec())); }
+
+    Energy get_energy() override
+    {
+        Energy e;
+        check(gbfmm_get_energy(h_, &e.coulomb_energy));
+        return e;
+    }
+
+    // zeta_fmm_solver.cpp:78-107
+    void compare_forces(const gmx::ArrayRef<gmx::RVec>& fs) override
+    {
+        double l2f = 0;
+        if (gbfmm_compare_forces(h_, fs.data()[0].as_vec(), &l2f) != GBFMM_OK) std::fprintf(stderr, "have nan!\n");
+        std::printf("L2f = %.8f\n", l2f);
+    }
+
+private:
+    static void check(int rc)
+    {
+        if (rc != GBFMM_OK)
+            throw std::runtime_error(std::string(gbfmm_status_string(rc)) + ": " + gbfmm_last_error());
+    }
+    gbfmm_handle* h_ = nullptr;
+};
+}  // namespace coulomb_solver
