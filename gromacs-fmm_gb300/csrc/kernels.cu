@@ -299,7 +299,7 @@ void launch_scatter(const uint32_t* code, int n, int* cursor, int* tmp_idx, cuda
 // Stable order inside each leaf (ascending input index), which makes the body
 // order identical to the per-level stable counting sort of tree.cpp:43-74.
 __global__ void __launch_bounds__(256) k_leaf_sort(const int* off, int nleaf, const int* tmp_idx, const float4* uq,
-                                                   int* order, float4* atoms, int* atom_leaf, int* counts)
+                                                   int* order, float4* atoms, int* inv, int* counts)
 {
     const int lane = threadIdx.x & 31;
     const int leaf = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -316,7 +316,7 @@ __global__ void __launch_bounds__(256) k_leaf_sort(const int* off, int nleaf, co
         if (lane < n) {
             order[b + rank] = v;
             atoms[b + rank] = uq[v];
-            atom_leaf[b + rank] = leaf;
+            inv[v] = b + rank;
         }
     } else {
         for (int e = lane; e < n; e += 32) {
@@ -325,18 +325,18 @@ __global__ void __launch_bounds__(256) k_leaf_sort(const int* off, int nleaf, co
             for (int j = 0; j < n; j++) rank += (tmp_idx[b + j] < v);
             order[b + rank] = v;
             atoms[b + rank] = uq[v];
-            atom_leaf[b + rank] = leaf;
+            inv[v] = b + rank;
         }
     }
 }
 
 void launch_leaf_sort(const int* offsets, int nleaf, int* tmp_idx, const float4* uq, const uint32_t* code, int* order,
-                      float4* atoms, int* atom_leaf, int* counts, cudaStream_t s)
+                      float4* atoms, int* inv, int* counts, cudaStream_t s)
 {
     (void)code;
     long threads = (long)nleaf * 32;
     COUNT_LAUNCH();
-    k_leaf_sort<<<(int)((threads + 255) / 256), 256, 0, s>>>(offsets, nleaf, tmp_idx, uq, order, atoms, atom_leaf,
+    k_leaf_sort<<<(int)((threads + 255) / 256), 256, 0, s>>>(offsets, nleaf, tmp_idx, uq, order, atoms, inv,
                                                             counts);
 }
 
@@ -1558,12 +1558,14 @@ __global__ void __launch_bounds__(256) k_finalize(FinalArgs a)
     float* __restrict__ forces = a.sc->out_forces;
     float* __restrict__ pots = a.sc->out_pots;
     f2sum e = {0.f, 0.f};
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) {
+    // in input order (coalesced writes, to device or host memory), gathering
+    // each body's fields from its sorted position
+    for (int o = blockIdx.x * blockDim.x + threadIdx.x; o < a.n; o += gridDim.x * blockDim.x) {
+        const int i = a.inv[o];
         const float4 nf = a.near[i], ff = a.far[i];
         const float q = a.atoms[i].w;
         const float phi = (nf.x + ff.x) * inv_h;
         const float gx = (nf.y + ff.y) * inv_h2, gy = (nf.z + ff.z) * inv_h2, gz = (nf.w + ff.w) * inv_h2;
-        const int o = a.order[i];
         const float qk = -q * (float)KE;
         forces[3 * o] = qk * gx + q * fM0;
         forces[3 * o + 1] = qk * gy + q * fM1;

@@ -114,8 +114,9 @@ void launch_tree_keys(const TreeArgs& a, cudaStream_t s);
 void launch_exclusive_scan(const int* in, int* out, int n, int* scratch, cudaStream_t s);
 void launch_scatter(const uint32_t* code, int n, int* cursor, int* tmp_idx, cudaStream_t s);
 // Also zeroes counts[0..nleaf) (consumed by then) when counts != NULL.
+// inv[input index] = sorted position (the inverse of order).
 void launch_leaf_sort(const int* offsets, int nleaf, int* tmp_idx, const float4* uq, const uint32_t* code, int* order,
-                      float4* atoms, int* atom_leaf, int* counts, cudaStream_t s);
+                      float4* atoms, int* inv, int* counts, cudaStream_t s);
 void launch_p2m(int P, const int* offsets, int nleaf, const float4* atoms, float* M_leaf, int Rpad, cudaStream_t s);
 // P2M of the leaves and M2M of their parents in one launch (8 sibling leaves per
 // CTA).  Returns false, launching nothing, when the order's shared memory does
@@ -216,7 +217,7 @@ struct FinalArgs {
     const StepConst* sc;
     int n;
     const float4* atoms;     // sorted (u, q)
-    const int* order;        // sorted -> input index
+    const int* inv;          // input index -> sorted position
     const float4* near;      // sorted (phi, grad) near field, scaled units
     const float4* far;       // sorted far field, scaled units
     const float* fconst;     // q*ke*coef*M (3) and ke*coef*|M|^2/N, FP32 (written by k_top)

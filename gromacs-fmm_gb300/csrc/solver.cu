@@ -155,7 +155,7 @@ struct gbfmm_handle {
     uint32_t* d_code = nullptr;
     float4* d_uq = nullptr;
     int *d_counts = nullptr, *d_off = nullptr, *d_cursor = nullptr, *d_scan = nullptr, *d_tmp = nullptr;
-    int *d_order = nullptr, *d_atom_leaf = nullptr;
+    int *d_order = nullptr, *d_inv = nullptr;  // sorted -> input index, and its inverse
     float4 *d_atoms = nullptr, *d_near = nullptr, *d_far = nullptr;
     float *d_M = nullptr, *d_L = nullptr;
     float* Mlev[8] = {};
@@ -304,7 +304,7 @@ static int layout(gbfmm_handle* h, Arena& a)
     h->d_scan = a.take<int>((h->nleaf + 2047) / 2048 + 1);
     h->d_tmp = a.take<int>(n);
     h->d_order = a.take<int>(n);
-    h->d_atom_leaf = a.take<int>(n);
+    h->d_inv = a.take<int>(n);
     h->d_atoms = a.take<float4>(n);
     h->d_near = a.take<float4>(n);
     h->d_far = a.take<float4>(n);
@@ -644,7 +644,7 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
         }
     }
     launch_scatter(h->d_code, n, h->d_cursor, h->d_tmp, s);
-    launch_leaf_sort(h->d_off, h->nleaf, h->d_tmp, h->d_uq, h->d_code, h->d_order, h->d_atoms, h->d_atom_leaf,
+    launch_leaf_sort(h->d_off, h->nleaf, h->d_tmp, h->d_uq, h->d_code, h->d_order, h->d_atoms, h->d_inv,
                      h->d_counts, s);
     mark(h, 1);
     // The near field needs only the tree: in graph mode it forks onto its own
@@ -756,7 +756,7 @@ static void enqueue_final(gbfmm_handle* h)
         fa.sc = h->d_sc;
         fa.n = n;
         fa.atoms = h->d_atoms;
-        fa.order = h->d_order;
+        fa.inv = h->d_inv;
         fa.near = h->d_near;
         fa.far = h->d_far;
         fa.fconst = h->d_fconst;
