@@ -544,15 +544,37 @@ def main():
                     help="skip the 1,002,002-atom line and the 250,002-atom trajectory line")
     ap.add_argument("--frames", type=int, default=200, help="frames of the trajectory line")
     ap.add_argument("--profile", default=None,
-                    help="precision,order,depth[,p2p_variant,m2l_split,m2l_stages]: only run --steps "
-                         "device-resident steps of that configuration and tuning (a short, fixed launch "
-                         "sequence for ncu captures); prints no bench line")
+                    help="precision,order,depth[,p2p_variant,m2l_split,m2l_stages], or 'batch': only run "
+                         "--steps device-resident steps of that configuration and tuning, or of the 64-system "
+                         "batch (a short, fixed launch sequence for ncu captures); prints no bench line")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_env()
     systems = G.load_module("systems")
     xyz, q, box = systems.cfg_96k()
     n = len(q)
+    if args.profile == "batch":
+        # device-resident steps of the 64-system batch of the batch line (orders
+        # 6-10, depths 3-5, BF16X3, default tiles)
+        import torch
+        pkg = G.load_package()
+        tuner_mod = G.load_module("tuner")
+        sy = systems.batch_systems(n_sys=64)
+        nat = [len(t[1]) for t in sy]
+        orders = [int(v) for v in np.random.default_rng(64).integers(6, 11, size=len(nat))]
+        depths = [min(5, max(3, tuner_mod.plain_depth(k))) for k in nat]
+        X = np.concatenate([t[0] for t in sy]).astype(np.float32)
+        Q = np.concatenate([t[1] for t in sy]).astype(np.float32)
+        B = np.array([float(t[2][0]) for t in sy], np.float32)
+        b = pkg.BatchSolver(nat, orders, depths, images=4, precision=1)
+        xd, qd = torch.from_numpy(X).cuda(), torch.from_numpy(Q).cuda()
+        st = torch.cuda.current_stream()
+        for _ in range(args.steps):
+            b.execute_device(xd.data_ptr(), qd.data_ptr(), B, st.cuda_stream)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": "batch", "steps": args.steps, "systems": len(nat), "atoms": int(sum(nat))}))
+        b.close()
+        return
     if args.profile:
         # device-resident steps (gbfmm_execute_device, as 'value' is measured)
         import torch
