@@ -8,7 +8,9 @@
 // with these differences: the device state lives for the solver's lifetime
 // (the reference allocates and frees it inside every execute); get_energy
 // returns 0.5 * sum(q * phi) (the reference's is a stub, :109-115); errors
-// throw instead of exit().
+// throw instead of exit(); and, given a force-error tolerance instead of fixed
+// parameters, the solver takes the learned tuner's checked choice of order,
+// depth and M2L precision.
 #pragma once
 
 #include <cstdio>
@@ -30,10 +32,27 @@ public:
         gbfmm_params p;
         if (params) p = *params;
         else gbfmm_params_default(&p);
-        check(gbfmm_create(&p, natoms, &h_));
-        check(gbfmm_set_charges(h_, natoms, chargeA_.data()));
+        create(p);
     }
-    ~GbFmmSolver() override { gbfmm_destroy(h_); }
+
+    // Learned parameters: at the first execute, the tuner network (weights file
+    // of gromacs-fmm_gb300/tuner_weights.bin) proposes order, depth and M2L
+    // precision for the relative force-error tolerance 'force_tol', checked
+    // against the plain order-10 FMM of that configuration (gbfmm_tuner_choose,
+    // which falls back to the plain FMM).
+    GbFmmSolver(FILE* f, const t_mdatoms& md, double force_tol, const char* weights) :
+        BaseSolver(f, md), tol_(force_tol), weights_(weights)
+    {
+    }
+    ~GbFmmSolver() override
+    {
+        if (h_) gbfmm_destroy(h_);
+    }
+    GbFmmSolver(const GbFmmSolver&) = delete;  // owns the library handle
+    GbFmmSolver& operator=(const GbFmmSolver&) = delete;
+
+    // The tuner's choice (valid after the first execute of a tolerance-driven solver).
+    const gbfmm_tuner_choice& choice() const { return choice_; }
 
     // basesolver.h:56-61.  The library copies the charges; mdrun calls this
     // every step (md.cpp:1252), so they are re-sent.
@@ -47,6 +66,7 @@ public:
     // pointers pass straight through.
     void execute(gmx::ArrayRef<const gmx::RVec> coord, const matrix box, int verbose = 0, int = 0) override
     {
+        if (!h_) choose(coord.data()[0].as_vec(), &box[0][0]);
         check(gbfmm_execute(h_, coord.data()[0].as_vec(), &box[0][0], verbose));
     }
 
@@ -74,6 +94,31 @@ private:
         if (rc != GBFMM_OK)
             throw std::runtime_error(std::string(gbfmm_status_string(rc)) + ": " + gbfmm_last_error());
     }
+    void create(const gbfmm_params& p)
+    {
+        check(gbfmm_create(&p, natoms, &h_));
+        check(gbfmm_set_charges(h_, natoms, chargeA_.data()));
+    }
+    void choose(const float* x, const float* box)
+    {
+        gbfmm_mlp* m = nullptr;
+        check(gbfmm_mlp_load(weights_.c_str(), &m));
+        const int rc = gbfmm_tuner_choose(m, natoms, chargeA_.data(), x, box, 4, tol_, 1.5, &choice_);
+        gbfmm_mlp_destroy(m);
+        check(rc);
+        gbfmm_params p;
+        gbfmm_params_default(&p);
+        p.order = choice_.order;
+        p.max_depth = choice_.depth;
+        p.precision = choice_.precision;
+        create(p);
+        if (fplog)
+            std::fprintf(fplog, "gbfmm: order %d, depth %d, precision %d for force tolerance %g%s\n", choice_.order,
+                         choice_.depth, choice_.precision, tol_, choice_.fallback ? " (plain FMM)" : "");
+    }
     gbfmm_handle* h_ = nullptr;
+    double tol_ = 0;
+    std::string weights_;
+    gbfmm_tuner_choice choice_{};
 };
 }  // namespace coulomb_solver

@@ -650,3 +650,112 @@ extern "C" int gbfmm_mlp_load(const char* path, gbfmm_mlp** out)
     *out = m;
     return GBFMM_OK;
 }
+
+// ---- checked choice: proposal, check against the plain FMM, fallback
+
+// Depth of the plain FMM: 16-128 bodies per leaf, as the reference's fixed depth
+// gives for its systems.
+extern "C" int gbfmm_plain_depth(int natoms)
+{
+    int d = 1;
+    while ((double)natoms / std::pow(8.0, d + 1) >= 16.0 && d < 7) d++;
+    return d;
+}
+
+namespace {
+
+// Forces of one solve of (order, depth, precision) on host inputs.
+int solve_forces(int n, const float* q, const float* x, const float* box, int P, int D, int prec, int images,
+                 std::vector<float>& f)
+{
+    gbfmm_params p;
+    gbfmm_params_default(&p);
+    p.order = P;
+    p.max_depth = D;
+    p.images = images;
+    p.precision = prec;
+    gbfmm_handle* h = nullptr;
+    int rc = gbfmm_create(&p, n, &h);
+    if (rc) return rc;
+    f.assign(3 * (size_t)n, 0.f);
+    rc = gbfmm_set_charges(h, n, q);
+    if (!rc) rc = gbfmm_execute(h, x, box, 0);
+    if (!rc) rc = gbfmm_get_forces(h, f.data());
+    gbfmm_destroy(h);
+    return rc;
+}
+
+double rel_rms(const std::vector<float>& a, const std::vector<float>& b)
+{
+    double num = 0, den = 0;
+    for (size_t i = 0; i < a.size(); i++) {
+        const double d = (double)a[i] - (double)b[i];
+        num += d * d;
+        den += (double)b[i] * (double)b[i];
+    }
+    return den > 0 ? std::sqrt(num / den) : (num > 0 ? INFINITY : 0.0);
+}
+
+}  // namespace
+
+extern "C" int gbfmm_tuner_choose(gbfmm_mlp* m, int natoms, const float* charges, const float* coords,
+                                  const float* box, int images, double tol, double margin, gbfmm_tuner_choice* out)
+{
+    if (!m || !charges || !coords || !box || !out || natoms <= 0 || tol <= 0) return GBFMM_ERR_ARG;
+    std::memset(out, 0, sizeof(*out));
+    const int n = natoms;
+    // statistics on the device
+    float feat[GBFMM_NFEAT];
+    {
+        void* d = nullptr;
+        cudaError_t e = cudaMalloc(&d, sizeof(float) * 4 * (size_t)n);
+        if (e != cudaSuccess) return status(e);
+        float* dx = static_cast<float*>(d);
+        float* dq = dx + 3 * (size_t)n;
+        e = cudaMemcpy(dx, coords, sizeof(float) * 3 * (size_t)n, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(dq, charges, sizeof(float) * (size_t)n, cudaMemcpyHostToDevice);
+        int rc = e == cudaSuccess ? gbfmm_features(dx, dq, n, box, feat, nullptr) : status(e);
+        if (rc == GBFMM_OK && cudaDeviceSynchronize() != cudaSuccess) rc = GBFMM_ERR_CUDA;
+        cudaFree(d);
+        if (rc) return rc;
+    }
+    // the judge: the plain order-10 FP32 FMM of this configuration
+    const int plain_order = 10, plain_depth = gbfmm_plain_depth(n);
+    std::vector<float> fj, fc;
+    int rc = solve_forces(n, charges, coords, box, plain_order, plain_depth, GBFMM_PREC_FP32, images, fj);
+    if (rc) return rc;
+    int P0 = 0, D = 0, prec = 0;
+    float pe = 0.f, pm = 0.f;
+    rc = gbfmm_tuner_propose(m, feat, tol, margin, &P0, &D, &prec, &pe, &pm);
+    if (rc != GBFMM_OK && rc != GBFMM_ERR_UNSUPPORTED) return rc;
+    if (rc == GBFMM_OK) {
+        out->proposed_order = P0;
+        out->proposed_depth = D;
+        out->proposed_precision = prec;
+        out->pred_rel_force_err = pe;
+        out->pred_ms = pm;
+        // the proposal, then up to two higher orders at the same depth and
+        // precision; each one is checked against the judge
+        for (int P = P0; P <= std::min(P0 + 2, plain_order); P++) {
+            rc = solve_forces(n, charges, coords, box, P, D, prec, images, fc);
+            if (rc) return rc;
+            const double diff = rel_rms(fc, fj);
+            const int k = out->nchecks++;
+            out->check_order[k] = P;
+            out->check_diff[k] = diff;
+            if (diff <= tol) {
+                out->order = P;
+                out->depth = D;
+                out->precision = prec;
+                out->diff_vs_plain = diff;
+                return GBFMM_OK;
+            }
+        }
+    }
+    out->order = plain_order;  // fallback: the plain FMM
+    out->depth = plain_depth;
+    out->precision = GBFMM_PREC_FP32;
+    out->fallback = 1;
+    out->diff_vs_plain = 0.0;
+    return GBFMM_OK;
+}

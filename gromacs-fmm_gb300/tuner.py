@@ -4,11 +4,12 @@ Host side of the tuner in include/gbfmm.h: per-step statistics computed on the
 GPU (gbfmm_features), a 3-layer MLP whose forward, backward and Adam kernels
 are the library's own (gbfmm_mlp_*), and the proposal (gbfmm_tuner_propose).
 
-`TunedSolver` checks every proposal: it solves the system once with the
-proposal and once with the plain fixed-parameter FMM (order 10, the judge) and
-keeps the proposal only if their forces agree within the tolerance; otherwise
-it falls back to the plain FMM.  Nothing here uses an FP64 reference: training
-tuples come from tests/golden/make_tuner_data.py.
+`TunedSolver` checks every proposal through the library's gbfmm_tuner_choose:
+it solves the system once with the proposal and once with the plain
+fixed-parameter FMM (order 10, the judge) and keeps the proposal only if their
+forces agree within the tolerance (retrying one and two orders higher);
+otherwise it falls back to the plain FMM.  Nothing here uses an FP64
+reference: training tuples come from tests/golden/make_tuner_data.py.
 """
 import ctypes
 import importlib
@@ -24,6 +25,16 @@ WEIGHTS = os.path.join(HERE, "tuner_weights.bin")
 NFEAT = 56
 N_IN = NFEAT + 4
 PLAIN_ORDER = 10
+
+class TunerChoice(ctypes.Structure):
+    """gbfmm_tuner_choice of include/gbfmm.h."""
+    _fields_ = [("order", ctypes.c_int), ("depth", ctypes.c_int), ("precision", ctypes.c_int),
+                ("fallback", ctypes.c_int), ("diff_vs_plain", ctypes.c_double),
+                ("proposed_order", ctypes.c_int), ("proposed_depth", ctypes.c_int),
+                ("proposed_precision", ctypes.c_int), ("pred_rel_force_err", ctypes.c_float),
+                ("pred_ms", ctypes.c_float), ("nchecks", ctypes.c_int), ("check_order", ctypes.c_int * 3),
+                ("check_diff", ctypes.c_double * 3)]
+
 
 _fp = ctypes.POINTER(ctypes.c_float)
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -53,6 +64,9 @@ def _sig():
         "gbfmm_mlp_load": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_vp)]),
         "gbfmm_tuner_input": (ctypes.c_int, [_fp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _fp]),
         "gbfmm_tuner_propose": (ctypes.c_int, [_vp, _fp, ctypes.c_double, ctypes.c_double, _ip, _ip, _ip, _fp, _fp]),
+        "gbfmm_tuner_choose": (ctypes.c_int, [_vp, ctypes.c_int, _fp, _fp, _fp, ctypes.c_int, ctypes.c_double,
+                                              ctypes.c_double, ctypes.POINTER(TunerChoice)]),
+        "gbfmm_plain_depth": (ctypes.c_int, [ctypes.c_int]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -194,11 +208,8 @@ def fit(x, t, n_hidden=64, epochs=400, batch=128, lr=2e-3, seed=0):
 
 def plain_depth(natoms):
     """Depth of the plain FMM: about 16-128 bodies per leaf, as the reference's
-    fixed depth gives for its systems."""
-    d = 1
-    while natoms / 8.0 ** (d + 1) >= 16 and d < 7:
-        d += 1
-    return d
+    fixed depth gives for its systems (gbfmm_plain_depth)."""
+    return int(_sig().gbfmm_plain_depth(int(natoms)))
 
 
 class TunedSolver:
@@ -218,35 +229,27 @@ class TunedSolver:
 
     def propose(self, coords, box):
         """Computes statistics, proposes, and checks the proposal against the
-        plain FMM on this configuration.  Returns the accepted choice."""
-        import torch
-        x = torch.from_numpy(_f(coords).reshape(-1, 3)).cuda()
-        qd = torch.from_numpy(self.q).cuda()
-        feat = features(x.data_ptr(), qd.data_ptr(), self.n, box, torch.cuda.current_stream().cuda_stream)
-        torch.cuda.synchronize()
-        prop = self.mlp.propose(feat, self.tol, self.margin)
-        judge = self._plain()
-        judge.execute(coords, box)
-        fj = judge.forces().astype(np.float64)
-        if prop is None:
+        plain FMM on this configuration (gbfmm_tuner_choose).  Returns the
+        accepted choice; self.solver holds a solver of that choice with this
+        configuration's results."""
+        x = _f(coords).reshape(-1)
+        m = _pkg.box_matrix(box)
+        c = TunerChoice()
+        _check(_sig().gbfmm_tuner_choose(self.mlp._h, self.n, self.q.ctypes.data_as(_fp), x.ctypes.data_as(_fp),
+                                         m.ctypes.data_as(_fp), self.images, float(self.tol), float(self.margin),
+                                         ctypes.byref(c)))
+        if c.proposed_order == 0:
             self.checks.append({"proposal": None, "accepted": False})
         else:
-            # the proposal, then up to two higher orders at the same depth and
-            # precision when the check rejects it; each one is checked
-            P0, D, prec = prop[:3]
-            for P in range(P0, min(P0 + 3, PLAIN_ORDER + 1)):
-                cand = _pkg.ZetaFmmSolver(self.n, self.q, order=P, max_depth=D, images=self.images, precision=prec)
-                cand.execute(coords, box)
-                diff = float(np.sqrt(np.sum((cand.forces() - fj) ** 2) / np.sum(fj ** 2)))
-                ok = diff <= self.tol
-                self.checks.append({"proposal": prop if P == P0 else (P, D, prec), "diff_vs_plain": diff,
-                                    "accepted": ok})
-                if ok:
-                    judge.close()
-                    self.solver, self.choice = cand, (P, D, prec)
-                    return self.choice
-                cand.close()
-        self.solver, self.choice = judge, (PLAIN_ORDER, plain_depth(self.n), _pkg.PREC_FP32)
+            prop = (c.proposed_order, c.proposed_depth, c.proposed_precision, c.pred_rel_force_err, c.pred_ms)
+            for k in range(c.nchecks):
+                self.checks.append({"proposal": prop if k == 0 else (c.check_order[k], prop[1], prop[2]),
+                                    "diff_vs_plain": c.check_diff[k],
+                                    "accepted": not c.fallback and k == c.nchecks - 1})
+        self.choice = (c.order, c.depth, c.precision)
+        self.solver = _pkg.ZetaFmmSolver(self.n, self.q, order=c.order, max_depth=c.depth, images=self.images,
+                                         precision=c.precision)
+        self.solver.execute(coords, box)
         return self.choice
 
     def execute(self, coords, box):

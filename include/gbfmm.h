@@ -189,6 +189,29 @@ int gbfmm_tuner_input(const float* features, int order, int depth, int precision
 int gbfmm_tuner_propose(gbfmm_mlp* m, const float* features, double tol, double margin, int* order, int* depth,
                         int* precision, float* pred_err, float* pred_ms);
 
+/* Depth of the plain FMM for natoms bodies: 16-128 bodies per leaf. */
+int gbfmm_plain_depth(int natoms);
+
+/* The checked choice (no counterpart in the reference, which fixes P=10 and
+ * depth 3, zeta_fmm_solver.cpp:10-11): statistics of the system on the device,
+ * the network's proposal for 'tol' (gbfmm_tuner_propose with 'margin'), then a
+ * check of the proposal's forces against the plain order-10 FP32 FMM of the
+ * same configuration (the judge), retried at one and two orders higher; when no
+ * candidate meets tol, or none is proposed, the plain FMM's parameters are
+ * chosen (fallback = 1).  Host inputs; each solve runs through gbfmm_execute. */
+typedef struct {
+    int order, depth, precision;  /* the choice */
+    int fallback;                 /* 1: the plain FMM */
+    double diff_vs_plain;         /* relative RMS force difference of the choice from the judge */
+    int proposed_order, proposed_depth, proposed_precision;  /* the network's proposal (0 if none) */
+    float pred_rel_force_err, pred_ms;
+    int nchecks;                  /* checked candidates (orders check_order[k]) */
+    int check_order[3];
+    double check_diff[3];
+} gbfmm_tuner_choice;
+int gbfmm_tuner_choose(gbfmm_mlp* m, int natoms, const float* charges, const float* coords, const float* box,
+                       int images, double tol, double margin, gbfmm_tuner_choice* out);
+
 /* ---- tree build without allocation ---- */
 
 /* No counterpart in the reference.  For callers that cannot allocate device

@@ -3,10 +3,12 @@
 // md.cpp of the fork): construct once, then per step set_parameter, execute,
 // add_force into the step's force buffer, get_energy; compare_forces at the end.
 //
-// usage: mdrun_steps in.bin out.bin order depth images
+// usage: mdrun_steps in.bin out.bin order depth images [tol weights]
 //   in.bin : int32 natoms, int32 nsteps, float box[9], float q[natoms],
 //            float x[nsteps][natoms][3]
 //   out.bin: per step float f[natoms][3] (added to a buffer of ones), double energy
+//   order 0: the learned tuner's checked choice for the force tolerance 'tol'
+//   (weights file 'weights'), printed as "choice order depth precision fallback"
 #include <cstdio>
 #include <cstdlib>
 #include <exception>
@@ -16,8 +18,8 @@
 
 int main(int argc, char** argv)
 {
-    if (argc != 6) {
-        std::fprintf(stderr, "usage: %s in.bin out.bin order depth images\n", argv[0]);
+    if (argc != 6 && argc != 8) {
+        std::fprintf(stderr, "usage: %s in.bin out.bin order depth images [tol weights]\n", argv[0]);
         return 2;
     }
     FILE* in = std::fopen(argv[1], "rb");
@@ -45,7 +47,9 @@ int main(int argc, char** argv)
         p.order = std::atoi(argv[3]);
         p.max_depth = std::atoi(argv[4]);
         p.images = std::atoi(argv[5]);
-        coulomb_solver::GbFmmSolver solver(stdout, md, &p);
+        const bool tuned = p.order == 0;
+        coulomb_solver::GbFmmSolver solver = tuned ? coulomb_solver::GbFmmSolver(stdout, md, std::atof(argv[6]), argv[7])
+                                                   : coulomb_solver::GbFmmSolver(stdout, md, &p);
         coulomb_solver::BaseSolver& s = solver;  // mdrun holds the base class
         std::vector<gmx::RVec> f(n);
         for (int step = 0; step < nsteps; step++) {
@@ -58,6 +62,9 @@ int main(int argc, char** argv)
             std::fwrite(f.data(), sizeof(float), 3 * (size_t)n, out);
             std::fwrite(&e.coulomb_energy, sizeof(double), 1, out);
         }
+        if (tuned)
+            std::printf("choice %d %d %d %d\n", solver.choice().order, solver.choice().depth,
+                        solver.choice().precision, solver.choice().fallback);
         for (auto& v : f) v = gmx::RVec(v[0] - 1.f, v[1] - 1.f, v[2] - 1.f);
         s.compare_forces(gmx::ArrayRef<gmx::RVec>(f.data(), n));
     } catch (const std::exception& ex) {

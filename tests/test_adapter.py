@@ -29,14 +29,11 @@ def test_adapter_compiles_against_the_base_solver_interface():
     subprocess.run([_gxx(), "-fsyntax-only", *FLAGS, DRIVER], check=True)
 
 
-@pytest.mark.gpu
-def test_adapter_steps_match_the_oracle(pkg, oracle, systems, tmp_path):
+def _run_driver(pkg, tmp_path, xyz, q, L, args):
     lib_dir = os.path.dirname(pkg.LIB_PATH)
     exe = str(tmp_path / "mdrun_steps")
     subprocess.run([_gxx(), *FLAGS, DRIVER, "-L", lib_dir, "-lgbfmm", f"-Wl,-rpath,{lib_dir}", "-o", exe],
                    check=True)
-    xyz, q, box = systems.water_ion_box(1500, 3.0, n_na=4, n_cl=4, seed=41)
-    L = float(box[0])
     rng = np.random.default_rng(5)
     steps = [xyz, np.mod(xyz + rng.normal(0, 0.01, xyz.shape), L).astype(np.float32)]
     n = len(q)
@@ -46,17 +43,48 @@ def test_adapter_steps_match_the_oracle(pkg, oracle, systems, tmp_path):
         q.astype(np.float32).tofile(f)
         for x in steps:
             x.astype(np.float32).tofile(f)
-    P, D, images = 8, 2, 4
-    r = subprocess.run([exe, str(tmp_path / "in.bin"), str(tmp_path / "out.bin"), str(P), str(D), str(images)],
-                       capture_output=True, text=True, timeout=120)
+    r = subprocess.run([exe, str(tmp_path / "in.bin"), str(tmp_path / "out.bin"), *[str(a) for a in args]],
+                       capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     assert "L2f = 0.00000000" in r.stdout
     raw = (tmp_path / "out.bin").read_bytes()
     rec = 12 * n + 8
     assert len(raw) == rec * len(steps)
+    out = []
     for k, x in enumerate(steps):
         f = np.frombuffer(raw[k * rec:k * rec + 12 * n], np.float32).reshape(n, 3) - 1.0  # added to ones
         e = np.frombuffer(raw[k * rec + 12 * n:(k + 1) * rec], np.float64)[0]
+        out.append((x, f, e))
+    return out, r.stdout
+
+
+@pytest.mark.gpu
+def test_adapter_steps_match_the_oracle(pkg, oracle, systems, tmp_path):
+    xyz, q, box = systems.water_ion_box(1500, 3.0, n_na=4, n_cl=4, seed=41)
+    L = float(box[0])
+    P, D, images = 8, 2, 4
+    steps, _ = _run_driver(pkg, tmp_path, xyz, q, L, [P, D, images])
+    for x, f, e in steps:
         po, fo, eo = oracle.zeta_solve(x.astype(np.float64), q.astype(np.float64), L, P, D, images)
         assert rel_rms(f, fo) < 1e-5
         assert abs(e - eo) / abs(eo) < 1e-6
+
+
+@pytest.mark.gpu
+def test_adapter_with_the_learned_tuner(pkg, oracle, systems, tmp_path):
+    """Given a force tolerance instead of fixed parameters, the adapter takes the
+    tuner's checked choice (gbfmm_tuner_choose) at the first step; both steps stay
+    within the tolerance of the plain order-10 FMM."""
+    tuner = pytest.importorskip("gromacs_fmm_gb300.tuner")
+    xyz, q, box = systems.water_ion_box(16000, 8.0, n_na=12, n_cl=12, seed=43)
+    L = float(box[0])
+    tol = 1e-3
+    steps, out = _run_driver(pkg, tmp_path, xyz, q, L, [0, 0, 4, tol, tuner.WEIGHTS])
+    line = [ln for ln in out.splitlines() if ln.startswith("choice ")][0]
+    order, depth, prec, fallback = (int(v) for v in line.split()[1:])
+    assert 4 <= order <= 10 and 1 <= depth <= 7 and prec in (0, 1, 2)
+    D0 = tuner.plain_depth(len(q))
+    for x, f, e in steps:
+        _, fo, eo = oracle.zeta_solve(x.astype(np.float64), q.astype(np.float64), L, 10, D0, 4)
+        assert rel_rms(f, fo) < tol
+        assert abs(e - eo) / abs(eo) < tol
