@@ -177,3 +177,21 @@ def test_checked_proposal_gain_over_plain(tuner, oracle, systems, pkg, n_sites, 
     plain.close()
     ts.solver.close()
     mlp.close()
+
+
+def test_unreachable_tolerance_falls_back_to_the_plain_fmm(tuner, systems, pkg):
+    """No candidate can meet 1e-9 against the plain FMM: gbfmm_tuner_choose keeps
+    the plain order-10 FP32 parameters and says so (the fallback of the checked
+    choice)."""
+    xyz, q, box = systems.water_ion_box(3000, 4.5, seed=77)
+    mlp = tuner.Mlp.load()
+    ts = tuner.TunedSolver(q, mlp, tol=1e-9)
+    choice = ts.propose(xyz, float(box[0]))
+    assert choice == (tuner.PLAIN_ORDER, tuner.plain_depth(len(q)), pkg.PREC_FP32)
+    assert not any(c["accepted"] for c in ts.checks)
+    plain = ts._plain()
+    plain.execute(xyz, float(box[0]))
+    assert rel_rms(ts.execute(xyz, float(box[0])), plain.forces()) < 1e-6
+    plain.close()
+    ts.solver.close()
+    mlp.close()
