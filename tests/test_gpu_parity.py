@@ -28,6 +28,10 @@ def _solve(pkg, xyz, q, box, **kw):
     (1500, 3.0, 6, 6, 3, 2),
     (3000, 4.5, 10, 12, 3, 4),
     (800, 2.0, 4, 5, 1, 4),
+    (800, 2.0, 4, 16, 2, 4),    # the highest order
+    (800, 2.0, 4, 2, 2, 4),     # the lowest order
+    (1500, 3.0, 6, 6, 3, 6),
+    (1500, 3.0, 6, 6, 3, 8),    # the most lattice images
 ])
 def test_parity_vs_oracle(pkg, oracle, systems, n_sites, L, ions, P, depth, images):
     xyz, q, box = systems.water_ion_box(n_sites, L, n_na=ions, n_cl=ions, seed=n_sites + P)
