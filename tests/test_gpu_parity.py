@@ -32,6 +32,7 @@ def _solve(pkg, xyz, q, box, **kw):
     (800, 2.0, 4, 2, 2, 4),     # the lowest order
     (1500, 3.0, 6, 6, 3, 6),
     (1500, 3.0, 6, 6, 3, 8),    # the most lattice images
+    (7000, 4.3, 6, 4, 5, 4),    # depth 5: 32,768 leaves, fewer than one body per leaf
 ])
 def test_parity_vs_oracle(pkg, oracle, systems, n_sites, L, ions, P, depth, images):
     xyz, q, box = systems.water_ion_box(n_sites, L, n_na=ions, n_cl=ions, seed=n_sites + P)
