@@ -62,3 +62,39 @@ def test_trajectory_frames_keep_the_checked_choice(pkg, systems):
     ts.solver.close()
     mlp.close()
     assert t_tuned * 2 < t_base
+
+
+def test_depth6_parity_vs_oracle(pkg, oracle, systems):
+    """Depth 6 (262,144 leaves, mostly empty): the FP32 path against the FP64 oracle."""
+    xyz, q, box = systems.water_ion_box(7000, 4.3, n_na=6, n_cl=6, seed=7003)
+    L = float(box[0])
+    s = pkg.ZetaFmmSolver(len(q), q, order=3, max_depth=6, images=2)
+    s.execute(xyz, L)
+    f, p, e = s.forces(), s.potentials(), s.get_energy()
+    s.close()
+    po, fo, eo = oracle.zeta_solve(xyz.astype(np.float64), q.astype(np.float64), L, 3, 6, 2)
+    assert rel_rms(f, fo) < 1e-5
+    assert rel_rms(p, po) < 1e-5
+    assert abs(e - eo) / abs(eo) < 1e-6
+
+
+def test_depth7_converges_to_ewald(pkg, oracle, systems):
+    """The deepest tree (2,097,152 leaves, about 100 cells per body), where the
+    oracle is too slow: against FP64 Ewald the error falls with the order as it
+    does at the depths the oracle pins, and stays in line with depth 6."""
+    xyz, q, box = systems.water_ion_box(7000, 4.3, n_na=6, n_cl=6, seed=7004)
+    L = float(box[0])
+    tg = np.arange(0, len(q), 7)
+    _, fe, _ = oracle.ewald(xyz.astype(np.float64), q.astype(np.float64), L, eps=1e-9, targets=tg)
+    _, _, ee = oracle.ewald(xyz.astype(np.float64), q.astype(np.float64), L, eps=1e-9, energy=True)
+    err = {}
+    for P, D in ((6, 6), (6, 7), (10, 7)):
+        s = pkg.ZetaFmmSolver(len(q), q, order=P, max_depth=D, images=4)
+        s.execute(xyz, L)
+        f, e = s.forces(), s.get_energy()
+        s.close()
+        assert np.isfinite(f).all()
+        err[(P, D)] = (rel_rms(f[tg], fe), abs(e - ee) / abs(ee))
+    assert err[(6, 7)][0] < 2.0 * err[(6, 6)][0], err
+    assert err[(10, 7)][0] < 0.2 * err[(6, 7)][0], err
+    assert err[(10, 7)][0] < 5e-4 and err[(10, 7)][1] < 1e-5, err
