@@ -19,6 +19,9 @@ pytestmark = pytest.mark.gpu
     (1500, 3.0, 10, 3, 4),
     (800, 2.0, 5, 1, 4),
     (8000, 6.2, 7, 4, 2),
+    (1000, 2.2, 2, 2, 4),     # the lowest orders
+    (1000, 2.2, 3, 2, 4),
+    (7000, 4.3, 4, 5, 4),     # depth 5
 ])
 def test_tc_bf16x3_parity(pkg, oracle, systems, n_sites, L, P, depth, images):
     xyz, q, box = systems.water_ion_box(n_sites, L, n_na=4, n_cl=4, seed=n_sites * 3 + P)
