@@ -95,7 +95,8 @@ __global__ void __launch_bounds__(256) k_tree_keys(TreeArgs a)
         uint32_t code = morton_encode(iv[0], iv[1], iv[2]);
         a.code[i] = code;
         a.uq[i] = make_float4(u[0], u[1], u[2], q);
-        atomicAdd(&a.counts[code], 1);
+        if (a.rank) a.rank[i] = atomicAdd(&a.counts[code], 1);
+        else atomicAdd(&a.counts[code], 1);
 #pragma unroll
         for (int d = 0; d < 3; d++) sd[d] = f2s_add(sd[d], f2s_prod(q, x[d]));
         sd[3] = f2s_add(sd[3], f2sum{q, 0.f});
@@ -178,7 +179,7 @@ __global__ void __launch_bounds__(256) k_tree_keys(TreeArgs a)
             for (int i = threadIdx.x; i < m; i += 256) {
                 const int v = tile[i];
                 a.off[base + i] = v;
-                a.cursor[base + i] = v;
+                if (a.cursor) a.cursor[base + i] = v;
             }
             carry = carry_s;
             __syncthreads();  // the tile is reused by the next 4096 leaves
@@ -294,6 +295,21 @@ __global__ void k_scatter(const uint32_t* code, int n, int* cursor, int* tmp_idx
 void launch_scatter(const uint32_t* code, int n, int* cursor, int* tmp_idx, cudaStream_t s)
 {
     if (n > 0) { COUNT_LAUNCH(); k_scatter<<<(n + 255) / 256, 256, 0, s>>>(code, n, cursor, tmp_idx); }
+}
+
+__global__ void k_scatter_ranked(const uint32_t* code, int n, const int* off, const int* rank, int* tmp_idx)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) tmp_idx[off[code[i]] + rank[i]] = i;
+}
+
+void launch_scatter_ranked(const uint32_t* code, int n, const int* off, const int* rank, int* tmp_idx,
+                           cudaStream_t s)
+{
+    if (n > 0) {
+        COUNT_LAUNCH();
+        k_scatter_ranked<<<(n + 255) / 256, 256, 0, s>>>(code, n, off, rank, tmp_idx);
+    }
 }
 
 // Stable order inside each leaf (ascending input index), which makes the body

@@ -80,6 +80,7 @@ struct TreeArgs {
     uint32_t* code;         // N leaf codes (input order)
     float4* uq;             // N scaled coords + charge (input order)
     int* counts;            // 8^D
+    int* rank = nullptr;    // N: each body's arrival index in its leaf (the count's atomic), or none
     double* partials;       // per block: dipole (3) and total charge, FP32 pairs (hi, lo)
     int* flags;             // [0] non-finite input seen
     // Last-block epilogue (done NULL: none).  The last block to finish sums the
@@ -113,6 +114,9 @@ extern std::atomic<long> g_kernel_launches;
 void launch_tree_keys(const TreeArgs& a, cudaStream_t s);
 void launch_exclusive_scan(const int* in, int* out, int n, int* scratch, cudaStream_t s);
 void launch_scatter(const uint32_t* code, int n, int* cursor, int* tmp_idx, cudaStream_t s);
+// The same without atomics: tmp_idx[off[code[i]] + rank[i]] = i (TreeArgs::rank).
+void launch_scatter_ranked(const uint32_t* code, int n, const int* off, const int* rank, int* tmp_idx,
+                           cudaStream_t s);
 // Also zeroes counts[0..nleaf) (consumed by then) when counts != NULL.
 // inv[input index] = sorted position (the inverse of order).
 void launch_leaf_sort(const int* offsets, int nleaf, int* tmp_idx, const float4* uq, const uint32_t* code, int* order,

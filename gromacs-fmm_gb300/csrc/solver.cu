@@ -154,7 +154,7 @@ struct gbfmm_handle {
     float* d_q = nullptr;
     uint32_t* d_code = nullptr;
     float4* d_uq = nullptr;
-    int *d_counts = nullptr, *d_off = nullptr, *d_cursor = nullptr, *d_scan = nullptr, *d_tmp = nullptr;
+    int *d_counts = nullptr, *d_off = nullptr, *d_scan = nullptr, *d_tmp = nullptr;
     int *d_order = nullptr, *d_inv = nullptr;  // sorted -> input index, and its inverse
     float4 *d_atoms = nullptr, *d_near = nullptr, *d_far = nullptr;
     float *d_M = nullptr, *d_L = nullptr;
@@ -300,7 +300,6 @@ static int layout(gbfmm_handle* h, Arena& a)
     h->d_uq = a.take<float4>(n);
     h->d_counts = a.take<int>(h->nleaf + 1 + 4);  // + the epilogue counters (zeroed per step)
     h->d_off = a.take<int>(h->nleaf + 1);
-    h->d_cursor = a.take<int>(h->nleaf + 1);
     h->d_scan = a.take<int>((h->nleaf + 2047) / 2048 + 1);
     h->d_tmp = a.take<int>(n);
     h->d_order = a.take<int>(n);
@@ -610,6 +609,7 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
         ta.code = h->d_code;
         ta.uq = h->d_uq;
         ta.counts = h->d_counts;
+        ta.rank = h->d_inv;  // arrival ranks, consumed by the scatter before the leaf sort writes inv
         ta.zero = reinterpret_cast<float4*>(h->d_L);  // lev_floats: levels of Rpad (a multiple of 4) floats
         ta.zero_n4 = (long)(h->lev_floats / 4);
         ta.partials = h->d_partials;
@@ -618,7 +618,6 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
         ta.sums = nullptr;  // summed by the upper-tree kernel, off the serial path
         if (h->nleaf <= TREE_EPILOGUE_MAX_LEAVES) {
             ta.off = h->d_off;
-            ta.cursor = h->d_cursor;
             ta.nleaf = h->nleaf;
         }
         // the small operators and lists of the later stages (the application's
@@ -638,12 +637,9 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
         pf(h->d_entries, h->tasks_bytes);
         pf(h->d_p2p_st, sizeof(int) * 3 * h->n_p2p_st);
         launch_tree_keys(ta, s);
-        if (!ta.off) {
-            launch_exclusive_scan(h->d_counts, h->d_off, h->nleaf, h->d_scan, s);
-            cudaMemcpyAsync(h->d_cursor, h->d_off, sizeof(int) * h->nleaf, cudaMemcpyDeviceToDevice, s);
-        }
+        if (!ta.off) launch_exclusive_scan(h->d_counts, h->d_off, h->nleaf, h->d_scan, s);
     }
-    launch_scatter(h->d_code, n, h->d_cursor, h->d_tmp, s);
+    launch_scatter_ranked(h->d_code, n, h->d_off, h->d_inv, h->d_tmp, s);
     launch_leaf_sort(h->d_off, h->nleaf, h->d_tmp, h->d_uq, h->d_code, h->d_order, h->d_atoms, h->d_inv,
                      h->d_counts, s);
     mark(h, 1);
