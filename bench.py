@@ -713,8 +713,12 @@ def main():
                                    "execute more"}
     if "p2p" in st:
         a = 20.0 * tuned["p2p_pairs"] / (st["p2p"] * 1e-3) / 1e12
+        # the FMA pipe's own bound: 13 FP32 lane operations per pair (3 differences, 3 for r^2,
+        # r^-2, q r^-1, its product with r^-2, the potential sum, 3 gradient FMAs)
+        floor_ms = 13.0 * tuned["p2p_pairs"] / (152 * 128 * pk.get("sm_max_mhz", 2070.0) * 1e6) * 1e3
         kern["p2p"] = {"ms": st["p2p"], "bound": "fp32-cuda-core", "achieved": a, "peak": fp32_peak,
-                       "unit": "TFLOP/s", "frac": a / fp32_peak, "pairs": tuned["p2p_pairs"]}
+                       "unit": "TFLOP/s", "frac": a / fp32_peak, "pairs": tuned["p2p_pairs"],
+                       "fma_pipe_floor_ms": floor_ms, "frac_of_fma_pipe_floor": floor_ms / st["p2p"]}
     dom = max((k for k in st if k in kern), key=lambda k: st[k], default=None)
     roof = None
     if dom:
