@@ -314,14 +314,22 @@ void launch_scatter_ranked(const uint32_t* code, int n, const int* off, const in
 
 // Stable order inside each leaf (ascending input index), which makes the body
 // order identical to the per-level stable counting sort of tree.cpp:43-74.
+// A body on or near a face of its leaf, or outside it (|u| >= 1/2 - 2^-20 in
+// scaled units): the near field then takes the r = 0 test on every pair.
+__device__ __forceinline__ bool at_leaf_face(float4 b)
+{
+    return fmaxf(fabsf(b.x), fmaxf(fabsf(b.y), fabsf(b.z))) >= 0.5f - 0x1p-20f;
+}
+
 __global__ void __launch_bounds__(256) k_leaf_sort(const int* off, int nleaf, const int* tmp_idx, const float4* uq,
-                                                   int* order, float4* atoms, int* inv, int* counts)
+                                                   int* order, float4* atoms, int* inv, int* counts, int* edge)
 {
     const int lane = threadIdx.x & 31;
     const int leaf = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (leaf >= nleaf) return;
     if (counts && lane == 0) counts[leaf] = 0;  // consumed by the scan: zero for the next step
     const int b = off[leaf], n = off[leaf + 1] - b;
+    bool face = false;
     if (n <= 32) {
         int v = lane < n ? tmp_idx[b + lane] : 0x7fffffff;
         int rank = 0;
@@ -331,8 +339,10 @@ __global__ void __launch_bounds__(256) k_leaf_sort(const int* off, int nleaf, co
         }
         if (lane < n) {
             order[b + rank] = v;
-            atoms[b + rank] = uq[v];
+            const float4 a = uq[v];
+            atoms[b + rank] = a;
             inv[v] = b + rank;
+            face = at_leaf_face(a);
         }
     } else {
         for (int e = lane; e < n; e += 32) {
@@ -340,20 +350,24 @@ __global__ void __launch_bounds__(256) k_leaf_sort(const int* off, int nleaf, co
             int rank = 0;
             for (int j = 0; j < n; j++) rank += (tmp_idx[b + j] < v);
             order[b + rank] = v;
-            atoms[b + rank] = uq[v];
+            const float4 a = uq[v];
+            atoms[b + rank] = a;
             inv[v] = b + rank;
+            face |= at_leaf_face(a);
         }
     }
+    const unsigned any = __ballot_sync(0xffffffffu, face);
+    if (edge && lane == 0) edge[leaf] = any != 0u;
 }
 
 void launch_leaf_sort(const int* offsets, int nleaf, int* tmp_idx, const float4* uq, const uint32_t* code, int* order,
-                      float4* atoms, int* inv, int* counts, cudaStream_t s)
+                      float4* atoms, int* inv, int* counts, cudaStream_t s, int* edge)
 {
     (void)code;
     long threads = (long)nleaf * 32;
     COUNT_LAUNCH();
     k_leaf_sort<<<(int)((threads + 255) / 256), 256, 0, s>>>(offsets, nleaf, tmp_idx, uq, order, atoms, inv,
-                                                            counts);
+                                                            counts, edge);
 }
 
 // ------------------------------------------------------------------ P2M
@@ -792,7 +806,7 @@ __device__ __forceinline__ void p2p_leaf(const P2PArgs& a, uint32_t tcode, P2PSh
     const int tb = a.off[tcode], nt = a.off[tcode + 1] - tb;
     if (nt == 0) return;  // uniform over the CTA
     // source leaves of the stencil
-    int cnt = 0;
+    int cnt = 0, eflag = 0;
     if (tid < a.nst) {
         int vx = tx + a.stencil[3 * tid], vy = ty + a.stencil[3 * tid + 1], vz = tz + a.stencil[3 * tid + 2];
         bool ok = true;
@@ -805,6 +819,7 @@ __device__ __forceinline__ void p2p_leaf(const P2PArgs& a, uint32_t tcode, P2PSh
             uint32_t sc = morton_encode(vx, vy, vz);
             sh.e_beg[tid] = a.off[sc];
             cnt = a.off[sc + 1] - a.off[sc];
+            eflag = a.leaf_edge[sc];
         } else {
             sh.e_beg[tid] = 0;
         }
@@ -826,17 +841,12 @@ __device__ __forceinline__ void p2p_leaf(const P2PArgs& a, uint32_t tcode, P2PSh
         __syncthreads();
         if (tid == 0) sh.e_off[a.nst] = sh.ws[0] + sh.ws[1] + sh.ws[2] + sh.ws[3];
     }
-    __syncthreads();
+    // any staged leaf (the target leaf included: a target outside its leaf can
+    // meet the image of a body well inside another leaf) with a body at a face:
+    // then every pass takes the r = 0 test (flags from the leaf sort)
+    const bool any_edge = __syncthreads_or(eflag) != 0;
     const int total = sh.e_off[a.nst], nself = sh.e_off[1];
     float* srcf = reinterpret_cast<float*>(sh.src);
-    // a target outside its leaf (outside the box) can meet the image of a body
-    // that lies well inside another leaf: then every pass takes the r = 0 test
-    bool tedge = false;
-    for (int i = tid; i < nt; i += P2P_THREADS) {
-        const float4 b = a.atoms[tb + i];
-        tedge |= fmaxf(fabsf(b.x), fmaxf(fabsf(b.y), fabsf(b.z))) >= 0.5f - 0x1p-20f;
-    }
-    const bool target_edge = __syncthreads_or(tedge) != 0;
     for (int t0 = 0; t0 < nt; t0 += P2P_MAXT) {
         const int ntc = min(P2P_MAXT, nt - t0);
         const float4* tgt = a.atoms + tb + t0;
@@ -848,14 +858,12 @@ __device__ __forceinline__ void p2p_leaf(const P2PArgs& a, uint32_t tcode, P2PSh
             __syncthreads();
             // warp w copies whole source leaves w, w+4, ...: lane = body of the leaf,
             // clipped to this pass's window [s0, s0+ns); far zero-charge padding to nsp
-            bool edge = false;
             for (int e = warp; e < a.nst; e += 4) {
                 const int b0 = max(sh.e_off[e], s0), b1 = min(sh.e_off[e + 1], s0 + ns);
                 const float4 d = sh.e_d[e];
                 const int gb = sh.e_beg[e] - sh.e_off[e];
                 for (int g = b0 + lane; g < b1; g += 32) {
                     const float4 b = a.atoms[gb + g];
-                    edge |= fmaxf(fabsf(b.x), fmaxf(fabsf(b.y), fabsf(b.z))) >= 0.5f - 0x1p-20f;
                     const int r = g - s0;
                     float* rec = srcf + 8 * (r >> 1) + (r & 1);
                     rec[0] = b.x + d.x;
@@ -870,7 +878,7 @@ __device__ __forceinline__ void p2p_leaf(const P2PArgs& a, uint32_t tcode, P2PSh
                 rec[0] = rec[2] = rec[4] = P2P_FAR;
                 rec[6] = 0.f;
             }
-            const bool any_edge = (__syncthreads_or(edge) != 0) || target_edge;
+            __syncthreads();
             // this warp's quarter of the source steps; the steps holding the
             // target leaf's own bodies need the r = 0 test
             const int nsteps = nsp / SPS;

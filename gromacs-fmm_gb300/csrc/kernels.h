@@ -118,9 +118,10 @@ void launch_scatter(const uint32_t* code, int n, int* cursor, int* tmp_idx, cuda
 void launch_scatter_ranked(const uint32_t* code, int n, const int* off, const int* rank, int* tmp_idx,
                            cudaStream_t s);
 // Also zeroes counts[0..nleaf) (consumed by then) when counts != NULL.
-// inv[input index] = sorted position (the inverse of order).
+// inv[input index] = sorted position (the inverse of order); edge[leaf] (when
+// not NULL) = 1 if a body of the leaf lies on or near its faces or outside it.
 void launch_leaf_sort(const int* offsets, int nleaf, int* tmp_idx, const float4* uq, const uint32_t* code, int* order,
-                      float4* atoms, int* inv, int* counts, cudaStream_t s);
+                      float4* atoms, int* inv, int* counts, cudaStream_t s, int* edge = nullptr);
 void launch_p2m(int P, const int* offsets, int nleaf, const float4* atoms, float* M_leaf, int Rpad, cudaStream_t s);
 // P2M of the leaves and M2M of their parents in one launch (8 sibling leaves per
 // CTA).  Returns false, launching nothing, when the order's shared memory does
@@ -142,6 +143,7 @@ struct P2PArgs {
     const int* stencil;       // nst offsets (3 ints), the zero offset first
     int nst;
     float4* field;            // sorted near field (phi, grad), scaled units
+    const int* leaf_edge;     // per leaf: a body on or near its faces or outside it (from the leaf sort)
 };
 int p2p_variants();
 // Near fields of many systems in one persistent launch (per_sm CTAs per SM).

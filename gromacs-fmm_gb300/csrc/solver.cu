@@ -156,6 +156,7 @@ struct gbfmm_handle {
     float4* d_uq = nullptr;
     int *d_counts = nullptr, *d_off = nullptr, *d_scan = nullptr, *d_tmp = nullptr;
     int *d_order = nullptr, *d_inv = nullptr;  // sorted -> input index, and its inverse
+    int* d_leaf_edge = nullptr;                 // per leaf: a body on or near a face (the P2P r = 0 test)
     float4 *d_atoms = nullptr, *d_near = nullptr, *d_far = nullptr;
     float *d_M = nullptr, *d_L = nullptr;
     float* Mlev[8] = {};
@@ -304,6 +305,7 @@ static int layout(gbfmm_handle* h, Arena& a)
     h->d_tmp = a.take<int>(n);
     h->d_order = a.take<int>(n);
     h->d_inv = a.take<int>(n);
+    h->d_leaf_edge = a.take<int>(h->nleaf);
     h->d_atoms = a.take<float4>(n);
     h->d_near = a.take<float4>(n);
     h->d_far = a.take<float4>(n);
@@ -577,6 +579,7 @@ static P2PArgs p2p_args(const gbfmm_handle* h)
     pa.stencil = h->d_p2p_st;
     pa.nst = h->n_p2p_st;
     pa.field = h->d_near;
+    pa.leaf_edge = h->d_leaf_edge;
     return pa;
 }
 
@@ -641,7 +644,7 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
     }
     launch_scatter_ranked(h->d_code, n, h->d_off, h->d_inv, h->d_tmp, s);
     launch_leaf_sort(h->d_off, h->nleaf, h->d_tmp, h->d_uq, h->d_code, h->d_order, h->d_atoms, h->d_inv,
-                     h->d_counts, s);
+                     h->d_counts, s, h->d_leaf_edge);
     mark(h, 1);
     // The near field needs only the tree: in graph mode it forks onto its own
     // stream and overlaps the far-field chain below (joined before finalize);
