@@ -792,9 +792,9 @@ struct P2PShared {
 // The r = 0 test is applied to the target leaf's own bodies only.  Bodies of two
 // different leaves cannot coincide when every staged body lies strictly inside
 // its leaf (|u| < 1/2 - 2^-20 in scaled units: the rounding of u and of the
-// integer shift is far below that margin); a CTA that stages any body outside
-// that range (bodies on or near a leaf face, or outside the box) applies the
-// test to every source.
+// integer shift is far below that margin); a CTA whose stencil holds any leaf
+// with a body outside that range (bodies on or near a leaf face, or outside the
+// box; flagged per leaf by the leaf sort) applies the test to every source.
 template <int LT, int KM = 3>
 __device__ __forceinline__ void p2p_leaf(const P2PArgs& a, uint32_t tcode, P2PShared& sh)
 {
