@@ -191,3 +191,24 @@ def test_systems_generator(systems):
     xb, qb, bb = systems.cfg_96k()
     assert len(qb) == 95600 and np.sum(qb == 1.0) == 100 and np.sum(qb == -1.0) == 100
     assert abs(float(qb.astype(np.float64).sum())) < 1e-2
+
+
+def test_batch_arguments_rejected_before_device_use(pkg):
+    import ctypes
+    lib = pkg.lib()
+    ip = ctypes.POINTER(ctypes.c_int)
+    b = ctypes.c_void_p()
+    off = np.array([0, 10, 5], np.int32)  # decreasing
+    o = np.array([4, 4], np.int32)
+    d = np.array([1, 1], np.int32)
+    assert lib.gbfmm_batch_create(2, off.ctypes.data_as(ip), o.ctypes.data_as(ip), d.ctypes.data_as(ip), 4, 0, 0,
+                                  ctypes.byref(b)) == 1
+    assert not b.value
+    off = np.array([1, 10, 20], np.int32)  # must start at 0
+    assert lib.gbfmm_batch_create(2, off.ctypes.data_as(ip), o.ctypes.data_as(ip), d.ctypes.data_as(ip), 4, 0, 0,
+                                  ctypes.byref(b)) == 1
+    assert lib.gbfmm_batch_create_mixed(2, off.ctypes.data_as(ip), o.ctypes.data_as(ip), d.ctypes.data_as(ip),
+                                        None, 4, 0, ctypes.byref(b)) == 1
+    assert lib.gbfmm_batch_set_tuning(None, 0, 4, 0, 0) == 1
+    assert lib.gbfmm_batch_get_tuning(None, None, None, None, None) == 1
+    assert lib.gbfmm_batch_autotune(None, None, None, None, 3, None) == 1

@@ -89,3 +89,33 @@ def test_training_tuples():
                 falls += int(e[-1] < e[0])
                 total += 1
     assert falls == total
+
+
+def test_plain_depth_rule(pkg):
+    """gbfmm_plain_depth: the deepest level with at least 16 bodies per leaf
+    (depths 1-7), the reference-like fixed depth the checked choice falls back to."""
+    lib = pkg.lib()
+    lib.gbfmm_plain_depth.restype = ctypes.c_int
+    lib.gbfmm_plain_depth.argtypes = [ctypes.c_int]
+    for n in (10, 300, 1023, 1024, 9000, 95600, 250002, 1002002, 2 ** 31 - 1):
+        d = lib.gbfmm_plain_depth(n)
+        want = 1
+        while n / 8.0 ** (want + 1) >= 16 and want < 7:
+            want += 1
+        assert d == want, n
+        if 1 < d < 7:
+            assert 16 <= n / 8.0 ** d < 128, n
+
+
+def test_tuner_choose_rejects_bad_arguments_before_device_use(pkg):
+    tuner = G.load_module("tuner")
+    f = tuner._sig().gbfmm_tuner_choose
+    q = np.ones(4, np.float32)
+    x = np.zeros(12, np.float32)
+    box = np.eye(3, dtype=np.float32).reshape(-1) * 2
+    fp = ctypes.POINTER(ctypes.c_float)
+    out = tuner.TunerChoice()
+    args = [q.ctypes.data_as(fp), x.ctypes.data_as(fp), box.ctypes.data_as(fp)]
+    assert f(None, 4, *args, 4, 1e-3, 1.5, ctypes.byref(out)) == 1   # no network
+    assert f(None, 0, *args, 4, 1e-3, 1.5, ctypes.byref(out)) == 1   # no atoms
+    assert f(None, 4, *args, 4, 1e-3, 1.5, None) == 1                # no output
