@@ -212,3 +212,17 @@ def test_batch_arguments_rejected_before_device_use(pkg):
     assert lib.gbfmm_batch_set_tuning(None, 0, 4, 0, 0) == 1
     assert lib.gbfmm_batch_get_tuning(None, None, None, None, None) == 1
     assert lib.gbfmm_batch_autotune(None, None, None, None, 3, None) == 1
+
+
+def test_bench_pair_count_matches_the_reference_lists(oracle, systems):
+    """bench.py's P2P pair count (the unit of its roofline) equals the sum over
+    the reference-ordered P2P list of |target leaf| x |source leaf|."""
+    import bench
+    xyz, q, box = systems.water_ion_box(3000, 4.5, n_na=5, n_cl=5, seed=9)
+    L, D = float(box[0]), 3
+    tree = oracle.zeta_tree(xyz.astype(np.float64), L, D)
+    leaves = np.nonzero(tree["depth"] == D)[0]
+    counts = tree["body_num"][leaves]  # BFS order = Morton order of the leaves
+    t, s, _ = oracle.zeta_lists(D, 4, L)["p2p"]
+    want = int(np.sum(tree["body_num"][t].astype(np.int64) * tree["body_num"][s]))
+    assert bench.p2p_pair_count(counts, D) == want
