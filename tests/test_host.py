@@ -226,3 +226,14 @@ def test_bench_pair_count_matches_the_reference_lists(oracle, systems):
     t, s, _ = oracle.zeta_lists(D, 4, L)["p2p"]
     want = int(np.sum(tree["body_num"][t].astype(np.int64) * tree["body_num"][s]))
     assert bench.p2p_pair_count(counts, D) == want
+
+
+@pytest.mark.parametrize("depth", [2, 3, 4])
+def test_bench_m2l_pair_count_matches_the_reference_lists(oracle, depth):
+    """bench.py's M2L pair count (levels 1..depth; the root row is the lattice
+    operator's) equals the reference-ordered M2L list's entries with targets below
+    the root."""
+    import bench
+    t, _, _ = oracle.zeta_lists(depth, 4, 1.0)["m2l"]
+    below_root = int(np.sum(t >= 1))  # BFS index 0 is the root
+    assert bench.m2l_pairs(depth) == below_root
