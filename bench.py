@@ -696,7 +696,8 @@ def main():
 
     tuned, plain = results["tuned"], results["plain"]
     pk, src = peaks()
-    fp32_peak = 152 * 128 * 2 * pk.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    fp32_peak = sms * 128 * 2 * pk.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
     P, D = tuned["P"], tuned["D"]
     st = tuned["stages"]
     kern = {}
@@ -715,7 +716,7 @@ def main():
         a = 20.0 * tuned["p2p_pairs"] / (st["p2p"] * 1e-3) / 1e12
         # the FMA pipe's own bound: 13 FP32 lane operations per pair (3 differences, 3 for r^2,
         # r^-2, q r^-1, its product with r^-2, the potential sum, 3 gradient FMAs)
-        floor_ms = 13.0 * tuned["p2p_pairs"] / (152 * 128 * pk.get("sm_max_mhz", 2070.0) * 1e6) * 1e3
+        floor_ms = 13.0 * tuned["p2p_pairs"] / (sms * 128 * pk.get("sm_max_mhz", 2070.0) * 1e6) * 1e3
         kern["p2p"] = {"ms": st["p2p"], "bound": "fp32-cuda-core", "achieved": a, "peak": fp32_peak,
                        "unit": "TFLOP/s", "frac": a / fp32_peak, "pairs": tuned["p2p_pairs"],
                        "fma_pipe_floor_ms": floor_ms, "frac_of_fma_pipe_floor": floor_ms / st["p2p"]}
@@ -727,8 +728,8 @@ def main():
         roof = {"kernel": dom, "bound": k["bound"], "achieved": k["achieved"], "peak": k["peak"], "unit": k["unit"],
                 "frac": k["frac"], "traffic": tb, "traffic_source": tsrc,
                 "peak_source": (f"bf16 dense, MEASURED_PEAKS.json ({src})" if k["bound"] == "tensor" else
-                                "nominal 152 SMs x 128 FP32 lanes x 2 x sm_max_mhz (no FP32 entry in "
-                                "MEASURED_PEAKS.json)")}
+                                f"nominal {sms} SMs x 128 FP32 lanes x 2 x sm_max_mhz (no FP32 entry in "
+                                "MEASURED_PEAKS.json)"), "sms": sms}
     line = {"metric": METRIC, "value": tuned["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": tuned["ms"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+bf16x3" if tuned["prec"] == 1 else (

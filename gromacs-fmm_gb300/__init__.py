@@ -89,6 +89,8 @@ def lib():
                                            ip, ip]),
             "gbfmm_debug_operator": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, ip, dp]),
             "gbfmm_debug_harmonics": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, dp, dp]),
+            "gbfmm_debug_bounded_wait": (ctypes.c_int, [ctypes.c_uint, vp]),
+            "gbfmm_batch_status": (ctypes.c_int, [vp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -348,6 +350,10 @@ class BatchSolver:
                                                 ctypes.c_void_p(int(charges_ptr)), _fp(b),
                                                 ctypes.c_void_p(int(stream_ptr))))
 
+    def status(self):
+        """Waits for the last step; raises FmmError if a system reported an error."""
+        _check(lib().gbfmm_batch_status(self._b))
+
     def tuning(self):
         v = [ctypes.c_int() for _ in range(4)]
         _check(lib().gbfmm_batch_get_tuning(self._b, *[ctypes.byref(x) for x in v]))
@@ -392,6 +398,12 @@ def debug_operator(order, kind, index, images=4):
     _check(lib().gbfmm_debug_operator(order, images, kind, index, mat.ctypes.data_as(dp), ctypes.byref(dim),
                                       cv.ctypes.data_as(dp)))
     return mat, cv
+
+
+def debug_bounded_wait(polls, stream_ptr=0):
+    """The library's bounded mbarrier wait on a barrier nothing completes
+    (gbfmm_debug_bounded_wait): raises FmmError(GBFMM_ERR_TIMEOUT) when it gives up."""
+    _check(lib().gbfmm_debug_bounded_wait(int(polls), ctypes.c_void_p(int(stream_ptr))))
 
 
 def debug_harmonics(order, kind, d):

@@ -34,13 +34,26 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
     return ok != 0;
 }
 
-// Bounded wait: gives up after ~2^24 polls (well over a second) and ORs 'bit'
-// into *err.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int bit = 2)
+// Default poll limit of the bounded waits: 2^24 polls, well over a second.
+constexpr uint32_t WAIT_POLLS_DEFAULT = 1u << 24;
+
+// Bounded wait: gives up after 'limit' polls and ORs 'bit' into *err.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int bit = 2,
+                                          uint32_t limit = WAIT_POLLS_DEFAULT)
 {
-    for (uint32_t i = 0; i < (1u << 24); i++)
+    for (uint32_t i = 0; i < limit; i++)
         if (mbar_try_wait(bar, parity)) return true;
     atomicOr(err, bit);
+    return false;
+}
+
+// Drain after a give-up: waits (again bounded, without reporting) for a phase
+// whose asynchronous copies or MMAs were issued, so that a CTA does not release
+// TMEM or exit while work it issued may still write its shared memory.
+__device__ __forceinline__ bool mbar_drain(uint64_t* bar, uint32_t parity, uint32_t limit = WAIT_POLLS_DEFAULT)
+{
+    for (uint32_t i = 0; i < limit; i++)
+        if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
 

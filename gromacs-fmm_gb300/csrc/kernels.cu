@@ -22,6 +22,25 @@ namespace gbfmm {
 std::atomic<long> g_kernel_launches{0};
 #define COUNT_LAUNCH() g_kernel_launches.fetch_add(1, std::memory_order_relaxed)
 
+int sm_count()
+{
+    static std::atomic<int> cache[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        cudaGetLastError();
+        return 1;
+    }
+    int v = cache[dev].load(std::memory_order_relaxed);
+    if (v <= 0) {
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) {
+            cudaGetLastError();
+            v = 1;
+        }
+        cache[dev].store(v, std::memory_order_relaxed);
+    }
+    return v;
+}
+
 // ------------------------------------------------------------------ tree
 
 // Sum over the tree-key blocks of one of the four per-block partials (dipole x, y,
@@ -974,9 +993,7 @@ int p2p_batch_shapes() { return 5; }
 void launch_p2p_batch(const P2PBatchArgs& b, int shape, int per_sm, cudaStream_t s)
 {
     if (b.nitems <= 0) return;
-    int sms = 152, dev = 0;
-    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int grid = std::min(b.nitems, sms * std::max(1, std::min(per_sm, 5)));
+    const int grid = std::min(b.nitems, sm_count() * std::max(1, std::min(per_sm, 5)));
     COUNT_LAUNCH();
     if (shape == 1) k_p2p_batch<4><<<grid, P2P_THREADS, 0, s>>>(b);
     else if (shape == 2) k_p2p_batch<16><<<grid, P2P_THREADS, 0, s>>>(b);
@@ -1003,10 +1020,7 @@ void launch_p2p(const P2PArgs& a, int variant, cudaStream_t s, int* counter)
         else k_p2p<8><<<nleaf, P2P_THREADS, 0, s>>>(a);
         return;
     }
-    int sms = 152;
-    int dev = 0;
-    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int grid = std::min(nleaf, sms * (per_sm + 1));  // 2..5 CTAs per SM
+    const int grid = std::min(nleaf, sm_count() * (per_sm + 1));  // 2..5 CTAs per SM
     if (shape == 1) k_p2p_queue<4><<<grid, P2P_THREADS, 0, s>>>(a, counter, nleaf);
     else if (shape == 2) k_p2p_queue<16><<<grid, P2P_THREADS, 0, s>>>(a, counter, nleaf);
     else k_p2p_queue<8><<<grid, P2P_THREADS, 0, s>>>(a, counter, nleaf);
@@ -1473,7 +1487,8 @@ __global__ void __launch_bounds__(TOP_THREADS) k_top(const TopArgs a)
             bulk_g2s(a.from == 3 ? in : a.from == 2 ? mid : m1, src_in, b_in, &bar);
         }
         __syncthreads();
-        mbar_wait(&bar, 0, a.err, 1);
+        if (!mbar_wait(&bar, 0, a.err, 1, a.wait_limit))
+            mbar_drain(&bar, 0, a.wait_limit);  // no exit while the copies may still land
         if (a.from == 3) top_m2m(in, red, mid, a.M2 + (size_t)8 * g * Rpad, 8, At, R, Rpad);
         if (a.from >= 2) top_m2m(mid, red, m1, a.M1 + (size_t)g * Rpad, 1, At, R, Rpad);
     } else {
@@ -1567,6 +1582,27 @@ void launch_top(const TopArgs& a, cudaStream_t s)
     if (staged) k_top<true><<<8, TOP_THREADS, shm, s>>>(a);
     else k_top<false><<<8, TOP_THREADS, shm, s>>>(a);
     if (!a.lattice) launch_root_lattice(a.root, s);
+}
+
+// ------------------------------------------------------------------ bounded-wait probe
+
+__global__ void k_wait_probe(uint32_t polls, int* err)
+{
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+    // nothing arrives on the barrier: phase 0 never completes
+    if (threadIdx.x == 0) mbar_wait(&bar, 0, err, 1, polls);
+    __syncthreads();
+}
+
+void launch_wait_probe(uint32_t polls, int* err, cudaStream_t s)
+{
+    COUNT_LAUNCH();
+    k_wait_probe<<<1, 32, 0, s>>>(polls, err);
 }
 
 // ------------------------------------------------------------------ finalize

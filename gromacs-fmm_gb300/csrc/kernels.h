@@ -104,12 +104,18 @@ struct TreeArgs {
 };
 // Leaf counts up to this size are scanned by the tree-key kernel's last block.
 constexpr int TREE_EPILOGUE_MAX_LEAVES = 1 << 15;
-constexpr int TREE_MAX_BLOCKS = 4 * 152;
-constexpr int FINAL_MAX_BLOCKS = 4 * 152;
+// Caps of the grid-stride tree-key and finalize grids (their per-block partial
+// sums are reduced by one warp): about four blocks per SM on a 152-SM GB300.
+constexpr int TREE_MAX_BLOCKS = 608;
+constexpr int FINAL_MAX_BLOCKS = 608;
 int tree_blocks(int n);
 int final_blocks(int n);
 
 extern std::atomic<long> g_kernel_launches;
+
+// Streaming multiprocessors of the current device (cudaDevAttrMultiProcessorCount,
+// cached per device).
+int sm_count();
 
 void launch_tree_keys(const TreeArgs& a, cudaStream_t s);
 void launch_exclusive_scan(const int* in, int* out, int n, int* scratch, cudaStream_t s);
@@ -213,11 +219,17 @@ struct TopArgs {
     int natoms;
     int* done;            // zero at launch
     int* err;             // bit 1: the bounded wait for the staged copies gave up
+    uint32_t wait_limit = 1u << 24;  // polls of the bounded wait
 };
 constexpr int TOP_STAGE_MAX_R = 49;
 constexpr int TOP_LATTICE_MAX_R = TOP_STAGE_MAX_R;  // larger: the multi-CTA k_root_lattice
 size_t top_smem_bytes(int R);
 void launch_top(const TopArgs& a, cudaStream_t s);
+
+// Bounded-wait probe: one warp waits on an mbarrier that nothing completes,
+// with no copies or MMAs in flight; after 'polls' polls the wait gives up and
+// sets bit 1 of *err.  Exercises the give-up path of the bounded waits.
+void launch_wait_probe(uint32_t polls, int* err, cudaStream_t s);
 
 struct FinalArgs {
     const StepConst* sc;

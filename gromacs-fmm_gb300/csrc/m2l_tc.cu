@@ -255,14 +255,22 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(const __grid_constant_
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
+    const uint32_t lim = a.wait_limit;
     bool ok = true;
 
+    // On a bounded wait that gives up, the waiting role records the error, stops
+    // issuing work and drains what it issued (again bounded); the CTA then skips
+    // the read-back and the adds, and releases TMEM only after the drain.
     if (warp == 0 && lane == 0) {
         // ---------------------------------------------------------------- producer
         const uint32_t tx_bytes = (split ? 2u : 1u) * (uint32_t)(a.k_atoms * rows * 128 + b_bytes);
+        int issued = 0;
         for (int i = 0; i < ne; i++) {
             const int st = i % NS, u = i / NS;
-            if (i >= NS) ok = mbar_wait(&bar_empty[st], (u - 1) & 1, a.err) && ok;
+            if (i >= NS && !mbar_wait(&bar_empty[st], (u - 1) & 1, a.err, 2, lim)) {
+                ok = false;
+                break;
+            }
             const CEntry en = ent[i];
             uint8_t* A_hi = sm + st * stage_bytes;
             uint8_t* A_lo = A_hi + a_bytes;
@@ -286,12 +294,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(const __grid_constant_
                 }
             }
             bulk_g2s(B, a.bimg + (size_t)en.op * 2 * b_bytes, (split ? 2u : 1u) * b_bytes, &bar_full[st]);
+            issued = i + 1;
         }
+        if (!ok)  // the copies this thread issued: the last phase of every stage
+            for (int st = 0; st < min(NS, issued); st++) mbar_drain(&bar_full[st], ((issued - 1 - st) / NS) & 1, lim);
     } else if (warp == 1 && lane == 0) {
         // ---------------------------------------------------------------- MMA issuer
         for (int i = 0; i < ne; i++) {
             const int st = i % NS, u = i / NS;
-            ok = mbar_wait(&bar_full[st], u & 1, a.err) && ok;
+            if (!mbar_wait(&bar_full[st], u & 1, a.err, 2, lim)) {
+                ok = false;
+                break;
+            }
             tc_fence_after();
             const uint32_t a_hi = smem_u32(sm + st * stage_bytes), a_lo = a_hi + (uint32_t)a_bytes,
                            b_hi = a_hi + (uint32_t)((split ? 2 : 1) * a_bytes), b_lo = b_hi + (uint32_t)b_bytes;
@@ -318,13 +332,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(const __grid_constant_
         // barrier's first phase completes), the others wait at the CTA barrier
         if (ne > 0) {
             mma_commit(bar_done);
-            ok = mbar_wait(bar_done, 0, a.err) && ok;
+            if (!mbar_wait(bar_done, 0, a.err, 2, lim)) {
+                ok = false;
+                mbar_drain(bar_done, 0, lim);
+            }
         }
     }
     tc_fence_before();
-    __syncthreads();
+    const bool failed = __syncthreads_or(!ok) != 0;
     tc_fence_after();
-    if (ne > 0) {
+    if (ne > 0 && !failed) {
         float* dst = a.dst_lvl[k];
         const int t = 32 * warp + lane;
         const bool wv = t < rows;

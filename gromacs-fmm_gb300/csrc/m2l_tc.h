@@ -87,6 +87,7 @@ struct alignas(64) TcArgs {
     const CTask* tasks;          // level, octant, q0 = tile index, entry range
     float* dst_lvl[TC_MAXLEV];
     int* err;                    // bit 1: a bounded wait gave up
+    uint32_t wait_limit;         // polls of each bounded wait (WAIT_POLLS_DEFAULT)
     int Rpad;
     int k_atoms, img_bytes, tmem_cols, nchunk;
     int nprod;                   // 3: hi*hi + hi*lo + lo*hi, 1: hi*hi

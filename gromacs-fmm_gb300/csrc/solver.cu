@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "../../include/gbfmm.h"
+#include "async.cuh"
 #include "common.cuh"
 #include "kernels.h"
 #include "m2l_tc.h"
@@ -384,7 +385,7 @@ static int build_tasks(gbfmm_handle* h)
     if (h->prm.m2l_split <= 0) {
         long tiles = 0;
         for (int k = 1; k <= D; k++) tiles += 8 * std::max<long>(1, (1L << (3 * (k - 1))) / CT_TILE);
-        while (tiles * split < 2 * 152 && split < 8) split *= 2;
+        while (tiles * split < 2 * sm_count() && split < 8) split *= 2;
     }
     if (h->prm.flags & GBFMM_FLAG_DETERMINISTIC) split = 1;
     h->m2l_task0 = (int)tasks.size();
@@ -432,7 +433,7 @@ static int build_tasks(gbfmm_handle* h)
         if (h->prm.m2l_split > 0) {
             while (def < 3 && (1 << def) < h->prm.m2l_split) def++;
         } else {
-            while (tiles * (1L << def) < 152 && def < 3) def++;
+            while (tiles * (1L << def) < sm_count() && def < 3) def++;
         }
         const bool det = (h->prm.flags & GBFMM_FLAG_DETERMINISTIC) != 0;
         if (det) def = 0;
@@ -492,6 +493,7 @@ static int make_tc_args(gbfmm_handle* h)
     a->entries = h->d_entries;
     a->tasks = h->d_tc_tasks_v[h->tc_split_v];
     a->err = h->d_flags + 1;
+    a->wait_limit = WAIT_POLLS_DEFAULT;
     a->Rpad = h->Rpad;
     a->k_atoms = pl.k_atoms;
     a->img_bytes = pl.img_bytes;
@@ -1375,6 +1377,26 @@ extern "C" int gbfmm_debug_operator(int order, int images, int kind, int index, 
     return fail(GBFMM_ERR_ARG, "kind %d", kind);
 }
 
+extern "C" int gbfmm_debug_bounded_wait(unsigned polls, void* stream)
+{
+    if (polls == 0) return fail(GBFMM_ERR_ARG, "polls must be positive");
+    int* d_err = nullptr;
+    CK(cudaMalloc(&d_err, sizeof(int)));
+    cudaStream_t s = (cudaStream_t)stream;
+    int flag = 0;
+    cudaError_t e = cudaMemsetAsync(d_err, 0, sizeof(int), s);
+    if (e == cudaSuccess) {
+        launch_wait_probe(polls, d_err, s);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&flag, d_err, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(d_err);
+    if (e != cudaSuccess) return fail(GBFMM_ERR_CUDA, "bounded-wait probe: %s", cudaGetErrorString(e));
+    if (flag) return fail(GBFMM_ERR_TIMEOUT, "the probe's bounded wait gave up after %u polls", polls);
+    return GBFMM_OK;
+}
+
 extern "C" int gbfmm_debug_harmonics(int order, int kind, const double* d, double* out)
 {
     if (order < 0 || order > 40 || !d || !out) return fail(GBFMM_ERR_ARG, "bad argument");
@@ -1771,6 +1793,8 @@ extern "C" int gbfmm_batch_autotune(gbfmm_batch* b, const void* d_coords, const 
     return GBFMM_OK;
 }
 
+static int batch_check(gbfmm_batch* b);
+
 extern "C" int gbfmm_batch_execute(gbfmm_batch* b, const float* coords, const float* charges, const float* box_edges,
                                    float* forces, float* potentials, double* energies)
 {
@@ -1786,16 +1810,37 @@ extern "C" int gbfmm_batch_execute(gbfmm_batch* b, const float* coords, const fl
     if (potentials) CK(cudaMemcpyAsync(potentials, b->d_pots, sizeof(float) * b->natoms, cudaMemcpyDeviceToHost, b->master));
     if (energies) CK(cudaMemcpyAsync(energies, b->d_energy, sizeof(double) * b->n_sys, cudaMemcpyDeviceToHost, b->master));
     CK(cudaStreamSynchronize(b->master));
-    // non-finite coordinates: each system's flag
+    return batch_check(b);
+}
+
+// Reads every system's step flags (bit 0 non-finite input, bits 1-2 a bounded
+// wait of the tensor-core M2L or of the upper-tree kernel gave up); on an error
+// clears the flags and the step counters, as fetch() does for one system.
+static int batch_check(gbfmm_batch* b)
+{
+    CK(cudaStreamSynchronize(b->master));
+    int rc = GBFMM_OK;
     for (gbfmm_handle* h : b->hs) {
         int fl[4];
         CK(cudaMemcpy(fl, h->d_flags, sizeof(fl), cudaMemcpyDeviceToHost));
-        if (fl[0] || fl[1]) {
+        if (fl[0] || fl[1] || fl[2]) {
             CK(cudaMemset(h->d_flags, 0, sizeof(int) * 4));
-            return fail(fl[1] ? GBFMM_ERR_TIMEOUT : GBFMM_ERR_COORD, "a system of the batch reported an error");
+            if (fl[1] || fl[2]) CK(cudaMemset(h->d_counts, 0, sizeof(int) * (h->nleaf + 1 + 4)));
+            if (rc == GBFMM_OK)
+                rc = fail(fl[1] || fl[2] ? GBFMM_ERR_TIMEOUT : GBFMM_ERR_COORD,
+                          fl[1] ? "a bounded device wait in a system's tensor-core M2L gave up"
+                                : fl[2] ? "a bounded device wait in a system's upper-tree kernel gave up"
+                                        : "a system of the batch has a non-finite coordinate");
         }
     }
-    return GBFMM_OK;
+    if (rc != GBFMM_OK) b->have_result = false;
+    return rc;
+}
+
+extern "C" int gbfmm_batch_status(gbfmm_batch* b)
+{
+    if (!b) return fail(GBFMM_ERR_ARG, "batch is NULL");
+    return batch_check(b);
 }
 
 extern "C" int gbfmm_batch_device_outputs(gbfmm_batch* b, void** f, void** p, void** e)

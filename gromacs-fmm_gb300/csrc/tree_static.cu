@@ -16,6 +16,13 @@
 // contents; the counters that must start at zero are cleared on every call.
 // Calls that overlap on the GPU (different streams, or different host threads)
 // race on the shared scratch: order them.
+//
+// The array's device address is looked up (cudaGetSymbolAddress, with the
+// device current) on the first call in each CUDA context and kept for that
+// context; a call from a new context (after cudaDeviceReset, say) looks it up
+// again.  The box-dependent constants reach the device as a kernel argument
+// (copied at launch), not by a copy from host memory.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -53,10 +60,42 @@ static __device__ __align__(256) unsigned char g_tree_scratch[SCRATCH_BYTES];
 // Status only: this entry point reports through its return value.
 int err(int code, const char*) { return code; }
 
-// Device address of g_tree_scratch per device, looked up once per device with
-// that device current (the host-side symbol is only a stand-in).
+// Device address of g_tree_scratch per device, looked up with that device
+// current (the host-side symbol is only a stand-in) and kept together with the
+// context it belongs to: a new context on the device gets a new lookup.
 std::mutex g_mu;
 unsigned char* g_addr[64] = {};
+CUcontext g_ctx[64] = {};
+
+typedef CUresult (*ctx_get_current_fn)(CUcontext*);
+
+// cuCtxGetCurrent through the runtime's driver entry point (no link to libcuda).
+CUcontext current_context()
+{
+    static ctx_get_current_fn fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<ctx_get_current_fn>(p);
+        else
+            cudaGetLastError();
+    }
+    CUcontext c = nullptr;
+    if (fn) fn(&c);
+    return c;
+}
+
+// Writes the step constants into the scratch: the constants travel as a kernel
+// argument (copied when the kernel is launched).
+__global__ void k_store_step_const(const StepConst sc, StepConst* dst)
+{
+    const uint32_t* s = reinterpret_cast<const uint32_t*>(&sc);
+    uint32_t* d = reinterpret_cast<uint32_t*>(dst);
+    for (int i = threadIdx.x; i < (int)(sizeof(StepConst) / 4); i += blockDim.x) d[i] = s[i];
+}
+static_assert(sizeof(StepConst) % 4 == 0, "StepConst is copied in 4-byte words");
 
 }  // namespace
 
@@ -80,8 +119,9 @@ extern "C" int gbfmm_tree_build_noalloc(const void* d_coords, const void* d_char
     }
     unsigned char* base;
     {
+        const CUcontext ctx = current_context();
         std::lock_guard<std::mutex> lk(g_mu);
-        if (!g_addr[dev]) {
+        if (!g_addr[dev] || !ctx || g_ctx[dev] != ctx) {
             void* p = nullptr;
             cudaError_t e = cudaGetSymbolAddress(&p, g_tree_scratch);
             if (e != cudaSuccess || !p) {
@@ -89,6 +129,7 @@ extern "C" int gbfmm_tree_build_noalloc(const void* d_coords, const void* d_char
                 return err(GBFMM_ERR_CUDA, "cudaGetSymbolAddress of the tree scratch failed");
             }
             g_addr[dev] = (unsigned char*)p;
+            g_ctx[dev] = current_context();  // the lookup made the runtime's context current
         }
         base = g_addr[dev];
     }
@@ -122,7 +163,8 @@ extern "C" int gbfmm_tree_build_noalloc(const void* d_coords, const void* d_char
     int* counts = (int*)(base + OFF_COUNTS);
     int* cursor = (int*)(base + OFF_CURSOR);
     int* off = (int*)d_leaf_offsets;
-    cudaError_t e = cudaMemcpyAsync(d_sc, &sc, sizeof(sc), cudaMemcpyHostToDevice, s);
+    k_store_step_const<<<1, 256, 0, s>>>(sc, d_sc);
+    cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemsetAsync(counts, 0, sizeof(int) * (nleaf + 1), s);
     if (e == cudaSuccess) e = cudaMemsetAsync(base + OFF_FLAGS, 0, sizeof(int) * 4, s);
     if (e != cudaSuccess) {

@@ -224,8 +224,9 @@ int gbfmm_tuner_choose(gbfmm_mlp* m, int natoms, const float* charges, const flo
  * pointers: coords float[3*natoms], charges float[natoms], order int[natoms],
  * leaf_offsets int[8^depth + 1]; box float[9] on the host (cubic).
  * Limits: natoms <= GBFMM_NOALLOC_MAX_ATOMS and depth <= GBFMM_NOALLOC_MAX_DEPTH;
- * larger inputs return GBFMM_ERR_ARG.  The first call on a device looks up the
- * array's device address (make it before any stream capture).  All calls share
+ * larger inputs return GBFMM_ERR_ARG.  The first call in each CUDA context of a
+ * device looks up the array's device address (make it before any stream capture;
+ * after cudaDeviceReset the next call looks it up again).  All calls share
  * the scratch: calls that overlap on the GPU race.  Asynchronous on 'stream';
  * non-finite coordinates are not reported (no host read-back). */
 #define GBFMM_NOALLOC_MAX_ATOMS 65536
@@ -241,6 +242,11 @@ int gbfmm_tree_build_noalloc(const void* coords, const void* charges, int natoms
  * periodic lattice operator.  Returns GBFMM_ERR_ARG for an unknown index. */
 int gbfmm_debug_operator(int order, int images, int kind, int index, double* mat, int* dim, double* class_vec);
 int gbfmm_debug_harmonics(int order, int kind, const double* d, double* out);
+/* Runs the library's bounded mbarrier wait in a one-warp kernel on a barrier
+ * that nothing completes (no copies or MMAs in flight), with a limit of 'polls'
+ * polls.  Returns GBFMM_ERR_TIMEOUT when the wait gave up (the context stays
+ * usable), as a step does when one of its bounded waits gives up. */
+int gbfmm_debug_bounded_wait(unsigned polls, void* stream);
 
 /* ---- autotuner (tile shapes) ----
  * gbfmm_autotune times whole steps (CUDA-graph replays, reps per candidate) of
@@ -271,8 +277,15 @@ int gbfmm_batch_create_mixed(int n_sys, const int* atom_offsets, const int* orde
                              const int* precisions, int images, int flags, gbfmm_batch** out);
 int gbfmm_batch_execute(gbfmm_batch* b, const float* coords, const float* charges, const float* box_edges,
                         float* forces, float* potentials, double* energies);
+/* Device-resident batch step, asynchronous on 'stream'.  It reads no device
+ * status back: a system's errors (non-finite input, a bounded device wait that
+ * gave up) are reported by gbfmm_batch_status, or by the next gbfmm_batch_execute. */
 int gbfmm_batch_execute_device(gbfmm_batch* b, const void* d_coords, const void* d_charges,
                                const float* box_edges, void* stream);
+/* Waits for the batch's last step and reports its systems' errors: GBFMM_ERR_COORD
+ * (a non-finite coordinate or charge) or GBFMM_ERR_TIMEOUT (a bounded device
+ * wait gave up); the flags and step counters are then cleared for the next step. */
+int gbfmm_batch_status(gbfmm_batch* b);
 int gbfmm_batch_device_outputs(gbfmm_batch* b, void** d_forces, void** d_potentials, void** d_energies);
 int gbfmm_batch_destroy(gbfmm_batch* b);
 

@@ -9,6 +9,9 @@ oracle/_ref/libzetaref.so by oracle/ref_build.sh) and records:
 * lists_small.npz -- complete P2P/M2L lists (target, source, offset in periods)
                   for depth 1-2 and images 0, 1, 2, 4;
 * lists_hash.json -- counts and SHA-256 of the complete lists for depth 3-4;
+* tree_water96k_d4.npz -- the 95,600-atom water/ion box at depth 4 (4,096
+                  leaves): coordinates, leaf body counts and the SHA-256 of the
+                  body order;
 * ref_outputs.npz -- FP64 potentials and forces of the reference's own kernels
                   (kernel.cu p2m ... l2p, run on the host by
                   oracle/ref_kernels_driver.cpp; before the dipole correction) on
@@ -86,6 +89,13 @@ def main():
         order, cnt = tree_case(xyz2, float(L), d)
         np.savez_compressed(os.path.join(HERE, f"tree_edges_d{d}.npz"), xyz=xyz2, order=order, leaf_count=cnt,
                             box=L)
+    # 2b. the 95,600-atom box of the benchmark at depth 4 (coordinates stored:
+    # the generator's floating-point steps need not round alike on every host)
+    xyz, q, box = systems.cfg_96k()
+    order, cnt = tree_case(xyz, float(box[0]), 4)
+    np.savez_compressed(os.path.join(HERE, "tree_water96k_d4.npz"), xyz=xyz, leaf_count=cnt,
+                        order_sha256=np.frombuffer(hashlib.sha256(order.astype("<i4").tobytes()).digest(), np.uint8),
+                        box=np.float32(box[0]))
     # 3. complete small lists
     small = {}
     for depth in (1, 2):

@@ -1,0 +1,62 @@
+"""The benchmark's headline configuration, pinned against FP64 oracles.
+
+The bench's `value` is measured on the 95,600-atom water/ion box (9.86 nm
+cube) at expansion order 5 and depth 4 with the single-product tensor-core
+M2L (BF16X1).  These tests solve exactly that configuration (and BF16X3 and
+FP32 at the same order and depth) through the C ABI and hold it to the metric's
+own bar: relative RMS force error <= 1e-3 against the converged FP64 Ewald sum
+(oracle/ewald64.c; forces on every 191st atom, the bench's sample) and total
+energy within 1e-5.  The tensor-core rounding alone (the same order against
+the FP64 restatement of the reference solver, oracle/zeta64.c) is bounded
+separately."""
+import numpy as np
+import pytest
+
+from conftest import rel_rms
+
+pytestmark = pytest.mark.gpu
+
+ORDER, DEPTH = 5, 4
+
+
+@pytest.fixture(scope="module")
+def headline(oracle, systems):
+    import os
+    xyz, q, box = systems.cfg_96k()
+    n = len(q)
+    oracle.set_threads(os.cpu_count() or 1)
+    tg = np.arange(0, n, 191)
+    x64, q64 = xyz.astype(np.float64), q.astype(np.float64)
+    _, fe, _ = oracle.ewald(x64, q64, box[0], eps=1e-9, targets=tg)
+    _, _, ee = oracle.ewald(x64, q64, box[0], eps=1e-7, energy=True)
+    po, fo, eo = oracle.zeta_solve(x64, q64, float(box[0]), ORDER, DEPTH, 4)
+    return {"xyz": xyz, "q": q, "box": box, "tg": tg, "f_ewald": fe, "e_ewald": ee, "f_zeta": fo, "p_zeta": po,
+            "e_zeta": eo}
+
+
+@pytest.mark.parametrize("prec_name", ["PREC_BF16X1", "PREC_BF16X3", "PREC_FP32"])
+def test_headline_configuration_meets_the_metric_tolerance(pkg, headline, prec_name):
+    h = headline
+    s = pkg.ZetaFmmSolver(len(h["q"]), h["q"], order=ORDER, max_depth=DEPTH, images=4,
+                          precision=getattr(pkg, prec_name))
+    s.execute(h["xyz"], h["box"])
+    f, e = s.forces(), s.get_energy()
+    s.close()
+    err = rel_rms(f[h["tg"]], h["f_ewald"])
+    assert err <= 1e-3, f"{prec_name}: relative RMS force error {err:.3e} against FP64 Ewald"
+    assert abs(e - h["e_ewald"]) / abs(h["e_ewald"]) <= 1e-5
+
+
+@pytest.mark.parametrize("prec_name,tol", [("PREC_BF16X1", 1e-3), ("PREC_BF16X3", 1e-4), ("PREC_FP32", 1e-5)])
+def test_headline_rounding_against_the_fp64_solver(pkg, headline, prec_name, tol):
+    """Same order and depth in FP64 (the oracle): what is left is the rounding of
+    the arithmetic, bounded per precision."""
+    h = headline
+    s = pkg.ZetaFmmSolver(len(h["q"]), h["q"], order=ORDER, max_depth=DEPTH, images=4,
+                          precision=getattr(pkg, prec_name))
+    s.execute(h["xyz"], h["box"])
+    f, p, e = s.forces(), s.potentials(), s.get_energy()
+    s.close()
+    assert rel_rms(f, h["f_zeta"]) <= tol
+    assert rel_rms(p, h["p_zeta"]) <= tol
+    assert abs(e - h["e_zeta"]) / abs(h["e_zeta"]) <= 1e-5

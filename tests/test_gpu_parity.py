@@ -96,6 +96,22 @@ def test_tree_bit_exact_vs_reference(pkg, name, depth):
     s.close()
 
 
+def test_tree_bit_exact_vs_reference_96k_depth4(pkg):
+    """The benchmark's 95,600-atom box at depth 4: the GPU tree's body order
+    (SHA-256) and leaf counts equal the reference tree.cpp's."""
+    import hashlib
+    g = golden("tree_water96k_d4.npz")
+    xyz = g["xyz"]
+    q = np.where(np.arange(len(xyz)) % 2 == 0, 1.0, -1.0).astype(np.float32)
+    s = pkg.ZetaFmmSolver(len(q), q, order=5, max_depth=4, images=4, precision=pkg.PREC_BF16X1)
+    s.execute(xyz, float(g["box"]))
+    order, lo, ln = s.tree()
+    assert hashlib.sha256(np.ascontiguousarray(order, dtype="<i4").tobytes()).digest() == g["order_sha256"].tobytes()
+    assert np.array_equal(ln, g["leaf_count"])
+    assert np.array_equal(lo, np.concatenate([[0], np.cumsum(ln)[:-1]]))
+    s.close()
+
+
 def test_crowded_leaves(pkg, oracle, systems):
     """Ragged occupancy: most bodies in a few leaves (> 256 per leaf, > 2048 near
     sources), many empty leaves."""

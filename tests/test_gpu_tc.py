@@ -2,7 +2,7 @@
 
 BF16X3 keeps ~16 bits of every operand (hi*hi + hi*lo + lo*hi); its force and
 potential error against the FP64 oracle is bounded at 1e-4 relative RMS here.
-BF16X1 (hi*hi) is bounded at 3e-3.  Both must agree with the plain FP32 path
+BF16X1 (hi*hi) is bounded at 1e-3, the benchmark metric's own tolerance.  Both must agree with the plain FP32 path
 on the near field exactly, so they are also compared against it."""
 import numpy as np
 import pytest
@@ -41,7 +41,7 @@ def test_tc_bf16x1_parity(pkg, oracle, systems):
     s.execute(xyz, box)
     f = s.forces()
     _, fo, _ = oracle.zeta_solve(xyz.astype(np.float64), q.astype(np.float64), float(box[0]), 8, 3, 4)
-    assert rel_rms(f, fo) < 3e-3
+    assert rel_rms(f, fo) < 1e-3
     s.close()
 
 

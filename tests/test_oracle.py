@@ -29,6 +29,17 @@ def test_oracle_tree_matches_reference(oracle, name, depth):
     assert np.array_equal(T["body_num"][leaf], g["leaf_count"])
 
 
+def test_oracle_tree_matches_reference_96k_depth4(oracle):
+    """The 95,600-atom box of the benchmark at depth 4 (4,096 leaves): leaf counts
+    and the SHA-256 of the body order of the reference's tree.cpp."""
+    g = golden("tree_water96k_d4.npz")
+    T = oracle.zeta_tree(g["xyz"].astype(np.float64), float(g["box"]), 4)
+    order = np.ascontiguousarray(T["order"], dtype="<i4")
+    assert hashlib.sha256(order.tobytes()).digest() == g["order_sha256"].tobytes()
+    leaf = T["depth"] == 4
+    assert np.array_equal(T["body_num"][leaf], g["leaf_count"])
+
+
 @pytest.mark.parametrize("depth", [1, 2])
 @pytest.mark.parametrize("images", [0, 1, 2, 4])
 def test_oracle_lists_match_reference(oracle, depth, images):
