@@ -38,7 +38,8 @@ class FmmError(RuntimeError):
 class Params(ctypes.Structure):
     _fields_ = [("order", ctypes.c_int), ("max_depth", ctypes.c_int), ("images", ctypes.c_int),
                 ("theta", ctypes.c_double), ("rega", ctypes.c_double), ("precision", ctypes.c_int),
-                ("m2l_tile", ctypes.c_int), ("m2l_split", ctypes.c_int), ("flags", ctypes.c_int)]
+                ("m2l_tile", ctypes.c_int), ("m2l_split", ctypes.c_int), ("flags", ctypes.c_int),
+                ("aspect_z", ctypes.c_int)]
 
 
 _lib = None
@@ -139,10 +140,10 @@ class ZetaFmmSolver:
     images=4, zeta_fmm_solver.cpp:10-13)."""
 
     def __init__(self, natoms, charges=None, order=10, max_depth=3, images=4, precision=PREC_FP32, flags=0,
-                 m2l_split=0):
+                 m2l_split=0, aspect_z=1):
         self.natoms = int(natoms)
         self.params = default_params(order=order, max_depth=max_depth, images=images, precision=precision,
-                                     flags=flags, m2l_split=m2l_split)
+                                     flags=flags, m2l_split=m2l_split, aspect_z=aspect_z)
         h = ctypes.c_void_p()
         _check(lib().gbfmm_create(ctypes.byref(self.params), self.natoms, ctypes.byref(h)))
         self._h = h
@@ -250,7 +251,8 @@ class ZetaFmmSolver:
         return {lib().gbfmm_stage_name(i).decode(): float(ms[i]) for i in range(n.value)}
 
     def tree(self):
-        nleaf = 8 ** self.params.max_depth
+        # stored leaves: all 8^depth of a cube, the box's quarter of the root cube of a slab
+        nleaf = 8 ** self.params.max_depth // (4 if self.params.aspect_z == 2 else 1)
         order = np.zeros(max(self.natoms, 1), np.int32)
         lo = np.zeros(nleaf, np.int32)
         ln = np.zeros(nleaf, np.int32)

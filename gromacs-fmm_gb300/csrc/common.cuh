@@ -56,6 +56,20 @@ GBFMM_HD void morton_decode(uint32_t c, int& ix, int& iy, int& iz) {
 // BFS index of the first cell of a level in the complete octree.
 GBFMM_HD long level_base(int k) { return ((1L << (3 * k)) - 1) / 7; }
 
+// Stored cells of one level along one axis: 2^(level - shift) (at least 1).
+// A cubic box stores all 8^level cells of every level (shift 0 on every axis).
+// A slab box with Lz = 2 Lx = 2 Ly is solved as the periodic virtual cube of edge
+// Lz that holds it twice along x and twice along y (the same periodic charge
+// density): the tree's root is that cube, and each level stores only the cells
+// of the box itself (shift 1 along x and y), which are the Morton prefix
+// [0, 8^level / 4) of every level >= 1; a cell outside it is the box cell at the
+// same position modulo the box (periodic wrap per axis).
+GBFMM_HD int grid_n(int level, int shift) { return level >= shift ? 1 << (level - shift) : 1; }
+GBFMM_HD long grid_cells(int level, const int shift[3])
+{
+    return (long)grid_n(level, shift[0]) * grid_n(level, shift[1]) * grid_n(level, shift[2]);
+}
+
 #ifdef __CUDACC__
 // Sums of FP32 products held as unevaluated FP32 pairs (hi + lo, about 48
 // significant bits) with error-free transformations: the exact product by FMA

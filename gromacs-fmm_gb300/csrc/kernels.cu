@@ -101,12 +101,13 @@ __global__ void __launch_bounds__(256) k_tree_keys(TreeArgs a)
         float u[3];
 #pragma unroll
         for (int d = 0; d < 3; d++) {
-            float kf = fminf(fmaxf(x[d] * inv_h, 0.0f), (float)(nd - 1));
+            const int ndd = sc->nd[d];  // leaf cells along this axis (nd, or nd / 2 across a slab)
+            float kf = fminf(fmaxf(x[d] * inv_h, 0.0f), (float)(ndd - 1));
             int k = (int)kf;
             const float* T = th + d * (nd + 1);
             // cell k holds T[k] < x <= T[k+1]: the strict '>' descent of tree.cpp:49-51
             while (k > 0 && !(x[d] > T[k])) k--;
-            while (k < nd - 1 && x[d] > T[k + 1]) k++;
+            while (k < ndd - 1 && x[d] > T[k + 1]) k++;
             iv[d] = k;
             float2 c = ce[d * nd + k];
             u[d] = ((x[d] - c.x) - c.y) * inv_h;
@@ -641,7 +642,7 @@ __global__ void __launch_bounds__(256) k_down(DownArgs a)
 void launch_down(int P, const DownArgs& a, cudaStream_t s)
 {
     COUNT_LAUNCH();
-    GBFMM_ORDER_SWITCH(P, (k_down<PP><<<1u << (3 * (a.depth - 1)), 256, 0, s>>>(a)));
+    GBFMM_ORDER_SWITCH(P, (k_down<PP><<<a.nparent, 256, 0, s>>>(a)));
 }
 
 
@@ -819,7 +820,6 @@ __device__ __forceinline__ void p2p_leaf(const P2PArgs& a, uint32_t tcode, P2PSh
 {
     constexpr int SL = 32 / LT, SPS = 2 * SL;  // sources per step
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int nd = 1 << a.depth;
     int tx, ty, tz;
     morton_decode(tcode, tx, ty, tz);
     const int tb = a.off[tcode], nt = a.off[tcode + 1] - tb;
@@ -830,9 +830,9 @@ __device__ __forceinline__ void p2p_leaf(const P2PArgs& a, uint32_t tcode, P2PSh
         int vx = tx + a.stencil[3 * tid], vy = ty + a.stencil[3 * tid + 1], vz = tz + a.stencil[3 * tid + 2];
         bool ok = true;
         if (a.periodic) {
-            vx &= nd - 1; vy &= nd - 1; vz &= nd - 1;
+            vx &= a.nd[0] - 1; vy &= a.nd[1] - 1; vz &= a.nd[2] - 1;
         } else {
-            ok = vx >= 0 && vy >= 0 && vz >= 0 && vx < nd && vy < nd && vz < nd;
+            ok = vx >= 0 && vy >= 0 && vz >= 0 && vx < a.nd[0] && vy < a.nd[1] && vz < a.nd[2];
         }
         if (ok) {
             uint32_t sc = morton_encode(vx, vy, vz);
@@ -1006,7 +1006,7 @@ int p2p_variants() { return 3 * 5 + 2; }
 
 void launch_p2p(const P2PArgs& a, int variant, cudaStream_t s, int* counter)
 {
-    const int nleaf = 1 << (3 * a.depth);
+    const int nleaf = a.nleaf;
     COUNT_LAUNCH();
     if (variant >= 15) {  // one CTA per leaf, up to 4 targets per thread
         if (variant == 15) k_p2p<8, 4><<<nleaf, P2P_THREADS, 0, s>>>(a);
@@ -1225,12 +1225,13 @@ __global__ void __launch_bounds__(CT_WARPS * 32) k_contract(ContractArgs a)
                 } else {
                     const int* base = en.mode == 0 ? vt : va;
                     int sx = base[0] + en.dx, sy = base[1] + en.dy, sz = base[2] + en.dz;
-                    const int ns = 1 << slev;
+                    const int nx = grid_n(slev, a.shift[0]), ny = grid_n(slev, a.shift[1]),
+                              nz = grid_n(slev, a.shift[2]);
                     bool ok = true;
                     if (a.periodic) {
-                        sx &= ns - 1; sy &= ns - 1; sz &= ns - 1;
+                        sx &= nx - 1; sy &= ny - 1; sz &= nz - 1;
                     } else {
-                        ok = sx >= 0 && sy >= 0 && sz >= 0 && sx < ns && sy < ns && sz < ns;
+                        ok = sx >= 0 && sy >= 0 && sz >= 0 && sx < nx && sy < ny && sz < nz;
                     }
                     if (ok) row = (int)(morton_encode(sx, sy, sz) * (uint32_t)Rpad);
                 }
@@ -1345,7 +1346,7 @@ __global__ void __launch_bounds__(256) k_root_l2l(RootArgs a)
     const int lane = threadIdx.x & 31;
     const int w = blockIdx.x * 8 + (threadIdx.x >> 5);
     const int o = w / a.R, r = w % a.R;
-    if (o >= 8) return;
+    if (o >= a.n1) return;
     const double* A = a.l2l + ((size_t)o * a.R + r) * a.R;
     double t = 0;
     for (int c = lane; c < a.R; c += 32) t += A[c] * a.L0[c];
@@ -1361,7 +1362,7 @@ void launch_root_lattice(const RootArgs& a, cudaStream_t s)
 void launch_root_l2l(const RootArgs& a, cudaStream_t s)
 {
     COUNT_LAUNCH();
-    k_root_l2l<<<(8 * a.R + 7) / 8, 256, 0, s>>>(a);
+    k_root_l2l<<<(a.n1 * a.R + 7) / 8, 256, 0, s>>>(a);
 }
 
 // ------------------------------------------------------------------ upper tree in one launch
@@ -1497,14 +1498,19 @@ __global__ void __launch_bounds__(TOP_THREADS) k_top(const TopArgs a)
     }
     for (int r = tid; r < R; r += TOP_THREADS) m1d[r] = (double)m1[r];
     __syncthreads();
-    const double* A0 = STAGED ? Ag : a.root.m2m + (size_t)g * R2p;
     const int qc = (R + 3) / 4;
-    for (int i = tid; i < 4 * R; i += TOP_THREADS) {
-        const int r = i >> 2, p = i & 3;
-        const double* A = A0 + (size_t)r * R;
-        double t = 0;
-        for (int c = p * qc; c < min(R, (p + 1) * qc); c++) t = fma(A[c], m1d[c], t);
-        a.part[((size_t)g * R + r) * 4 + p] = t;
+    // the root-M2M shares of every octant whose cell is this CTA's stored cell
+    // (a slab's root cube repeats the box along x and y: octants g, g+2, g+4, g+6)
+    for (int o = g; o < 8; o++) {
+        if ((o & a.umask) != g) continue;
+        const double* A0 = (STAGED && o == g) ? Ag : a.root.m2m + (size_t)o * R2p;
+        for (int i = tid; i < 4 * R; i += TOP_THREADS) {
+            const int r = i >> 2, p = i & 3;
+            const double* A = A0 + (size_t)r * R;
+            double t = 0;
+            for (int c = p * qc; c < min(R, (p + 1) * qc); c++) t = fma(A[c], m1d[c], t);
+            a.part[((size_t)o * R + r) * 4 + p] = t;
+        }
     }
     __shared__ int s_last;
     __threadfence();
@@ -1531,11 +1537,14 @@ __global__ void __launch_bounds__(TOP_THREADS) k_top(const TopArgs a)
         for (int k = 0; k < 32; k++) v[k] = __ldcg(&a.part[((size_t)(k >> 2) * R + r) * 4 + (k & 3)]);
         double s = tree_sum32(v);
         if (r < 4) {
-            const double Q = sums[3], L = a.root.sc->box_len, c = 0.5 * L;
-            if (r == 0) s = Q;
-            else if (r == 1) s = -(sums[2] - Q * c) / L;
-            else if (r == 2) s = (sums[0] - Q * c) / (2.0 * L);
-            else s = -(sums[1] - Q * c) / (2.0 * L);
+            // the root cube holds 'copies' copies of the box, whose dipole about
+            // the root centre is copies x (box dipole about the box centre)
+            const StepConst* sc = a.root.sc;
+            const double Q = sums[3], L = sc->box_len, k = (double)sc->copies;
+            if (r == 0) s = k * Q;
+            else if (r == 1) s = -k * (sums[2] - Q * sc->box_centre[2]) / L;
+            else if (r == 2) s = k * (sums[0] - Q * sc->box_centre[0]) / (2.0 * L);
+            else s = -k * (sums[1] - Q * sc->box_centre[1]) / (2.0 * L);
         }
         M0s[r] = s;
         a.root.M0[r] = s;
@@ -1579,8 +1588,8 @@ void launch_top(const TopArgs& a, cudaStream_t s)
         attr[staged] = shm;
     }
     COUNT_LAUNCH();
-    if (staged) k_top<true><<<8, TOP_THREADS, shm, s>>>(a);
-    else k_top<false><<<8, TOP_THREADS, shm, s>>>(a);
+    if (staged) k_top<true><<<a.root.n1, TOP_THREADS, shm, s>>>(a);
+    else k_top<false><<<a.root.n1, TOP_THREADS, shm, s>>>(a);
     if (!a.lattice) launch_root_lattice(a.root, s);
 }
 

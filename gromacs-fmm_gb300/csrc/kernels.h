@@ -50,6 +50,7 @@ struct ContractArgs {
     int R, Rpad, nblk;
     int periodic;
     int write_mode;           // 0 store, 1 add, 2 atomic add
+    int shift[3];             // stored cells per axis of level l: grid_n(l, shift[d])
 };
 
 // Per-step constants that depend on the box, read by the kernels from device
@@ -64,10 +65,13 @@ struct StepConst {
     float* out_pots;                     // N
     double* out_energy;
     int* out_flags;                      // non-NULL: the finalize's last block copies the step's 4 flags here
-    float inv_h;                         // 2^D / L
-    float pad_;
-    double coef;                         // 4 pi / (3 V), dipole correction
-    double box_len;                      // period L (nm)
+    float inv_h;                         // 2^D / C (C: edge of the root cube)
+    int copies;                          // copies of the box in the root cube (1 cubic, 4 slab)
+    double coef;                         // 4 pi / (3 V), dipole correction (V: box volume)
+    double box_len;                      // C, the edge of the root cube (nm): the period of a cubic box
+    double box_centre[3];                // centre of the box (nm)
+    int nd[3];                           // leaf cells per axis of the stored grid
+    int pad_;
     float thresh[3][(1 << MAX_DEPTH) + 1];  // leaf boundaries rounded down to float (T[0] = -inf)
     float2 centre[3][1 << MAX_DEPTH];   // leaf centres as hi + lo floats
 };
@@ -143,8 +147,9 @@ void launch_l2p(int P, const int* offsets, int nleaf, const float4* atoms, const
 // to the order of the additions.  Variants 15 and 16: one CTA per leaf, up to 4
 // targets per thread, shapes 8 x 4 and 4 x 8.
 struct P2PArgs {
-    const int* off;           // leaf offsets (8^depth + 1)
-    int depth, periodic;
+    const int* off;           // leaf offsets (nleaf + 1)
+    int nleaf, periodic;
+    int nd[3];                // leaf cells per axis (periodic wrap of the stencil)
     const float4* atoms;      // sorted (u, q)
     const int* stencil;       // nst offsets (3 ints), the zero offset first
     int nst;
@@ -167,6 +172,7 @@ void launch_p2p(const P2PArgs& a, int variant, cudaStream_t s, int* counter);
 void launch_contract(const ContractArgs& a, int ntasks, cudaStream_t s);
 // Fused downward pass (depth >= 2): L2L of levels 2..depth and L2P, one launch.
 struct DownArgs {
+    int nparent;              // stored cells of level depth-1 (one CTA each)
     const int* off;
     const float4* atoms;
     const float* L[8];        // per level: L~ rows holding their M2L part (level 1: complete)
@@ -192,6 +198,7 @@ struct RootArgs {
     float* L1;              // level-1 locals (8 rows)
     const StepConst* sc;
     int images;
+    int n1 = 8;             // stored level-1 cells: octants 0..n1-1 (8 cubic, 2 slab)
 };
 void launch_root_lattice(const RootArgs& a, cudaStream_t s);
 void launch_root_l2l(const RootArgs& a, cudaStream_t s);
@@ -219,6 +226,10 @@ struct TopArgs {
     int natoms;
     int* done;            // zero at launch
     int* err;             // bit 1: the bounded wait for the staged copies gave up
+    // CTA g < root.n1 owns stored level-1 cell g and the root-M2M shares of the
+    // octants o with (o & umask) == g (umask 7 cubic; 1 slab: the x and y halves
+    // of the root cube repeat the box)
+    int umask = 7;
     uint32_t wait_limit = 1u << 24;  // polls of the bounded wait
 };
 constexpr int TOP_STAGE_MAX_R = 49;

@@ -110,13 +110,14 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v)
     for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
-// Target tile of level k: bx x by x bz parent cells (at most 8 x 4 x 4 = 128).
-__host__ __device__ __forceinline__ void tc_tile_shape_dev(int level, int& bx, int& by, int& bz)
+// Target tile of level k: bx x by x bz parent cells (at most 8 x 4 x 4 = 128) of
+// the stored parent grid (grid_n(k - 1, shift) cells per axis).
+__host__ __device__ __forceinline__ void tc_tile_shape_dev(int level, const int* shift, int& bx, int& by, int& bz)
 {
-    const int m = 1 << (level - 1);
-    bx = m < 8 ? m : 8;
-    by = m < 4 ? m : 4;
-    bz = m < 4 ? m : 4;
+    const int mx = grid_n(level - 1, shift[0]), my = grid_n(level - 1, shift[1]), mz = grid_n(level - 1, shift[2]);
+    bx = mx < 8 ? mx : 8;
+    by = my < 4 ? my : 4;
+    bz = mz < 4 ? mz : 4;
 }
 
 }  // namespace
@@ -134,7 +135,7 @@ __global__ void __launch_bounds__(256) k_tc_grids(const TcGridArgs g)
         const int lane = threadIdx.x & 31, R = g.root_R;
         const int w = (int)(blockIdx.x - conv_blocks) * 8 + (threadIdx.x >> 5);
         const int o = w / R, r = w % R;
-        if (o >= 8) return;
+        if (o >= g.root_n1) return;
         const double* A = g.root_l2l + ((size_t)o * R + r) * R;
         double t = 0;
         for (int c = lane; c < R; c += 32) t += A[c] * g.L0[c];
@@ -149,13 +150,14 @@ __global__ void __launch_bounds__(256) k_tc_grids(const TcGridArgs g)
     int q = 0;
     while (q + 1 < g.ngrid && g.row0[q + 1] <= row) q++;
     long r = row - g.row0[q];
-    const int W = g.W[q], n = 1 << g.level[q];
-    const int xh = (int)(r % W);
-    r /= W;
-    const int yh = (int)(r % W);
-    r /= W;
-    const int zh = (int)(r % W);
-    r /= W;
+    const int Wx = g.W[q][0], Wy = g.W[q][1], Wz = g.W[q][2];
+    const int nx = g.n[q][0], ny = g.n[q][1], nz = g.n[q][2];
+    const int xh = (int)(r % Wx);
+    r /= Wx;
+    const int yh = (int)(r % Wy);
+    r /= Wy;
+    const int zh = (int)(r % Wz);
+    r /= Wz;
     int x, y, z;
     if (g.parity[q]) {
         const int par = (int)r;
@@ -169,11 +171,11 @@ __global__ void __launch_bounds__(256) k_tc_grids(const TcGridArgs g)
     }
     bool valid = true;
     if (g.periodic) {
-        x = ((x % n) + n) % n;
-        y = ((y % n) + n) % n;
-        z = ((z % n) + n) % n;
+        x = ((x % nx) + nx) % nx;
+        y = ((y % ny) + ny) % ny;
+        z = ((z % nz) + nz) % nz;
     } else {
-        valid = x >= 0 && y >= 0 && z >= 0 && x < n && y < n && z < n;
+        valid = x >= 0 && y >= 0 && z >= 0 && x < nx && y < ny && z < nz;
     }
     const float* src = g.src[q] + (size_t)(valid ? morton_encode(x, y, z) : 0u) * g.Rpad;
     alignas(16) __nv_bfloat16 h[8], l[8];
@@ -192,7 +194,7 @@ void launch_tc_grids(const TcGridArgs& g, cudaStream_t s)
 {
     const long n = g.rows * (g.KP / 8);
     if (n <= 0) return;
-    const long root_blocks = g.root_l2l ? (8L * g.root_R + 7) / 8 : 0;
+    const long root_blocks = g.root_l2l ? ((long)g.root_n1 * g.root_R + 7) / 8 : 0;
     g_kernel_launches.fetch_add(1, std::memory_order_relaxed);
     k_tc_grids<<<(unsigned)((n + 255) / 256 + root_blocks), 256, 0, s>>>(g);
 }
@@ -226,8 +228,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(const __grid_constant_
     const CTask task = a.tasks[blockIdx.x];
     const int k = task.level, s = task.octant;
     int bx, by, bz;
-    tc_tile_shape_dev(k, bx, by, bz);
-    const int m = 1 << (k - 1), tx = m / bx, ty = m / by;
+    tc_tile_shape_dev(k, a.shift, bx, by, bz);
+    const int tx = grid_n(k - 1, a.shift[0]) / bx, ty = grid_n(k - 1, a.shift[1]) / by;
     const int i0 = (task.q0 % tx) * bx, j0 = ((task.q0 / tx) % ty) * by, l0 = (task.q0 / (tx * ty)) * bz;
     const int rows = bx * by * bz;
     const int ox = (s >> 2) & 1, oy = (s >> 1) & 1, oz = s & 1;
@@ -372,31 +374,41 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(const __grid_constant_
 
 // ------------------------------------------------------------------ host side
 
-void tc_tile_shape(int level, int& bx, int& by, int& bz) { tc_tile_shape_dev(level, bx, by, bz); }
-
-int tc_tiles(int level)
+void tc_tile_shape(int level, const int shift[3], int& bx, int& by, int& bz)
 {
-    int bx, by, bz;
-    tc_tile_shape(level, bx, by, bz);
-    const int m = 1 << (level - 1);
-    return (m / bx) * (m / by) * (m / bz);
+    tc_tile_shape_dev(level, shift, bx, by, bz);
 }
 
-TcGrids tc_grid_layout(int D, int k_atoms)
+int tc_tiles(int level, const int shift[3])
+{
+    int bx, by, bz;
+    tc_tile_shape(level, shift, bx, by, bz);
+    return (grid_n(level - 1, shift[0]) / bx) * (grid_n(level - 1, shift[1]) / by) *
+           (grid_n(level - 1, shift[2]) / bz);
+}
+
+bool tc_octant_stored(int level, const int shift[3], int octant)
+{
+    for (int d = 0; d < 3; d++)
+        if (grid_n(level, shift[d]) == 1 && ((octant >> (2 - d)) & 1)) return false;
+    return true;
+}
+
+TcGrids tc_grid_layout(int D, int k_atoms, const int shift[3])
 {
     TcGrids g;
     g.KP = 64 * k_atoms;
     long rows = 0;
     for (int k = 0; k <= D; k++) {
         if (k < D) {  // natural grid: parent-level sources of level k+1
-            g.n_w[k] = (1 << k) + 2 * TC_HALO;
+            for (int d = 0; d < 3; d++) g.n_w[k][d] = grid_n(k, shift[d]) + 2 * TC_HALO;
             g.n_row0[k] = rows;
-            rows += (long)g.n_w[k] * g.n_w[k] * g.n_w[k];
+            rows += (long)g.n_w[k][0] * g.n_w[k][1] * g.n_w[k][2];
         }
         if (k >= 1) {  // parity grid: same-level sources of level k
-            g.p_w[k] = (1 << (k - 1)) + 2 * TC_HALO;
+            for (int d = 0; d < 3; d++) g.p_w[k][d] = (grid_n(k, shift[d]) + 1) / 2 + 2 * TC_HALO;
             g.p_row0[k] = rows;
-            rows += 8L * g.p_w[k] * g.p_w[k] * g.p_w[k];
+            rows += 8L * g.p_w[k][0] * g.p_w[k][1] * g.p_w[k][2];
         }
     }
     g.rows = rows;
@@ -419,16 +431,16 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
     return fn;
 }
 
-// rank-4 (natural) or rank-5 (parity) map of one grid: dims (KP, W, W, W[, 8]),
+// rank-4 (natural) or rank-5 (parity) map of one grid: dims (KP, Wx, Wy, Wz[, 8]),
 // box (64, bx, by, bz[, 1]) of the target level's tile, 128-byte swizzle
-static bool encode_grid(CUtensorMap* map, void* base, int KP, int W, bool parity, int bx, int by, int bz)
+static bool encode_grid(CUtensorMap* map, void* base, int KP, const int* W, bool parity, int bx, int by, int bz)
 {
     PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
     if (!enc) return false;
     const cuuint32_t rank = parity ? 5 : 4;
-    cuuint64_t dims[5] = {(cuuint64_t)KP, (cuuint64_t)W, (cuuint64_t)W, (cuuint64_t)W, 8};
+    cuuint64_t dims[5] = {(cuuint64_t)KP, (cuuint64_t)W[0], (cuuint64_t)W[1], (cuuint64_t)W[2], 8};
     const cuuint64_t row = (cuuint64_t)KP * 2;
-    cuuint64_t strides[4] = {row, row * W, row * W * W, row * W * W * W};
+    cuuint64_t strides[4] = {row, row * W[0], row * W[0] * W[1], row * W[0] * W[1] * W[2]};
     cuuint32_t box[5] = {64, (cuuint32_t)bx, (cuuint32_t)by, (cuuint32_t)bz, 1};
     cuuint32_t es[5] = {1, 1, 1, 1, 1};
     return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, rank, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -442,7 +454,7 @@ bool tc_encode_maps(TcArgs& a, int D, const TcGrids& g, void* hi, void* lo)
     __nv_bfloat16* l = static_cast<__nv_bfloat16*>(lo);
     for (int k = 1; k <= D; k++) {
         int bx, by, bz;
-        tc_tile_shape(k, bx, by, bz);
+        tc_tile_shape(k, a.shift, bx, by, bz);
         if (!encode_grid(&a.p_hi[k], h + g.p_row0[k] * g.KP, g.KP, g.p_w[k], true, bx, by, bz)) return false;
         if (!encode_grid(&a.n_hi[k - 1], h + g.n_row0[k - 1] * g.KP, g.KP, g.n_w[k - 1], false, bx, by, bz))
             return false;

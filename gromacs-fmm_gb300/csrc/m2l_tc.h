@@ -13,8 +13,10 @@
 
 namespace gbfmm {
 
-constexpr int TC_KMAX = 128;     // longest split (bf16) multipole row; orders P <= 10
-constexpr int TC_MAX_ORDER = 10;
+// Orders of the tensor-core M2L: up to 12 (a multipole row of 169 coefficients,
+// three 64-element K atoms; one pipeline stage of the split-precision form fits
+// a CTA's shared memory at orders 11-12, two or more of the single product).
+constexpr int TC_MAX_ORDER = 12;
 constexpr int TC_MAXCHUNK = 8;
 constexpr int TC_TILE = 128;     // MMA M: rows of the target tile
 constexpr int TC_MAXSTAGE = 8;   // pipeline stages (operands of one entry each)
@@ -41,11 +43,13 @@ TcPlan make_tc_plan(int P);
 void append_tc_image(const TcPlan& pl, int R, const double* A, std::vector<uint8_t>& out);
 
 // Source grids.  Every grid row holds KP = 64 * k_atoms bf16 coefficients of one
-// cell (zero past R), hi and lo splits in two arrays of the same layout.
+// cell (zero past R), hi and lo splits in two arrays of the same layout.  With
+// n_d stored cells of the level along axis d (grid_n):
 //   parity grid of level k >= 1 (same-level sources): [par][zh][yh][xh][KP] with
-//     W = 2^(k-1) + 2 TC_HALO, cell x = 2 (xh - TC_HALO) + px, par = px + 2 py + 4 pz;
+//     W_d = ceil(n_d / 2) + 2 TC_HALO, cell x = 2 (xh - TC_HALO) + px,
+//     par = px + 2 py + 4 pz;
 //   natural grid of level k >= 0 (parent-level sources): [z][y][x][KP] with
-//     W = 2^k + 2 TC_HALO, cell x = x' - TC_HALO.
+//     W_d = n_d + 2 TC_HALO, cell x = x' - TC_HALO.
 // Halo cells hold the periodic images (or zeros without periodicity), so the
 // sources of a tile of same-octant targets for one stencil entry form one
 // rectangular box: a single TMA tile load.
@@ -53,18 +57,21 @@ struct TcGrids {
     int KP = 0;
     long rows = 0;
     long p_row0[TC_MAXLEV] = {}, n_row0[TC_MAXLEV] = {};
-    int p_w[TC_MAXLEV] = {}, n_w[TC_MAXLEV] = {};
+    int p_w[TC_MAXLEV][3] = {}, n_w[TC_MAXLEV][3] = {};
 };
-TcGrids tc_grid_layout(int D, int k_atoms);
+TcGrids tc_grid_layout(int D, int k_atoms, const int shift[3]);
 
 // Target tile of level k: a box of bx x by x bz parent cells (one octant).
-void tc_tile_shape(int level, int& bx, int& by, int& bz);
-int tc_tiles(int level);
+void tc_tile_shape(int level, const int shift[3], int& bx, int& by, int& bz);
+int tc_tiles(int level, const int shift[3]);
+// Target octants of level k that the stored grid holds (all 8 except at levels
+// where an axis has one cell: that axis's octant bit is then 0).
+bool tc_octant_stored(int level, const int shift[3], int octant);
 
 struct TcGridArgs {
     int ngrid = 0;
     long row0[2 * TC_MAXLEV];
-    int level[2 * TC_MAXLEV], parity[2 * TC_MAXLEV], W[2 * TC_MAXLEV];
+    int level[2 * TC_MAXLEV], parity[2 * TC_MAXLEV], W[2 * TC_MAXLEV][3], n[2 * TC_MAXLEV][3];
     const float* src[2 * TC_MAXLEV];  // FP32 rows of that level (Morton order)
     int R, Rpad, KP, periodic;
     long rows;
@@ -76,6 +83,7 @@ struct TcGridArgs {
     const double* L0 = nullptr;
     float* L1 = nullptr;
     int root_R = 0;
+    int root_n1 = 8;  // stored level-1 cells
 };
 void launch_tc_grids(const TcGridArgs& g, cudaStream_t s);
 
@@ -93,6 +101,7 @@ struct alignas(64) TcArgs {
     int nprod;                   // 3: hi*hi + hi*lo + lo*hi, 1: hi*hi
     int nstage;                  // pipeline stages, 2..TC_MAXSTAGE (tc_pick_stages)
     int atomic;                  // 1: atomicAdd into L (split entry ranges), 0: plain add
+    int shift[3];                // stored cells per axis of level l: grid_n(l, shift[d])
     int chunk_n[TC_MAXCHUNK], chunk_k[TC_MAXCHUNK], chunk_col[TC_MAXCHUNK], chunk_row0[TC_MAXCHUNK],
         chunk_rows[TC_MAXCHUNK], chunk_img[TC_MAXCHUNK];
 };

@@ -135,6 +135,12 @@ struct gbfmm_handle {
     gbfmm_params prm{};
     int n = 0, P = 0, R = 0, Rpad = 0, D = 0, nleaf = 0;
     bool periodic = true;
+    // box shape: stored cells per axis of level l = grid_n(l, shift[d]); ncell[l]
+    // stored cells of level l (8^l for a cube; a slab stores the box's quarter of
+    // the root cube at every level >= 1)
+    int aspect_z = 1;
+    int shift[3] = {0, 0, 0};
+    long ncell[MAX_DEPTH + 1] = {};
     const OpTables* tab = nullptr;
     cudaStream_t stream = nullptr;
     // P2P runs on its own low-priority stream, concurrently with the far field
@@ -229,6 +235,7 @@ void gbfmm_params_default(gbfmm_params* p)
     p->theta = 0.4;
     p->rega = 0.0;
     p->precision = GBFMM_PREC_FP32;
+    p->aspect_z = 1;
 }
 
 const char* gbfmm_status_string(int s)
@@ -311,12 +318,12 @@ static int layout(gbfmm_handle* h, Arena& a)
     h->d_near = a.take<float4>(n);
     h->d_far = a.take<float4>(n);
     size_t lev = 0;
-    for (int k = 0; k <= D; k++) lev += ((size_t)1 << (3 * k)) * Rpad;
+    for (int k = 0; k <= D; k++) lev += (size_t)h->ncell[k] * Rpad;
     h->lev_floats = lev;
     h->d_M = a.take<float>(lev);
     h->d_L = a.take<float>(lev);
     if (h->tc) {
-        h->tcg = tc_grid_layout(D, t->tc.k_atoms);
+        h->tcg = tc_grid_layout(D, t->tc.k_atoms, h->shift);
         h->d_gh = a.take<__nv_bfloat16>((size_t)h->tcg.rows * h->tcg.KP);
         if (h->prm.precision != GBFMM_PREC_BF16X1) h->d_gl = a.take<__nv_bfloat16>((size_t)h->tcg.rows * h->tcg.KP);
         h->d_img = a.take<uint8_t>(t->tc_img.size());
@@ -354,7 +361,7 @@ static void level_ptrs(gbfmm_handle* h)
     for (int k = 0; k <= h->D; k++) {
         h->Mlev[k] = h->d_M + o;
         h->Llev[k] = h->d_L + o;
-        o += ((size_t)1 << (3 * k)) * h->Rpad;
+        o += (size_t)h->ncell[k] * h->Rpad;
     }
 }
 
@@ -378,21 +385,21 @@ static int build_tasks(gbfmm_handle* h)
                 ent.push_back(e);
             }
         }
-    // M2L tasks
-    long work = 0;
-    for (int k = 1; k <= D; k++) work += (1L << (3 * k)) * (k == 1 ? 107 : 182);
+    // M2L tasks (target octants of the stored grid only: a slab's level 1 holds
+    // two of the root's eight octants)
     int split = h->prm.m2l_split > 0 ? h->prm.m2l_split : 1;
     if (h->prm.m2l_split <= 0) {
         long tiles = 0;
-        for (int k = 1; k <= D; k++) tiles += 8 * std::max<long>(1, (1L << (3 * (k - 1))) / CT_TILE);
+        for (int k = 1; k <= D; k++) tiles += 8 * std::max<long>(1, h->ncell[k - 1] / CT_TILE);
         while (tiles * split < 2 * sm_count() && split < 8) split *= 2;
     }
     if (h->prm.flags & GBFMM_FLAG_DETERMINISTIC) split = 1;
     h->m2l_task0 = (int)tasks.size();
     for (int k = 1; k <= D; k++) {
         const int lt = k == 1 ? 0 : 1;
-        long npar = 1L << (3 * (k - 1));
+        const long npar = h->ncell[k - 1];
         for (int s = 0; s < 8; s++) {
+            if (!tc_octant_stored(k, h->shift, s)) continue;
             int eb = e_m2l[lt][s], ne = (int)t->st.m2l[lt][s].size();
             for (long q0 = 0; q0 < npar; q0 += CT_TILE) {
                 int ch = (ne + split - 1) / split;
@@ -409,7 +416,6 @@ static int build_tasks(gbfmm_handle* h)
         }
     }
     h->m2l_ntask = (int)tasks.size() - h->m2l_task0;
-    (void)work;
     // tensor-core M2L: entries carry the class index, tiles of TC_TILE targets
     if (h->tc) {
         int e_tc[2][8];
@@ -428,7 +434,7 @@ static int build_tasks(gbfmm_handle* h)
         // cut into that many ranges; split > 1 adds into L with atomics); the
         // autotuner picks one, the default fills the GPU with CTAs
         long tiles = 0;
-        for (int k = 1; k <= D; k++) tiles += 8L * tc_tiles(k);
+        for (int k = 1; k <= D; k++) tiles += 8L * tc_tiles(k, h->shift);
         int def = 0;
         if (h->prm.m2l_split > 0) {
             while (def < 3 && (1 << def) < h->prm.m2l_split) def++;
@@ -447,11 +453,12 @@ static int build_tasks(gbfmm_handle* h)
             for (int k = 1; k <= D; k++) {
                 const int lt = k == 1 ? 0 : 1;
                 int bx, by, bz;
-                tc_tile_shape(k, bx, by, bz);
+                tc_tile_shape(k, h->shift, bx, by, bz);
                 for (int s = 0; s < 8; s++) {
+                    if (!tc_octant_stored(k, h->shift, s)) continue;
                     int eb = e_tc[lt][s], ne = (int)t->st.m2l[lt][s].size();
                     int ch = (ne + sp - 1) / sp;
-                    for (int q = 0; q < tc_tiles(k); q++)
+                    for (int q = 0; q < tc_tiles(k, h->shift); q++)
                         for (int e0 = 0; e0 < ne; e0 += ch) {
                             CTask c;
                             c.level = k; c.octant = s; c.q0 = q; c.ntgt = bx * by * bz;
@@ -486,6 +493,7 @@ static int make_tc_args(gbfmm_handle* h)
     std::memset(a, 0, sizeof(TcArgs));
     h->tca = a;
     const TcPlan& pl = h->tab->tc;
+    for (int d = 0; d < 3; d++) a->shift[d] = h->shift[d];
     if (!tc_encode_maps(*a, h->D, h->tcg, h->d_gh, h->d_gl))
         return fail(GBFMM_ERR_CUDA, "tensor map encoding of the M2L source grids failed");
     for (int k = 0; k <= h->D; k++) a->dst_lvl[k] = h->Llev[k];
@@ -502,6 +510,9 @@ static int make_tc_args(gbfmm_handle* h)
     a->nprod = h->prm.precision == GBFMM_PREC_BF16X1 ? 1 : 3;
     a->nstage = tc_pick_stages(pl.k_atoms, pl.img_bytes, a->nprod);
     h->tc_nstage = a->nstage;
+    if (tc_smem_bytes(*a) > 227 * 1024 - TC_MAXENT * sizeof(CEntry))
+        return fail(GBFMM_ERR_UNSUPPORTED, "tensor-core M2L of order %d: one pipeline stage exceeds shared memory",
+                    h->P);
     a->atomic = h->tc_split_v > 0 ? 1 : 0;
     for (int c = 0; c < pl.nchunk; c++) {
         a->chunk_n[c] = pl.n[c];
@@ -523,14 +534,20 @@ static TcGridArgs tc_grid_args(gbfmm_handle* h)
             g.row0[g.ngrid] = l.n_row0[k];
             g.level[g.ngrid] = k;
             g.parity[g.ngrid] = 0;
-            g.W[g.ngrid] = l.n_w[k];
+            for (int d = 0; d < 3; d++) {
+                g.W[g.ngrid][d] = l.n_w[k][d];
+                g.n[g.ngrid][d] = grid_n(k, h->shift[d]);
+            }
             g.src[g.ngrid++] = h->Mlev[k];
         }
         if (k >= 1) {
             g.row0[g.ngrid] = l.p_row0[k];
             g.level[g.ngrid] = k;
             g.parity[g.ngrid] = 1;
-            g.W[g.ngrid] = l.p_w[k];
+            for (int d = 0; d < 3; d++) {
+                g.W[g.ngrid][d] = l.p_w[k][d];
+                g.n[g.ngrid][d] = grid_n(k, h->shift[d]);
+            }
             g.src[g.ngrid++] = h->Mlev[k];
         }
     }
@@ -563,6 +580,7 @@ static ContractArgs contract_args(gbfmm_handle* h, int optype, int write_mode, b
     a.nblk = h->tab->plan[optype].nblk;
     a.periodic = h->periodic ? 1 : 0;
     a.write_mode = write_mode;
+    for (int d = 0; d < 3; d++) a.shift[d] = h->shift[d];
     return a;
 }
 
@@ -575,7 +593,8 @@ static P2PArgs p2p_args(const gbfmm_handle* h)
 {
     P2PArgs pa;
     pa.off = h->d_off;
-    pa.depth = h->D;
+    pa.nleaf = h->nleaf;
+    for (int d = 0; d < 3; d++) pa.nd[d] = grid_n(h->D, h->shift[d]);
     pa.periodic = h->periodic ? 1 : 0;
     pa.atoms = h->d_atoms;
     pa.stencil = h->d_p2p_st;
@@ -669,7 +688,7 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
     mark(h, 2);
     const int top_from = D == 1 || h->R > TOP_STAGE_MAX_R ? 1 : std::min(3, fused ? D - 1 : D);
     for (int k = fused ? D - 2 : D - 1; k >= top_from; k--)
-        launch_m2m(h->Mlev[k + 1], h->Mlev[k], h->d_m2m_t, 1 << (3 * k), h->R, h->Rpad, s);
+        launch_m2m(h->Mlev[k + 1], h->Mlev[k], h->d_m2m_t, (int)h->ncell[k], h->R, h->Rpad, s);
     mark(h, 3);
     RootArgs ra;
     ra.R = h->R;
@@ -684,6 +703,7 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
     ra.L1 = h->Llev[1];
     ra.sc = h->d_sc;
     ra.images = h->prm.images;
+    ra.n1 = (int)h->ncell[1];
     TopArgs top;
     top.root = ra;
     top.from = top_from;
@@ -700,6 +720,7 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
     top.natoms = h->n;
     top.done = sync + 3;
     top.err = h->d_flags + 2;
+    top.umask = (h->shift[0] == 0 ? 4 : 0) | (h->shift[1] == 0 ? 2 : 0) | (h->shift[2] == 0 ? 1 : 0);
     launch_top(top, s);
     mark(h, 4);
     if (h->tc) {
@@ -709,6 +730,7 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
         tg.L0 = h->d_L0;
         tg.L1 = h->Llev[1];
         tg.root_R = h->R;
+        tg.root_n1 = (int)h->ncell[1];
         launch_tc_grids(tg, s);
         TcArgs& ta = *h->tca;  // the current tuning: entry split and pipeline depth
         ta.tasks = h->d_tc_tasks_v[h->tc_split_v];
@@ -724,6 +746,7 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
     if (D >= 2) {
         // L2L of levels 2..D and L2P in one launch
         DownArgs da;
+        da.nparent = (int)h->ncell[D - 1];
         da.off = h->d_off;
         da.atoms = h->d_atoms;
         for (int k = 0; k <= D; k++) da.L[k] = h->Llev[k];
@@ -792,6 +815,11 @@ extern "C" int gbfmm_create(const gbfmm_params* prm, int natoms, gbfmm_handle** 
         return fail(GBFMM_ERR_UNSUPPORTED, "tensor-core M2L supports orders <= %d (got %d)", TC_MAX_ORDER, p.order);
     if (p.m2l_tile != 0 && p.m2l_tile != CT_TILE) return fail(GBFMM_ERR_ARG, "m2l_tile must be 0 or %d", CT_TILE);
     if (p.m2l_split < 0 || p.m2l_split > 16) return fail(GBFMM_ERR_ARG, "m2l_split outside [0,16]");
+    if (p.aspect_z == 0) p.aspect_z = 1;
+    if (p.aspect_z != 1 && p.aspect_z != 2)
+        return fail(GBFMM_ERR_ARG, "aspect_z %d: 1 (cube) or 2 (slab, Lz = 2 Lx = 2 Ly)", p.aspect_z);
+    if (p.aspect_z == 2 && p.images < 1)
+        return fail(GBFMM_ERR_UNSUPPORTED, "a slab box is solved as periodic (images >= 1)");
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) {
         cudaGetLastError();
@@ -812,7 +840,13 @@ extern "C" int gbfmm_create(const gbfmm_params* prm, int natoms, gbfmm_handle** 
     h->R = nreal(p.order);
     h->Rpad = (h->R + 3) & ~3;
     h->D = p.max_depth;
-    h->nleaf = 1 << (3 * h->D);
+    h->aspect_z = p.aspect_z;
+    if (p.aspect_z == 2) {
+        h->shift[0] = h->shift[1] = 1;
+        h->shift[2] = 0;
+    }
+    for (int k = 0; k <= h->D; k++) h->ncell[k] = grid_cells(k, h->shift);
+    h->nleaf = (int)h->ncell[h->D];
     h->periodic = p.images > 0;
     h->tc = p.precision != GBFMM_PREC_FP32;
     h->tab = get_tables(h->P, p.images);
@@ -926,9 +960,12 @@ extern "C" int gbfmm_set_charges(gbfmm_handle* h, int natoms, const float* q)
     return GBFMM_OK;
 }
 
-// Fills the box-dependent step constants.  Cubic boxes only: the reference takes
-// the period from box[XX][XX] and the root half-width as its half
-// (zeta_fmm_solver.cpp:38-40).
+// Fills the box-dependent step constants.  A cubic box: the reference takes the
+// period from box[XX][XX] and the root half-width as its half
+// (zeta_fmm_solver.cpp:38-40).  A slab (aspect_z 2, Lx = Ly, Lz = 2 Lx): the root
+// is the cube of edge Lz; the stored leaf grid covers the box itself, with cubic
+// leaves of edge Lz / 2^D (2^(D-1) along x and y, 2^D along z), and the dipole
+// correction takes the box's own volume.
 // host_out: the finalize writes the results into the handle's pinned host
 // buffers (a host call whose coordinates the device reads in place).
 static int set_box(gbfmm_handle* h, const float* box, const float* d_coords, bool host_out = false)
@@ -938,9 +975,15 @@ static int set_box(gbfmm_handle* h, const float* box, const float* d_coords, boo
         if (!std::isfinite(box[i])) return fail(GBFMM_ERR_BOX, "box entry %d is not finite", i);
     if (!(box[0] > 0) || box[1] != 0 || box[2] != 0 || box[3] != 0 || box[5] != 0 || box[6] != 0 || box[7] != 0)
         return fail(GBFMM_ERR_BOX, "box must be rectangular with positive diagonal");
-    if (box[4] != box[0] || box[8] != box[0])
+    if (h->aspect_z == 1 && (box[4] != box[0] || box[8] != box[0]))
         return fail(GBFMM_ERR_BOX, "box must be cubic (got %g x %g x %g)", box[0], box[4], box[8]);
-    const double L = (double)box[0];
+    if (h->aspect_z == 2 &&
+        (box[4] != box[0] || std::fabs((double)box[8] - 2.0 * (double)box[0]) > 1e-6 * (double)box[8]))
+        return fail(GBFMM_ERR_BOX, "slab box must have Lx = Ly and Lz = 2 Lx (got %g x %g x %g)", box[0], box[4],
+                    box[8]);
+    const double a = (double)box[0];
+    const double C = h->aspect_z == 2 ? 2.0 * a : a;  // edge of the root cube
+    const double E[3] = {a, a, C};                    // the box's extents
     const int D = h->D, nd = 1 << D;
     // the previous step's copy of the constants must have been made before they
     // are rewritten (it runs first in that step, so this rarely waits)
@@ -951,24 +994,27 @@ static int set_box(gbfmm_handle* h, const float* box, const float* d_coords, boo
     sc->out_pots = host_out ? h->h_pots : h->d_pots;
     sc->out_energy = host_out ? h->h_energy : h->d_energy;
     sc->out_flags = host_out ? h->h_flags : nullptr;
-    sc->inv_h = (float)(nd / L);
-    sc->coef = 4.0 * M_PI / (3.0 * L * L * L);
-    sc->box_len = L;
-    const double centre[3] = {(double)box[0] / 2, (double)box[4] / 2, (double)box[8] / 2};
+    sc->inv_h = (float)(nd / C);
+    sc->coef = 4.0 * M_PI / (3.0 * E[0] * E[1] * E[2]);
+    sc->box_len = C;
+    sc->copies = h->aspect_z == 2 ? 4 : 1;
     for (int d = 0; d < 3; d++) {
+        const int n = grid_n(D, h->shift[d]);
+        sc->nd[d] = n;
+        sc->box_centre[d] = E[d] / 2;
         // leaf boundaries of the strict '>' descent: the descent around centre c with
         // half-width L/2 compares against c + L*(j/2^D - 1/2), exactly representable
-        const double lo = centre[d] - L / 2;
+        const double lo = E[d] / 2 - E[d] / 2;
         sc->thresh[d][0] = -INFINITY;
-        for (int j = 1; j < nd; j++) {
-            double b = lo + L * j / nd;
+        for (int j = 1; j < n; j++) {
+            double b = lo + E[d] * j / n;
             float f = (float)b;
             if ((double)f > b) f = std::nextafter(f, -INFINITY);
             sc->thresh[d][j] = f;
         }
-        sc->thresh[d][nd] = INFINITY;
+        for (int j = n; j <= nd; j++) sc->thresh[d][j] = INFINITY;
         for (int j = 0; j < nd; j++) {
-            double c = lo + L * (2 * j + 1) / (2.0 * nd);
+            double c = lo + E[d] * (2 * std::min(j, n - 1) + 1) / (2.0 * n);
             float hi = (float)c;
             float lo_f = (float)(c - (double)hi);
             sc->centre[d][j] = make_float2(hi, lo_f);
@@ -1339,6 +1385,8 @@ extern "C" int gbfmm_lists(int max_depth, int images, int which, long* count, in
 extern "C" int gbfmm_get_lists(gbfmm_handle* h, int which, long* count, int* tgt, int* src, int* off3)
 {
     if (!h || !count || (which != 0 && which != 1)) return fail(GBFMM_ERR_ARG, "bad argument");
+    if (h->aspect_z != 1)
+        return fail(GBFMM_ERR_UNSUPPORTED, "interaction lists in the reference's order exist for cubic boxes only");
     RefLists p2p, m2l;
     emit_lists(h->tab->st, h->D, h->prm.images, p2p, m2l);
     const RefLists& l = which == 0 ? p2p : m2l;

@@ -117,6 +117,14 @@ def cfg_1m():
     return water_ion_box(333402 + 1796, 21.5, n_na=898, n_cl=898, seed=3)
 
 
+def cfg_slab_1m():
+    """The inhomogeneous 1,002,002-atom system: a periodic 21.5 x 21.5 x 43 nm box
+    whose lower half is water (333,402 waters) with 0.15 M NaCl (898 Na+ and 898
+    Cl-, about 0.0903 pairs per nm^3 of water) placed uniformly in the water, and
+    whose upper half is vacuum."""
+    return water_ion_box(333402 + 1796, [21.5, 21.5, 43.0], n_na=898, n_cl=898, seed=3, fill_z=0.5)
+
+
 def kicked_frames(xyz, box, n_frames, sigma=0.01, seed=7):
     """Frames of a trajectory: each frame adds Gaussian kicks of sigma nm to the
     previous one (wrapped into the box).  Yields float32 coordinates."""

@@ -56,6 +56,12 @@ typedef struct gbfmm_params {
     int m2l_tile;       /* 0 = autotuned, else targets per M2L tile (32 or 64) */
     int m2l_split;      /* 0 = autotuned, else entry splits per M2L tile (1..16) */
     int flags;          /* GBFMM_FLAG_* */
+    int aspect_z;       /* box shape: 1 (or 0) = cube; 2 = slab with Lx = Ly and Lz = 2 Lx.  A slab is
+                           solved as the periodic cube of edge Lz that holds it twice along x and y (the
+                           same periodic charge density): the tree's root is that cube (max_depth counts
+                           from it, leaves of edge Lz / 2^max_depth), and only the box's own cells are
+                           stored and computed.  The reference takes box[XX][XX] as the period of a cube
+                           (zeta_fmm_solver.cpp:38-40) and has no slab. */
 } gbfmm_params;
 
 #define GBFMM_FLAG_NO_GRAPH 1        /* launch the step kernel by kernel instead of replaying a CUDA graph */
@@ -82,7 +88,8 @@ int gbfmm_set_charges(gbfmm_handle* h, int natoms, const float* charges);
 
 /* BaseSolver::execute (basesolver.h:67; zeta_fmm_solver.cpp:16-64): host
  * coordinates (float[3*natoms], nm) and the box (float[9], row-major 3x3, nm;
- * must be cubic: the reference uses box[XX][XX] as the period).  Synchronous,
+ * rectangular, of the handle's shape: cubic, or Lx = Ly and Lz = 2 Lx for
+ * aspect_z = 2; the reference uses box[XX][XX] as the period of a cube).  Synchronous,
  * like the reference: results are on the host when it returns.  On a device
  * that reads pageable host memory coherently (GB300 over NVLink-C2C) the step
  * reads 'coords' in place and writes the results straight into the handle's

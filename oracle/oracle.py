@@ -84,6 +84,22 @@ def zeta_solve(xyz, q, cycle, P, depth, images=4, theta=0.4, stages=7):
     return pot, force, float(e[0])
 
 
+def zeta_solve_slab(xyz, q, a, P, depth, images=4, theta=0.4):
+    """The same FP64 solver for a periodic slab box a x a x 2a: the slab is the
+    periodic cube of edge 2a that holds it twice along x and twice along y (the
+    same periodic charge density, so the same tin-foil Ewald limit), solved here
+    literally on the four copies (4N bodies, cycle 2a, depth counted from that
+    cube).  Returns the first copy's potentials and forces, and the box's energy."""
+    xyz = np.asarray(xyz, dtype=np.float64)
+    q = np.asarray(q, dtype=np.float64)
+    n = len(q)
+    shifts = np.array([[0.0, 0.0, 0.0], [a, 0.0, 0.0], [0.0, a, 0.0], [a, a, 0.0]])
+    x4 = np.concatenate([xyz + s for s in shifts])
+    q4 = np.concatenate([q] * 4)
+    pot, force, e = zeta_solve(x4, q4, 2.0 * a, P, depth, images, theta)
+    return pot[:n], force[:n], e / 4.0
+
+
 def zeta_tree(xyz, cycle, depth):
     xyz = np.ascontiguousarray(xyz, dtype=np.float64)
     n = len(xyz)

@@ -62,5 +62,20 @@ def test_tc_matches_fp32_path_and_is_deterministic(pkg, systems):
 
 def test_tc_rejects_high_order(pkg):
     with pytest.raises(pkg.FmmError) as e:
-        pkg.ZetaFmmSolver(10, np.zeros(10, np.float32), order=12, max_depth=1, precision=pkg.PREC_BF16X3)
+        pkg.ZetaFmmSolver(10, np.zeros(10, np.float32), order=13, max_depth=1, precision=pkg.PREC_BF16X3)
     assert e.value.status == 6
+
+
+@pytest.mark.parametrize("P,prec,tol", [(11, 1, 1e-4), (12, 1, 1e-4), (12, 2, 1e-3)])
+def test_tc_orders_11_and_12(pkg, oracle, systems, P, prec, tol):
+    """Three K atoms per multipole row (up to 169 coefficients); one pipeline
+    stage of the split-precision form, two of the single product."""
+    xyz, q, box = systems.water_ion_box(1500, 3.0, n_na=4, n_cl=4, seed=50 + P)
+    s = pkg.ZetaFmmSolver(len(q), q, order=P, max_depth=3, images=4, precision=prec)
+    s.execute(xyz, box)
+    f, p, e = s.forces(), s.potentials(), s.get_energy()
+    s.close()
+    po, fo, eo = oracle.zeta_solve(xyz.astype(np.float64), q.astype(np.float64), float(box[0]), P, 3, 4)
+    assert rel_rms(f, fo) < tol
+    assert rel_rms(p, po) < 3 * tol
+    assert abs(e - eo) / abs(eo) < 1e-5

@@ -153,7 +153,9 @@ def test_lists_bit_exact_vs_reference_hash(pkg):
 
 @pytest.mark.parametrize("kw,status", [({"order": 1}, 1), ({"order": 17}, 1), ({"max_depth": 0}, 1),
                                        ({"max_depth": 8}, 1), ({"images": -1}, 1), ({"theta": 0.5}, 6),
-                                       ({"rega": 0.1}, 6), ({"precision": 7}, 1), ({"m2l_split": 99}, 1)])
+                                       ({"rega": 0.1}, 6), ({"precision": 7}, 1), ({"m2l_split": 99}, 1),
+                                       ({"aspect_z": 3}, 1), ({"aspect_z": 2, "images": 0}, 6),
+                                       ({"precision": 1, "order": 13}, 6)])
 def test_invalid_parameters_rejected_before_device_use(pkg, kw, status):
     import ctypes
     p = pkg.default_params(**kw)

@@ -151,3 +151,21 @@ def test_reference_kernels_reproduce_their_fixture(oracle, systems):
         assert np.array_equal(force[idx], g[f"case{k}_force"])
         break
 
+
+
+def test_oracle_slab_converges_to_rectangular_ewald(oracle, systems):
+    """A half-vacuum slab a x a x 2a: the four-copy periodic cube of edge 2a has
+    the slab's periodic charge density, so the solver on it converges with the
+    order to the FP64 Ewald sum of the rectangular box."""
+    a = 2.6
+    xyz, q, _ = systems.water_ion_box(500, [a, a, 2 * a], n_na=2, n_cl=2, seed=91, fill_z=0.5)
+    x64, q64 = xyz.astype(np.float64), q.astype(np.float64)
+    a32 = float(np.float32(a))
+    _, fe, _ = oracle.ewald(x64, q64, np.array([a32, a32, 2 * a32]), eps=1e-10)
+    _, _, ee = oracle.ewald(x64, q64, np.array([a32, a32, 2 * a32]), eps=1e-9, energy=True)
+    errs = []
+    for P in (4, 8):
+        _, fo, eo = oracle.zeta_solve_slab(x64, q64, a32, P, 2, 4)
+        errs.append(rel_rms(fo, fe))
+        assert abs(eo - ee) / abs(ee) < 1e-4
+    assert errs[1] < 0.2 * errs[0] and errs[1] < 5e-4
