@@ -1198,6 +1198,15 @@ __global__ void __launch_bounds__(CT_WARPS * 32) k_contract(ContractArgs a)
         morton_decode(tcode, vt[0], vt[1], vt[2]);
         trow[tid] = tvalid ? (int)(tcode * (uint32_t)Rpad) : -1;
     }
+    // a tile whose targets hold no bodies (vacuum) needs no locals
+    if (a.leaf_off) {
+        bool occupied = false;
+        if (tid < T && tvalid) {
+            const int sh = 3 * (a.depth - task.level);
+            occupied = a.leaf_off[(tcode + 1) << sh] > a.leaf_off[tcode << sh];
+        }
+        if (!__syncthreads_or(occupied)) return;
+    }
     // this warp's work items (row block, column range) and their accumulators,
     // kept in registers across all entries of the task
     const int ib = a.warp_begin[task.group * (CT_WARPS + 1) + warp];

@@ -51,6 +51,8 @@ struct ContractArgs {
     int periodic;
     int write_mode;           // 0 store, 1 add, 2 atomic add
     int shift[3];             // stored cells per axis of level l: grid_n(l, shift[d])
+    const int* leaf_off;      // M2L: leaf offsets of the step (tiles of empty targets are skipped), or NULL
+    int depth;                // leaf level
 };
 
 // Per-step constants that depend on the box, read by the kernels from device

@@ -234,6 +234,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(const __grid_constant_
     const int rows = bx * by * bz;
     const int ox = (s >> 2) & 1, oy = (s >> 1) & 1, oz = s & 1;
 
+    // a tile whose targets hold no bodies (vacuum) needs no locals: their only
+    // readers are their own descendants' L2P
+    if (a.leaf_off) {
+        bool occupied = false;
+        if (tid < rows) {
+            const int bi = tid % bx, bj = (tid / bx) % by, bl = tid / (bx * by);
+            const uint32_t code = (morton_encode(i0 + bi, j0 + bj, l0 + bl) << 3) | (uint32_t)s;
+            const int sh = 3 * (a.depth - k);
+            occupied = a.leaf_off[(code + 1) << sh] > a.leaf_off[code << sh];
+        }
+        if (!__syncthreads_or(occupied)) return;
+    }
+
     // the task's stencil entries, read once (the producer must not wait on
     // global loads between its copies)
     __shared__ CEntry ent[TC_MAXENT];

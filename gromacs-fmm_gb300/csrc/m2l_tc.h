@@ -102,6 +102,8 @@ struct alignas(64) TcArgs {
     int nstage;                  // pipeline stages, 2..TC_MAXSTAGE (tc_pick_stages)
     int atomic;                  // 1: atomicAdd into L (split entry ranges), 0: plain add
     int shift[3];                // stored cells per axis of level l: grid_n(l, shift[d])
+    const int* leaf_off;         // leaf offsets of the step (tiles of empty targets are skipped), or NULL
+    int depth;                   // leaf level
     int chunk_n[TC_MAXCHUNK], chunk_k[TC_MAXCHUNK], chunk_col[TC_MAXCHUNK], chunk_row0[TC_MAXCHUNK],
         chunk_rows[TC_MAXCHUNK], chunk_img[TC_MAXCHUNK];
 };

@@ -494,6 +494,8 @@ static int make_tc_args(gbfmm_handle* h)
     h->tca = a;
     const TcPlan& pl = h->tab->tc;
     for (int d = 0; d < 3; d++) a->shift[d] = h->shift[d];
+    a->leaf_off = h->d_off;
+    a->depth = h->D;
     if (!tc_encode_maps(*a, h->D, h->tcg, h->d_gh, h->d_gl))
         return fail(GBFMM_ERR_CUDA, "tensor map encoding of the M2L source grids failed");
     for (int k = 0; k <= h->D; k++) a->dst_lvl[k] = h->Llev[k];
@@ -581,6 +583,8 @@ static ContractArgs contract_args(gbfmm_handle* h, int optype, int write_mode, b
     a.periodic = h->periodic ? 1 : 0;
     a.write_mode = write_mode;
     for (int d = 0; d < 3; d++) a.shift[d] = h->shift[d];
+    a.leaf_off = optype == OP_M2L ? h->d_off : nullptr;
+    a.depth = h->D;
     return a;
 }
 
