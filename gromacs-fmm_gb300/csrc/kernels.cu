@@ -43,24 +43,38 @@ int sm_count()
 
 // ------------------------------------------------------------------ tree
 
-// Sum over the tree-key blocks of one of the four per-block partials (dipole x, y,
-// z, total charge; FP32 pairs) by one warp: every load issued first (one round
-// trip), the blocks added in a fixed order, then a fixed butterfly.
-__device__ __forceinline__ f2sum sum_tree_partials(const double* partials, int nblocks, int quantity)
+// FP64 sum of per-block partials held as FP32 pairs (hi, lo) at part[stride * b]
+// for b < nblocks, by one warp: every load issued first (one round trip), each
+// pair made exact in FP64, the lane's blocks added by a fixed pairwise tree, then
+// a butterfly (FP64 addition commutes, so every lane ends with the same sum).
+// The final reductions of the step (energy, dipole, total charge) are FP64.
+__device__ __forceinline__ double sum_partials_f64(const float2* part, int stride, int nblocks)
 {
+    static_assert(TREE_MAX_BLOCKS == FINAL_MAX_BLOCKS, "one tree shape for both reductions");
+    constexpr int K = (TREE_MAX_BLOCKS + 31) / 32, K2 = K <= 16 ? 16 : 32;
     const int lane = threadIdx.x & 31;
-    constexpr int K = (TREE_MAX_BLOCKS + 31) / 32;
-    f2sum v[K];
-    const float2* part = reinterpret_cast<const float2*>(partials);
+    double v[K2];
 #pragma unroll
-    for (int k = 0; k < K; k++) {
+    for (int k = 0; k < K2; k++) {
         const int b = lane + 32 * k;
-        const float2 p = b < nblocks ? __ldcg(&part[4 * b + quantity]) : make_float2(0.f, 0.f);
-        v[k] = f2sum{p.x, p.y};
+        const float2 p = (k < K && b < nblocks) ? __ldcg(&part[(size_t)stride * b]) : make_float2(0.f, 0.f);
+        v[k] = (double)p.x + (double)p.y;
     }
 #pragma unroll
-    for (int k = 1; k < K; k++) v[0] = f2s_add(v[0], v[k]);
-    return f2s_warp_sum(v[0]);
+    for (int w = K2 / 2; w >= 1; w >>= 1)
+#pragma unroll
+        for (int k = 0; k < w; k++) v[k] = v[k] + v[k + w];
+    double t = v[0];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    return t;
+}
+
+// Sum over the tree-key blocks of one of the four per-block partials (dipole x, y,
+// z, total charge; FP32 pairs), in FP64 (sum_partials_f64).
+__device__ __forceinline__ double sum_tree_partials(const double* partials, int nblocks, int quantity)
+{
+    return sum_partials_f64(reinterpret_cast<const float2*>(partials) + quantity, 4, nblocks);
 }
 
 __global__ void __launch_bounds__(256) k_tree_keys(TreeArgs a)
@@ -149,8 +163,8 @@ __global__ void __launch_bounds__(256) k_tree_keys(TreeArgs a)
     __threadfence();
     if (threadIdx.x == 0) *a.done = 0;  // every block has counted: ready for the next step
     if (a.sums && warp < 4) {
-        const f2sum t = sum_tree_partials(a.partials, (int)gridDim.x, warp);
-        if (lane == 0) a.sums[warp] = f2s_value(t);
+        const double t = sum_tree_partials(a.partials, (int)gridDim.x, warp);
+        if (lane == 0) a.sums[warp] = t;
     }
     if (a.off) {
         // exclusive scan of counts in tiles of 4096 staged in shared memory
@@ -1533,10 +1547,10 @@ __global__ void __launch_bounds__(TOP_THREADS) k_top(const TopArgs a)
     // partials, one warp per quantity
     __shared__ double sums[4];
     if (tid < 128) {
-        const f2sum t = sum_tree_partials(a.tree_part, a.tree_nblocks, tid >> 5);
+        const double t = sum_tree_partials(a.tree_part, a.tree_nblocks, tid >> 5);
         if ((tid & 31) == 0) {
-            sums[tid >> 5] = f2s_value(t);
-            a.sums[tid >> 5] = f2s_value(t);
+            sums[tid >> 5] = t;
+            a.sums[tid >> 5] = t;
         }
     }
     __syncthreads();
@@ -1648,7 +1662,8 @@ __global__ void __launch_bounds__(256) k_finalize(FinalArgs a)
         forces[3 * o] = qk * gx + q * fM0;
         forces[3 * o + 1] = qk * gy + q * fM1;
         forces[3 * o + 2] = qk * gz + q * fM2;
-        // FP32 per body (no FP64 division), FP64 accumulation of the energy
+        // FP32 per body (no FP64 division); the exact products of the energy are
+        // summed per block as FP32 pairs, and the blocks in FP64
         float pot = phi * (float)KE;
         if (q != 0.f) pot -= corr_f / q;
         pots[o] = pot;
@@ -1677,20 +1692,10 @@ __global__ void __launch_bounds__(256) k_finalize(FinalArgs a)
         *a.done = 0;
         if (a.zero_after) *a.zero_after = 0;
     }
-    constexpr int K = (FINAL_MAX_BLOCKS + 31) / 32;
-    f2sum v[K];
-    const float2* part = reinterpret_cast<const float2*>(a.partials);
-#pragma unroll
-    for (int k = 0; k < K; k++) {
-        const int b = threadIdx.x + 32 * k;
-        const float2 p = b < (int)gridDim.x ? __ldcg(&part[b]) : make_float2(0.f, 0.f);
-        v[k] = f2sum{p.x, p.y};
-    }
-#pragma unroll
-    for (int k = 1; k < K; k++) v[0] = f2s_add(v[0], v[k]);
-    const f2sum t = f2s_warp_sum(v[0]);
+    // the energy: the blocks' FP32-pair partials summed in FP64
+    const double t = sum_partials_f64(reinterpret_cast<const float2*>(a.partials), 1, (int)gridDim.x);
     if (threadIdx.x == 0) {
-        *a.sc->out_energy = f2s_value(t);
+        *a.sc->out_energy = t;
         int* fl = a.sc->out_flags;
         if (fl)
             for (int k = 0; k < 4; k++) fl[k] = __ldcg(&a.flags[k]);
