@@ -8,7 +8,11 @@
 //   [6 + 9(k-2) + b]  levels k = 2..6: fraction of cells whose body count is in
 //                     bin b = 0: empty, b >= 1: [2^(b-1), 2^b) (last bin open)
 //   [51 + (k-2)]      levels k = 2..6: log2 of the mean count of non-empty cells
-// MLP input = statistics ++ candidate (P/10, depth/6, precision, log2(N/8^depth)/5),
+//   [56] log2(Lz / Lx): the box shape (0 cube, 1 slab with Lx = Ly, Lz = 2 Lx)
+// The cells are those of the tree's levels 2..6, whose root is the cube of edge
+// L = Lz; of a slab only the box's own cells count (a quarter of each level).
+// MLP input = statistics ++ candidate (P/10, depth/6, precision,
+// log2(bodies per stored leaf)/5),
 // outputs = (log10 relative RMS force error, log10 step time in ms).
 #include <cuda_runtime.h>
 
@@ -36,19 +40,21 @@ constexpr int NBIN = 9;
 
 int status(cudaError_t e) { return e == cudaSuccess ? GBFMM_OK : (e == cudaErrorMemoryAllocation ? GBFMM_ERR_NOMEM : GBFMM_ERR_CUDA); }
 
-__device__ __forceinline__ int cell_index(float x, float inv)
+__device__ __forceinline__ int cell_index(float x, float inv, int ncell)
 {
     int k = (int)floorf(x * inv);
-    return min(max(k, 0), (1 << FL) - 1);
+    return min(max(k, 0), ncell - 1);
 }
 
-// Body counts of the 64^3 grid and FP64 charge moments (per-block partials).
-__global__ void k_feat_counts(const float* xyz, const float* q, int n, float inv, int* counts, double* part)
+// Body counts of the finest grid (64 cells of the root cube per axis; of a slab
+// the box's 32 x 32 x 64) and FP64 charge moments (per-block partials).
+__global__ void k_feat_counts(const float* xyz, const float* q, int n, float inv, int sxy, int* counts, double* part)
 {
     double s[5] = {0, 0, 0, 0, 0};  // sum q, sum q^2, dipole x, y, z
+    const int nxy = (1 << FL) >> sxy;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2], c = q[i];
-        const int ix = cell_index(x, inv), iy = cell_index(y, inv), iz = cell_index(z, inv);
+        const int ix = cell_index(x, inv, nxy), iy = cell_index(y, inv, nxy), iz = cell_index(z, inv, 1 << FL);
         atomicAdd(&counts[(ix << (2 * FL)) | (iy << FL) | iz], 1);
         s[0] += c;
         s[1] += (double)c * c;
@@ -70,11 +76,11 @@ __global__ void k_feat_counts(const float* xyz, const float* q, int n, float inv
 }
 
 // Occupancy histogram of level k (cells of 2^(FL-k) fine cells per axis).
-__global__ void k_feat_hist(const int* counts, int k, int* hist, long long* sum_nonempty)
+__global__ void k_feat_hist(const int* counts, int k, int sxy, int* hist, long long* sum_nonempty)
 {
-    const int nk = 1 << k, c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= nk * nk * nk) return;
-    const int ix = c / (nk * nk), iy = (c / nk) % nk, iz = c % nk, w = 1 << (FL - k);
+    const int nk = 1 << k, nxy = nk >> sxy, c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nxy * nxy * nk) return;
+    const int ix = c / (nxy * nk), iy = (c / nk) % nxy, iz = c % nk, w = 1 << (FL - k);
     long long tot = 0;
     for (int a = 0; a < w; a++)
         for (int b = 0; b < w; b++)
@@ -179,7 +185,10 @@ extern "C" int gbfmm_features(const void* d_coords, const void* d_charges, int n
                               void* stream)
 {
     if (!feat || !box || n < 0 || (n > 0 && (!d_coords || !d_charges))) return GBFMM_ERR_ARG;
-    if (!(box[0] > 0) || box[4] != box[0] || box[8] != box[0]) return GBFMM_ERR_BOX;
+    if (!(box[0] > 0) || box[4] != box[0]) return GBFMM_ERR_BOX;
+    const bool slab = std::fabs((double)box[8] - 2.0 * (double)box[0]) <= 1e-6 * (double)box[8];
+    if (box[8] != box[0] && !slab) return GBFMM_ERR_BOX;
+    const int sxy = slab ? 1 : 0;  // the box's cells of the root cube: half of it along x and y
     cudaStream_t s = (cudaStream_t)stream;
     const int nb = std::max(1, std::min(608, (n + 255) / 256));
     // one scratch allocation per call: counts + histograms + partials
@@ -193,14 +202,16 @@ extern "C" int gbfmm_features(const void* d_coords, const void* d_charges, int n
     sums = (long long*)(((uintptr_t)sums + 7) & ~(uintptr_t)7);
     double* part = (double*)(sums + 5);
     cudaMemsetAsync(buf, 0, sizeof(int) * NCELL + sizeof(int) * (5 * NBIN + 2) + sizeof(long long) * 5, s);
-    const float inv = (float)((1 << FL) / (double)box[0]);
+    const double C = slab ? 2.0 * (double)box[0] : (double)box[0];  // edge of the tree's root cube
+    const float inv = (float)((1 << FL) / C);
     if (n > 0) {
         g_kernel_launches.fetch_add(1);
-        k_feat_counts<<<nb, 256, 0, s>>>((const float*)d_coords, (const float*)d_charges, n, inv, counts, part);
+        k_feat_counts<<<nb, 256, 0, s>>>((const float*)d_coords, (const float*)d_charges, n, inv, sxy, counts, part);
     }
     for (int k = 2; k <= FL; k++) {
         g_kernel_launches.fetch_add(1);
-        k_feat_hist<<<blocks(1L << (3 * k), 128), 128, 0, s>>>(counts, k, hist + NBIN * (k - 2), sums + (k - 2));
+        k_feat_hist<<<blocks((1L << (3 * k)) >> (2 * sxy), 128), 128, 0, s>>>(counts, k, sxy, hist + NBIN * (k - 2),
+                                                                              sums + (k - 2));
     }
     int h_hist[5 * NBIN];
     long long h_sums[5];
@@ -214,17 +225,17 @@ extern "C" int gbfmm_features(const void* d_coords, const void* d_charges, int n
     double m[5] = {0, 0, 0, 0, 0};
     for (int b = 0; b < nb; b++)
         for (int k = 0; k < 5; k++) m[k] += h_part[5 * b + k];
-    const double L = box[0], V = L * L * L, N = std::max(n, 1);
+    const double Lx = box[0], Lz = slab ? C : Lx, V = Lx * Lx * Lz, N = std::max(n, 1);
     feat[0] = (float)std::log10(N);
     feat[1] = (float)std::log10(N / V);
-    feat[2] = (float)std::log10(L);
+    feat[2] = (float)std::log10(C);
     feat[3] = (float)(m[1] / N);
     feat[4] = (float)(std::fabs(m[0]) / std::sqrt(m[1] + 1e-30));
-    const double c = L / 2;
-    const double dx = m[2] - m[0] * c, dy = m[3] - m[0] * c, dz = m[4] - m[0] * c;
+    const double dx = m[2] - m[0] * Lx / 2, dy = m[3] - m[0] * Lx / 2, dz = m[4] - m[0] * Lz / 2;
     feat[5] = (float)std::log10((dx * dx + dy * dy + dz * dz) / (V * (m[1] + 1e-30)) + 1e-12);
+    feat[56] = slab ? 1.f : 0.f;
     for (int k = 2; k <= FL; k++) {
-        const double cells = std::pow(8.0, k);
+        const double cells = std::pow(8.0, k) / (slab ? 4.0 : 1.0);
         int nonempty = 0;
         for (int b = 0; b < NBIN; b++) {
             feat[6 + NBIN * (k - 2) + b] = (float)(h_hist[NBIN * (k - 2) + b] / cells);
@@ -515,6 +526,10 @@ extern "C" int gbfmm_mlp_predict(gbfmm_mlp* m, const float* x, int B, float* y)
 // Candidate encoding appended to the statistics.  The precision enters as the
 // mantissa bits its M2L operands carry, over 24: FP32 1, BF16X3 (hi+lo split)
 // 16/24, BF16X1 8/24.
+// Leaves the tree of depth D stores: 8^D of a cube, the box's quarter of a slab's
+// root cube (statistic [56] is 1 for a slab).
+static double stored_leaves(const float* feat, int D) { return std::pow(8.0, D) / (feat[56] > 0.5f ? 4.0 : 1.0); }
+
 static void candidate_input(const float* feat, int P, int D, int prec, float* row)
 {
     std::memcpy(row, feat, sizeof(float) * GBFMM_NFEAT);
@@ -522,7 +537,7 @@ static void candidate_input(const float* feat, int P, int D, int prec, float* ro
     row[GBFMM_NFEAT + 0] = P / 10.f;
     row[GBFMM_NFEAT + 1] = D / 6.f;
     row[GBFMM_NFEAT + 2] = prec == GBFMM_PREC_BF16X1 ? 8.f / 24.f : (prec == GBFMM_PREC_BF16X3 ? 16.f / 24.f : 1.f);
-    row[GBFMM_NFEAT + 3] = (float)(std::log2(N / std::pow(8.0, D)) / 5.0);
+    row[GBFMM_NFEAT + 3] = (float)(std::log2(N / stored_leaves(feat, D)) / 5.0);
 }
 
 extern "C" int gbfmm_tuner_input(const float* feat, int order, int depth, int precision, float* row)
@@ -544,7 +559,7 @@ extern "C" int gbfmm_tuner_propose(gbfmm_mlp* m, const float* feat, double tol, 
     std::vector<float> rows;
     std::vector<int> cand;
     for (int D = 1; D <= 7; D++) {
-        const double per = N / std::pow(8.0, D);
+        const double per = N / stored_leaves(feat, D);
         if (per < 2 || per > 200) continue;
         for (int P = 4; P <= 10; P++)
             for (int prec = GBFMM_PREC_BF16X3; prec <= GBFMM_PREC_BF16X1; prec++) {
@@ -674,6 +689,7 @@ int solve_forces(int n, const float* q, const float* x, const float* box, int P,
     p.max_depth = D;
     p.images = images;
     p.precision = prec;
+    p.aspect_z = box[8] != box[0] ? 2 : 1;  // a slab (the box check is gbfmm_execute's)
     gbfmm_handle* h = nullptr;
     int rc = gbfmm_create(&p, n, &h);
     if (rc) return rc;
@@ -720,7 +736,8 @@ extern "C" int gbfmm_tuner_choose(gbfmm_mlp* m, int natoms, const float* charges
         if (rc) return rc;
     }
     // the judge: the plain order-10 FP32 FMM of this configuration
-    const int plain_order = 10, plain_depth = gbfmm_plain_depth(n);
+    // (of a slab the depth of a cube of four copies: the same bodies per leaf)
+    const int plain_order = 10, plain_depth = gbfmm_plain_depth(feat[56] > 0.5f ? 4 * n : n);
     std::vector<float> fj, fc;
     int rc = solve_forces(n, charges, coords, box, plain_order, plain_depth, GBFMM_PREC_FP32, images, fj);
     if (rc) return rc;

@@ -22,7 +22,7 @@ lib, _check, FmmError = _pkg.lib, _pkg._check, _pkg.FmmError
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 WEIGHTS = os.path.join(HERE, "tuner_weights.bin")
-NFEAT = 56
+NFEAT = 57
 N_IN = NFEAT + 4
 PLAIN_ORDER = 10
 
@@ -224,8 +224,10 @@ class TunedSolver:
         self.choice = None
         self.checks = []
 
-    def _plain(self):
-        return _pkg.ZetaFmmSolver(self.n, self.q, order=PLAIN_ORDER, max_depth=plain_depth(self.n), images=self.images)
+    def _plain(self, box=None):
+        slab = box is not None and np.size(box) == 3 and float(np.ravel(box)[2]) != float(np.ravel(box)[0])
+        return _pkg.ZetaFmmSolver(self.n, self.q, order=PLAIN_ORDER, max_depth=plain_depth(4 * self.n if slab else self.n),
+                                  images=self.images, aspect_z=2 if slab else 1)
 
     def propose(self, coords, box):
         """Computes statistics, proposes, and checks the proposal against the
@@ -248,7 +250,7 @@ class TunedSolver:
                                     "accepted": not c.fallback and k == c.nchecks - 1})
         self.choice = (c.order, c.depth, c.precision)
         self.solver = _pkg.ZetaFmmSolver(self.n, self.q, order=c.order, max_depth=c.depth, images=self.images,
-                                         precision=c.precision)
+                                         precision=c.precision, aspect_z=2 if m[8] != m[0] else 1)
         self.solver.execute(coords, box)
         return self.choice
 

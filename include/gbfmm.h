@@ -158,10 +158,11 @@ int gbfmm_lists(int max_depth, int images, int which, long* count, int* target, 
 
 /* Per-step statistics of a system (no counterpart in the reference, which fixes
  * P=10 and depth 3, zeta_fmm_solver.cpp:10-11): GBFMM_NFEAT floats -- log N,
- * log density, log L, mean q^2, net-charge and dipole ratios, and the body
- * occupancy histograms of octree levels 2..6 -- computed on the GPU from device
- * coordinates and charges.  Written to host memory 'features'. */
-#define GBFMM_NFEAT 56
+ * log density, log L, mean q^2, net-charge and dipole ratios, the body
+ * occupancy histograms of octree levels 2..6, and the box shape (log2 Lz/Lx: a
+ * cube or a slab) -- computed on the GPU from device coordinates and charges.
+ * Written to host memory 'features'. */
+#define GBFMM_NFEAT 57
 int gbfmm_features(const void* coords, const void* charges, int natoms, const float* box, float* features,
                    void* stream);
 

@@ -9,7 +9,8 @@ Ewald sum):
       --out gromacs-fmm_gb300/tuner_weights.bin
 
 One tuple = the statistics of one seeded system (gbfmm_features) + one candidate
-(order 4..10, every depth with 2..200 bodies per leaf, BF16X3 and BF16X1 M2L) +
+(order 4..10, every depth with 2..200 bodies per stored leaf, BF16X3 and BF16X1
+M2L) +
 two labels: log10 of the candidate's relative RMS force error against FP64 Ewald
 (eps 1e-9) on a stride sample of at most 1000 atoms, and log10 of its step time
 in ms (device-resident inputs, CUDA events, L2 flushed before every step, median
@@ -36,28 +37,43 @@ SITE_DENSITY = 33.4     # water sites per nm^3 at 1 g/cm^3
 
 
 def system_specs(n, seed0):
-    """Seeded system descriptions: size, density, ion content, slab fraction."""
+    """Seeded system descriptions: size (1,000 to 330,000 water sites, about 3,000
+    to 1,000,000 atoms, log-uniform), density, ion content, box shape (a cube, or
+    a slab Lx = Ly, Lz = 2 Lx) and the filled fraction of the box's height (the
+    rest is vacuum)."""
     out = []
     for i in range(n):
         rng = np.random.default_rng(seed0 + i)
-        n_sites = int(round(10 ** rng.uniform(3.0, 4.92)))
+        n_sites = int(round(10 ** rng.uniform(3.0, 5.52)))
         dens = float(rng.choice([0.7, 1.0, 1.0, 1.35]))
         ion = float(rng.choice([0.0, 0.002, 0.01, 0.03]))
-        fill = float(rng.choice([1.0, 1.0, 1.0, 0.55]))
-        out.append(dict(n_sites=n_sites, dens=dens, ion=ion, fill=fill, seed=seed0 + i))
+        slab = bool(rng.random() < 0.3)
+        fill = float(rng.choice([1.0, 0.5, 0.5])) if slab else float(rng.choice([1.0, 1.0, 1.0, 0.55]))
+        out.append(dict(n_sites=n_sites, dens=dens, ion=ion, fill=fill, slab=slab, seed=seed0 + i))
     return out
 
 
 def make_system(systems, spec):
-    L = (spec["n_sites"] / (SITE_DENSITY * spec["dens"] * spec["fill"])) ** (1.0 / 3.0)
+    """(coords, charges, box [Lx, Ly, Lz])."""
+    vol = spec["n_sites"] / (SITE_DENSITY * spec["dens"] * spec["fill"])
+    if spec.get("slab"):
+        a = (vol / 2.0) ** (1.0 / 3.0)
+        box = [a, a, 2 * a]
+    else:
+        L = vol ** (1.0 / 3.0)
+        box = [L, L, L]
     ions = int(spec["n_sites"] * spec["ion"] / 2)
-    xyz, q, box = systems.water_ion_box(spec["n_sites"], L, n_na=ions, n_cl=ions, seed=spec["seed"],
-                                        fill_z=spec["fill"])
-    return xyz, q, float(box[0])
+    xyz, q, b = systems.water_ion_box(spec["n_sites"], box, n_na=ions, n_cl=ions, seed=spec["seed"],
+                                      fill_z=spec["fill"])
+    b32 = [float(np.float32(v)) for v in b]
+    b32[2] = 2 * b32[0] if spec.get("slab") else b32[0]
+    b32[1] = b32[0]
+    return xyz, q, b32
 
 
-def depths_for(natoms):
-    return [d for d in range(1, 8) if 2 <= natoms / 8.0 ** d <= 200]
+def depths_for(natoms, slab=False):
+    stored = (lambda d: 8.0 ** d / 4) if slab else (lambda d: 8.0 ** d)
+    return [d for d in range(1, 8) if 2 <= natoms / stored(d) <= 200]
 
 
 class Timer:
@@ -95,20 +111,22 @@ def generate(args):
     timer = Timer(torch)
     rows = []
     t_start = time.time()
+    O.set_threads(os.cpu_count() or 1)
     for k, spec in enumerate(system_specs(args.systems, args.seed)):
         xyz, q, L = make_system(systems, spec)
         n = len(q)
         stride = max(97, n // 1000)
         tg = np.arange(0, n, stride)
-        _, fe, _ = O.ewald(xyz.astype(np.float64), q.astype(np.float64), L, eps=1e-9, targets=tg)
+        _, fe, _ = O.ewald(xyz.astype(np.float64), q.astype(np.float64), np.array(L), eps=1e-9, targets=tg)
         xd = torch.from_numpy(np.ascontiguousarray(xyz, np.float32)).cuda()
         qd = torch.from_numpy(np.ascontiguousarray(q, np.float32)).cuda()
         feat = tuner.features(xd.data_ptr(), qd.data_ptr(), n, L, torch.cuda.current_stream().cuda_stream)
         torch.cuda.synchronize()
-        for D in depths_for(n):
+        aspect = 2 if spec.get("slab") else 1
+        for D in depths_for(n, aspect == 2):
             for P in ORDERS:
                 for prec in PRECS:
-                    s = pkg.ZetaFmmSolver(n, q, order=P, max_depth=D, images=4, precision=prec)
+                    s = pkg.ZetaFmmSolver(n, q, order=P, max_depth=D, images=4, precision=prec, aspect_z=aspect)
                     s.execute(xyz, L)
                     f = s.forces()
                     err = float(np.sqrt(np.sum((f[tg] - fe) ** 2) / np.sum(fe ** 2)))
@@ -192,7 +210,7 @@ def main():
     sub = ap.add_subparsers(dest="cmd", required=True)
     g = sub.add_parser("generate")
     g.add_argument("--out", default=os.path.join(ROOT, "tests", "golden", "tuner_tuples.npz"))
-    g.add_argument("--systems", type=int, default=40)
+    g.add_argument("--systems", type=int, default=70)
     g.add_argument("--seed", type=int, default=5000)
     tr = sub.add_parser("train")
     tr.add_argument("--tuples", default=os.path.join(ROOT, "tests", "golden", "tuner_tuples.npz"))

@@ -81,46 +81,56 @@ def test_save_load_and_corruption(tuner, tmp_path, pkg):
     m2.close()
 
 
-def _features_numpy(xyz, q, L):
-    """Restatement of gbfmm_features' statistics."""
+def _features_numpy(xyz, q, box):
+    """Restatement of gbfmm_features' statistics: a cube of edge L, or a slab
+    L x L x 2L whose tree root is the cube of edge 2L (only the box's cells)."""
+    b = np.broadcast_to(np.asarray(box, np.float64), (3,))
+    slab = b[2] != b[0]
+    C = b[2]
+    sxy = 1 if slab else 0
     x = np.asarray(xyz, np.float32)
-    inv = np.float32(64 / np.float64(L))
-    idx = np.clip(np.floor(x * inv).astype(np.int64), 0, 63)
+    inv = np.float32(64 / np.float64(C))
+    hi = np.array([64 >> sxy, 64 >> sxy, 64])
+    idx = np.clip(np.floor(x * inv).astype(np.int64), 0, hi - 1)
     N = len(q)
     q64 = q.astype(np.float64)
-    V = L ** 3
-    f = np.zeros(56)
+    V = b[0] * b[1] * b[2]
+    f = np.zeros(57)
     f[0] = np.log10(N)
     f[1] = np.log10(N / V)
-    f[2] = np.log10(L)
+    f[2] = np.log10(C)
     f[3] = np.sum(q64 ** 2) / N
     f[4] = abs(q64.sum()) / np.sqrt(np.sum(q64 ** 2))
-    d = (q64[:, None] * x.astype(np.float64)).sum(0) - q64.sum() * L / 2
-    f[5] = np.log10(np.sum(d ** 2) / (V * np.sum(q64 ** 2)) + 1e-12)
+    d = (q64[:, None] * x.astype(np.float64)).sum(0) - q64.sum() * b / 2
+    f[5] = np.log10(np.sum(d * d) / (V * np.sum(q64 ** 2)) + 1e-12)
+    f[56] = 1.0 if slab else 0.0
     for k in range(2, 7):
         c = idx >> (6 - k)
-        cell = (c[:, 0] << (2 * k)) | (c[:, 1] << k) | c[:, 2]
-        cnt = np.bincount(cell, minlength=8 ** k)
-        b = np.zeros(len(cnt), np.int64)
+        nxy = (1 << k) >> sxy
+        cell = (c[:, 0] * nxy + c[:, 1]) * (1 << k) + c[:, 2]
+        cnt = np.bincount(cell, minlength=nxy * nxy * (1 << k))
+        bb = np.zeros(len(cnt), np.int64)
         nz = cnt > 0
-        b[nz] = np.minimum(1 + np.floor(np.log2(cnt[nz])).astype(np.int64), 8)
-        f[6 + 9 * (k - 2):6 + 9 * (k - 1)] = np.bincount(b, minlength=9) / 8.0 ** k
+        bb[nz] = np.minimum(1 + np.floor(np.log2(cnt[nz])).astype(np.int64), 8)
+        f[6 + 9 * (k - 2):6 + 9 * (k - 1)] = np.bincount(bb, minlength=9) / len(cnt)
         f[51 + k - 2] = np.log2(N / nz.sum())
     return f
 
 
 def test_features_match_numpy(tuner, systems):
-    for spec in [(3000, 4.0, 0, 1.0), (9000, 5.2, 20, 0.55)]:
-        n_sites, L, ions, fill = spec
-        xyz, q, box = systems.water_ion_box(n_sites, L, n_na=ions, n_cl=ions, seed=11, fill_z=fill)
+    for spec in [(3000, 4.0, 0, 1.0, False), (9000, 5.2, 20, 0.55, False), (6000, 3.6, 10, 0.5, True)]:
+        n_sites, L, ions, fill, slab = spec
+        box = [L, L, 2 * L] if slab else L
+        xyz, q, b = systems.water_ion_box(n_sites, box, n_na=ions, n_cl=ions, seed=11, fill_z=fill)
         xd = torch.from_numpy(xyz).cuda()
         qd = torch.from_numpy(q).cuda()
-        f = tuner.features(xd.data_ptr(), qd.data_ptr(), len(q), float(box[0]),
-                           torch.cuda.current_stream().cuda_stream)
+        bx = [float(np.float32(v)) for v in np.broadcast_to(b, (3,))]
+        f = tuner.features(xd.data_ptr(), qd.data_ptr(), len(q), bx, torch.cuda.current_stream().cuda_stream)
         torch.cuda.synchronize()
-        ref = _features_numpy(xyz, q, float(box[0]))
+        ref = _features_numpy(xyz, q, bx)
         assert np.allclose(f[6:51], ref[6:51], atol=1e-7)   # occupancy histograms: exact counts
-        assert np.allclose(f[[0, 1, 2, 3, 51, 52, 53, 54, 55]], ref[[0, 1, 2, 3, 51, 52, 53, 54, 55]], rtol=1e-5)
+        assert np.allclose(f[[0, 1, 2, 3, 51, 52, 53, 54, 55, 56]], ref[[0, 1, 2, 3, 51, 52, 53, 54, 55, 56]],
+                           rtol=1e-5)
         assert abs(f[4] - ref[4]) <= 1e-4 * max(1.0, ref[4]) + 1e-6
         assert abs(f[5] - ref[5]) <= 1e-3 * max(1.0, abs(ref[5]))
 

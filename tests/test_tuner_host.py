@@ -38,6 +38,7 @@ def test_candidate_encoding(pkg):
     tuner = G.load_module("tuner")
     feat = np.arange(tuner.NFEAT, dtype=np.float32) * 0.01
     feat[0] = np.log10(95600)
+    feat[56] = 0.0  # a cube
     for prec, bits in [(0, 1.0), (1, 16 / 24), (2, 8 / 24)]:
         r = tuner.tuner_input(feat, 7, 4, prec)
         assert np.array_equal(r[:tuner.NFEAT], feat)
@@ -45,6 +46,10 @@ def test_candidate_encoding(pkg):
         assert np.isclose(r[tuner.NFEAT + 1], 4 / 6)
         assert np.isclose(r[tuner.NFEAT + 2], bits)
         assert np.isclose(r[tuner.NFEAT + 3], np.log2(95600 / 8 ** 4) / 5, rtol=1e-5)
+    # a slab (statistic 56 = 1) stores a quarter of the root cube's leaves
+    feat[56] = 1.0
+    r = tuner.tuner_input(feat, 7, 4, 1)
+    assert np.isclose(r[tuner.NFEAT + 3], np.log2(95600 / (8 ** 4 / 4)) / 5, rtol=1e-5)
     with pytest.raises(pkg.FmmError):
         tuner.tuner_input(feat, 7, 4, 3)
 
@@ -75,10 +80,13 @@ def test_weights_file_format_and_checksum():
 def test_training_tuples():
     d = np.load(TUPLES)
     n = len(d["order"])
-    assert n >= 500
+    assert n >= 2000
+    assert d["natoms"].max() >= 500000  # sizes up to about a million atoms
     assert np.all(np.isfinite(d["err"])) and np.all(d["err"] > 0)
     assert np.all(np.isfinite(d["ms"])) and np.all(d["ms"] > 0)
-    assert d["feat"].shape == (n, 56)
+    assert d["feat"].shape == (n, 57)
+    slab = d["feat"][:, 56] > 0.5
+    assert slab.any() and (~slab).any()  # both box shapes
     # within one system, depth and precision: the error falls with the order
     falls = total = 0
     for k in np.unique(d["system"]):
