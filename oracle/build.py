@@ -4,7 +4,8 @@ Compiles oracle/zeta64.c and oracle/ewald64.c into oracle/lib/liboracle.so with
 OpenMP.  Portable C: no architecture flags, so the same recipe builds on x86_64
 and aarch64.  ``build(ref=True)`` additionally runs oracle/ref_build.sh, which
 compiles the reference's own tree/traverser sources when the reference checkout
-is present (it is absent on GPU machines; the recipe then does nothing).
+is present (it is absent on GPU machines; the recipe then does nothing), and
+oracle/rtfmm_build.sh, which builds the reference's own CPU FMM there (x86-64).
 """
 import os
 import platform
@@ -36,6 +37,11 @@ def build(ref=False, force=False):
         subprocess.run(cmd, check=True)
     if ref:
         subprocess.run(["bash", os.path.join(HERE, "ref_build.sh")], check=True)
+        rt = os.path.join(HERE, "_ref", "librtfmmref.so")
+        deps = [os.path.join(HERE, f) for f in ("rtfmm_build.sh", "rtfmm_driver.cpp", "rtfmm_fftw.cpp",
+                                                 "rtfmm_lapack.cpp")]
+        if force or not os.path.exists(rt) or any(os.path.getmtime(d) > os.path.getmtime(rt) for d in deps):
+            subprocess.run(["bash", os.path.join(HERE, "rtfmm_build.sh")], check=True)
     return LIB
 
 

@@ -177,6 +177,38 @@ def direct(xyz, q, L, nmax):
 
 # ------------------------------------------------------------------ reference itself
 
+RTFMM_LIB = os.path.join(HERE, "_ref", "librtfmmref.so")
+_rt = None
+
+
+def rtfmm_available():
+    """The reference's own CPU FMM (src/gromacs/rtfmm, built by rtfmm_build.sh on
+    an x86-64 host where the reference checkout exists)."""
+    return os.path.exists(RTFMM_LIB)
+
+
+def rtfmm_solve(xyz, q, cycle, P=10, depth=3, images=4):
+    """The reference's own CPU FMM (kernel-independent, P surface points per
+    edge, OpenMP) on a cubic periodic box: potentials and forces in GROMACS
+    units, as rtFmmSolver::execute leaves them."""
+    global _rt
+    if _rt is None:
+        L = ctypes.CDLL(RTFMM_LIB)
+        L.rtfmm_ref_solve.restype = ctypes.c_int
+        L.rtfmm_ref_solve.argtypes = [ctypes.c_int, _dp, _dp, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                      ctypes.c_int, _dp, _dp]
+        _rt = L
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    n = len(q)
+    pot = np.zeros(n)
+    force = np.zeros((n, 3))
+    rc = _rt.rtfmm_ref_solve(n, _d(xyz), _d(q), float(cycle), int(P), int(depth), int(images), _d(pot), _d(force))
+    if rc != 0:
+        raise ValueError("rtfmm_ref_solve rejected its arguments")
+    return pot, force
+
+
 def ref_available():
     return os.path.exists(REF_LIB)
 

@@ -169,3 +169,22 @@ def test_oracle_slab_converges_to_rectangular_ewald(oracle, systems):
         errs.append(rel_rms(fo, fe))
         assert abs(eo - ee) / abs(ee) < 1e-4
     assert errs[1] < 0.2 * errs[0] and errs[1] < 5e-4
+
+
+def test_reference_cpu_fmm_converges_to_ewald(oracle, systems):
+    """The reference's own CPU FMM (src/gromacs/rtfmm, built unmodified by
+    oracle/rtfmm_build.sh with the FFTW-subset and BLAS shims) on the 9,000-atom
+    box: its forces agree with the FP64 Ewald sum (P = 10 surface points, depth
+    3, images 4), and with this FP64 restatement of the GPU solver's algorithm.
+    It builds only on an x86-64 host with the reference checkout."""
+    if not oracle.rtfmm_available():
+        pytest.skip("reference CPU FMM not built on this host")
+    xyz, q, box = systems.cfg_small()
+    L = float(box[0])
+    x64, q64 = xyz.astype(np.float64), q.astype(np.float64)
+    p, f = oracle.rtfmm_solve(x64, q64, L, 10, 3, 4)
+    tg = np.arange(0, len(q), 7)
+    _, fe, _ = oracle.ewald(x64, q64, L, eps=1e-10, targets=tg)
+    assert rel_rms(f[tg], fe) < 1e-5
+    _, fo, _ = oracle.zeta_solve(x64, q64, L, 10, 3, 4)
+    assert rel_rms(fo, f) < 1e-4
