@@ -382,12 +382,17 @@ def large_line(pkg, torch, dev, systems, steps):
     t0 = time.perf_counter()
     pe, fe, _ = O.ewald(xyz.astype(np.float64), q.astype(np.float64), b3, eps=1e-9, targets=tg)
     ewald_s = time.perf_counter() - t0
+    # the FP64 Ewald energy of this system (about 15 minutes of host time) is
+    # stored with the script that computed it (tests/golden/make_slab_energy.py)
+    with open(os.path.join(ROOT, "tests", "golden", "ewald_slab1m.json")) as fh:
+        e_ref = json.load(fh)["energy_kj_mol"]
     run = Runner(pkg, torch, dev, xyz, q, [a, a, 2 * a])
     D = 6
     out = {"workload": "water+ion slab, 1,002,002 atoms: periodic 21.5 x 21.5 x 43 nm box, lower half 333,402 SPC/E "
                        "waters + 898 Na+ + 898 Cl- (0.15 M), upper half vacuum", "atoms": n, "depth": D,
            "box_nm": [a, a, 2 * a], "ewald": f"FP64 Ewald (oracle/ewald64.c) of the rectangular box: forces and "
-                                           f"potentials on {len(tg)} atoms (every 997th), eps 1e-9, {ewald_s:.1f} s"}
+                                           f"potentials on {len(tg)} atoms (every 997th), eps 1e-9, {ewald_s:.1f} s; "
+                                           "energy (eps 1e-7) from tests/golden/ewald_slab1m.json", "ewald_energy": e_ref}
     rows = []
     for P in (6, 8, 10, 12):
         for prec in (1, 2):
@@ -398,7 +403,7 @@ def large_line(pkg, torch, dev, systems, steps):
             pr, pc = pot_err(p[tg], pe)
             rows.append({"order": P, "precision": PREC_NAME[prec], "ms_per_step": ms, "value": n / (ms * 1e-3),
                          "rel_force_err_vs_ewald": rel_diff(f[tg], fe), "rel_pot_err_vs_ewald_modulo_constant": pr,
-                         "pot_offset_vs_ewald": pc, "energy": e})
+                         "pot_offset_vs_ewald": pc, "energy": e, "rel_energy_err_vs_ewald": abs(e - e_ref) / abs(e_ref)})
             s.close()
     s = pkg.ZetaFmmSolver(n, q, order=10, max_depth=D, images=4, precision=0, aspect_z=2)
     s.execute(xyz, [a, a, 2 * a])
@@ -408,7 +413,8 @@ def large_line(pkg, torch, dev, systems, steps):
     pr, pc = pot_err(p[tg], pe)
     out["plain_fp32_order10"] = {"ms_per_step": ms, "value": n / (ms * 1e-3), "rel_force_err_vs_ewald":
                                  rel_diff(f[tg], fe), "rel_pot_err_vs_ewald_modulo_constant": pr,
-                                 "pot_offset_vs_ewald": pc, "energy": e}
+                                 "pot_offset_vs_ewald": pc, "energy": e,
+                                 "rel_energy_err_vs_ewald": abs(e - e_ref) / abs(e_ref)}
     out["per_order"] = rows
     ok = [r for r in rows if r["rel_force_err_vs_ewald"] <= TOL]
     if ok:

@@ -37,8 +37,14 @@ static double wrap01(double x, double L)
     return y;
 }
 
-int ew64_solve(int n, const double* xyz, const double* q, const double box[3], double eps, double rc_in,
-               int n_tgt, const int* tgt, double* pot, double* force, int want_energy, double* energy)
+/* The Ewald sum; with 'vir' (and want_energy) also the virial tensor
+ * Xi = -1/2 sum_pairs r_ij (x) F_ij = 1/2 dE/d(strain), row-major 3 x 3:
+ * real space -1/4 sum_{i,j,n}' r_ijn (x) f_ijn, reciprocal space
+ * 1/2 sum_k E_k [2 k k / k^2 (1 + k^2 / (4 alpha^2)) - I], the self and
+ * background terms strain-free. */
+static int ew64_core(int n, const double* xyz, const double* q, const double box[3], double eps, double rc_in,
+                     int n_tgt, const int* tgt, double* pot, double* force, int want_energy, double* energy,
+                     double* vir)
 {
     if (n <= 0 || eps <= 0 || eps >= 1) return -1;
     double V = box[0] * box[1] * box[2];
@@ -154,6 +160,7 @@ int ew64_solve(int n, const double* xyz, const double* q, const double box[3], d
 
     int ntg = want_energy ? n : n_tgt;
     double* epart = (double*)calloc(ntg > 0 ? ntg : 1, sizeof(double));
+    double* vpart = vir ? (double*)calloc(6 * (size_t)(ntg > 0 ? ntg : 1), sizeof(double)) : NULL;
     const double rc2 = rc * rc;
     const double tsp = 2.0 / sqrt(M_PI);
 #pragma omp parallel
@@ -171,6 +178,7 @@ int ew64_solve(int n, const double* xyz, const double* q, const double box[3], d
                 if (ci[d] >= g[d]) ci[d] = g[d] - 1;
             }
             double phi = 0, f[3] = {0, 0, 0};
+            double w6[6] = {0, 0, 0, 0, 0, 0};  /* sum_j fs d (x) d (xx, yy, zz, xy, xz, yz) */
             for (int ox = -R[0]; ox <= R[0]; ox++) {
                 int cx = ci[0] + ox;
                 int wxi = ((cx % g[0]) + g[0]) % g[0];
@@ -196,6 +204,10 @@ int ew64_solve(int n, const double* xyz, const double* q, const double box[3], d
                             phi += q[j] * ec / r;
                             double fs = q[j] * (ec / r + tsp * alpha * exp(-alpha * alpha * r2)) / r2;
                             f[0] += fs * d0; f[1] += fs * d1; f[2] += fs * d2;
+                            if (vir) {
+                                w6[0] += fs * d0 * d0; w6[1] += fs * d1 * d1; w6[2] += fs * d2 * d2;
+                                w6[3] += fs * d0 * d1; w6[4] += fs * d0 * d2; w6[5] += fs * d1 * d2;
+                            }
                         }
                     }
                 }
@@ -225,6 +237,8 @@ int ew64_solve(int n, const double* xyz, const double* q, const double box[3], d
             phi -= tsp * alpha * q[i];
             phi -= M_PI * Q / (V * alpha * alpha);
             if (want_energy) epart[t] = q[i] * phi;
+            if (vir && want_energy)
+                for (int c = 0; c < 6; c++) vpart[6 * (size_t)t + c] = q[i] * w6[c];
             if (pot) pot[t] = phi * KE_GMX;
             if (force) {
                 force[3 * t] = q[i] * f[0] * KE_GMX;
@@ -239,8 +253,43 @@ int ew64_solve(int n, const double* xyz, const double* q, const double box[3], d
         for (int t = 0; t < ntg; t++) e += epart[t];
         *energy = 0.5 * e * KE_GMX;
     }
+    if (vir && want_energy) {
+        double w6[6] = {0, 0, 0, 0, 0, 0};
+        for (int t = 0; t < ntg; t++)
+            for (int c = 0; c < 6; c++) w6[c] += vpart[6 * (size_t)t + c];
+        /* reciprocal space: E_k = 1/2 kw |S_k|^2 per half-space vector */
+        double r6[6] = {0, 0, 0, 0, 0, 0};
+        for (int k = 0; k < nk; k++) {
+            double kx = 2 * M_PI * kv[3 * k] / box[0], ky = 2 * M_PI * kv[3 * k + 1] / box[1],
+                   kz = 2 * M_PI * kv[3 * k + 2] / box[2];
+            double k2 = kx * kx + ky * ky + kz * kz;
+            double Ek = 0.5 * kw[k] * (S[k].re * S[k].re + S[k].im * S[k].im);
+            double b = 2.0 * (1.0 + k2 / (4 * alpha * alpha)) / k2;
+            r6[0] += Ek * (b * kx * kx - 1); r6[1] += Ek * (b * ky * ky - 1); r6[2] += Ek * (b * kz * kz - 1);
+            r6[3] += Ek * b * kx * ky; r6[4] += Ek * b * kx * kz; r6[5] += Ek * b * ky * kz;
+        }
+        double v6[6];
+        for (int c = 0; c < 6; c++) v6[c] = (-0.25 * w6[c] + 0.5 * r6[c]) * KE_GMX;
+        vir[0] = v6[0]; vir[4] = v6[1]; vir[8] = v6[2];
+        vir[1] = vir[3] = v6[3];
+        vir[2] = vir[6] = v6[4];
+        vir[5] = vir[7] = v6[5];
+    }
+    free(vpart);
     free(epart); free(head); free(lst); free(wx); free(S); free(kv); free(kw);
     return nk;
+}
+
+int ew64_solve(int n, const double* xyz, const double* q, const double box[3], double eps, double rc_in,
+               int n_tgt, const int* tgt, double* pot, double* force, int want_energy, double* energy)
+{
+    return ew64_core(n, xyz, q, box, eps, rc_in, n_tgt, tgt, pot, force, want_energy, energy, NULL);
+}
+
+int ew64_virial(int n, const double* xyz, const double* q, const double box[3], double eps, double* energy,
+                double* vir)
+{
+    return ew64_core(n, xyz, q, box, eps, 0.0, 0, NULL, NULL, NULL, 1, energy, vir);
 }
 
 /* Direct lattice sum in spherical shells for tiny systems, tin-foil corrected:

@@ -58,6 +58,8 @@ def lib():
         L.ew64_solve.restype = ctypes.c_int
         L.ew64_solve.argtypes = [ctypes.c_int, _dp, _dp, _dp, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                  _ip, _dp, _dp, ctypes.c_int, _dp]
+        L.ew64_virial.restype = ctypes.c_int
+        L.ew64_virial.argtypes = [ctypes.c_int, _dp, _dp, _dp, ctypes.c_double, _dp, _dp]
         L.direct64_solve.restype = ctypes.c_int
         L.direct64_solve.argtypes = [ctypes.c_int, _dp, _dp, ctypes.c_double, ctypes.c_int, _dp, _dp]
         _lib = L
@@ -163,6 +165,18 @@ def ewald(xyz, q, box, eps=1e-10, targets=None, rc=0.0, energy=False):
     lib().ew64_solve(n, _d(xyz), _d(q), _d(box), float(eps), float(rc), nt, _i(tg), _d(pot), _d(force),
                      1 if energy else 0, _d(e))
     return pot, force, (float(e[0]) if energy else None)
+
+
+def ewald_virial(xyz, q, box, eps=1e-9):
+    """FP64 Ewald energy and virial tensor Xi = -1/2 sum_pairs r_ij (x) F_ij
+    (kJ/mol, 3 x 3), tin-foil boundary."""
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    box = np.ascontiguousarray(np.broadcast_to(np.asarray(box, dtype=np.float64), (3,)))
+    e = np.zeros(1)
+    vir = np.zeros(9)
+    lib().ew64_virial(len(q), _d(xyz), _d(q), _d(box), float(eps), _d(e), _d(vir))
+    return float(e[0]), vir.reshape(3, 3)
 
 
 def direct(xyz, q, L, nmax):

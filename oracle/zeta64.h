@@ -18,6 +18,9 @@ void z64_apply(int kind, int P, const double d[3], const double* in, double* out
 
 int ew64_solve(int n, const double* xyz, const double* q, const double box[3], double eps, double rc,
                int n_tgt, const int* tgt, double* pot, double* force, int want_energy, double* energy);
+/* Ewald energy and virial tensor Xi = -1/2 sum_pairs r_ij (x) F_ij (kJ/mol), 3 x 3 row-major. */
+int ew64_virial(int n, const double* xyz, const double* q, const double box[3], double eps, double* energy,
+                double* vir);
 int direct64_solve(int n, const double* xyz, const double* q, double L, int nmax, double* pot, double* force);
 
 #ifdef __cplusplus
