@@ -92,6 +92,7 @@ def lib():
             "gbfmm_debug_harmonics": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, dp, dp]),
             "gbfmm_debug_bounded_wait": (ctypes.c_int, [ctypes.c_uint, vp]),
             "gbfmm_batch_status": (ctypes.c_int, [vp]),
+            "gbfmm_get_virial": (ctypes.c_int, [vp, dp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -200,6 +201,12 @@ class ZetaFmmSolver:
         f = np.zeros((self.natoms, 3), np.float32)
         _check(lib().gbfmm_get_forces(self._h, _fp(f)))
         return f
+
+    def virial(self):
+        """Coulomb virial of the last execute, -1/2 sum_pairs r_ij (x) F_ij (kJ/mol, 3 x 3)."""
+        v = np.zeros(9)
+        _check(lib().gbfmm_get_virial(self._h, v.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        return v.reshape(3, 3)
 
     def potentials(self):
         p = np.zeros(self.natoms, np.float32)

@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "lib")
 LIB = os.path.join(OUT, "libgbfmm.so")
 
-SOURCES = ["kernels.cu", "m2l_tc.cu", "solver.cu", "operators.cpp", "tree_static.cu", "tuner.cu"]
+SOURCES = ["kernels.cu", "m2l_tc.cu", "solver.cu", "operators.cpp", "tree_static.cu", "tuner.cu", "virial.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -244,6 +244,41 @@ void launch_top(const TopArgs& a, cudaStream_t s);
 // sets bit 1 of *err.  Exercises the give-up path of the bounded waits.
 void launch_wait_probe(uint32_t polls, int* err, cudaStream_t s);
 
+// ---- virial (virial.cu): the image-shift terms of Xi = -1/2 sum_pairs r (x) F
+constexpr int VIR_MAXR = 320;  // rows of the largest expansion (order 16: 289)
+struct VirialM2LArgs {
+    int depth, R, Rpad;
+    long ncell[MAX_DEPTH + 1];     // stored cells per level
+    int shift[3];                  // stored cells per axis: grid_n(level, shift[d])
+    const CEntry* entries;         // M2L stencil entries, op = class index
+    int e_first[2][8], e_count[2][8];  // [level 1 | levels >= 2][target octant]
+    const float* ops;              // per class R x R FP32, [column][row]
+    const float* M[MAX_DEPTH + 1]; // multipoles per level (level 0: the root's FP32 copy)
+    float* lam[3][MAX_DEPTH + 1];  // shift-weighted locals per axis and level
+};
+struct VirialRootArgs {
+    int R, Rpad, n1;
+    const double* lat_shift;       // 3 x R x R (lattice_shift_operators)
+    const double* M0;              // root multipole (FP64)
+    const double* l2l;             // 8 x R x R root L2L (FP64)
+    double scale[3];               // root-cube edge / period along the axis
+    float* lam1[3];                // level-1 rows of the three shift-weighted locals
+};
+struct VirialReduceArgs {
+    const StepConst* sc;
+    int nleaf;
+    const int* off;
+    const float4* atoms;           // sorted (u, q)
+    const float4 *near, *far;      // sorted fields of the step
+    const float4* lam_field[3];    // sorted fields of the shift-weighted locals
+    const double* p2p_part;        // 9 per leaf (k_vir_p2p)
+    double* out;                   // 27 per block: sum r (x) F, sum F[Lambda], sum of the p2p partials
+};
+void launch_virial_p2p(const P2PArgs& a, double* part, cudaStream_t s);
+void launch_virial_m2l(const VirialM2LArgs& a, cudaStream_t s);
+void launch_virial_root(const VirialRootArgs& a, cudaStream_t s);
+void launch_virial_reduce(const VirialReduceArgs& a, int blocks, cudaStream_t s);
+
 struct FinalArgs {
     const StepConst* sc;
     int n;

@@ -291,6 +291,84 @@ void lattice_operator(int P, int images, double* A)
     }
 }
 
+// The lattice operator weighted by the image index of each source box: three
+// R x R FP64 matrices A_a (a = x, y, z) with L~_a = A_a M~_root the local
+// expansion, at the root, of the field of every far image box n weighted by
+// n_a (in periods).  Same hierarchy as lattice_operator: a level-m supercell
+// holds 3^m boxes per axis; with C_m its multipole operator, its first moment
+// C^a_m = sum over its boxes of (box offset from the supercell centre)_a x the
+// box's M2M satisfies C^a_{m+1} = sum_p M2M(p 3^m) (C^a_m + p_a 3^m C_m); a
+// source supercell centred at offset o contributes M2L (C^a_m + o_a C_m).  Used
+// by the virial's image-shift term.
+void lattice_shift_operators(int P, int images, double* A3)
+{
+    const int R = nreal(P);
+    const size_t RR = (size_t)R * R;
+    std::memset(A3, 0, sizeof(double) * 3 * RR);
+    if (images < 2) return;
+    // per level: S = sum of the source M2L operators and Sa = sum of o_a times
+    // them, so that sum T (C^a + o_a C) = S C^a + Sa C; likewise for the M2M step
+    std::vector<double> C(RR, 0.0), Ca[3], T(RR), S(RR), Sa[3], tmp(RR), B(RR), Ba[3], Cn(RR), Can[3];
+    for (int a = 0; a < 3; a++) {
+        Ca[a].assign(RR, 0.0);
+        Sa[a].assign(RR, 0.0);
+        Ba[a].assign(RR, 0.0);
+        Can[a].assign(RR, 0.0);
+    }
+    for (int i = 0; i < R; i++) C[(size_t)i * R + i] = 1.0;
+    double c3 = 1.0;
+    for (int m = 0; m < images - 1; m++) {
+        std::fill(S.begin(), S.end(), 0.0);
+        for (int a = 0; a < 3; a++) std::fill(Sa[a].begin(), Sa[a].end(), 0.0);
+        for (int pz = -1; pz <= 1; pz++)
+            for (int py = -1; py <= 1; py++)
+                for (int px = -1; px <= 1; px++) {
+                    if (px == 0 && py == 0 && pz == 0) continue;
+                    for (int cz = -1; cz <= 1; cz++)
+                        for (int cy = -1; cy <= 1; cy++)
+                            for (int cx = -1; cx <= 1; cx++) {
+                                const double o[3] = {(px * 3 + cx) * c3, (py * 3 + cy) * c3, (pz * 3 + cz) * c3};
+                                const double d[3] = {-o[0], -o[1], -o[2]};
+                                m2l_matrix(P, d, T.data());
+                                for (size_t i = 0; i < RR; i++) {
+                                    S[i] += T[i];
+                                    for (int a = 0; a < 3; a++) Sa[a][i] += o[a] * T[i];
+                                }
+                            }
+                }
+        for (int a = 0; a < 3; a++) {
+            matmul(R, S.data(), Ca[a].data(), tmp.data());
+            for (size_t i = 0; i < RR; i++) A3[a * RR + i] += tmp[i];
+            matmul(R, Sa[a].data(), C.data(), tmp.data());
+            for (size_t i = 0; i < RR; i++) A3[a * RR + i] += tmp[i];
+        }
+        if (m < images - 2) {
+            std::fill(B.begin(), B.end(), 0.0);
+            for (int a = 0; a < 3; a++) std::fill(Ba[a].begin(), Ba[a].end(), 0.0);
+            for (int pz = -1; pz <= 1; pz++)
+                for (int py = -1; py <= 1; py++)
+                    for (int px = -1; px <= 1; px++) {
+                        const double p[3] = {px * c3, py * c3, pz * c3};
+                        const double d[3] = {-p[0], -p[1], -p[2]};
+                        m2m_matrix(P, d, T.data());
+                        for (size_t i = 0; i < RR; i++) {
+                            B[i] += T[i];
+                            for (int a = 0; a < 3; a++) Ba[a][i] += p[a] * T[i];
+                        }
+                    }
+            for (int a = 0; a < 3; a++) {
+                matmul(R, B.data(), Ca[a].data(), Can[a].data());
+                matmul(R, Ba[a].data(), C.data(), tmp.data());
+                for (size_t i = 0; i < RR; i++) Can[a][i] += tmp[i];
+            }
+            matmul(R, B.data(), C.data(), Cn.data());
+            C = Cn;
+            for (int a = 0; a < 3; a++) Ca[a] = Can[a];
+        }
+        c3 *= 3.0;
+    }
+}
+
 // ------------------------------------------------------------------ stencils
 
 Stencils build_stencils(double theta)

@@ -50,6 +50,9 @@ void scaled_l2l(int P, int octant, double* A);
 void scaled_m2l(int P, const M2LClass& c, double* A);
 // Periodic lattice operator L~_root = A M~_root (root cell size 1), FP64.
 void lattice_operator(int P, int images, double* A);
+// The same lattice weighted by each far image box's index n_a (periods), a = x, y, z:
+// 3 consecutive R x R matrices (the virial's image-shift term).
+void lattice_shift_operators(int P, int images, double* A3);
 
 // Packed layout of an operator for the SIMT contraction kernel: rows in blocks of
 // 8; block b covers input columns [c0[b], c1[b]); stored as (c1-c0) x 8 floats.

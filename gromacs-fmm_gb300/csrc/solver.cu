@@ -219,6 +219,17 @@ struct gbfmm_handle {
     float stage_ms[16] = {};
     int n_stage = 0;
     int step_launches = 0;
+    // virial pass (allocated on the first gbfmm_get_virial)
+    void* vir_buf = nullptr;
+    float* vir_lam = nullptr;         // 3 x lev_floats shift-weighted locals
+    float4* vir_field = nullptr;      // 3 x N sorted fields of those locals
+    double* vir_p2p = nullptr;        // 9 per leaf
+    double* vir_out = nullptr;        // 27 per reduction block
+    float* vir_ops = nullptr;         // dense transposed M2L operators per class
+    CEntry* vir_entries = nullptr;    // M2L stencil entries, op = class index
+    double* vir_lat = nullptr;        // 3 x R x R shift-weighted lattice operators
+    int vir_e_first[2][8] = {}, vir_e_count[2][8] = {};
+    int vir_blocks = 0;
 };
 
 static const char* k_stage_names[] = {"tree", "p2m", "m2m", "root", "m2l", "l2l", "l2p", "p2p", "finalize"};
@@ -272,6 +283,7 @@ static void free_handle(gbfmm_handle* h)
     for (int i = 0; i < 16; i++)
         if (h->ev[i]) cudaEventDestroy(h->ev[i]);
     if (h->arena) cudaFree(h->arena);
+    if (h->vir_buf) cudaFree(h->vir_buf);
     if (h->h_sc) cudaFreeHost(h->h_sc);
     if (h->h_flags) cudaFreeHost(h->h_flags);
     if (h->h_forces) cudaFreeHost(h->h_forces);
@@ -1460,6 +1472,177 @@ extern "C" int gbfmm_debug_harmonics(int order, int kind, const double* d, doubl
         out[2 * i] = re[i];
         out[2 * i + 1] = im[i];
     }
+    return GBFMM_OK;
+}
+
+// ---- virial of the last step (virial.cu): Xi = -1/2 sum_i r_i (x) F_i + G / 4 plus
+// the tin-foil term, G the image-shift-weighted forces of the interactions that
+// cross the box (near-field and M2L stencil entries that wrap, far lattice).
+
+static int virial_setup(gbfmm_handle* h)
+{
+    const OpTables* t = h->tab;
+    const int R = h->R, ncls = (int)t->st.classes.size();
+    std::vector<CEntry> ent;
+    for (int lt = 0; lt < 2; lt++)
+        for (int s = 0; s < 8; s++) {
+            h->vir_e_first[lt][s] = (int)ent.size();
+            for (const StencilEntry& se : t->st.m2l[lt][s]) {
+                CEntry e;
+                e.dx = (int8_t)se.d[0]; e.dy = (int8_t)se.d[1]; e.dz = (int8_t)se.d[2];
+                e.mode = (int8_t)se.mode;
+                e.op = se.cls;
+                ent.push_back(e);
+            }
+            h->vir_e_count[lt][s] = (int)ent.size() - h->vir_e_first[lt][s];
+        }
+    std::vector<float> ops((size_t)ncls * R * R);
+    std::vector<double> A((size_t)R * R);
+    for (int c = 0; c < ncls; c++) {
+        scaled_m2l(h->P, t->st.classes[c], A.data());
+        for (int r = 0; r < R; r++)
+            for (int col = 0; col < R; col++) ops[(size_t)c * R * R + (size_t)col * R + r] = (float)A[(size_t)r * R + col];
+    }
+    std::vector<double> lat(3 * (size_t)R * R);
+    lattice_shift_operators(h->P, h->prm.images, lat.data());
+    h->vir_blocks = std::max(1, std::min(4 * sm_count(), h->nleaf));
+    Arena sz;
+    for (int pass = 0; pass < 2; pass++) {
+        Arena a;
+        a.base = pass ? (char*)h->vir_buf : nullptr;
+        h->vir_lam = a.take<float>(3 * h->lev_floats);
+        h->vir_field = a.take<float4>(3 * (size_t)std::max(h->n, 1));
+        h->vir_p2p = a.take<double>(9 * (size_t)h->nleaf);
+        h->vir_out = a.take<double>(27 * (size_t)h->vir_blocks);
+        h->vir_ops = a.take<float>(ops.size());
+        h->vir_entries = a.take<CEntry>(ent.size());
+        h->vir_lat = a.take<double>(lat.size());
+        if (pass == 0) {
+            cudaError_t e = cudaMalloc(&h->vir_buf, a.off + 256);
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                h->vir_buf = nullptr;
+                return fail(GBFMM_ERR_NOMEM, "virial buffers: %s", cudaGetErrorString(e));
+            }
+        }
+    }
+    CK(cudaMemcpy(h->vir_ops, ops.data(), sizeof(float) * ops.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->vir_entries, ent.data(), sizeof(CEntry) * ent.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->vir_lat, lat.data(), sizeof(double) * lat.size(), cudaMemcpyHostToDevice));
+    return GBFMM_OK;
+}
+
+extern "C" int gbfmm_get_virial(gbfmm_handle* h, double* vir)
+{
+    if (!h || !vir) return fail(GBFMM_ERR_ARG, "NULL argument");
+    if (!h->have_result) return fail(GBFMM_ERR_STATE, "no result: call gbfmm_execute first");
+    if (h->P > 16 || h->R > VIR_MAXR) return fail(GBFMM_ERR_UNSUPPORTED, "virial: order %d", h->P);
+    int rc = fetch(h);  // the step has completed without an error
+    if (rc) return rc;
+    if (!h->vir_buf) {
+        rc = virial_setup(h);
+        if (rc) return rc;
+    }
+    cudaStream_t s = h->stream;
+    const int D = h->D;
+    CK(cudaMemsetAsync(h->vir_lam, 0, sizeof(float) * 3 * h->lev_floats, s));
+    float* lam[3][MAX_DEPTH + 1] = {};
+    for (int x = 0; x < 3; x++) {
+        size_t o = 0;
+        for (int k = 0; k <= D; k++) {
+            lam[x][k] = h->vir_lam + x * h->lev_floats + o;
+            o += (size_t)h->ncell[k] * h->Rpad;
+        }
+    }
+    // near field: the wrapped stencil entries
+    P2PArgs pa = p2p_args(h);
+    launch_virial_p2p(pa, h->vir_p2p, s);
+    // M2L: the wrapped entries into the shift-weighted locals
+    if (h->periodic) {
+        VirialM2LArgs va;
+        std::memset(&va, 0, sizeof(va));
+        va.depth = D;
+        va.R = h->R;
+        va.Rpad = h->Rpad;
+        for (int k = 0; k <= D; k++) va.ncell[k] = h->ncell[k];
+        for (int d = 0; d < 3; d++) va.shift[d] = h->shift[d];
+        va.entries = h->vir_entries;
+        std::memcpy(va.e_first, h->vir_e_first, sizeof(va.e_first));
+        std::memcpy(va.e_count, h->vir_e_count, sizeof(va.e_count));
+        va.ops = h->vir_ops;
+        for (int k = 0; k <= D; k++) va.M[k] = h->Mlev[k];
+        for (int x = 0; x < 3; x++)
+            for (int k = 0; k <= D; k++) va.lam[x][k] = lam[x][k];
+        launch_virial_m2l(va, s);
+    }
+    // far lattice images, weighted by their index, at the root and L2L to level 1
+    const double a_edge = (double)h->h_sc->box_len / (h->aspect_z == 2 ? 2.0 : 1.0);
+    const double E[3] = {a_edge, a_edge, (double)h->h_sc->box_len};  // the box's periods
+    if (h->prm.images >= 2) {
+        VirialRootArgs ra;
+        ra.R = h->R;
+        ra.Rpad = h->Rpad;
+        ra.n1 = (int)h->ncell[1];
+        ra.lat_shift = h->vir_lat;
+        ra.M0 = h->d_M0;
+        ra.l2l = h->d_root_l2l;
+        for (int x = 0; x < 3; x++) {
+            ra.scale[x] = (double)h->h_sc->box_len / E[x];  // root-cube images in periods of the box
+            ra.lam1[x] = lam[x][1];
+        }
+        launch_virial_root(ra, s);
+    }
+    // downward pass of each shift-weighted local to the bodies
+    for (int x = 0; x < 3; x++) {
+        float4* field = h->vir_field + (size_t)x * std::max(h->n, 1);
+        if (D >= 2) {
+            DownArgs da;
+            da.nparent = (int)h->ncell[D - 1];
+            da.off = h->d_off;
+            da.atoms = h->d_atoms;
+            for (int k = 0; k <= D; k++) da.L[k] = lam[x][k];
+            da.l2l_t = h->d_l2l_t;
+            da.field = field;
+            da.depth = D;
+            da.Rpad = h->Rpad;
+            launch_down(h->P, da, s);
+        } else {
+            launch_l2p(h->P, h->d_off, h->nleaf, h->d_atoms, lam[x][1], h->Rpad, field, s);
+        }
+    }
+    VirialReduceArgs rd;
+    rd.sc = h->d_sc;
+    rd.nleaf = h->nleaf;
+    rd.off = h->d_off;
+    rd.atoms = h->d_atoms;
+    rd.near = h->d_near;
+    rd.far = h->d_far;
+    for (int x = 0; x < 3; x++) rd.lam_field[x] = h->vir_field + (size_t)x * std::max(h->n, 1);
+    rd.p2p_part = h->vir_p2p;
+    rd.out = h->vir_out;
+    launch_virial_reduce(rd, h->vir_blocks, s);
+    CK(cudaGetLastError());
+    std::vector<double> out(27 * (size_t)h->vir_blocks);
+    double sums[4];
+    CK(cudaMemcpyAsync(out.data(), h->vir_out, sizeof(double) * out.size(), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(sums, h->d_sums, sizeof(sums), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    double W[9] = {}, Gf[9] = {}, Gp[9] = {};
+    for (int b = 0; b < h->vir_blocks; b++)
+        for (int c = 0; c < 9; c++) {
+            W[c] += out[27 * (size_t)b + c];
+            Gf[c] += out[27 * (size_t)b + 9 + c];
+            Gp[c] += out[27 * (size_t)b + 18 + c];
+        }
+    const double inv_h = (double)h->h_sc->inv_h, kp = KE * inv_h * inv_h;
+    const double V = E[0] * E[1] * E[2];
+    const double M[3] = {sums[0], sums[1], sums[2]}, M2 = M[0] * M[0] + M[1] * M[1] + M[2] * M[2];
+    for (int x = 0; x < 3; x++)
+        for (int y = 0; y < 3; y++) {
+            const double G = h->periodic ? E[x] * (Gf[3 * x + y] + kp * Gp[3 * x + y]) : 0.0;
+            const double corr = -M_PI * KE / (3.0 * V) * (2.0 * M[x] * M[y] - (x == y ? M2 : 0.0));
+            vir[3 * x + y] = -0.5 * W[3 * x + y] + 0.25 * G + corr;
+        }
     return GBFMM_OK;
 }
 

@@ -118,6 +118,17 @@ int gbfmm_get_potentials(gbfmm_handle* h, float* potentials);
  * zeta_fmm::FMM::get_energy does (src/gromacs/zeta_fmm/fmm.cpp:89-98). */
 int gbfmm_get_energy(gbfmm_handle* h, double* coulomb_energy);
 
+/* Coulomb virial of the last execute, Xi = -1/2 sum over pairs (periodic images
+ * included) of r_ij (x) F_ij, kJ/mol, row-major 3 x 3, tin-foil boundary: what
+ * mdrun's ForceWithVirial takes for a force provider with its own virial
+ * (src/gromacs/mdlib/sim_util.cpp:2085), where the reference's plugin adds forces
+ * only (zeta_fmm_solver.cpp:66-76).  Computed on request by an extra pass over
+ * the step's tree, expansions and fields: -1/2 sum_i r_i (x) F_i, the forces of
+ * the interactions that cross the box (near-field and M2L stencil entries that
+ * wrap, the far lattice) weighted by their image shift, and the tin-foil term.
+ * The first call on a handle allocates its buffers. */
+int gbfmm_get_virial(gbfmm_handle* h, double* virial);
+
 /* BaseSolver::compare_forces (basesolver.h:82; zeta_fmm_solver.cpp:78-107):
  * relative L2 force error sqrt(sum|f-g|^2 / sum|g|^2) against host forces g.
  * Returns GBFMM_ERR_COORD (and l2f = NaN) if a result is NaN, where the

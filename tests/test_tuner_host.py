@@ -65,7 +65,7 @@ def test_weights_file_format_and_checksum():
     raw = open(WEIGHTS, "rb").read()
     assert raw[:8] == b"GBFMMMLP"
     ver, I, H, O = struct.unpack("<4i", raw[8:24])
-    assert (ver, I, O) == (1, 60, 2) and 8 <= H <= 256
+    assert (ver, I, O) == (1, 61, 2) and 8 <= H <= 256
     npar = H * I + H + H * H + H + O * H + O
     body = raw[24:24 + 4 * (npar + 2 * I + 2 * O)]
     assert len(raw) == 24 + len(body) + 8
