@@ -113,10 +113,11 @@ class Mlp:
     def load(cls, path=WEIGHTS):
         h = _vp()
         _check(_sig().gbfmm_mlp_load(path.encode(), ctypes.byref(h)))
-        m = cls(_handle=h)
-        n = ctypes.c_int()
-        _check(_sig().gbfmm_mlp_num_params(h, ctypes.byref(n)))
-        return m
+        # the network's shape from the file header: "GBFMMMLP", version, I, H, O (int32)
+        with open(path, "rb") as fh:
+            hdr = fh.read(24)
+        _, n_in, n_hidden, n_out = np.frombuffer(hdr[8:24], "<i4")
+        return cls(n_in=int(n_in), n_hidden=int(n_hidden), n_out=int(n_out), _handle=h)
 
     def close(self):
         if getattr(self, "_h", None):
