@@ -7,10 +7,11 @@
 // Mirrors zeta_fmm::ZetaFmmSolver (src/gromacs/zeta_fmm/zeta_fmm_solver.cpp),
 // with these differences: the device state lives for the solver's lifetime
 // (the reference allocates and frees it inside every execute); get_energy
-// returns 0.5 * sum(q * phi) (the reference's is a stub, :109-115); errors
-// throw instead of exit(); and, given a force-error tolerance instead of fixed
-// parameters, the solver takes the learned tuner's checked choice of order,
-// depth and M2L precision.
+// returns 0.5 * sum(q * phi) (the reference's is a stub, :109-115); add_force
+// also adds the Coulomb virial on the steps mdrun computes one (the reference
+// adds none, :66-76); errors throw instead of exit(); and, given a
+// force-error tolerance instead of fixed parameters, the solver takes the
+// learned tuner's checked choice of order, depth and M2L precision.
 #pragma once
 
 #include <cstdio>
@@ -70,8 +71,22 @@ public:
         check(gbfmm_execute(h_, coord.data()[0].as_vec(), &box[0][0], verbose));
     }
 
-    // zeta_fmm_solver.cpp:66-76: accumulates into the force buffer (no virial).
-    void add_force(gmx::ForceWithVirial* fv) override { check(gbfmm_add_forces(h_, fv->force_.data()[0].as_vec())); }
+    // zeta_fmm_solver.cpp:66-76: accumulates into the force buffer; on the steps
+    // mdrun computes the virial (computeVirial_), also the Coulomb virial
+    // -1/2 sum r_ij (x) F_ij of the lattice sum (gbfmm_get_virial), which a
+    // ForceWithVirial provider must add itself (sim_util.cpp:2085).
+    void add_force(gmx::ForceWithVirial* fv) override
+    {
+        check(gbfmm_add_forces(h_, fv->force_.data()[0].as_vec()));
+        if (fv->computeVirial_) {
+            double v[9];
+            check(gbfmm_get_virial(h_, v));
+            matrix m;
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++) m[i][j] = (real)v[3 * i + j];
+            fv->addVirialContribution(m);
+        }
+    }
 
     Energy get_energy() override
     {

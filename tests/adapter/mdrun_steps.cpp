@@ -6,7 +6,8 @@
 // usage: mdrun_steps in.bin out.bin order depth images [tol weights]
 //   in.bin : int32 natoms, int32 nsteps, float box[9], float q[natoms],
 //            float x[nsteps][natoms][3]
-//   out.bin: per step float f[natoms][3] (added to a buffer of ones), double energy
+//   out.bin: per step float f[natoms][3] (added to a buffer of ones), double energy,
+//            double virial[3][3] (the step's ForceWithVirial computes the virial)
 //   order 0: the learned tuner's checked choice for the force tolerance 'tol'
 //   (weights file 'weights'), printed as "choice order depth precision fallback"
 #include <cstdio>
@@ -56,11 +57,15 @@ int main(int argc, char** argv)
             s.set_parameter(md);
             s.execute(gmx::ArrayRef<const gmx::RVec>(x.data() + (size_t)step * n, n), box, 0, 0);
             for (auto& v : f) v = gmx::RVec(1.f, 1.f, 1.f);
-            gmx::ForceWithVirial fv(gmx::ArrayRef<gmx::RVec>(f.data(), n));
+            gmx::ForceWithVirial fv(gmx::ArrayRef<gmx::RVec>(f.data(), n), true);
             s.add_force(&fv);
             const coulomb_solver::Energy e = s.get_energy();
             std::fwrite(f.data(), sizeof(float), 3 * (size_t)n, out);
             std::fwrite(&e.coulomb_energy, sizeof(double), 1, out);
+            double vir[9];
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++) vir[3 * i + j] = fv.virial(i, j);
+            std::fwrite(vir, sizeof(double), 9, out);
         }
         if (tuned)
             std::printf("choice %d %d %d %d\n", solver.choice().order, solver.choice().depth,

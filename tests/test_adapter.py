@@ -48,13 +48,14 @@ def _run_driver(pkg, tmp_path, xyz, q, L, args):
     assert r.returncode == 0, r.stderr
     assert "L2f = 0.00000000" in r.stdout
     raw = (tmp_path / "out.bin").read_bytes()
-    rec = 12 * n + 8
+    rec = 12 * n + 8 + 72
     assert len(raw) == rec * len(steps)
     out = []
     for k, x in enumerate(steps):
         f = np.frombuffer(raw[k * rec:k * rec + 12 * n], np.float32).reshape(n, 3) - 1.0  # added to ones
-        e = np.frombuffer(raw[k * rec + 12 * n:(k + 1) * rec], np.float64)[0]
-        out.append((x, f, e))
+        e = np.frombuffer(raw[k * rec + 12 * n:k * rec + 12 * n + 8], np.float64)[0]
+        v = np.frombuffer(raw[k * rec + 12 * n + 8:(k + 1) * rec], np.float64).reshape(3, 3)
+        out.append((x, f, e, v))
     return out, r.stdout
 
 
@@ -64,10 +65,13 @@ def test_adapter_steps_match_the_oracle(pkg, oracle, systems, tmp_path):
     L = float(box[0])
     P, D, images = 8, 2, 4
     steps, _ = _run_driver(pkg, tmp_path, xyz, q, L, [P, D, images])
-    for x, f, e in steps:
+    for x, f, e, v in steps:
         po, fo, eo = oracle.zeta_solve(x.astype(np.float64), q.astype(np.float64), L, P, D, images)
         assert rel_rms(f, fo) < 1e-5
         assert abs(e - eo) / abs(eo) < 1e-6
+        # the virial the adapter adds to ForceWithVirial, against the FP64 Ewald virial
+        _, ve = oracle.ewald_virial(x.astype(np.float64), q.astype(np.float64), np.full(3, L), eps=1e-10)
+        assert np.linalg.norm(v - ve) / np.linalg.norm(ve) < 5e-3
 
 
 @pytest.mark.gpu
@@ -84,7 +88,7 @@ def test_adapter_with_the_learned_tuner(pkg, oracle, systems, tmp_path):
     order, depth, prec, fallback = (int(v) for v in line.split()[1:])
     assert 4 <= order <= 10 and 1 <= depth <= 7 and prec in (0, 1, 2)
     D0 = tuner.plain_depth(len(q))
-    for x, f, e in steps:
+    for x, f, e, _ in steps:
         _, fo, eo = oracle.zeta_solve(x.astype(np.float64), q.astype(np.float64), L, 10, D0, 4)
         assert rel_rms(f, fo) < tol
         assert abs(e - eo) / abs(eo) < tol
