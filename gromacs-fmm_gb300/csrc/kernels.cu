@@ -77,7 +77,7 @@ __device__ __forceinline__ double sum_tree_partials(const double* partials, int 
     return sum_partials_f64(reinterpret_cast<const float2*>(partials) + quantity, 4, nblocks);
 }
 
-__global__ void __launch_bounds__(256) k_tree_keys(TreeArgs a)
+__device__ __forceinline__ void tree_keys_body(const TreeArgs& a, const int bid, const int nb)
 {
     extern __shared__ float sh[];
     const int nd = 1 << a.depth;
@@ -95,19 +95,19 @@ __global__ void __launch_bounds__(256) k_tree_keys(TreeArgs a)
             const char* base = static_cast<const char*>(a.pf[k]);
             const unsigned long long bytes = a.pf_bytes[k] & ~15ull;
             const unsigned long long chunks = (bytes + 4095) >> 12;
-            for (unsigned long long c = blockIdx.x; c < chunks; c += gridDim.x) {
+            for (unsigned long long c = bid; c < chunks; c += nb) {
                 const unsigned long long o = c << 12;
                 const unsigned sz = (unsigned)min(4096ull, bytes - o);
                 asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(base + o), "r"(sz) : "memory");
             }
         }
     }
-    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < a.zero_n4; i += (long)gridDim.x * blockDim.x)
+    for (long i = (long)bid * blockDim.x + threadIdx.x; i < a.zero_n4; i += (long)nb * blockDim.x)
         a.zero[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     __syncthreads();
     f2sum sd[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};  // dipole (3), total charge
     int bad = 0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) {
+    for (int i = bid * blockDim.x + threadIdx.x; i < a.n; i += nb * blockDim.x) {
         float x[3] = {coords[3 * i], coords[3 * i + 1], coords[3 * i + 2]};
         float q = a.charges[i];
         if (!isfinite(x[0]) || !isfinite(x[1]) || !isfinite(x[2]) || !isfinite(q)) bad = 1;
@@ -148,7 +148,7 @@ __global__ void __launch_bounds__(256) k_tree_keys(TreeArgs a)
     if (threadIdx.x < 4) {
         f2sum t = red[0][threadIdx.x];
         for (int w = 1; w < (int)(blockDim.x >> 5); w++) t = f2s_add(t, red[w][threadIdx.x]);
-        reinterpret_cast<f2sum*>(a.partials)[4 * blockIdx.x + threadIdx.x] = t;
+        reinterpret_cast<f2sum*>(a.partials)[4 * bid + threadIdx.x] = t;
     }
     if (bad) atomicOr(&a.flags[0], 1);
     if (!a.done) return;
@@ -157,13 +157,13 @@ __global__ void __launch_bounds__(256) k_tree_keys(TreeArgs a)
     __shared__ int s_last;
     __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) s_last = atomicAdd(a.done, 1) == (int)gridDim.x - 1;
+    if (threadIdx.x == 0) s_last = atomicAdd(a.done, 1) == (int)nb - 1;
     __syncthreads();
     if (!s_last) return;
     __threadfence();
     if (threadIdx.x == 0) *a.done = 0;  // every block has counted: ready for the next step
     if (a.sums && warp < 4) {
-        const double t = sum_tree_partials(a.partials, (int)gridDim.x, warp);
+        const double t = sum_tree_partials(a.partials, (int)nb, warp);
         if (lane == 0) a.sums[warp] = t;
     }
     if (a.off) {
@@ -221,6 +221,8 @@ __global__ void __launch_bounds__(256) k_tree_keys(TreeArgs a)
         if (threadIdx.x == 0) a.off[n] = carry;
     }
 }
+
+__global__ void __launch_bounds__(256) k_tree_keys(TreeArgs a) { tree_keys_body(a, blockIdx.x, gridDim.x); }
 
 int tree_blocks(int n) { return n <= 0 ? 1 : (n + 255) / 256 < TREE_MAX_BLOCKS ? (n + 255) / 256 : TREE_MAX_BLOCKS; }
 int final_blocks(int n) { return n <= 0 ? 1 : (n + 255) / 256 < FINAL_MAX_BLOCKS ? (n + 255) / 256 : FINAL_MAX_BLOCKS; }
@@ -331,18 +333,21 @@ void launch_scatter(const uint32_t* code, int n, int* cursor, int* tmp_idx, cuda
     if (n > 0) { COUNT_LAUNCH(); k_scatter<<<(n + 255) / 256, 256, 0, s>>>(code, n, cursor, tmp_idx); }
 }
 
-__global__ void k_scatter_ranked(const uint32_t* code, int n, const int* off, const int* rank, int* tmp_idx)
+__device__ __forceinline__ void scatter_ranked_body(const ScatterArgs& a, const int bid)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) tmp_idx[off[code[i]] + rank[i]] = i;
+    int i = bid * blockDim.x + threadIdx.x;
+    if (i < a.n) a.tmp[a.off[a.code[i]] + a.rank[i]] = i;
 }
+
+__global__ void k_scatter_ranked(const ScatterArgs a) { scatter_ranked_body(a, blockIdx.x); }
 
 void launch_scatter_ranked(const uint32_t* code, int n, const int* off, const int* rank, int* tmp_idx,
                            cudaStream_t s)
 {
     if (n > 0) {
         COUNT_LAUNCH();
-        k_scatter_ranked<<<(n + 255) / 256, 256, 0, s>>>(code, n, off, rank, tmp_idx);
+        ScatterArgs a{code, n, off, rank, tmp_idx};
+        k_scatter_ranked<<<(n + 255) / 256, 256, 0, s>>>(a);
     }
 }
 
@@ -355,11 +360,19 @@ __device__ __forceinline__ bool at_leaf_face(float4 b)
     return fmaxf(fabsf(b.x), fmaxf(fabsf(b.y), fabsf(b.z))) >= 0.5f - 0x1p-20f;
 }
 
-__global__ void __launch_bounds__(256) k_leaf_sort(const int* off, int nleaf, const int* tmp_idx, const float4* uq,
-                                                   int* order, float4* atoms, int* inv, int* counts, int* edge)
+__device__ __forceinline__ void leaf_sort_body(const LeafSortArgs& la, const int bid)
 {
+    const int* off = la.off;
+    const int nleaf = la.nleaf;
+    const int* tmp_idx = la.tmp_idx;
+    const float4* uq = la.uq;
+    int* order = la.order;
+    float4* atoms = la.atoms;
+    int* inv = la.inv;
+    int* counts = la.counts;
+    int* edge = la.edge;
     const int lane = threadIdx.x & 31;
-    const int leaf = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int leaf = (bid * blockDim.x + threadIdx.x) >> 5;
     if (leaf >= nleaf) return;
     if (counts && lane == 0) counts[leaf] = 0;  // consumed by the scan: zero for the next step
     const int b = off[leaf], n = off[leaf + 1] - b;
@@ -394,14 +407,16 @@ __global__ void __launch_bounds__(256) k_leaf_sort(const int* off, int nleaf, co
     if (edge && lane == 0) edge[leaf] = any != 0u;
 }
 
+__global__ void __launch_bounds__(256) k_leaf_sort(const LeafSortArgs a) { leaf_sort_body(a, blockIdx.x); }
+
 void launch_leaf_sort(const int* offsets, int nleaf, int* tmp_idx, const float4* uq, const uint32_t* code, int* order,
                       float4* atoms, int* inv, int* counts, cudaStream_t s, int* edge)
 {
     (void)code;
     long threads = (long)nleaf * 32;
     COUNT_LAUNCH();
-    k_leaf_sort<<<(int)((threads + 255) / 256), 256, 0, s>>>(offsets, nleaf, tmp_idx, uq, order, atoms, inv,
-                                                            counts, edge);
+    LeafSortArgs a{offsets, nleaf, tmp_idx, uq, order, atoms, inv, counts, edge};
+    k_leaf_sort<<<(int)((threads + 255) / 256), 256, 0, s>>>(a);
 }
 
 // ------------------------------------------------------------------ P2M
@@ -442,13 +457,18 @@ __device__ __forceinline__ void stream_regular(float x, float y, float z, F&& f)
 }
 
 template <int P, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32) k_p2m(const int* off, int nleaf, const float4* atoms, float* M, int Rpad)
+__device__ __forceinline__ void p2m_body(const P2MArgs& pa, const int bid)
 {
     constexpr int R = (P + 1) * (P + 1);
     constexpr int LD = 33;
     extern __shared__ float sm[];
+    const int* off = pa.off;
+    const int nleaf = pa.nleaf;
+    const float4* atoms = pa.atoms;
+    float* M = pa.M;
+    const int Rpad = pa.Rpad;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int leaf = blockIdx.x * WARPS + warp;
+    const int leaf = bid * WARPS + warp;
     if (leaf >= nleaf) return;
     float* S = sm + warp * R * LD;
     for (int r = 0; r < R; r++) S[r * LD + lane] = 0.f;
@@ -472,6 +492,9 @@ __global__ void __launch_bounds__(WARPS * 32) k_p2m(const int* off, int nleaf, c
     }
 }
 
+template <int P, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) k_p2m(const P2MArgs a) { p2m_body<P, WARPS>(a, blockIdx.x); }
+
 template <int P>
 static void p2m_dispatch(const int* off, int nleaf, const float4* atoms, float* M, int Rpad, cudaStream_t s)
 {
@@ -484,7 +507,8 @@ static void p2m_dispatch(const int* off, int nleaf, const float4* atoms, float* 
         attr = true;
     }
     COUNT_LAUNCH();
-    k_p2m<P, W><<<(nleaf + W - 1) / W, W * 32, shm, s>>>(off, nleaf, atoms, M, Rpad);
+    P2MArgs a{off, nleaf, atoms, M, nullptr, nullptr, Rpad};
+    k_p2m<P, W><<<(nleaf + W - 1) / W, W * 32, shm, s>>>(a);
 }
 
 #define GBFMM_ORDER_SWITCH(P, CALL)            \
@@ -519,13 +543,18 @@ void launch_p2m(int P, const int* offsets, int nleaf, const float4* atoms, float
 //   dz Y_nm = -Y_{n-1,m};  (dx+i dy) Y_nm = -Y_{n-1,m+1};
 //   (dx-i dy) Y_nm = Y_{n-1,m-1} (m>0),  (dx-i dy) Y_n0 = -conj(Y_{n-1,1}).
 template <int P, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32) k_l2p(const int* off, int nleaf, const float4* atoms, const float* L,
-                                                   int Rpad, float4* field)
+__device__ __forceinline__ void l2p_body(const L2PArgs& la, const int bid)
 {
     constexpr int R = (P + 1) * (P + 1);
     __shared__ float Ls[WARPS][R + 1];
+    const int* off = la.off;
+    const int nleaf = la.nleaf;
+    const float4* atoms = la.atoms;
+    const float* L = la.L;
+    const int Rpad = la.Rpad;
+    float4* field = la.field;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int leaf = blockIdx.x * WARPS + warp;
+    const int leaf = bid * WARPS + warp;
     if (leaf >= nleaf) return;
     const float* src = L + (long)leaf * Rpad;
     float* Lw = Ls[warp];
@@ -566,11 +595,15 @@ __global__ void __launch_bounds__(WARPS * 32) k_l2p(const int* off, int nleaf, c
     }
 }
 
+template <int P, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) k_l2p(const L2PArgs a) { l2p_body<P, WARPS>(a, blockIdx.x); }
+
 void launch_l2p(int P, const int* offsets, int nleaf, const float4* atoms, const float* L_leaf, int Rpad,
                 float4* field, cudaStream_t s)
 {
     COUNT_LAUNCH();
-    GBFMM_ORDER_SWITCH(P, (k_l2p<PP, 4><<<(nleaf + 3) / 4, 128, 0, s>>>(offsets, nleaf, atoms, L_leaf, Rpad, field)));
+    L2PArgs a{offsets, nleaf, atoms, L_leaf, Rpad, field};
+    GBFMM_ORDER_SWITCH(P, (k_l2p<PP, 4><<<(nleaf + 3) / 4, 128, 0, s>>>(a)));
 }
 
 // ------------------------------------------------------------------ fused downward pass
@@ -583,13 +616,13 @@ __device__ __forceinline__ int real_degree(int r) { return (int)sqrtf((float)r +
 // same for every CTA of the subtree), then p's 8 leaves, then L2P of their bodies
 // (one warp per leaf).
 template <int P>
-__global__ void __launch_bounds__(256) k_down(DownArgs a)
+__device__ __forceinline__ void down_body(const DownArgs& a, const int bid)
 {
     constexpr int R = (P + 1) * (P + 1);
     __shared__ float Lc[R], Ln[R];
     __shared__ float Lleaf[8][R + 1];
     const int D = a.depth;
-    const uint32_t p = blockIdx.x;
+    const uint32_t p = bid;
     const uint32_t a1 = p >> (3 * (D - 2));  // level-1 ancestor
     for (int r = threadIdx.x; r < R; r += blockDim.x) Lc[r] = a.L[1][(size_t)a1 * a.Rpad + r];
     __syncthreads();
@@ -652,6 +685,9 @@ __global__ void __launch_bounds__(256) k_down(DownArgs a)
         a.field[b + c0 + lane] = make_float4(phi, gx, gy, gz);
     }
 }
+
+template <int P>
+__global__ void __launch_bounds__(256) k_down(const DownArgs a) { down_body<P>(a, blockIdx.x); }
 
 void launch_down(int P, const DownArgs& a, cudaStream_t s)
 {
@@ -1056,12 +1092,15 @@ void launch_p2p(const P2PArgs& a, int variant, cudaStream_t s, int* counter)
 // M2M: M~_parent[r] = sum_oct sum_{c < (deg r + 1)^2} A_oct[r][c] M~_child(oct)[c];
 // the 8 children of a parent are Morton-consecutive.  The octant sum is taken in
 // octant order (deterministic).  grid = (nparent, ceil(R/32)), block = (32, 8).
-__global__ void __launch_bounds__(256) k_m2m(const float* __restrict__ Mc, float* __restrict__ Mp,
-                                             const float* __restrict__ At, int R, int Rpad)
+__device__ __forceinline__ void m2m_body(const M2MArgs& ma, const int p, const int rb)
 {
     extern __shared__ float ms[];  // the 8 children, 8 x R
     __shared__ float red[8][32];
-    const int o = threadIdx.y, r = blockIdx.y * 32 + threadIdx.x, p = blockIdx.x;
+    const float* __restrict__ Mc = ma.Mc;
+    float* __restrict__ Mp = ma.Mp;
+    const float* __restrict__ At = ma.At;
+    const int R = ma.R, Rpad = ma.Rpad;
+    const int o = threadIdx.y, r = rb * 32 + threadIdx.x;
     const int tid = threadIdx.y * 32 + threadIdx.x;
     for (int i = tid; i < 8 * R; i += 256) {
         const int oo = i / R;
@@ -1086,10 +1125,13 @@ __global__ void __launch_bounds__(256) k_m2m(const float* __restrict__ Mc, float
     }
 }
 
+__global__ void __launch_bounds__(256) k_m2m(const M2MArgs a) { m2m_body(a, blockIdx.x, blockIdx.y); }
+
 void launch_m2m(const float* M_child, float* M_parent, const float* At, int nparent, int R, int Rpad, cudaStream_t s)
 {
     COUNT_LAUNCH();
-    k_m2m<<<dim3(nparent, (R + 31) / 32), dim3(32, 8), sizeof(float) * 8 * R, s>>>(M_child, M_parent, At, R, Rpad);
+    M2MArgs a{M_child, M_parent, At, nparent, R, Rpad};
+    k_m2m<<<dim3(nparent, (R + 31) / 32), dim3(32, 8), sizeof(float) * 8 * R, s>>>(a);
 }
 
 // P2M of 8 sibling leaves (one warp each, the arithmetic of k_p2m) followed by
@@ -1097,14 +1139,19 @@ void launch_m2m(const float* M_child, float* M_parent, const float* At, int npar
 // per (octant, row), the octant sum in octant order), so that the leaf level
 // and the level above it come out of one launch.  grid = nleaf / 8, block = 256.
 template <int P>
-__global__ void __launch_bounds__(256) k_p2m_m2m(const int* off, const float4* atoms, float* M, float* Mp,
-                                                 const float* __restrict__ At, int Rpad)
+__device__ __forceinline__ void p2m_m2m_body(const P2MArgs& pa, const int bid)
 {
     constexpr int R = (P + 1) * (P + 1);
     constexpr int LD = 33;
     extern __shared__ float sm[];
+    const int* off = pa.off;
+    const float4* atoms = pa.atoms;
+    float* M = pa.M;
+    float* Mp = pa.Mp;
+    const float* __restrict__ At = pa.At;
+    const int Rpad = pa.Rpad;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int leaf = blockIdx.x * 8 + warp;
+    const int leaf = bid * 8 + warp;
     float* S = sm + warp * R * LD;
     float* ch = sm + 8 * R * LD;  // the 8 leaf multipoles
     float* red = ch + 8 * R;      // per-octant partial sums of the parent
@@ -1143,9 +1190,12 @@ __global__ void __launch_bounds__(256) k_p2m_m2m(const int* off, const float4* a
         float t = red[r];
 #pragma unroll
         for (int k = 1; k < 8; k++) t += red[k * R + r];
-        Mp[(size_t)blockIdx.x * Rpad + r] = t;
+        Mp[(size_t)bid * Rpad + r] = t;
     }
 }
+
+template <int P>
+__global__ void __launch_bounds__(256) k_p2m_m2m(const P2MArgs a) { p2m_m2m_body<P>(a, blockIdx.x); }
 
 // Fused only while a CTA's shared memory allows several CTAs per SM (orders up
 // to 7): at higher orders the standalone P2M keeps more warps resident.
@@ -1164,7 +1214,8 @@ static bool p2m_m2m_dispatch(const int* off, int nleaf, const float4* atoms, flo
         attr = true;
     }
     COUNT_LAUNCH();
-    k_p2m_m2m<P><<<nleaf / 8, 256, shm, s>>>(off, atoms, M, Mp, At, Rpad);
+    P2MArgs a{off, nleaf, atoms, M, Mp, At, Rpad};
+    k_p2m_m2m<P><<<nleaf / 8, 256, shm, s>>>(a);
     return true;
 }
 
@@ -1346,10 +1397,10 @@ void launch_contract(const ContractArgs& a, int ntasks, cudaStream_t s)
 
 // L~_0 = A_lattice M~_0 (images >= 2), and the FP32 copy of M~_0.  One warp per
 // output row; lanes split the FP64 dot product, reduced by a fixed butterfly.
-__global__ void __launch_bounds__(256) k_root_lattice(RootArgs a)
+__device__ __forceinline__ void root_lattice_body(const RootArgs& a, const int bid)
 {
     const int lane = threadIdx.x & 31;
-    const int r = blockIdx.x * 8 + (threadIdx.x >> 5);
+    const int r = bid * 8 + (threadIdx.x >> 5);
     if (r >= a.R) return;
     double t = 0;
     if (a.images >= 2) {
@@ -1362,6 +1413,8 @@ __global__ void __launch_bounds__(256) k_root_lattice(RootArgs a)
         a.M0f[r] = (float)a.M0[r];
     }
 }
+
+__global__ void __launch_bounds__(256) k_root_lattice(const RootArgs a) { root_lattice_body(a, blockIdx.x); }
 
 // L~_1[o] += A_o L~_0 (FP64 arithmetic, FP32 result).  One warp per (child, row).
 __global__ void __launch_bounds__(256) k_root_l2l(RootArgs a)
@@ -1478,13 +1531,13 @@ __device__ __forceinline__ double tree_sum32(double (&v)[32])
 // the periodic lattice operator (about 81 periods wide) turns into a constant
 // shift of every potential.
 template <bool STAGED>
-__global__ void __launch_bounds__(TOP_THREADS) k_top(const TopArgs a)
+__device__ __forceinline__ void top_body(const TopArgs& a, const int bid, const int nb)
 {
     extern __shared__ float4 topsm[];
     __shared__ uint64_t bar;
     static_assert(TOP_LATTICE_MAX_R <= 64, "lattice quarters buffer");
     __shared__ double lq[4 * 64];  // lattice quarters (R <= TOP_LATTICE_MAX_R rows)
-    const int R = a.root.R, Rpad = a.root.Rpad, R2p = top_r2p(R), g = blockIdx.x, tid = threadIdx.x;
+    const int R = a.root.R, Rpad = a.root.Rpad, R2p = top_r2p(R), g = bid, tid = threadIdx.x;
     float* At = reinterpret_cast<float*>(topsm);
     double* Ag = reinterpret_cast<double*>(At + (STAGED ? 8 * R * R : 0));
     double* lat = Ag + (STAGED ? R2p : 0);
@@ -1538,7 +1591,7 @@ __global__ void __launch_bounds__(TOP_THREADS) k_top(const TopArgs a)
     __shared__ int s_last;
     __threadfence();
     __syncthreads();
-    if (tid == 0) s_last = atomicAdd(a.done, 1) == (int)gridDim.x - 1;
+    if (tid == 0) s_last = atomicAdd(a.done, 1) == (int)nb - 1;
     __syncthreads();
     if (!s_last) return;
     __threadfence();
@@ -1600,6 +1653,9 @@ __global__ void __launch_bounds__(TOP_THREADS) k_top(const TopArgs a)
     }
 }
 
+template <bool STAGED>
+__global__ void __launch_bounds__(TOP_THREADS) k_top(const TopArgs a) { top_body<STAGED>(a, blockIdx.x, gridDim.x); }
+
 void launch_top(const TopArgs& a, cudaStream_t s)
 {
     const size_t shm = top_smem_bytes(a.root.R);
@@ -1642,7 +1698,7 @@ void launch_wait_probe(uint32_t polls, int* err, cudaStream_t s)
 // Unit conversion of gpu_solver.cu:250-256 (phi*ke, F = -q*ke*grad phi), the
 // tin-foil dipole correction of solver.cpp:30-49, scatter back to input order
 // (solver.cpp:58-67) and the FP64 energy 0.5*sum(q*phi) (fmm.cpp:89-98).
-__global__ void __launch_bounds__(256) k_finalize(FinalArgs a)
+__device__ __forceinline__ void finalize_body(const FinalArgs& a, const int bid, const int nb)
 {
     // FP32 constants of the dipole correction, computed once in FP64 by k_top
     const float fM0 = a.fconst[0], fM1 = a.fconst[1], fM2 = a.fconst[2], corr_f = a.fconst[3];
@@ -1652,7 +1708,7 @@ __global__ void __launch_bounds__(256) k_finalize(FinalArgs a)
     f2sum e = {0.f, 0.f};
     // in input order (coalesced writes, to device or host memory), gathering
     // each body's fields from its sorted position
-    for (int o = blockIdx.x * blockDim.x + threadIdx.x; o < a.n; o += gridDim.x * blockDim.x) {
+    for (int o = bid * blockDim.x + threadIdx.x; o < a.n; o += nb * blockDim.x) {
         const int i = a.inv[o];
         const float4 nf = a.near[i], ff = a.far[i];
         const float q = a.atoms[i].w;
@@ -1676,14 +1732,14 @@ __global__ void __launch_bounds__(256) k_finalize(FinalArgs a)
     if (threadIdx.x == 0) {
         f2sum t = red[0];
         for (int w = 1; w < (int)(blockDim.x >> 5); w++) t = f2s_add(t, red[w]);
-        reinterpret_cast<f2sum*>(a.partials)[blockIdx.x] = t;
+        reinterpret_cast<f2sum*>(a.partials)[bid] = t;
     }
     if (!a.done) return;
     // last block: the energy, partials summed in a fixed order
     __shared__ int s_last;
     __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) s_last = atomicAdd(a.done, 1) == (int)gridDim.x - 1;
+    if (threadIdx.x == 0) s_last = atomicAdd(a.done, 1) == (int)nb - 1;
     __syncthreads();
     if (!s_last || threadIdx.x >= 32) return;
     __threadfence();
@@ -1693,7 +1749,7 @@ __global__ void __launch_bounds__(256) k_finalize(FinalArgs a)
         if (a.zero_after) *a.zero_after = 0;
     }
     // the energy: the blocks' FP32-pair partials summed in FP64
-    const double t = sum_partials_f64(reinterpret_cast<const float2*>(a.partials), 1, (int)gridDim.x);
+    const double t = sum_partials_f64(reinterpret_cast<const float2*>(a.partials), 1, (int)nb);
     if (threadIdx.x == 0) {
         *a.sc->out_energy = t;
         int* fl = a.sc->out_flags;
@@ -1702,11 +1758,224 @@ __global__ void __launch_bounds__(256) k_finalize(FinalArgs a)
     }
 }
 
+__global__ void __launch_bounds__(256) k_finalize(const FinalArgs a) { finalize_body(a, blockIdx.x, gridDim.x); }
+
 void launch_finalize(const FinalArgs& a, cudaStream_t s)
 {
     int blocks = final_blocks(a.n);
     COUNT_LAUNCH();
     k_finalize<<<blocks, 256, 0, s>>>(a);
+}
+
+}  // namespace gbfmm
+
+namespace gbfmm {
+
+// ------------------------------------------------------------------ batched launches
+//
+// One launch runs a kernel for many systems: CTA b runs block b - first[s] of
+// system s, where first[] (device) holds the prefix sums of the systems' grid
+// sizes; each system's arguments are a struct in device memory.  The bodies are
+// those of the single-system kernels, so every system's arithmetic is the same.
+
+__device__ __forceinline__ int batch_system(const int* first, int nsys, int b)
+{
+    int lo = 0, hi = nsys - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(&first[mid]) <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+#define GBFMM_BATCH_PROLOGUE                                     \
+    const int sys = batch_system(first, nsys, (int)blockIdx.x); \
+    const int b0 = __ldg(&first[sys]), nb = __ldg(&first[sys + 1]) - b0, bid = (int)blockIdx.x - b0;
+
+__global__ void __launch_bounds__(256) k_tree_keys_batch(const TreeArgs* as, const int* first, int nsys)
+{
+    GBFMM_BATCH_PROLOGUE
+    tree_keys_body(as[sys], bid, nb);
+}
+
+__global__ void k_scatter_ranked_batch(const ScatterArgs* as, const int* first, int nsys)
+{
+    GBFMM_BATCH_PROLOGUE
+    (void)nb;
+    scatter_ranked_body(as[sys], bid);
+}
+
+__global__ void __launch_bounds__(256) k_leaf_sort_batch(const LeafSortArgs* as, const int* first, int nsys)
+{
+    GBFMM_BATCH_PROLOGUE
+    (void)nb;
+    leaf_sort_body(as[sys], bid);
+}
+
+template <int P, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) k_p2m_batch(const P2MArgs* as, const int* first, int nsys)
+{
+    GBFMM_BATCH_PROLOGUE
+    (void)nb;
+    p2m_body<P, WARPS>(as[sys], bid);
+}
+
+template <int P>
+__global__ void __launch_bounds__(256) k_p2m_m2m_batch(const P2MArgs* as, const int* first, int nsys)
+{
+    GBFMM_BATCH_PROLOGUE
+    (void)nb;
+    p2m_m2m_body<P>(as[sys], bid);
+}
+
+template <int P, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) k_l2p_batch(const L2PArgs* as, const int* first, int nsys)
+{
+    GBFMM_BATCH_PROLOGUE
+    (void)nb;
+    l2p_body<P, WARPS>(as[sys], bid);
+}
+
+template <int P>
+__global__ void __launch_bounds__(256) k_down_batch(const DownArgs* as, const int* first, int nsys)
+{
+    GBFMM_BATCH_PROLOGUE
+    (void)nb;
+    down_body<P>(as[sys], bid);
+}
+
+// M2M: system s's block lb is (parent lb / row blocks, row block lb % row blocks).
+__global__ void __launch_bounds__(256) k_m2m_batch(const M2MArgs* as, const int* first, int nsys)
+{
+    GBFMM_BATCH_PROLOGUE
+    (void)nb;
+    const M2MArgs& a = as[sys];
+    const int nrb = (a.R + 31) / 32;
+    m2m_body(a, bid / nrb, bid % nrb);
+}
+
+template <bool STAGED>
+__global__ void __launch_bounds__(TOP_THREADS) k_top_batch(const TopArgs* as, const int* first, int nsys)
+{
+    GBFMM_BATCH_PROLOGUE
+    top_body<STAGED>(as[sys], bid, nb);
+}
+
+__global__ void __launch_bounds__(256) k_root_lattice_batch(const RootArgs* as, const int* first, int nsys)
+{
+    GBFMM_BATCH_PROLOGUE
+    (void)nb;
+    root_lattice_body(as[sys], bid);
+}
+
+__global__ void __launch_bounds__(256) k_finalize_batch(const FinalArgs* as, const int* first, int nsys)
+{
+    GBFMM_BATCH_PROLOGUE
+    finalize_body(as[sys], bid, nb);
+}
+
+template <int P>
+static void launch_p2m_batch_t(const P2MArgs* args, const int* first, int nsys, int nblocks, size_t smem,
+                               cudaStream_t s)
+{
+    constexpr int R = (P + 1) * (P + 1);
+    constexpr int W = R <= 169 ? 4 : 2;
+    static size_t attr = 0;
+    if (smem > attr) {
+        cudaFuncSetAttribute(k_p2m_batch<P, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr = smem;
+    }
+    k_p2m_batch<P, W><<<nblocks, W * 32, smem, s>>>(args, first, nsys);
+}
+
+template <int P>
+static void launch_p2m_m2m_batch_t(const P2MArgs* args, const int* first, int nsys, int nblocks, size_t smem,
+                                   cudaStream_t s)
+{
+    static size_t attr = 0;
+    if (smem > attr) {
+        cudaFuncSetAttribute(k_p2m_m2m_batch<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr = smem;
+    }
+    k_p2m_m2m_batch<P><<<nblocks, 256, smem, s>>>(args, first, nsys);
+}
+
+void launch_batch(BatchKernel k, int P, const void* args, const int* first, int nsys, int nblocks, size_t smem,
+                  cudaStream_t s)
+{
+    if (nsys <= 0 || nblocks <= 0) return;
+    COUNT_LAUNCH();
+    switch (k) {
+        case BatchKernel::TREE_KEYS:
+            k_tree_keys_batch<<<nblocks, 256, smem, s>>>((const TreeArgs*)args, first, nsys);
+            break;
+        case BatchKernel::SCATTER:
+            k_scatter_ranked_batch<<<nblocks, 256, 0, s>>>((const ScatterArgs*)args, first, nsys);
+            break;
+        case BatchKernel::LEAF_SORT:
+            k_leaf_sort_batch<<<nblocks, 256, 0, s>>>((const LeafSortArgs*)args, first, nsys);
+            break;
+        case BatchKernel::P2M:
+            GBFMM_ORDER_SWITCH(P, launch_p2m_batch_t<PP>((const P2MArgs*)args, first, nsys, nblocks, smem, s));
+            break;
+        case BatchKernel::P2M_M2M:
+            GBFMM_ORDER_SWITCH(P, launch_p2m_m2m_batch_t<PP>((const P2MArgs*)args, first, nsys, nblocks, smem, s));
+            break;
+        case BatchKernel::L2P:
+            GBFMM_ORDER_SWITCH(P, (k_l2p_batch<PP, 4><<<nblocks, 128, 0, s>>>((const L2PArgs*)args, first, nsys)));
+            break;
+        case BatchKernel::DOWN:
+            GBFMM_ORDER_SWITCH(P, (k_down_batch<PP><<<nblocks, 256, 0, s>>>((const DownArgs*)args, first, nsys)));
+            break;
+        case BatchKernel::M2M:
+            k_m2m_batch<<<nblocks, dim3(32, 8), smem, s>>>((const M2MArgs*)args, first, nsys);
+            break;
+        case BatchKernel::TOP_STAGED:
+        case BatchKernel::TOP_UNSTAGED: {
+            const bool staged = k == BatchKernel::TOP_STAGED;
+            static size_t attr[2] = {0, 0};
+            if (smem > attr[staged]) {
+                if (staged) cudaFuncSetAttribute(k_top_batch<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                else cudaFuncSetAttribute(k_top_batch<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                attr[staged] = smem;
+            }
+            if (staged) k_top_batch<true><<<nblocks, TOP_THREADS, smem, s>>>((const TopArgs*)args, first, nsys);
+            else k_top_batch<false><<<nblocks, TOP_THREADS, smem, s>>>((const TopArgs*)args, first, nsys);
+            break;
+        }
+        case BatchKernel::ROOT_LATTICE:
+            k_root_lattice_batch<<<nblocks, 256, 0, s>>>((const RootArgs*)args, first, nsys);
+            break;
+        case BatchKernel::FINALIZE:
+            k_finalize_batch<<<nblocks, 256, 0, s>>>((const FinalArgs*)args, first, nsys);
+            break;
+        default:
+            break;
+    }
+}
+
+}  // namespace gbfmm
+
+namespace gbfmm {
+
+size_t p2m_smem_bytes(int P)
+{
+    const int R = (P + 1) * (P + 1);
+    return sizeof(float) * (size_t)p2m_warps(P) * R * 33;
+}
+
+int p2m_warps(int P)
+{
+    const int R = (P + 1) * (P + 1);
+    return R <= 169 ? 4 : 2;
+}
+
+size_t p2m_m2m_smem_bytes(int P)
+{
+    const int R = (P + 1) * (P + 1);
+    const size_t shm = sizeof(float) * ((size_t)8 * R * 33 + 16 * R);
+    return shm > P2M_M2M_MAX_SMEM ? 0 : shm;
 }
 
 }  // namespace gbfmm

@@ -117,6 +117,50 @@ constexpr int FINAL_MAX_BLOCKS = 608;
 int tree_blocks(int n);
 int final_blocks(int n);
 
+// Arguments of the per-system kernels that a batch also launches for many
+// systems at once (one struct per system in device memory).
+struct ScatterArgs {
+    const uint32_t* code;
+    int n;
+    const int* off;
+    const int* rank;
+    int* tmp;
+};
+struct LeafSortArgs {
+    const int* off;
+    int nleaf;
+    const int* tmp_idx;
+    const float4* uq;
+    int* order;
+    float4* atoms;
+    int* inv;
+    int* counts;
+    int* edge;
+};
+struct P2MArgs {          // P2M of the leaves (and, fused, the M2M of their parents)
+    const int* off;
+    int nleaf;
+    const float4* atoms;
+    float* M;
+    float* Mp;            // parents (fused form)
+    const float* At;      // transposed M2M operators (fused form)
+    int Rpad;
+};
+struct L2PArgs {
+    const int* off;
+    int nleaf;
+    const float4* atoms;
+    const float* L;
+    int Rpad;
+    float4* field;
+};
+struct M2MArgs {
+    const float* Mc;
+    float* Mp;
+    const float* At;
+    int nparent, R, Rpad;
+};
+
 extern std::atomic<long> g_kernel_launches;
 
 // Streaming multiprocessors of the current device (cudaDevAttrMultiProcessorCount,
@@ -243,6 +287,22 @@ void launch_top(const TopArgs& a, cudaStream_t s);
 // with no copies or MMAs in flight; after 'polls' polls the wait gives up and
 // sets bit 1 of *err.  Exercises the give-up path of the bounded waits.
 void launch_wait_probe(uint32_t polls, int* err, cudaStream_t s);
+
+// ---- batched launches: one launch of a kernel for many systems (CTA b runs block
+// b - first[s] of system s; args = one struct per system in device memory).
+enum class BatchKernel {
+    TREE_KEYS, SCATTER, LEAF_SORT, P2M, P2M_M2M, L2P, DOWN, M2M, TOP_STAGED, TOP_UNSTAGED, ROOT_LATTICE, FINALIZE,
+    TC_GRIDS, M2L_TC
+};
+// P: the order (templated kernels); smem: dynamic shared memory of the launch.
+void launch_batch(BatchKernel k, int P, const void* args, const int* first, int nsys, int nblocks, size_t smem,
+                  cudaStream_t s);
+// The tensor-core kernels (m2l_tc.cu).
+void launch_batch_tc(BatchKernel k, const void* args, const int* first, int nsys, int nblocks, size_t smem,
+                     cudaStream_t s);
+size_t p2m_smem_bytes(int P);        // dynamic shared memory of k_p2m<P>
+size_t p2m_m2m_smem_bytes(int P);    // of k_p2m_m2m<P> (0: the fused kernel is not used for P)
+int p2m_warps(int P);                // warps (leaves) per CTA of k_p2m<P>
 
 // ---- virial (virial.cu): the image-shift terms of Xi = -1/2 sum_pairs r (x) F
 constexpr int VIR_MAXR = 320;  // rows of the largest expansion (order 16: 289)

@@ -127,13 +127,13 @@ __host__ __device__ __forceinline__ void tc_tile_shape_dev(int level, const int*
 // One thread per (grid row, 8 coefficients): the FP32 multipole of the row's
 // cell (periodic image in the halo, zero outside a non-periodic box) split into
 // bf16 hi and lo.
-__global__ void __launch_bounds__(256) k_tc_grids(const TcGridArgs g)
+__device__ __forceinline__ void tc_grids_body(const TcGridArgs& g, const int bid)
 {
     const int groups = g.KP / 8;
     const long conv_blocks = (g.rows * groups + 255) / 256;
-    if (blockIdx.x >= conv_blocks) {
+    if (bid >= conv_blocks) {
         const int lane = threadIdx.x & 31, R = g.root_R;
-        const int w = (int)(blockIdx.x - conv_blocks) * 8 + (threadIdx.x >> 5);
+        const int w = (int)(bid - conv_blocks) * 8 + (threadIdx.x >> 5);
         const int o = w / R, r = w % R;
         if (o >= g.root_n1) return;
         const double* A = g.root_l2l + ((size_t)o * R + r) * R;
@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(256) k_tc_grids(const TcGridArgs g)
         if (lane == 0) g.L1[(size_t)o * g.Rpad + r] += (float)t;
         return;
     }
-    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long i = (long)bid * blockDim.x + threadIdx.x;
     if (i >= g.rows * groups) return;
     const long row = i / groups;
     const int c0 = (int)(i - row * groups) * 8;
@@ -190,6 +190,8 @@ __global__ void __launch_bounds__(256) k_tc_grids(const TcGridArgs g)
     if (g.lo) *reinterpret_cast<uint4*>(g.lo + row * g.KP + c0) = *reinterpret_cast<const uint4*>(l);
 }
 
+__global__ void __launch_bounds__(256) k_tc_grids(const TcGridArgs g) { tc_grids_body(g, blockIdx.x); }
+
 void launch_tc_grids(const TcGridArgs& g, cudaStream_t s)
 {
     const long n = g.rows * (g.KP / 8);
@@ -210,7 +212,7 @@ void launch_tc_grids(const TcGridArgs& g, cudaStream_t s)
 //     tcgen05.mma sequence into TMEM and commits to the stage's empty barrier.
 // After the last commit, warps 0-3 read their 32 TMEM lanes (tcgen05.ld) and add
 // the results to the target locals.
-__global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(const __grid_constant__ TcArgs a)
+__device__ __forceinline__ void m2l_tc_body(const TcArgs& a, const int bid)
 {
     extern __shared__ uint8_t smraw[];
     uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~(uintptr_t)1023);
@@ -225,7 +227,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(const __grid_constant_
     uint64_t* bar_done = bar_empty + TC_MAXSTAGE;  // one phase: every MMA of the CTA has completed
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar_done + 1);
 
-    const CTask task = a.tasks[blockIdx.x];
+    const CTask task = a.tasks[bid];
     const int k = task.level, s = task.octant;
     int bx, by, bz;
     tc_tile_shape_dev(k, a.shift, bx, by, bz);
@@ -385,6 +387,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(const __grid_constant_
     (void)ok;
 }
 
+__global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc(const __grid_constant__ TcArgs a) { m2l_tc_body(a, blockIdx.x); }
+
 // ------------------------------------------------------------------ host side
 
 void tc_tile_shape(int level, const int shift[3], int& bx, int& by, int& bz)
@@ -527,6 +531,62 @@ void launch_m2l_tc(const TcArgs& a, int ntasks, cudaStream_t s)
     }
     g_kernel_launches.fetch_add(1, std::memory_order_relaxed);
     k_m2l_tc<<<ntasks, TC_THREADS, shm, s>>>(a);
+}
+
+}  // namespace gbfmm
+
+namespace gbfmm {
+
+// Batched launches of the grid conversion and the tensor-core M2L (one struct
+// of arguments per system in device memory; the tensor maps are read there).
+namespace {
+__device__ __forceinline__ int tc_batch_system(const int* first, int nsys, int b)
+{
+    int lo = 0, hi = nsys - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(&first[mid]) <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+}  // namespace
+
+__global__ void __launch_bounds__(256) k_tc_grids_batch(const TcGridArgs* as, const int* first, int nsys)
+{
+    const int sys = tc_batch_system(first, nsys, (int)blockIdx.x);
+    tc_grids_body(as[sys], (int)blockIdx.x - __ldg(&first[sys]));
+}
+
+__global__ void __launch_bounds__(TC_THREADS, 1) k_m2l_tc_batch(const TcArgs* as, const int* first, int nsys)
+{
+    const int sys = tc_batch_system(first, nsys, (int)blockIdx.x);
+    m2l_tc_body(as[sys], (int)blockIdx.x - __ldg(&first[sys]));
+}
+
+void launch_batch_tc(BatchKernel k, const void* args, const int* first, int nsys, int nblocks, size_t smem,
+                     cudaStream_t s)
+{
+    if (nsys <= 0 || nblocks <= 0) return;
+    g_kernel_launches.fetch_add(1, std::memory_order_relaxed);
+    if (k == BatchKernel::TC_GRIDS) {
+        k_tc_grids_batch<<<nblocks, 256, 0, s>>>((const TcGridArgs*)args, first, nsys);
+    } else if (k == BatchKernel::M2L_TC) {
+        static size_t attr = 0;
+        if (smem > attr) {
+            cudaFuncSetAttribute(k_m2l_tc_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            attr = smem;
+        }
+        k_m2l_tc_batch<<<nblocks, TC_THREADS, smem, s>>>((const TcArgs*)args, first, nsys);
+    }
+}
+
+// Blocks of one system's grid conversion (and root L2L).
+long tc_grids_blocks(const TcGridArgs& g)
+{
+    const long n = g.rows * (g.KP / 8);
+    if (n <= 0) return 0;
+    return (n + 255) / 256 + (g.root_l2l ? ((long)g.root_n1 * g.root_R + 7) / 8 : 0);
 }
 
 }  // namespace gbfmm

@@ -86,6 +86,7 @@ struct TcGridArgs {
     int root_n1 = 8;  // stored level-1 cells
 };
 void launch_tc_grids(const TcGridArgs& g, cudaStream_t s);
+long tc_grids_blocks(const TcGridArgs& g);  // CTAs of one system's launch_tc_grids
 
 struct alignas(64) TcArgs {
     CUtensorMap p_hi[TC_MAXLEV], p_lo[TC_MAXLEV];  // parity grids (level k)

@@ -765,6 +765,22 @@ extern "C" int gbfmm_tuner_choose(gbfmm_mlp* m, int natoms, const float* charges
                 out->depth = D;
                 out->precision = prec;
                 out->diff_vs_plain = diff;
+                // the network's error model is conservative where it has seen
+                // few systems like this one: a lower order whose measured
+                // difference from the judge stays within tol / margin is cheaper
+                // at the same depth and precision
+                if (P == P0)
+                    for (int Q = P - 1; Q >= 4 && out->nchecks < GBFMM_TUNER_MAX_CHECKS; Q--) {
+                        rc = solve_forces(n, charges, coords, box, Q, D, prec, images, fc);
+                        if (rc) return rc;
+                        const double dq = rel_rms(fc, fj);
+                        const int kq = out->nchecks++;
+                        out->check_order[kq] = Q;
+                        out->check_diff[kq] = dq;
+                        if (dq > tol / std::max(margin, 1.0)) break;
+                        out->order = Q;
+                        out->diff_vs_plain = dq;
+                    }
                 return GBFMM_OK;
             }
         }

@@ -25,6 +25,7 @@ WEIGHTS = os.path.join(HERE, "tuner_weights.bin")
 NFEAT = 57
 N_IN = NFEAT + 4
 PLAIN_ORDER = 10
+MAX_CHECKS = 8  # GBFMM_TUNER_MAX_CHECKS
 
 class TunerChoice(ctypes.Structure):
     """gbfmm_tuner_choice of include/gbfmm.h."""
@@ -32,8 +33,8 @@ class TunerChoice(ctypes.Structure):
                 ("fallback", ctypes.c_int), ("diff_vs_plain", ctypes.c_double),
                 ("proposed_order", ctypes.c_int), ("proposed_depth", ctypes.c_int),
                 ("proposed_precision", ctypes.c_int), ("pred_rel_force_err", ctypes.c_float),
-                ("pred_ms", ctypes.c_float), ("nchecks", ctypes.c_int), ("check_order", ctypes.c_int * 3),
-                ("check_diff", ctypes.c_double * 3)]
+                ("pred_ms", ctypes.c_float), ("nchecks", ctypes.c_int), ("check_order", ctypes.c_int * MAX_CHECKS),
+                ("check_diff", ctypes.c_double * MAX_CHECKS)]
 
 
 _fp = ctypes.POINTER(ctypes.c_float)
@@ -248,7 +249,7 @@ class TunedSolver:
             for k in range(c.nchecks):
                 self.checks.append({"proposal": prop if k == 0 else (c.check_order[k], prop[1], prop[2]),
                                     "diff_vs_plain": c.check_diff[k],
-                                    "accepted": not c.fallback and k == c.nchecks - 1})
+                                    "accepted": not c.fallback and c.check_order[k] == c.order})
         self.choice = (c.order, c.depth, c.precision)
         self.solver = _pkg.ZetaFmmSolver(self.n, self.q, order=c.order, max_depth=c.depth, images=self.images,
                                          precision=c.precision, aspect_z=2 if m[8] != m[0] else 1)
