@@ -92,6 +92,7 @@ def lib():
             "gbfmm_debug_harmonics": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, dp, dp]),
             "gbfmm_debug_bounded_wait": (ctypes.c_int, [ctypes.c_uint, vp]),
             "gbfmm_batch_status": (ctypes.c_int, [vp]),
+            "gbfmm_batch_step_launches": (ctypes.c_int, [vp, ip]),
             "gbfmm_get_virial": (ctypes.c_int, [vp, dp]),
         }
         for name, (res, args) in sig.items():
@@ -362,6 +363,12 @@ class BatchSolver:
     def status(self):
         """Waits for the last step; raises FmmError if a system reported an error."""
         _check(lib().gbfmm_batch_status(self._b))
+
+    def step_launches(self):
+        """Kernels one batch step launches (counted when its graph is captured)."""
+        n = ctypes.c_int()
+        _check(lib().gbfmm_batch_step_launches(self._b, ctypes.byref(n)))
+        return n.value
 
     def tuning(self):
         v = [ctypes.c_int() for _ in range(4)]

@@ -428,13 +428,17 @@ void launch_leaf_sort(const int* offsets, int nleaf, int* tmp_idx, const float4*
 template <int P, typename F>
 __device__ __forceinline__ void stream_regular(float x, float y, float z, F&& f)
 {
-    const float r2 = x * x + y * y + z * z;
+    // Every product and fused multiply-add is spelled out (no contraction left
+    // to the compiler), so that each kernel that inlines this recurrence, the
+    // single-system and the batched instances alike, rounds it the same way.
+    const float r2 = fmaf(x, x, fmaf(y, y, __fmul_rn(z, z)));
     float sr = 1.f, si = 0.f;
 #pragma unroll
     for (int m = 0; m <= P; m++) {
         if (m > 0) {
             const float inv = 1.0f / (2 * m);
-            float tr = (sr * x - si * y) * inv, ti = (sr * y + si * x) * inv;
+            float tr = __fmul_rn(fmaf(sr, x, -__fmul_rn(si, y)), inv);
+            float ti = __fmul_rn(fmaf(sr, y, __fmul_rn(si, x)), inv);
             sr = tr;
             si = ti;
         }
@@ -446,8 +450,9 @@ __device__ __forceinline__ void stream_regular(float x, float y, float z, F&& f)
 #pragma unroll
             for (int n = m + 1; n < P; n++) {
                 const float c = 1.0f / ((n + m + 1) * (n - m + 1));
-                float cr = -((2 * n + 1) * z * br + r2 * ar) * c;
-                float ci = -((2 * n + 1) * z * bi + r2 * ai) * c;
+                const float kz = __fmul_rn((float)(2 * n + 1), z);
+                float cr = -__fmul_rn(fmaf(kz, br, __fmul_rn(r2, ar)), c);
+                float ci = -__fmul_rn(fmaf(kz, bi, __fmul_rn(r2, ai)), c);
                 f(n + 1, m, cr, ci);
                 ar = br; ai = bi;
                 br = cr; bi = ci;
@@ -478,8 +483,12 @@ __device__ __forceinline__ void p2m_body(const P2MArgs& pa, const int bid)
         const float q = a.w;
         // M~ += q conj(Y(u)), kernel.cu:228-240 evaluated at -phi
         stream_regular<P>(a.x, a.y, a.z, [&](int nn, int mm, float yr, float yi) {
-            S[ridx_re(nn, mm) * LD + lane] += q * yr;
-            if (mm > 0) S[ridx_im(nn, mm) * LD + lane] -= q * yi;
+            float* sre = &S[ridx_re(nn, mm) * LD + lane];
+            *sre = fmaf(q, yr, *sre);
+            if (mm > 0) {
+                float* sim = &S[ridx_im(nn, mm) * LD + lane];
+                *sim = fmaf(-q, yi, *sim);
+            }
         });
     }
     __syncwarp();
@@ -1161,8 +1170,12 @@ __device__ __forceinline__ void p2m_m2m_body(const P2MArgs& pa, const int bid)
         float4 a = c0 + lane < n ? atoms[b + c0 + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
         const float q = a.w;
         stream_regular<P>(a.x, a.y, a.z, [&](int nn, int mm, float yr, float yi) {
-            S[ridx_re(nn, mm) * LD + lane] += q * yr;
-            if (mm > 0) S[ridx_im(nn, mm) * LD + lane] -= q * yi;
+            float* sre = &S[ridx_re(nn, mm) * LD + lane];
+            *sre = fmaf(q, yr, *sre);
+            if (mm > 0) {
+                float* sim = &S[ridx_im(nn, mm) * LD + lane];
+                *sim = fmaf(-q, yi, *sim);
+            }
         });
     }
     __syncwarp();

@@ -1679,6 +1679,10 @@ struct gbfmm_batch {
     cudaStream_t near_stream = nullptr;
     std::vector<cudaEvent_t> ev_tree;
     cudaEvent_t ev_near = nullptr;
+    // argument tables of the grouped launches (rebuilt at each capture)
+    void* group_buf = nullptr;
+    size_t group_bytes = 0;
+    int step_launches = 0;  // kernels one batch step launches
 };
 
 static void free_batch(gbfmm_batch* b)
@@ -1696,6 +1700,7 @@ static void free_batch(gbfmm_batch* b)
     if (b->buf) cudaFree(b->buf);
     if (b->h_sc) cudaFreeHost(b->h_sc);
     if (b->p2p_buf) cudaFree(b->p2p_buf);
+    if (b->group_buf) cudaFree(b->group_buf);
     if (b->near_stream) cudaStreamDestroy(b->near_stream);
     for (cudaEvent_t e : b->ev_tree) cudaEventDestroy(e);
     if (b->ev_near) cudaEventDestroy(b->ev_near);
@@ -1839,50 +1844,422 @@ static int batch_create(int n_sys, const int* atom_offsets, const int* orders, c
     return GBFMM_OK;
 }
 
+// One system's step as launch descriptions: the arguments and grid sizes of the
+// kernels enqueue_step launches for it, in the same order and with the same
+// arithmetic (the batch runs each kind of kernel for all systems in one launch).
+struct StepDesc {
+    gbfmm_handle* h = nullptr;
+    TreeArgs tree;
+    int tree_blocks = 0;
+    size_t tree_smem = 0;
+    ScatterArgs scatter{};
+    int scatter_blocks = 0;
+    LeafSortArgs leaf{};
+    int leaf_blocks = 0;
+    bool fused = false;
+    P2MArgs p2m{};
+    int p2m_blocks = 0;
+    std::vector<M2MArgs> m2m;  // levels from the finest up
+    TopArgs top;
+    size_t top_smem = 0;
+    bool top_staged = false;
+    RootArgs root{};
+    TcGridArgs grids;
+    int grids_blocks = 0;
+    int m2l_blocks = 0;
+    size_t m2l_smem = 0;
+    DownArgs down{};
+    L2PArgs l2p{};
+    FinalArgs fin;
+    int fin_blocks = 0;
+};
+
+static void describe_step(gbfmm_handle* h, StepDesc& d)
+{
+    const int D = h->D, n = h->n;
+    d.h = h;
+    int* sync = h->d_counts + h->nleaf + 1;
+    TreeArgs& ta = d.tree;
+    ta.sc = h->d_sc;
+    ta.charges = h->d_q;
+    ta.n = n;
+    ta.depth = D;
+    ta.code = h->d_code;
+    ta.uq = h->d_uq;
+    ta.counts = h->d_counts;
+    ta.rank = h->d_inv;
+    ta.zero = reinterpret_cast<float4*>(h->d_L);
+    ta.zero_n4 = (long)(h->lev_floats / 4);
+    ta.partials = h->d_partials;
+    ta.flags = h->d_flags;
+    ta.done = sync;
+    ta.sums = nullptr;
+    if (h->nleaf <= TREE_EPILOGUE_MAX_LEAVES) {
+        ta.off = h->d_off;
+        ta.nleaf = h->nleaf;
+    }
+    {
+        int k = 0;
+        auto pf = [&](const void* p, size_t bytes) {
+            if (p && bytes >= 16 && k < TreeArgs::MAX_PREFETCH) {
+                ta.pf[k] = p;
+                ta.pf_bytes[k++] = bytes;
+            }
+        };
+        const OpTables* t = h->tab;
+        pf(h->d_m2m_t, sizeof(float) * t->m2m_t.size());
+        pf(h->d_l2l_t, sizeof(float) * t->l2l_t.size());
+        pf(h->d_entries, h->tasks_bytes);
+    }
+    d.tree_blocks = tree_blocks(n);
+    const int nd = 1 << D;
+    d.tree_smem = sizeof(float) * (((3 * (nd + 1) + 1) & ~1) + 6 * nd);
+    d.scatter = ScatterArgs{h->d_code, n, h->d_off, h->d_inv, h->d_tmp};
+    d.scatter_blocks = (n + 255) / 256;
+    d.leaf = LeafSortArgs{h->d_off, h->nleaf, h->d_tmp, h->d_uq, h->d_order, h->d_atoms, h->d_inv, h->d_counts,
+                          h->d_leaf_edge};
+    d.leaf_blocks = (int)(((long)h->nleaf * 32 + 255) / 256);
+    d.fused = D >= 2 && p2m_m2m_smem_bytes(h->P) > 0 && h->nleaf % 8 == 0;
+    if (d.fused) {
+        d.p2m = P2MArgs{h->d_off, h->nleaf, h->d_atoms, h->Mlev[D], h->Mlev[D - 1], h->d_m2m_t, h->Rpad};
+        d.p2m_blocks = h->nleaf / 8;
+    } else {
+        d.p2m = P2MArgs{h->d_off, h->nleaf, h->d_atoms, h->Mlev[D], nullptr, nullptr, h->Rpad};
+        d.p2m_blocks = (h->nleaf + p2m_warps(h->P) - 1) / p2m_warps(h->P);
+    }
+    const int top_from = D == 1 || h->R > TOP_STAGE_MAX_R ? 1 : std::min(3, d.fused ? D - 1 : D);
+    for (int k = d.fused ? D - 2 : D - 1; k >= top_from; k--)
+        d.m2m.push_back(M2MArgs{h->Mlev[k + 1], h->Mlev[k], h->d_m2m_t, (int)h->ncell[k], h->R, h->Rpad});
+    RootArgs& ra = d.root;
+    ra.R = h->R;
+    ra.Rpad = h->Rpad;
+    ra.m2m = h->d_root_m2m;
+    ra.l2l = h->d_root_l2l;
+    ra.lattice = h->d_lattice;
+    ra.M1 = h->Mlev[1];
+    ra.M0 = h->d_M0;
+    ra.L0 = h->d_L0;
+    ra.M0f = h->Mlev[0];
+    ra.L1 = h->Llev[1];
+    ra.sc = h->d_sc;
+    ra.images = h->prm.images;
+    ra.n1 = (int)h->ncell[1];
+    TopArgs& top = d.top;
+    top.root = ra;
+    top.from = top_from;
+    top.lattice = h->R <= TOP_LATTICE_MAX_R ? 1 : 0;
+    top.Min = h->Mlev[top_from];
+    top.M2 = D >= 2 ? h->Mlev[2] : nullptr;
+    top.M1 = h->Mlev[1];
+    top.m2m_t = h->d_m2m_t;
+    top.part = h->d_root_part;
+    top.tree_part = h->d_partials;
+    top.tree_nblocks = tree_blocks(h->n);
+    top.sums = h->d_sums;
+    top.fconst = h->d_fconst;
+    top.natoms = h->n;
+    top.done = sync + 3;
+    top.err = h->d_flags + 2;
+    top.umask = (h->shift[0] == 0 ? 4 : 0) | (h->shift[1] == 0 ? 2 : 0) | (h->shift[2] == 0 ? 1 : 0);
+    d.top_smem = top_smem_bytes(h->R);
+    d.top_staged = h->R <= TOP_STAGE_MAX_R;
+    if (h->tc) {
+        d.grids = tc_grid_args(h);
+        d.grids.root_l2l = h->d_root_l2l;
+        d.grids.L0 = h->d_L0;
+        d.grids.L1 = h->Llev[1];
+        d.grids.root_R = h->R;
+        d.grids.root_n1 = (int)h->ncell[1];
+        d.grids_blocks = (int)tc_grids_blocks(d.grids);
+        TcArgs& t = *h->tca;
+        t.tasks = h->d_tc_tasks_v[h->tc_split_v];
+        t.atomic = h->tc_split_v > 0 ? 1 : 0;
+        t.nstage = h->tc_nstage;
+        d.m2l_blocks = h->tc_ntask_v[h->tc_split_v];
+        d.m2l_smem = tc_smem_bytes(t);
+    }
+    if (D >= 2) {
+        DownArgs& da = d.down;
+        da.nparent = (int)h->ncell[D - 1];
+        da.off = h->d_off;
+        da.atoms = h->d_atoms;
+        for (int k = 0; k <= D; k++) da.L[k] = h->Llev[k];
+        da.l2l_t = h->d_l2l_t;
+        da.field = h->d_far;
+        da.depth = D;
+        da.Rpad = h->Rpad;
+    } else {
+        d.l2p = L2PArgs{h->d_off, h->nleaf, h->d_atoms, h->Llev[D], h->Rpad, h->d_far};
+    }
+    FinalArgs& fa = d.fin;
+    fa.sc = h->d_sc;
+    fa.n = n;
+    fa.atoms = h->d_atoms;
+    fa.inv = h->d_inv;
+    fa.near = h->d_near;
+    fa.far = h->d_far;
+    fa.fconst = h->d_fconst;
+    fa.flags = h->d_flags;
+    fa.partials = h->d_partials;
+    fa.done = sync + 1;
+    fa.zero_after = sync + 2;
+    d.fin_blocks = final_blocks(n);
+}
+
+// Argument tables of the grouped launches, laid out in one host buffer and
+// uploaded in one copy: per group, the systems' argument structs (64-byte
+// aligned, for the tensor maps) and the prefix sums of their grid sizes.
+struct GroupTable {
+    std::vector<uint8_t> host;
+    struct Group {
+        BatchKernel kind;
+        int P = 0;
+        size_t args_off = 0, first_off = 0;
+        int nsys = 0, nblocks = 0;
+        size_t smem = 0;
+    };
+    std::vector<Group> groups;
+    template <typename T>
+    void add(BatchKernel kind, int P, size_t smem, const std::vector<const T*>& args, const std::vector<int>& blocks)
+    {
+        if (args.empty()) return;
+        Group g;
+        g.kind = kind;
+        g.P = P;
+        g.smem = smem;
+        g.nsys = (int)args.size();
+        size_t o = (host.size() + 63) & ~(size_t)63;
+        g.args_off = o;
+        host.resize(o + sizeof(T) * args.size());
+        for (size_t i = 0; i < args.size(); i++) std::memcpy(&host[o + i * sizeof(T)], args[i], sizeof(T));
+        o = (host.size() + 15) & ~(size_t)15;
+        g.first_off = o;
+        host.resize(o + sizeof(int) * (args.size() + 1));
+        int acc = 0;
+        for (size_t i = 0; i <= args.size(); i++) {
+            std::memcpy(&host[o + i * sizeof(int)], &acc, sizeof(int));
+            if (i < args.size()) acc += blocks[i];
+        }
+        g.nblocks = acc;
+        if (acc > 0) groups.push_back(g);
+    }
+};
+
+// The batch step in one captured graph: each kind of kernel runs for every
+// system in one launch (one per order where the kernel is templated on the
+// order, or per shared-memory size), the near fields of all systems in one
+// persistent kernel beside the far fields.
 static int batch_capture(gbfmm_batch* b)
 {
+    const int ns = b->n_sys;
+    std::vector<StepDesc> d(ns);
+    for (int i = 0; i < ns; i++) describe_step(b->hs[i], d[i]);
+    // tables: tree keys; scatter and leaf sort; the far chain to the M2L; the
+    // downward pass; the finalize (after the near fields join)
+    GroupTable tree, sort, far, down, fin;
+    {
+        std::vector<const TreeArgs*> ta;
+        std::vector<const ScatterArgs*> sa;
+        std::vector<const LeafSortArgs*> la;
+        std::vector<int> tb, sb, lb;
+        size_t tsm = 0;
+        for (auto& x : d) {
+            if (x.h->n <= 0) continue;
+            ta.push_back(&x.tree);
+            tb.push_back(x.tree_blocks);
+            tsm = std::max(tsm, x.tree_smem);
+            sa.push_back(&x.scatter);
+            sb.push_back(x.scatter_blocks);
+        }
+        for (auto& x : d) {
+            la.push_back(&x.leaf);
+            lb.push_back(x.leaf_blocks);
+        }
+        tree.add(BatchKernel::TREE_KEYS, 0, tsm, ta, tb);
+        sort.add(BatchKernel::SCATTER, 0, 0, sa, sb);
+        sort.add(BatchKernel::LEAF_SORT, 0, 0, la, lb);
+    }
+    for (int P = 2; P <= MAX_ORDER; P++) {
+        std::vector<const P2MArgs*> fa, ua;
+        std::vector<int> fb, ub;
+        for (auto& x : d)
+            if (x.h->P == P) {
+                (x.fused ? fa : ua).push_back(&x.p2m);
+                (x.fused ? fb : ub).push_back(x.p2m_blocks);
+            }
+        far.add(BatchKernel::P2M_M2M, P, p2m_m2m_smem_bytes(P), fa, fb);
+        far.add(BatchKernel::P2M, P, p2m_smem_bytes(P), ua, ub);
+    }
+    size_t rounds = 0;
+    for (auto& x : d) rounds = std::max(rounds, x.m2m.size());
+    for (size_t r = 0; r < rounds; r++) {
+        std::vector<const M2MArgs*> ma;
+        std::vector<int> mb;
+        size_t sm = 0;
+        for (auto& x : d)
+            if (r < x.m2m.size()) {
+                ma.push_back(&x.m2m[r]);
+                mb.push_back(x.m2m[r].nparent * ((x.m2m[r].R + 31) / 32));
+                sm = std::max(sm, sizeof(float) * 8 * (size_t)x.m2m[r].R);
+            }
+        far.add(BatchKernel::M2M, 0, sm, ma, mb);
+    }
+    {
+        std::vector<int> Rs;
+        for (auto& x : d) Rs.push_back(x.h->R);
+        std::sort(Rs.begin(), Rs.end());
+        Rs.erase(std::unique(Rs.begin(), Rs.end()), Rs.end());
+        for (int R : Rs) {
+            std::vector<const TopArgs*> ta;
+            std::vector<int> tb;
+            bool staged = false;
+            size_t sm = 0;
+            for (auto& x : d)
+                if (x.h->R == R) {
+                    ta.push_back(&x.top);
+                    tb.push_back((int)x.h->ncell[1]);
+                    staged = x.top_staged;
+                    sm = x.top_smem;
+                }
+            far.add(staged ? BatchKernel::TOP_STAGED : BatchKernel::TOP_UNSTAGED, 0, sm, ta, tb);
+        }
+        std::vector<const RootArgs*> ra;
+        std::vector<int> rb;
+        for (auto& x : d)
+            if (!x.top.lattice) {
+                ra.push_back(&x.root);
+                rb.push_back((x.h->R + 7) / 8);
+            }
+        far.add(BatchKernel::ROOT_LATTICE, 0, 0, ra, rb);
+        std::vector<const TcGridArgs*> ga;
+        std::vector<int> gb;
+        for (auto& x : d)
+            if (x.h->tc) {
+                ga.push_back(&x.grids);
+                gb.push_back(x.grids_blocks);
+            }
+        far.add(BatchKernel::TC_GRIDS, 0, 0, ga, gb);
+        std::vector<size_t> sms;
+        for (auto& x : d)
+            if (x.h->tc) sms.push_back(x.m2l_smem);
+        std::sort(sms.begin(), sms.end());
+        sms.erase(std::unique(sms.begin(), sms.end()), sms.end());
+        for (size_t sm : sms) {
+            std::vector<const TcArgs*> ma;
+            std::vector<int> mb;
+            for (auto& x : d)
+                if (x.h->tc && x.m2l_smem == sm) {
+                    ma.push_back(x.h->tca);
+                    mb.push_back(x.m2l_blocks);
+                }
+            far.add(BatchKernel::M2L_TC, 0, sm, ma, mb);
+        }
+    }
+    for (int P = 2; P <= MAX_ORDER; P++) {
+        std::vector<const DownArgs*> da;
+        std::vector<const L2PArgs*> la;
+        std::vector<int> db, lb;
+        for (auto& x : d)
+            if (x.h->P == P) {
+                if (x.h->D >= 2) {
+                    da.push_back(&x.down);
+                    db.push_back(x.down.nparent);
+                } else {
+                    la.push_back(&x.l2p);
+                    lb.push_back((x.h->nleaf + 3) / 4);
+                }
+            }
+        down.add(BatchKernel::DOWN, P, 0, da, db);
+        down.add(BatchKernel::L2P, P, 0, la, lb);
+    }
+    {
+        std::vector<const FinalArgs*> fa;
+        std::vector<int> fb;
+        for (auto& x : d)
+            if (x.h->n > 0) {
+                fa.push_back(&x.fin);
+                fb.push_back(x.fin_blocks);
+            }
+        fin.add(BatchKernel::FINALIZE, 0, 0, fa, fb);
+    }
+    // one device buffer for every table
+    GroupTable* tabs[5] = {&tree, &sort, &far, &down, &fin};
+    size_t total = 0, base[5];
+    for (int t = 0; t < 5; t++) {
+        base[t] = total;
+        total = (total + tabs[t]->host.size() + 255) & ~(size_t)255;
+    }
+    if (total > b->group_bytes) {
+        if (b->group_buf) cudaFree(b->group_buf);
+        b->group_buf = nullptr;
+        b->group_bytes = 0;
+        CK(cudaMalloc(&b->group_buf, std::max<size_t>(total, 256)));
+        b->group_bytes = std::max<size_t>(total, 256);
+    }
+    for (int t = 0; t < 5; t++)
+        if (!tabs[t]->host.empty())
+            CK(cudaMemcpy((char*)b->group_buf + base[t], tabs[t]->host.data(), tabs[t]->host.size(),
+                          cudaMemcpyHostToDevice));
+    int launches = 0;
+    auto run = [&](int t, cudaStream_t st) {
+        const char* dev = (const char*)b->group_buf + base[t];
+        for (const auto& g : tabs[t]->groups) {
+            const void* args = dev + g.args_off;
+            const int* first = reinterpret_cast<const int*>(dev + g.first_off);
+            if (g.kind == BatchKernel::TC_GRIDS || g.kind == BatchKernel::M2L_TC)
+                launch_batch_tc(g.kind, args, first, g.nsys, g.nblocks, g.smem, st);
+            else
+                launch_batch(g.kind, g.P, args, first, g.nsys, g.nblocks, g.smem, st);
+            launches++;
+        }
+    };
+    const long launches0 = g_kernel_launches.load();
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(b->master, cudaStreamCaptureModeThreadLocal));
     CK(cudaEventRecord(b->ein, b->master));
-    const int nw = (int)b->workers.size();
-    for (int w = 0; w < nw; w++) CK(cudaStreamWaitEvent(b->workers[w], b->ein, 0));
-    // largest systems first, round-robin over the worker streams
-    std::vector<int> ord(b->n_sys);
-    for (int i = 0; i < b->n_sys; i++) ord[i] = i;
-    std::sort(ord.begin(), ord.end(), [&](int x, int y) { return b->hs[x]->n > b->hs[y]->n; });
-    // 1) every system's tree and far field on the worker streams (the handles
-    //    keep, and later destroy, their own streams; only the capture moves)
-    for (int k = 0; k < b->n_sys; k++) {
-        gbfmm_handle* h = b->hs[ord[k]];
-        cudaStream_t own = h->stream;
-        h->stream = b->workers[k % nw];
-        enqueue_step(h, 0, b->ev_tree[k]);
-        h->stream = own;
-    }
+    // 1) every system's tree (one launch per kernel); the leaf scan of systems too
+    //    large for the tree kernel's epilogue runs between the keys and the scatter
+    run(0, b->master);
+    for (auto& x : d)
+        if (x.h->n > 0 && !x.tree.off)
+            launch_exclusive_scan(x.h->d_counts, x.h->d_off, x.h->nleaf, x.h->d_scan, b->master);
+    run(1, b->master);
+    CK(cudaEventRecord(b->ev_near, b->master));
     // 2) all near fields: one persistent kernel over every system's leaves
-    CK(cudaStreamWaitEvent(b->near_stream, b->ein, 0));
+    CK(cudaStreamWaitEvent(b->near_stream, b->ev_near, 0));
     CK(cudaMemsetAsync(b->p2p.counter, 0, sizeof(int), b->near_stream));
-    for (int k = 0; k < b->n_sys; k++) CK(cudaStreamWaitEvent(b->near_stream, b->ev_tree[k], 0));
     launch_p2p_batch(b->p2p, b->p2p_shape, b->p2p_per_sm, b->near_stream);
-    CK(cudaEventRecord(b->ev_near, b->near_stream));
-    // 3) every system's forces, potentials and energy
-    for (int w = 0; w < nw; w++) CK(cudaStreamWaitEvent(b->workers[w], b->ev_near, 0));
-    for (int k = 0; k < b->n_sys; k++) {
-        gbfmm_handle* h = b->hs[ord[k]];
-        cudaStream_t own = h->stream;
-        h->stream = b->workers[k % nw];
-        enqueue_final(h);
-        h->stream = own;
-    }
-    for (int w = 0; w < nw; w++) {
-        CK(cudaEventRecord(b->ev[w], b->workers[w]));
-        CK(cudaStreamWaitEvent(b->master, b->ev[w], 0));
-    }
+    cudaEvent_t ev_nf = b->ev_tree[0];
+    CK(cudaEventRecord(ev_nf, b->near_stream));
+    // 3) the far fields: one launch per kind (per order / shared-memory size);
+    //    systems with the FP32 M2L keep their own contraction and root L2L
+    run(2, b->master);
+    for (auto& x : d)
+        if (!x.h->tc) {
+            ContractArgs a = contract_args(x.h, OP_M2L, 2, false, x.h->m2l_task0);
+            launch_contract(a, x.h->m2l_ntask, b->master);
+            launch_root_l2l(x.root, b->master);
+        }
+    run(3, b->master);
+    // 4) join the near fields, then every system's forces, potentials and energy
+    CK(cudaStreamWaitEvent(b->master, ev_nf, 0));
+    run(4, b->master);
+    for (auto& x : d)
+        if (x.h->n <= 0) CK(cudaMemsetAsync(x.h->d_energy, 0, sizeof(double), b->master));
     cudaError_t e = cudaStreamEndCapture(b->master, &g);
     if (e != cudaSuccess) return fail(GBFMM_ERR_CUDA, "batch graph capture: %s", cudaGetErrorString(e));
     e = cudaGraphInstantiate(&b->gexec, g, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(GBFMM_ERR_CUDA, "batch graph instantiate: %s", cudaGetErrorString(e));
+    b->step_launches = (int)(g_kernel_launches.load() - launches0);
+    (void)launches;
+    return GBFMM_OK;
+}
+
+extern "C" int gbfmm_batch_step_launches(gbfmm_batch* b, int* n)
+{
+    if (!b || !n) return fail(GBFMM_ERR_ARG, "NULL argument");
+    *n = b->step_launches;
     return GBFMM_OK;
 }
 

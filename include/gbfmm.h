@@ -310,6 +310,10 @@ int gbfmm_batch_execute_device(gbfmm_batch* b, const void* d_coords, const void*
  * wait gave up); the flags and step counters are then cleared for the next step. */
 int gbfmm_batch_status(gbfmm_batch* b);
 int gbfmm_batch_device_outputs(gbfmm_batch* b, void** d_forces, void** d_potentials, void** d_energies);
+/* Number of device kernels one batch step launches: each kind of kernel runs for
+ * every system in one launch (one per expansion order or shared-memory size
+ * where the kernel depends on them), the near fields in one persistent kernel. */
+int gbfmm_batch_step_launches(gbfmm_batch* b, int* n);
 int gbfmm_batch_destroy(gbfmm_batch* b);
 
 /* Batch autotuner: times replays of the batch graph on the caller's device
