@@ -520,8 +520,9 @@ def frames_line(pkg, torch, dev, systems, tuner_mod, n_frames):
 def batch_line(pkg, torch, dev, systems, steps, warmup):
     """64 independent systems (atom counts log-uniform in [2,000, 200,000], water +
     0.15 M NaCl, one cubic box each), solved in one batched CUDA graph
-    (gbfmm_batch_*, near fields in one persistent kernel, tiles from
-    gbfmm_batch_autotune), device-resident, L2 flushed before every step:
+    (gbfmm_batch_*: each kind of kernel runs for every system in one launch,
+    the near fields in one persistent kernel, tiles from gbfmm_batch_autotune),
+    device-resident, L2 flushed before every step:
       value  each system's own order drawn (seeded) from 6..10 and its depth in
              3..5 (16-128 bodies per leaf where that range allows), BF16X3;
       tuned  each system's order and depth proposed by the learned tuner for the
@@ -567,6 +568,7 @@ def batch_line(pkg, torch, dev, systems, steps, warmup):
         tiles = b.autotune(xd.data_ptr(), qd.data_ptr(), B, reps=2)  # gbfmm_batch_autotune
         b.execute(X, Q, B)  # captures the tuned graph
         ms = timed(lambda: b.execute_device(xd.data_ptr(), qd.data_ptr(), B, st.cuda_stream))
+        launches = b.step_launches()
         b.close()
         singles = []
         for i, (xyz, q, box) in enumerate(sy):
@@ -580,14 +582,16 @@ def batch_line(pkg, torch, dev, systems, steps, warmup):
                 s.execute_device(xd.data_ptr() + 12 * int(off[i]), float(B[i]), st.cuda_stream)
 
         ms_seq = timed(seq)
+        seq_launches = sum(s.step_launches() for s in singles)
         per = [timed(lambda s=s, i=i: s.execute_device(xd.data_ptr() + 12 * int(off[i]), float(B[i]),
                                                        st.cuda_stream), 3) for i, s in enumerate(singles)]
         for s in singles:
             s.close()
         pn = sorted({PREC_NAME[v] for v in prec}) if isinstance(prec, list) else PREC_NAME[prec]
         return f, {"value": n / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "tile_autotune": tiles,
-                   "ms_per_step_default_tiles": ms_default, "precision": pn,
-                   "sequential_single_solves": {"value": n / (ms_seq * 1e-3), "ms_per_step": ms_seq},
+                   "ms_per_step_default_tiles": ms_default, "precision": pn, "launches_per_step": launches,
+                   "sequential_single_solves": {"value": n / (ms_seq * 1e-3), "ms_per_step": ms_seq,
+                                                "launches_per_step": seq_launches},
                    "speedup_vs_sequential": ms_seq / ms}, per
 
     rng = np.random.default_rng(64)
@@ -673,7 +677,8 @@ def main():
         for _ in range(args.steps):
             b.execute_device(xd.data_ptr(), qd.data_ptr(), B, st.cuda_stream)
         torch.cuda.synchronize()
-        print(json.dumps({"profile": "batch", "steps": args.steps, "systems": len(nat), "atoms": int(sum(nat))}))
+        print(json.dumps({"profile": "batch", "steps": args.steps, "systems": len(nat), "atoms": int(sum(nat)),
+                          "launches_per_step": b.step_launches()}))
         b.close()
         return
     if args.profile:

@@ -93,6 +93,8 @@ def lib():
             "gbfmm_debug_bounded_wait": (ctypes.c_int, [ctypes.c_uint, vp]),
             "gbfmm_batch_status": (ctypes.c_int, [vp]),
             "gbfmm_batch_step_launches": (ctypes.c_int, [vp, ip]),
+            "gbfmm_batch_set_schedule": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+            "gbfmm_batch_get_schedule": (ctypes.c_int, [vp, ip, ip, ip]),
             "gbfmm_get_virial": (ctypes.c_int, [vp, dp]),
         }
         for name, (res, args) in sig.items():
@@ -364,6 +366,14 @@ class BatchSolver:
         """Waits for the last step; raises FmmError if a system reported an error."""
         _check(lib().gbfmm_batch_status(self._b))
 
+    def schedule(self):
+        v = [ctypes.c_int() for _ in range(3)]
+        _check(lib().gbfmm_batch_get_schedule(self._b, *[ctypes.byref(x) for x in v]))
+        return {"far_lanes": v[0].value, "far_prio": v[1].value, "near_after": v[2].value}
+
+    def set_schedule(self, far_lanes=1, far_prio=0, near_after=0):
+        _check(lib().gbfmm_batch_set_schedule(self._b, int(far_lanes), int(far_prio), int(near_after)))
+
     def step_launches(self):
         """Kernels one batch step launches (counted when its graph is captured)."""
         n = ctypes.c_int()
@@ -387,7 +397,7 @@ class BatchSolver:
         ms = ctypes.c_float()
         _check(lib().gbfmm_batch_autotune(self._b, ctypes.c_void_p(int(coords_ptr)), ctypes.c_void_p(int(charges_ptr)),
                                           _fp(b), int(reps), ctypes.byref(ms)))
-        return dict(self.tuning(), ms=ms.value)
+        return dict(self.tuning(), **self.schedule(), ms=ms.value)
 
 
 def lists(max_depth, images, which):

@@ -1683,6 +1683,14 @@ struct gbfmm_batch {
     void* group_buf = nullptr;
     size_t group_bytes = 0;
     int step_launches = 0;  // kernels one batch step launches
+    // Far-field lanes: the systems' far chains split by expansion order over
+    // 'far_lanes' streams (workers, or workers_hi at the greatest stream priority
+    // when far_prio), and the point at which the near-field kernel starts
+    // (near_after 0: after the tree; 1: with the M2L; 2: after the M2L).
+    std::vector<cudaStream_t> workers_hi;
+    std::vector<cudaEvent_t> ev_up;
+    int far_lanes = 1, near_after = 0;
+    bool far_prio = false;
 };
 
 static void free_batch(gbfmm_batch* b)
@@ -1692,7 +1700,9 @@ static void free_batch(gbfmm_batch* b)
         if (h) gbfmm_destroy(h);
     if (b->gexec) cudaGraphExecDestroy(b->gexec);
     for (cudaStream_t s : b->workers) cudaStreamDestroy(s);
+    for (cudaStream_t s : b->workers_hi) cudaStreamDestroy(s);
     for (cudaEvent_t e : b->ev) cudaEventDestroy(e);
+    for (cudaEvent_t e : b->ev_up) cudaEventDestroy(e);
     if (b->ein) cudaEventDestroy(b->ein);
     if (b->ev_sc) cudaEventDestroy(b->ev_sc);
     if (b->eout) cudaEventDestroy(b->eout);
@@ -1794,6 +1804,19 @@ static int batch_create(int n_sys, const int* atom_offsets, const int* orders, c
             return bail(fail(GBFMM_ERR_CUDA, "stream create"));
         b->workers.push_back(s);
         b->ev.push_back(e);
+    }
+    {
+        int least = 0, greatest = 0;
+        cudaDeviceGetStreamPriorityRange(&least, &greatest);
+        for (int w = 0; w < nw; w++) {
+            cudaStream_t s;
+            cudaEvent_t e;
+            if (cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, greatest) != cudaSuccess ||
+                cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+                return bail(fail(GBFMM_ERR_CUDA, "stream create"));
+            b->workers_hi.push_back(s);
+            b->ev_up.push_back(e);
+        }
     }
     if (cudaEventCreateWithFlags(&b->ein, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&b->ev_sc, cudaEventDisableTiming) != cudaSuccess ||
@@ -2046,17 +2069,41 @@ struct GroupTable {
 };
 
 // The batch step in one captured graph: each kind of kernel runs for every
-// system in one launch (one per order where the kernel is templated on the
-// order, or per shared-memory size), the near fields of all systems in one
-// persistent kernel beside the far fields.
+// system of a far-field lane in one launch (one per order where the kernel is
+// templated on the order, or per shared-memory size), the near fields of all
+// systems in one persistent kernel beside the far fields.
 static int batch_capture(gbfmm_batch* b)
 {
     const int ns = b->n_sys;
     std::vector<StepDesc> d(ns);
     for (int i = 0; i < ns; i++) describe_step(b->hs[i], d[i]);
-    // tables: tree keys; scatter and leaf sort; the far chain to the M2L; the
-    // downward pass; the finalize (after the near fields join)
-    GroupTable tree, sort, far, down, fin;
+    // Far-field lanes: the orders, heaviest first (atoms x rows^2), each to the
+    // least loaded lane; a lane's systems share its grouped launches.
+    const int L = std::max(1, std::min(b->far_lanes, (int)b->workers.size()));
+    std::vector<int> lane(ns, 0);
+    if (L > 1) {
+        std::vector<std::pair<double, int>> work;  // (work, order)
+        for (int P = 2; P <= MAX_ORDER; P++) {
+            double w = 0;
+            for (auto& x : d)
+                if (x.h->P == P) w += (double)x.h->n * x.h->R * x.h->R;
+            if (w > 0) work.push_back({w, P});
+        }
+        std::sort(work.begin(), work.end(), [](auto& x, auto& y) { return x.first > y.first; });
+        std::vector<double> load(L, 0.0);
+        int lane_of_P[MAX_ORDER + 1] = {};
+        for (auto& wp : work) {
+            const int l = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+            load[l] += wp.first;
+            lane_of_P[wp.second] = l;
+        }
+        for (int i = 0; i < ns; i++) lane[i] = lane_of_P[d[i].h->P];
+    }
+    // tables: tree keys; scatter and leaf sort; per lane the upward pass to the
+    // tensor-core grids, the tensor-core M2L and the downward pass; the finalize
+    // (after the near fields join)
+    GroupTable tree, sort, fin;
+    std::vector<GroupTable> up(L), m2l(L), down(L);
     {
         std::vector<const TreeArgs*> ta;
         std::vector<const ScatterArgs*> sa;
@@ -2079,34 +2126,37 @@ static int batch_capture(gbfmm_batch* b)
         sort.add(BatchKernel::SCATTER, 0, 0, sa, sb);
         sort.add(BatchKernel::LEAF_SORT, 0, 0, la, lb);
     }
-    for (int P = 2; P <= MAX_ORDER; P++) {
-        std::vector<const P2MArgs*> fa, ua;
-        std::vector<int> fb, ub;
+    for (int l = 0; l < L; l++) {
+        auto in = [&](const StepDesc& x) { return lane[&x - d.data()] == l; };
+        for (int P = 2; P <= MAX_ORDER; P++) {
+            std::vector<const P2MArgs*> fa, ua;
+            std::vector<int> fb, ub;
+            for (auto& x : d)
+                if (in(x) && x.h->P == P) {
+                    (x.fused ? fa : ua).push_back(&x.p2m);
+                    (x.fused ? fb : ub).push_back(x.p2m_blocks);
+                }
+            up[l].add(BatchKernel::P2M_M2M, P, p2m_m2m_smem_bytes(P), fa, fb);
+            up[l].add(BatchKernel::P2M, P, p2m_smem_bytes(P), ua, ub);
+        }
+        size_t rounds = 0;
         for (auto& x : d)
-            if (x.h->P == P) {
-                (x.fused ? fa : ua).push_back(&x.p2m);
-                (x.fused ? fb : ub).push_back(x.p2m_blocks);
-            }
-        far.add(BatchKernel::P2M_M2M, P, p2m_m2m_smem_bytes(P), fa, fb);
-        far.add(BatchKernel::P2M, P, p2m_smem_bytes(P), ua, ub);
-    }
-    size_t rounds = 0;
-    for (auto& x : d) rounds = std::max(rounds, x.m2m.size());
-    for (size_t r = 0; r < rounds; r++) {
-        std::vector<const M2MArgs*> ma;
-        std::vector<int> mb;
-        size_t sm = 0;
-        for (auto& x : d)
-            if (r < x.m2m.size()) {
-                ma.push_back(&x.m2m[r]);
-                mb.push_back(x.m2m[r].nparent * ((x.m2m[r].R + 31) / 32));
-                sm = std::max(sm, sizeof(float) * 8 * (size_t)x.m2m[r].R);
-            }
-        far.add(BatchKernel::M2M, 0, sm, ma, mb);
-    }
-    {
+            if (in(x)) rounds = std::max(rounds, x.m2m.size());
+        for (size_t r = 0; r < rounds; r++) {
+            std::vector<const M2MArgs*> ma;
+            std::vector<int> mb;
+            size_t sm = 0;
+            for (auto& x : d)
+                if (in(x) && r < x.m2m.size()) {
+                    ma.push_back(&x.m2m[r]);
+                    mb.push_back(x.m2m[r].nparent * ((x.m2m[r].R + 31) / 32));
+                    sm = std::max(sm, sizeof(float) * 8 * (size_t)x.m2m[r].R);
+                }
+            up[l].add(BatchKernel::M2M, 0, sm, ma, mb);
+        }
         std::vector<int> Rs;
-        for (auto& x : d) Rs.push_back(x.h->R);
+        for (auto& x : d)
+            if (in(x)) Rs.push_back(x.h->R);
         std::sort(Rs.begin(), Rs.end());
         Rs.erase(std::unique(Rs.begin(), Rs.end()), Rs.end());
         for (int R : Rs) {
@@ -2115,62 +2165,62 @@ static int batch_capture(gbfmm_batch* b)
             bool staged = false;
             size_t sm = 0;
             for (auto& x : d)
-                if (x.h->R == R) {
+                if (in(x) && x.h->R == R) {
                     ta.push_back(&x.top);
                     tb.push_back((int)x.h->ncell[1]);
                     staged = x.top_staged;
                     sm = x.top_smem;
                 }
-            far.add(staged ? BatchKernel::TOP_STAGED : BatchKernel::TOP_UNSTAGED, 0, sm, ta, tb);
+            up[l].add(staged ? BatchKernel::TOP_STAGED : BatchKernel::TOP_UNSTAGED, 0, sm, ta, tb);
         }
         std::vector<const RootArgs*> ra;
         std::vector<int> rb;
         for (auto& x : d)
-            if (!x.top.lattice) {
+            if (in(x) && !x.top.lattice) {
                 ra.push_back(&x.root);
                 rb.push_back((x.h->R + 7) / 8);
             }
-        far.add(BatchKernel::ROOT_LATTICE, 0, 0, ra, rb);
+        up[l].add(BatchKernel::ROOT_LATTICE, 0, 0, ra, rb);
         std::vector<const TcGridArgs*> ga;
         std::vector<int> gb;
         for (auto& x : d)
-            if (x.h->tc) {
+            if (in(x) && x.h->tc) {
                 ga.push_back(&x.grids);
                 gb.push_back(x.grids_blocks);
             }
-        far.add(BatchKernel::TC_GRIDS, 0, 0, ga, gb);
+        up[l].add(BatchKernel::TC_GRIDS, 0, 0, ga, gb);
         std::vector<size_t> sms;
         for (auto& x : d)
-            if (x.h->tc) sms.push_back(x.m2l_smem);
+            if (in(x) && x.h->tc) sms.push_back(x.m2l_smem);
         std::sort(sms.begin(), sms.end());
         sms.erase(std::unique(sms.begin(), sms.end()), sms.end());
         for (size_t sm : sms) {
             std::vector<const TcArgs*> ma;
             std::vector<int> mb;
             for (auto& x : d)
-                if (x.h->tc && x.m2l_smem == sm) {
+                if (in(x) && x.h->tc && x.m2l_smem == sm) {
                     ma.push_back(x.h->tca);
                     mb.push_back(x.m2l_blocks);
                 }
-            far.add(BatchKernel::M2L_TC, 0, sm, ma, mb);
+            m2l[l].add(BatchKernel::M2L_TC, 0, sm, ma, mb);
         }
-    }
-    for (int P = 2; P <= MAX_ORDER; P++) {
-        std::vector<const DownArgs*> da;
-        std::vector<const L2PArgs*> la;
-        std::vector<int> db, lb;
-        for (auto& x : d)
-            if (x.h->P == P) {
-                if (x.h->D >= 2) {
-                    da.push_back(&x.down);
-                    db.push_back(x.down.nparent);
-                } else {
-                    la.push_back(&x.l2p);
-                    lb.push_back((x.h->nleaf + 3) / 4);
+        for (int P = 2; P <= MAX_ORDER; P++) {
+            std::vector<const DownArgs*> da;
+            std::vector<const L2PArgs*> la;
+            std::vector<int> db, lb;
+            for (auto& x : d)
+                if (in(x) && x.h->P == P) {
+                    if (x.h->D >= 2) {
+                        da.push_back(&x.down);
+                        db.push_back(x.down.nparent);
+                    } else {
+                        la.push_back(&x.l2p);
+                        lb.push_back((x.h->nleaf + 3) / 4);
+                    }
                 }
-            }
-        down.add(BatchKernel::DOWN, P, 0, da, db);
-        down.add(BatchKernel::L2P, P, 0, la, lb);
+            down[l].add(BatchKernel::DOWN, P, 0, da, db);
+            down[l].add(BatchKernel::L2P, P, 0, la, lb);
+        }
     }
     {
         std::vector<const FinalArgs*> fa;
@@ -2183,9 +2233,15 @@ static int batch_capture(gbfmm_batch* b)
         fin.add(BatchKernel::FINALIZE, 0, 0, fa, fb);
     }
     // one device buffer for every table
-    GroupTable* tabs[5] = {&tree, &sort, &far, &down, &fin};
-    size_t total = 0, base[5];
-    for (int t = 0; t < 5; t++) {
+    std::vector<GroupTable*> tabs = {&tree, &sort, &fin};
+    for (int l = 0; l < L; l++) {
+        tabs.push_back(&up[l]);
+        tabs.push_back(&m2l[l]);
+        tabs.push_back(&down[l]);
+    }
+    std::vector<size_t> base(tabs.size());
+    size_t total = 0;
+    for (size_t t = 0; t < tabs.size(); t++) {
         base[t] = total;
         total = (total + tabs[t]->host.size() + 255) & ~(size_t)255;
     }
@@ -2196,54 +2252,71 @@ static int batch_capture(gbfmm_batch* b)
         CK(cudaMalloc(&b->group_buf, std::max<size_t>(total, 256)));
         b->group_bytes = std::max<size_t>(total, 256);
     }
-    for (int t = 0; t < 5; t++)
+    for (size_t t = 0; t < tabs.size(); t++)
         if (!tabs[t]->host.empty())
             CK(cudaMemcpy((char*)b->group_buf + base[t], tabs[t]->host.data(), tabs[t]->host.size(),
                           cudaMemcpyHostToDevice));
-    int launches = 0;
-    auto run = [&](int t, cudaStream_t st) {
+    auto run = [&](const GroupTable& tab, cudaStream_t st) {
+        const size_t t = std::find(tabs.begin(), tabs.end(), &tab) - tabs.begin();
         const char* dev = (const char*)b->group_buf + base[t];
-        for (const auto& g : tabs[t]->groups) {
+        for (const auto& g : tab.groups) {
             const void* args = dev + g.args_off;
             const int* first = reinterpret_cast<const int*>(dev + g.first_off);
             if (g.kind == BatchKernel::TC_GRIDS || g.kind == BatchKernel::M2L_TC)
                 launch_batch_tc(g.kind, args, first, g.nsys, g.nblocks, g.smem, st);
             else
                 launch_batch(g.kind, g.P, args, first, g.nsys, g.nblocks, g.smem, st);
-            launches++;
         }
     };
     const long launches0 = g_kernel_launches.load();
+    const bool forked = L > 1 || b->far_prio;
+    std::vector<cudaStream_t> ls(L, b->master);
+    if (forked)
+        for (int l = 0; l < L; l++) ls[l] = b->far_prio ? b->workers_hi[l] : b->workers[l];
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(b->master, cudaStreamCaptureModeThreadLocal));
     CK(cudaEventRecord(b->ein, b->master));
     // 1) every system's tree (one launch per kernel); the leaf scan of systems too
     //    large for the tree kernel's epilogue runs between the keys and the scatter
-    run(0, b->master);
+    run(tree, b->master);
     for (auto& x : d)
         if (x.h->n > 0 && !x.tree.off)
             launch_exclusive_scan(x.h->d_counts, x.h->d_off, x.h->nleaf, x.h->d_scan, b->master);
-    run(1, b->master);
+    run(sort, b->master);
     CK(cudaEventRecord(b->ev_near, b->master));
-    // 2) all near fields: one persistent kernel over every system's leaves
+    // 2) the far fields, lane by lane: one launch per kind (per order or shared-
+    //    memory size); systems with the FP32 M2L keep their own contraction and
+    //    root L2L
+    for (int l = 0; l < L; l++) {
+        if (forked) CK(cudaStreamWaitEvent(ls[l], b->ev_near, 0));
+        run(up[l], ls[l]);
+        CK(cudaEventRecord(b->ev_up[l], ls[l]));
+        run(m2l[l], ls[l]);
+        for (int i = 0; i < ns; i++)
+            if (lane[i] == l && !d[i].h->tc) {
+                ContractArgs a = contract_args(d[i].h, OP_M2L, 2, false, d[i].h->m2l_task0);
+                launch_contract(a, d[i].h->m2l_ntask, ls[l]);
+                launch_root_l2l(d[i].root, ls[l]);
+            }
+        if (b->near_after == 2) CK(cudaEventRecord(b->ev_up[l], ls[l]));
+        run(down[l], ls[l]);
+        if (forked) CK(cudaEventRecord(b->ev[l], ls[l]));
+    }
+    // 3) all near fields: one persistent kernel over every system's leaves, from
+    //    the tree on, or from the far fields' M2L on (near_after)
     CK(cudaStreamWaitEvent(b->near_stream, b->ev_near, 0));
+    if (b->near_after > 0)
+        for (int l = 0; l < L; l++) CK(cudaStreamWaitEvent(b->near_stream, b->ev_up[l], 0));
     CK(cudaMemsetAsync(b->p2p.counter, 0, sizeof(int), b->near_stream));
     launch_p2p_batch(b->p2p, b->p2p_shape, b->p2p_per_sm, b->near_stream);
     cudaEvent_t ev_nf = b->ev_tree[0];
     CK(cudaEventRecord(ev_nf, b->near_stream));
-    // 3) the far fields: one launch per kind (per order / shared-memory size);
-    //    systems with the FP32 M2L keep their own contraction and root L2L
-    run(2, b->master);
-    for (auto& x : d)
-        if (!x.h->tc) {
-            ContractArgs a = contract_args(x.h, OP_M2L, 2, false, x.h->m2l_task0);
-            launch_contract(a, x.h->m2l_ntask, b->master);
-            launch_root_l2l(x.root, b->master);
-        }
-    run(3, b->master);
-    // 4) join the near fields, then every system's forces, potentials and energy
+    // 4) join the lanes and the near fields, then every system's forces,
+    //    potentials and energy
+    if (forked)
+        for (int l = 0; l < L; l++) CK(cudaStreamWaitEvent(b->master, b->ev[l], 0));
     CK(cudaStreamWaitEvent(b->master, ev_nf, 0));
-    run(4, b->master);
+    run(fin, b->master);
     for (auto& x : d)
         if (x.h->n <= 0) CK(cudaMemsetAsync(x.h->d_energy, 0, sizeof(double), b->master));
     cudaError_t e = cudaStreamEndCapture(b->master, &g);
@@ -2252,7 +2325,6 @@ static int batch_capture(gbfmm_batch* b)
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(GBFMM_ERR_CUDA, "batch graph instantiate: %s", cudaGetErrorString(e));
     b->step_launches = (int)(g_kernel_launches.load() - launches0);
-    (void)launches;
     return GBFMM_OK;
 }
 
@@ -2348,6 +2420,37 @@ extern "C" int gbfmm_batch_get_tuning(gbfmm_batch* b, int* p2p_shape, int* p2p_p
     return GBFMM_OK;
 }
 
+static int apply_batch_schedule(gbfmm_batch* b, int far_lanes, int far_prio, int near_after)
+{
+    if (far_lanes < 1 || far_lanes > (int)b->workers.size())
+        return fail(GBFMM_ERR_ARG, "far lanes %d outside [1,%d]", far_lanes, (int)b->workers.size());
+    if (near_after < 0 || near_after > 2) return fail(GBFMM_ERR_ARG, "near_after %d outside [0,2]", near_after);
+    if (b->gexec) {
+        CK(cudaStreamSynchronize(b->master));
+        cudaGraphExecDestroy(b->gexec);
+        b->gexec = nullptr;
+    }
+    b->far_lanes = far_lanes;
+    b->far_prio = far_prio != 0;
+    b->near_after = near_after;
+    return GBFMM_OK;
+}
+
+extern "C" int gbfmm_batch_set_schedule(gbfmm_batch* b, int far_lanes, int far_prio, int near_after)
+{
+    if (!b) return fail(GBFMM_ERR_ARG, "batch is NULL");
+    return apply_batch_schedule(b, far_lanes, far_prio, near_after);
+}
+
+extern "C" int gbfmm_batch_get_schedule(gbfmm_batch* b, int* far_lanes, int* far_prio, int* near_after)
+{
+    if (!b) return fail(GBFMM_ERR_ARG, "batch is NULL");
+    if (far_lanes) *far_lanes = b->far_lanes;
+    if (far_prio) *far_prio = b->far_prio ? 1 : 0;
+    if (near_after) *near_after = b->near_after;
+    return GBFMM_OK;
+}
+
 extern "C" int gbfmm_batch_autotune(gbfmm_batch* b, const void* d_coords, const void* d_charges,
                                     const float* box_edges, int reps, float* best_ms)
 {
@@ -2395,6 +2498,34 @@ extern "C" int gbfmm_batch_autotune(gbfmm_batch* b, const void* d_coords, const 
             const float t = measure(bs, bp, bv, ns);
             if (t < bt) { bt = t; bn = ns; }
         }
+    }
+    // schedule: far-field lanes (up to one per expansion order), their stream
+    // priority, and when the near-field kernel starts
+    {
+        bool seen[MAX_ORDER + 1] = {};
+        int norders = 0;
+        for (gbfmm_handle* h : b->hs)
+            if (!seen[h->P]) {
+                seen[h->P] = true;
+                norders++;
+            }
+        const int maxl = std::max(1, std::min(norders, (int)b->workers.size()));
+        int bl = b->far_lanes, bq = b->far_prio ? 1 : 0, ba = b->near_after;
+        if (!err && apply_batch_tuning(b, bs, bp, bv, bn) == GBFMM_OK) {
+            auto measure_sched = [&](int l, int q, int a) -> float {
+                if (apply_batch_schedule(b, l, q, a) != GBFMM_OK) return 1e30f;
+                return measure(bs, bp, bv, bn);
+            };
+            bt = measure_sched(bl, bq, ba);
+            for (int l = 1; l <= maxl && !err; l++)
+                for (int q = 0; q <= 1 && !err; q++)
+                    for (int a = 0; a <= 1 && !err; a++) {
+                        if (l == bl && q == bq && a == ba) continue;
+                        const float t = measure_sched(l, q, a);
+                        if (t < bt) { bt = t; bl = l; bq = q; ba = a; }
+                    }
+        }
+        if (!err) err = apply_batch_schedule(b, bl, bq, ba);
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

@@ -316,12 +316,23 @@ int gbfmm_batch_device_outputs(gbfmm_batch* b, void** d_forces, void** d_potenti
 int gbfmm_batch_step_launches(gbfmm_batch* b, int* n);
 int gbfmm_batch_destroy(gbfmm_batch* b);
 
+/* Batch schedule: the far fields run as 'far_lanes' concurrent chains of
+ * grouped launches (1..min(n_sys, 8); the expansion orders are spread over the
+ * lanes, heaviest first), on streams of the greatest priority when far_prio is
+ * non-zero, and the near-field kernel starts after the tree (near_after 0),
+ * together with the M2L (1) or after it (2).  The results do not depend on the
+ * schedule.  Default 1, 0, 0; gbfmm_batch_autotune searches it too. */
+int gbfmm_batch_set_schedule(gbfmm_batch* b, int far_lanes, int far_prio, int near_after);
+int gbfmm_batch_get_schedule(gbfmm_batch* b, int* far_lanes, int* far_prio, int* near_after);
+
 /* Batch autotuner: times replays of the batch graph on the caller's device
  * inputs (as gbfmm_batch_execute_device) for the near-field kernel's warp-step
  * shape (0: 8 targets x 4 source lanes, 1: 4 x 8, 2: 16 x 2, 3 and 4: 8 x 4 and
  * 4 x 8 with up to 4 targets per thread) and CTAs per SM (2..5), then, when
  * any system uses the tensor-core M2L, a batch-wide M2L entry split (1, 2, 4,
- * 8) and pipeline depth, and keeps the fastest (best_ms: its step time).
+ * 8) and pipeline depth, then the schedule (gbfmm_batch_set_schedule: lanes
+ * up to one per expansion order, their priority, near_after 0 or 1), and keeps
+ * the fastest (best_ms: its step time).
  * m2l_split / m2l_stages 0 in get/set mean each system's own.  Results are the
  * same up to the order of floating-point additions.  No reference counterpart:
  * the reference solves one system per call with fixed launch shapes

@@ -160,3 +160,58 @@ def test_batch_mixed_precisions_match_single_solves(pkg, systems):
         assert e[i] == s.get_energy(), i
         s.close()
     b.close()
+
+
+def test_batch_launch_count_does_not_grow_with_systems(pkg, systems):
+    """The batch step launches each kind of kernel once for all systems (once per
+    order or shared-memory size where the kernel depends on them): doubling the
+    systems at the same orders and depths keeps the launch count, which stays
+    below the sum of the systems' single-solve launches."""
+    sy = _systems(systems)
+    counts = []
+    for rep in (1, 2):
+        s2 = sy * rep
+        b = pkg.BatchSolver([len(s[1]) for s in s2], [s[3] for s in s2], [s[4] for s in s2], images=4,
+                            precision=1, flags=pkg.FLAG_DETERMINISTIC)
+        X = np.concatenate([s[0] for s in s2])
+        Q = np.concatenate([s[1] for s in s2])
+        B = np.array([s[2] for s in s2], np.float32)
+        f, _, _ = b.execute(X, Q, B)
+        counts.append(b.step_launches())
+        if rep == 2:
+            n1 = b.offsets[len(sy)]
+            assert np.array_equal(f[:n1], f[n1:])  # the same systems twice: the same bits
+        b.close()
+    singles = 0
+    for xyz, q, L, P, D in sy:
+        s = pkg.ZetaFmmSolver(len(q), q, order=P, max_depth=D, images=4, precision=1, flags=pkg.FLAG_DETERMINISTIC)
+        s.execute(xyz, L)
+        singles += s.step_launches()
+        s.close()
+    assert counts[0] == counts[1], counts
+    assert counts[0] < singles, (counts, singles)
+
+
+def test_batch_schedule_leaves_results_unchanged(pkg, systems):
+    """Far-field lanes, their stream priority and the near field's start point
+    only move work between streams: under GBFMM_FLAG_DETERMINISTIC every
+    schedule gives the same bits."""
+    sy = _systems(systems)
+    b = pkg.BatchSolver([len(s[1]) for s in sy], [s[3] for s in sy], [s[4] for s in sy], images=4,
+                        precision=1, flags=pkg.FLAG_DETERMINISTIC)
+    X = np.concatenate([s[0] for s in sy])
+    Q = np.concatenate([s[1] for s in sy])
+    B = np.array([s[2] for s in sy], np.float32)
+    f0, p0, e0 = b.execute(X, Q, B)
+    n0 = b.step_launches()
+    for sched in [(2, 0, 0), (3, 1, 1), (5, 0, 2), (1, 1, 1)]:
+        b.set_schedule(*sched)
+        assert b.schedule() == dict(zip(("far_lanes", "far_prio", "near_after"), sched))
+        f, p, e = b.execute(X, Q, B)
+        assert np.array_equal(f, f0) and np.array_equal(p, p0) and np.array_equal(e, e0), sched
+        assert b.step_launches() >= n0
+    with pytest.raises(pkg.FmmError):
+        b.set_schedule(9, 0, 0)
+    with pytest.raises(pkg.FmmError):
+        b.set_schedule(1, 0, 3)
+    b.close()
