@@ -1047,13 +1047,39 @@ __global__ void __launch_bounds__(P2P_THREADS) k_p2p_batch(const P2PBatchArgs b)
     }
 }
 
+// Grid form of the batched near field: one CTA per queue item (no resident
+// CTAs), so that the block scheduler interleaves the near field with the far-
+// field kernels as CTAs retire (the far fields' stream priority then decides).
+template <int LT, int KM = 3>
+__global__ void __launch_bounds__(P2P_THREADS) k_p2p_batch_grid(const P2PBatchArgs b)
+{
+    __shared__ P2PShared sh;
+    const int item = (int)blockIdx.x;
+    int lo = 0, hi = b.nsys - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(&b.first[mid]) <= item) lo = mid;
+        else hi = mid - 1;
+    }
+    p2p_leaf<LT, KM>(b.sys[lo], (uint32_t)(item - __ldg(&b.first[lo])), sh);
+}
+
 int p2p_batch_shapes() { return 5; }
 
 void launch_p2p_batch(const P2PBatchArgs& b, int shape, int per_sm, cudaStream_t s)
 {
     if (b.nitems <= 0) return;
-    const int grid = std::min(b.nitems, sm_count() * std::max(1, std::min(per_sm, 5)));
     COUNT_LAUNCH();
+    if (per_sm <= 0) {
+        const int grid = b.nitems;
+        if (shape == 1) k_p2p_batch_grid<4><<<grid, P2P_THREADS, 0, s>>>(b);
+        else if (shape == 2) k_p2p_batch_grid<16><<<grid, P2P_THREADS, 0, s>>>(b);
+        else if (shape == 3) k_p2p_batch_grid<8, 4><<<grid, P2P_THREADS, 0, s>>>(b);
+        else if (shape == 4) k_p2p_batch_grid<4, 4><<<grid, P2P_THREADS, 0, s>>>(b);
+        else k_p2p_batch_grid<8><<<grid, P2P_THREADS, 0, s>>>(b);
+        return;
+    }
+    const int grid = std::min(b.nitems, sm_count() * std::min(per_sm, 5));
     if (shape == 1) k_p2p_batch<4><<<grid, P2P_THREADS, 0, s>>>(b);
     else if (shape == 2) k_p2p_batch<16><<<grid, P2P_THREADS, 0, s>>>(b);
     else if (shape == 3) k_p2p_batch<8, 4><<<grid, P2P_THREADS, 0, s>>>(b);

@@ -211,7 +211,8 @@ struct P2PBatchArgs {
     int* counter;        // zero at launch
 };
 // shape: 0 8 targets x 4 source lanes, 1 4 x 8, 2 16 x 2, 3 and 4 the shapes 8 x 4
-// and 4 x 8 with up to 4 targets per thread; per_sm 1..5.
+// and 4 x 8 with up to 4 targets per thread; per_sm 1..5 resident CTAs per SM
+// walking the queue, or 0: one CTA per queue item.
 int p2p_batch_shapes();
 void launch_p2p_batch(const P2PBatchArgs& b, int shape, int per_sm, cudaStream_t s);
 void launch_p2p(const P2PArgs& a, int variant, cudaStream_t s, int* counter);

@@ -2372,7 +2372,7 @@ extern "C" int gbfmm_batch_execute_device(gbfmm_batch* b, const void* d_coords, 
 static int apply_batch_tuning(gbfmm_batch* b, int shape, int per_sm, int split_v, int nstage)
 {
     if (shape < 0 || shape >= p2p_batch_shapes()) return fail(GBFMM_ERR_ARG, "batch p2p shape %d", shape);
-    if (per_sm < 1 || per_sm > 5) return fail(GBFMM_ERR_ARG, "batch p2p CTAs per SM %d outside [1,5]", per_sm);
+    if (per_sm < 0 || per_sm > 5) return fail(GBFMM_ERR_ARG, "batch p2p CTAs per SM %d outside [0,5]", per_sm);
     if (split_v >= TC_NSPLIT) return fail(GBFMM_ERR_ARG, "m2l split");
     for (gbfmm_handle* h : b->hs)
         if (h->tc && split_v >= 0 && h->tc_ntask_v[split_v] == 0)
@@ -2478,8 +2478,8 @@ extern "C" int gbfmm_batch_autotune(gbfmm_batch* b, const void* d_coords, const 
     float bt = measure(bs, bp, bv, bn);
     // coordinate search: near-field shape and CTAs per SM, then M2L split, then M2L depth
     for (int sh = 0; sh < p2p_batch_shapes() && !err; sh++)
-        for (int ps = 2; ps <= 5 && !err; ps++) {
-            if (sh == bs && ps == bp) continue;
+        for (int ps = 0; ps <= 5 && !err; ps++) {
+            if (ps == 1 || (sh == bs && ps == bp)) continue;
             const float t = measure(sh, ps, bv, bn);
             if (t < bt) { bt = t; bs = sh; bp = ps; }
         }
@@ -2526,6 +2526,12 @@ extern "C" int gbfmm_batch_autotune(gbfmm_batch* b, const void* d_coords, const 
                     }
         }
         if (!err) err = apply_batch_schedule(b, bl, bq, ba);
+        // the near field's residency again, under the chosen schedule
+        for (int ps = 0; ps <= 5 && !err; ps++) {
+            if (ps == 1 || ps == bp) continue;
+            const float t = measure(bs, ps, bv, bn);
+            if (t < bt) { bt = t; bp = ps; }
+        }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

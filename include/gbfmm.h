@@ -328,7 +328,8 @@ int gbfmm_batch_get_schedule(gbfmm_batch* b, int* far_lanes, int* far_prio, int*
 /* Batch autotuner: times replays of the batch graph on the caller's device
  * inputs (as gbfmm_batch_execute_device) for the near-field kernel's warp-step
  * shape (0: 8 targets x 4 source lanes, 1: 4 x 8, 2: 16 x 2, 3 and 4: 8 x 4 and
- * 4 x 8 with up to 4 targets per thread) and CTAs per SM (2..5), then, when
+ * 4 x 8 with up to 4 targets per thread) and CTAs per SM (2..5 resident CTAs
+ * walking the queue, or 0: one CTA per leaf), then, when
  * any system uses the tensor-core M2L, a batch-wide M2L entry split (1, 2, 4,
  * 8) and pipeline depth, then the schedule (gbfmm_batch_set_schedule: lanes
  * up to one per expansion order, their priority, near_after 0 or 1), and keeps
