@@ -853,20 +853,36 @@ __device__ __forceinline__ void p2p_cluster(const float4* __restrict__ src, cons
 struct P2PShared {
     float4 src[P2P_MAXS];      // P2P_MAXS sources in P2P_MAXS/2 records of two float4
     float4 part[4][P2P_MAXT];  // per-warp partial sums, reduced in warp order
-    int e_off[128];
-    int e_beg[128];
+    int e_off[128];            // window position of each stencil leaf (even)
+    int e_beg[128];            // first body of the leaf in the sorted atoms
+    int e_cnt[128];            // its body count
     float4 e_d[128];
     int ws[4];
+    uint64_t bar;              // completion of the bulk copies of one window
 };
 
+// Initialises the staging barrier of a CTA (before its first p2p_leaf).
+__device__ __forceinline__ void p2p_init(P2PShared& sh)
+{
+    if (threadIdx.x == 0) {
+        mbar_init(&sh.bar, 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+}
+
 // The near field of one target leaf (the CTA's 128 threads).  The source bodies
-// of the 81 near leaves are staged in shared memory, shifted into the target
+// of the 81 near leaves are staged in shared memory in windows of P2P_MAXS
+// bodies, each leaf at an even window position (an odd count leaves one far,
+// chargeless padding body): one bulk copy per leaf (its bodies are contiguous in
+// tree order, 16 bytes each) on an mbarrier, then, in place, every pair of
+// bodies of a leaf becomes one record of two float4 shifted into the target
 // leaf's frame (scaled units, integer offsets of the stencil, so the periodic
-// shift is exact), two per record; the target leaf itself is staged first
-// (stencil entry 0).  A warp step covers LT targets x SL = 32/LT source records;
-// a thread carries up to 3 targets (clusters of 3 LT).  Warp w sweeps a quarter of
-// the sources; the SL source lanes of a target are reduced by shuffles and the
-// per-warp partial sums are added in warp order (deterministic).
+// shift is exact); the target leaf itself is staged first (stencil entry 0).  A
+// warp step covers LT targets x SL = 32/LT source records; a thread carries up to
+// KM targets (clusters of KM LT).  Warp w sweeps a quarter of the sources; the SL
+// source lanes of a target are reduced by shuffles and the per-warp partial sums
+// are added in warp order (deterministic).
 //
 // The r = 0 test is applied to the target leaf's own bodies only.  Bodies of two
 // different leaves cannot coincide when every staged body lies strictly inside
@@ -874,8 +890,11 @@ struct P2PShared {
 // integer shift is far below that margin); a CTA whose stencil holds any leaf
 // with a body outside that range (bodies on or near a leaf face, or outside the
 // box; flagged per leaf by the leaf sort) applies the test to every source.
+//
+// 'phase' is the parity of the staging barrier's current phase (the same in
+// every thread); a bounded wait that gives up sets bit 2 of *a.err.
 template <int LT, int KM = 3>
-__device__ __forceinline__ void p2p_leaf(const P2PArgs& a, uint32_t tcode, P2PShared& sh)
+__device__ __forceinline__ void p2p_leaf(const P2PArgs& a, uint32_t tcode, P2PShared& sh, uint32_t& phase)
 {
     constexpr int SL = 32 / LT, SPS = 2 * SL;  // sources per step
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -901,12 +920,14 @@ __device__ __forceinline__ void p2p_leaf(const P2PArgs& a, uint32_t tcode, P2PSh
         } else {
             sh.e_beg[tid] = 0;
         }
+        sh.e_cnt[tid] = cnt;
         sh.e_d[tid] = make_float4((float)a.stencil[3 * tid], (float)a.stencil[3 * tid + 1],
                                   (float)a.stencil[3 * tid + 2], 0.f);
     }
-    // exclusive prefix over the stencil entries (nst <= 128)
+    // exclusive prefix of the even-rounded counts over the stencil entries (nst <= 128)
     {
-        int x = cnt;
+        const int c2 = (cnt + 1) & ~1;
+        int x = c2;
         for (int o = 1; o < 32; o <<= 1) {
             int y = __shfl_up_sync(0xffffffffu, x, o);
             if (lane >= o) x += y;
@@ -915,7 +936,7 @@ __device__ __forceinline__ void p2p_leaf(const P2PArgs& a, uint32_t tcode, P2PSh
         __syncthreads();
         int add = 0;
         for (int w = 0; w < warp; w++) add += sh.ws[w];
-        sh.e_off[tid] = x - cnt + add;
+        sh.e_off[tid] = x - c2 + add;
         __syncthreads();
         if (tid == 0) sh.e_off[a.nst] = sh.ws[0] + sh.ws[1] + sh.ws[2] + sh.ws[3];
     }
@@ -933,28 +954,44 @@ __device__ __forceinline__ void p2p_leaf(const P2PArgs& a, uint32_t tcode, P2PSh
         for (int s0 = 0; s0 < total; s0 += P2P_MAXS) {
             const int ns = min(P2P_MAXS, total - s0);
             const int nsp = (ns + SPS - 1) / SPS * SPS;
-            __syncthreads();
-            // warp w copies whole source leaves w, w+4, ...: lane = body of the leaf,
-            // clipped to this pass's window [s0, s0+ns); far zero-charge padding to nsp
-            for (int e = warp; e < a.nst; e += 4) {
-                const int b0 = max(sh.e_off[e], s0), b1 = min(sh.e_off[e + 1], s0 + ns);
-                const float4 d = sh.e_d[e];
-                const int gb = sh.e_beg[e] - sh.e_off[e];
-                for (int g = b0 + lane; g < b1; g += 32) {
-                    const float4 b = a.atoms[gb + g];
-                    const int r = g - s0;
-                    float* rec = srcf + 8 * (r >> 1) + (r & 1);
-                    rec[0] = b.x + d.x;
-                    rec[2] = b.y + d.y;
-                    rec[4] = b.z + d.z;
-                    rec[6] = b.w;
+            __syncthreads();  // the previous window's readers are done
+            // one bulk copy per stencil leaf: its bodies inside this window
+            if (tid < a.nst) {
+                const int b0 = max(sh.e_off[tid], s0), b1 = min(sh.e_off[tid] + sh.e_cnt[tid], s0 + ns);
+                if (b1 > b0) {
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    asm volatile("mbarrier.expect_tx.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&sh.bar)),
+                                 "r"((uint32_t)(16 * (b1 - b0)))
+                                 : "memory");
+                    bulk_g2s(sh.src + (b0 - s0), a.atoms + sh.e_beg[tid] + (b0 - sh.e_off[tid]),
+                             (uint32_t)(16 * (b1 - b0)), &sh.bar);
                 }
             }
-            if (tid < nsp - ns) {
-                const int r = ns + tid;
-                float* rec = srcf + 8 * (r >> 1) + (r & 1);
-                rec[0] = rec[2] = rec[4] = P2P_FAR;
-                rec[6] = 0.f;
+            __syncthreads();  // every expected byte count is on the barrier
+            if (tid == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&sh.bar)) : "memory");
+            if (!mbar_wait(&sh.bar, phase, a.err, 2, a.wait_limit)) mbar_drain(&sh.bar, phase, a.wait_limit);
+            phase ^= 1u;
+            // records, in place: warp w turns the body pairs of leaves w, w+4, ...
+            for (int e = warp; e < a.nst; e += 4) {
+                const int eo = sh.e_off[e], real = eo + sh.e_cnt[e];
+                const int p0 = max(eo, s0), p1 = min(sh.e_off[e + 1], s0 + ns);
+                const float4 d = sh.e_d[e];
+                for (int g = p0 + 2 * lane; g < p1; g += 64) {
+                    const int r = g - s0;
+                    const float4 far = make_float4(P2P_FAR, P2P_FAR, P2P_FAR, 0.f);
+                    const float4 ba = g < real ? sh.src[r] : far;
+                    const float4 bb = g + 1 < real ? sh.src[r + 1] : far;
+                    const bool sa = g < real, sb = g + 1 < real;
+                    sh.src[r] = make_float4(sa ? ba.x + d.x : P2P_FAR, sb ? bb.x + d.x : P2P_FAR,
+                                            sa ? ba.y + d.y : P2P_FAR, sb ? bb.y + d.y : P2P_FAR);
+                    sh.src[r + 1] = make_float4(sa ? ba.z + d.z : P2P_FAR, sb ? bb.z + d.z : P2P_FAR, ba.w, bb.w);
+                }
+            }
+            // far zero-charge padding of the last step
+            if (tid < (nsp - ns) / 2) {
+                const int r = ns + 2 * tid;
+                sh.src[r] = make_float4(P2P_FAR, P2P_FAR, P2P_FAR, P2P_FAR);
+                sh.src[r + 1] = make_float4(P2P_FAR, P2P_FAR, 0.f, 0.f);
             }
             __syncthreads();
             // this warp's quarter of the source steps; the steps holding the
@@ -991,7 +1028,9 @@ template <int LT, int KM = 3>
 __global__ void __launch_bounds__(P2P_THREADS) k_p2p(const P2PArgs a)
 {
     __shared__ P2PShared sh;
-    p2p_leaf<LT, KM>(a, blockIdx.x, sh);
+    p2p_init(sh);
+    uint32_t phase = 0;
+    p2p_leaf<LT, KM>(a, blockIdx.x, sh, phase);
 }
 
 // Persistent form: a fixed number of CTAs per SM walk the queue of leaves
@@ -1003,13 +1042,15 @@ __global__ void __launch_bounds__(P2P_THREADS) k_p2p_queue(const P2PArgs a, int*
 {
     __shared__ P2PShared sh;
     __shared__ int next;
+    p2p_init(sh);
+    uint32_t phase = 0;
     if (threadIdx.x == 0) next = atomicAdd(counter, 1);
     __syncthreads();
     int item = next;
     while (item < nitems) {
         __syncthreads();  // every thread has read 'next'
         if (threadIdx.x == 0) next = atomicAdd(counter, 1);
-        p2p_leaf<LT>(a, (uint32_t)item, sh);
+        p2p_leaf<LT>(a, (uint32_t)item, sh, phase);
         __syncthreads();
         item = next;
     }
@@ -1024,6 +1065,8 @@ __global__ void __launch_bounds__(P2P_THREADS) k_p2p_batch(const P2PBatchArgs b)
     __shared__ P2PShared sh;
     __shared__ int next, leaf;
     __shared__ P2PArgs cur;
+    p2p_init(sh);
+    uint32_t phase = 0;
     if (threadIdx.x == 0) next = atomicAdd(b.counter, 1);
     __syncthreads();
     int item = next;
@@ -1041,7 +1084,7 @@ __global__ void __launch_bounds__(P2P_THREADS) k_p2p_batch(const P2PBatchArgs b)
             leaf = item - b.first[lo];
         }
         __syncthreads();
-        p2p_leaf<LT, KM>(cur, (uint32_t)leaf, sh);
+        p2p_leaf<LT, KM>(cur, (uint32_t)leaf, sh, phase);
         __syncthreads();
         item = next;
     }
@@ -1054,6 +1097,8 @@ template <int LT, int KM = 3>
 __global__ void __launch_bounds__(P2P_THREADS) k_p2p_batch_grid(const P2PBatchArgs b)
 {
     __shared__ P2PShared sh;
+    p2p_init(sh);
+    uint32_t phase = 0;
     const int item = (int)blockIdx.x;
     int lo = 0, hi = b.nsys - 1;
     while (lo < hi) {
@@ -1061,7 +1106,7 @@ __global__ void __launch_bounds__(P2P_THREADS) k_p2p_batch_grid(const P2PBatchAr
         if (__ldg(&b.first[mid]) <= item) lo = mid;
         else hi = mid - 1;
     }
-    p2p_leaf<LT, KM>(b.sys[lo], (uint32_t)(item - __ldg(&b.first[lo])), sh);
+    p2p_leaf<LT, KM>(b.sys[lo], (uint32_t)(item - __ldg(&b.first[lo])), sh, phase);
 }
 
 int p2p_batch_shapes() { return 5; }

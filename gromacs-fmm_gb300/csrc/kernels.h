@@ -201,6 +201,8 @@ struct P2PArgs {
     int nst;
     float4* field;            // sorted near field (phi, grad), scaled units
     const int* leaf_edge;     // per leaf: a body on or near its faces or outside it (from the leaf sort)
+    int* err = nullptr;       // bit 2: a bounded wait on the staging copies gave up
+    uint32_t wait_limit = 0;  // polls of that wait
 };
 int p2p_variants();
 // Near fields of many systems in one persistent launch (per_sm CTAs per SM).

@@ -617,6 +617,8 @@ static P2PArgs p2p_args(const gbfmm_handle* h)
     pa.nst = h->n_p2p_st;
     pa.field = h->d_near;
     pa.leaf_edge = h->d_leaf_edge;
+    pa.err = h->d_flags + 3;
+    pa.wait_limit = WAIT_POLLS_DEFAULT;
     return pa;
 }
 
@@ -1124,12 +1126,13 @@ static int fetch(gbfmm_handle* h)
         for (int s = 0; s < 9; s++) cudaEventElapsedTime(&h->stage_ms[s], h->ev[s], h->ev[s + 1]);
     }
     h->results_on_host = true;
-    if (h->h_flags[1] || h->h_flags[2]) {
+    if (h->h_flags[1] || h->h_flags[2] || h->h_flags[3]) {
         CK(cudaMemsetAsync(h->d_flags, 0, sizeof(int) * 4, h->stream));
         CK(cudaMemsetAsync(h->d_counts, 0, sizeof(int) * (h->nleaf + 1 + 4), h->stream));
         h->have_result = false;
-        return fail(GBFMM_ERR_TIMEOUT, h->h_flags[1] ? "a bounded device wait in the tensor-core M2L gave up"
-                                                      : "a bounded device wait in the upper-tree kernel gave up");
+        return fail(GBFMM_ERR_TIMEOUT, h->h_flags[1]   ? "a bounded device wait in the tensor-core M2L gave up"
+                                       : h->h_flags[2] ? "a bounded device wait in the upper-tree kernel gave up"
+                                                       : "a bounded device wait in the near-field kernel gave up");
     }
     if (h->h_flags[0]) {
         CK(cudaMemsetAsync(h->d_flags, 0, sizeof(int) * 4, h->stream));
@@ -2372,7 +2375,8 @@ extern "C" int gbfmm_batch_execute_device(gbfmm_batch* b, const void* d_coords, 
 static int apply_batch_tuning(gbfmm_batch* b, int shape, int per_sm, int split_v, int nstage)
 {
     if (shape < 0 || shape >= p2p_batch_shapes()) return fail(GBFMM_ERR_ARG, "batch p2p shape %d", shape);
-    if (per_sm < 0 || per_sm > 5) return fail(GBFMM_ERR_ARG, "batch p2p CTAs per SM %d outside [0,5]", per_sm);
+    if (per_sm < 0 || per_sm > 5)
+        return fail(GBFMM_ERR_ARG, "batch p2p residency %d outside [0,5] (0: a CTA per leaf)", per_sm);
     if (split_v >= TC_NSPLIT) return fail(GBFMM_ERR_ARG, "m2l split");
     for (gbfmm_handle* h : b->hs)
         if (h->tc && split_v >= 0 && h->tc_ntask_v[split_v] == 0)
@@ -2562,8 +2566,8 @@ extern "C" int gbfmm_batch_execute(gbfmm_batch* b, const float* coords, const fl
     return batch_check(b);
 }
 
-// Reads every system's step flags (bit 0 non-finite input, bits 1-2 a bounded
-// wait of the tensor-core M2L or of the upper-tree kernel gave up); on an error
+// Reads every system's step flags (word 0 non-finite input, words 1-3 a bounded
+// wait of the tensor-core M2L, the upper-tree or the near-field kernel gave up); on an error
 // clears the flags and the step counters, as fetch() does for one system.
 static int batch_check(gbfmm_batch* b)
 {
@@ -2572,14 +2576,15 @@ static int batch_check(gbfmm_batch* b)
     for (gbfmm_handle* h : b->hs) {
         int fl[4];
         CK(cudaMemcpy(fl, h->d_flags, sizeof(fl), cudaMemcpyDeviceToHost));
-        if (fl[0] || fl[1] || fl[2]) {
+        if (fl[0] || fl[1] || fl[2] || fl[3]) {
             CK(cudaMemset(h->d_flags, 0, sizeof(int) * 4));
-            if (fl[1] || fl[2]) CK(cudaMemset(h->d_counts, 0, sizeof(int) * (h->nleaf + 1 + 4)));
+            if (fl[1] || fl[2] || fl[3]) CK(cudaMemset(h->d_counts, 0, sizeof(int) * (h->nleaf + 1 + 4)));
             if (rc == GBFMM_OK)
-                rc = fail(fl[1] || fl[2] ? GBFMM_ERR_TIMEOUT : GBFMM_ERR_COORD,
-                          fl[1] ? "a bounded device wait in a system's tensor-core M2L gave up"
-                                : fl[2] ? "a bounded device wait in a system's upper-tree kernel gave up"
-                                        : "a system of the batch has a non-finite coordinate");
+                rc = fail(fl[1] || fl[2] || fl[3] ? GBFMM_ERR_TIMEOUT : GBFMM_ERR_COORD,
+                          fl[1]   ? "a bounded device wait in a system's tensor-core M2L gave up"
+                          : fl[2] ? "a bounded device wait in a system's upper-tree kernel gave up"
+                          : fl[3] ? "a bounded device wait in a system's near-field kernel gave up"
+                                  : "a system of the batch has a non-finite coordinate");
         }
     }
     if (rc != GBFMM_OK) b->have_result = false;

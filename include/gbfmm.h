@@ -273,7 +273,10 @@ int gbfmm_debug_bounded_wait(unsigned polls, void* stream);
 
 /* ---- autotuner (tile shapes) ----
  * gbfmm_autotune times whole steps (CUDA-graph replays, reps per candidate) of
- * the given configuration for the P2P warp-step shapes and, on the tensor-core
+ * the given configuration for the P2P variants (0-14: warp-step shape 8 x 4,
+ * 4 x 8 or 16 x 2 by variant % 3, one CTA per leaf or 2-5 resident CTAs per SM
+ * by variant / 3; 15-16: 8 x 4 and 4 x 8 with up to 4 targets per thread, one
+ * CTA per leaf) and, on the tensor-core
  * path, the M2L entry split (1, 2, 4, 8; 1 only on a deterministic handle) and
  * pipeline depth, and keeps the fastest (best_ms: its step time; may be NULL).
  * Results are the same up to the order of floating-point additions.  No
@@ -328,8 +331,8 @@ int gbfmm_batch_get_schedule(gbfmm_batch* b, int* far_lanes, int* far_prio, int*
 /* Batch autotuner: times replays of the batch graph on the caller's device
  * inputs (as gbfmm_batch_execute_device) for the near-field kernel's warp-step
  * shape (0: 8 targets x 4 source lanes, 1: 4 x 8, 2: 16 x 2, 3 and 4: 8 x 4 and
- * 4 x 8 with up to 4 targets per thread) and CTAs per SM (2..5 resident CTAs
- * walking the queue, or 0: one CTA per leaf), then, when
+ * 4 x 8 with up to 4 targets per thread) and residency (2..5 resident CTAs
+ * per SM walking the queue, or 0: one CTA per leaf), then, when
  * any system uses the tensor-core M2L, a batch-wide M2L entry split (1, 2, 4,
  * 8) and pipeline depth, then the schedule (gbfmm_batch_set_schedule: lanes
  * up to one per expansion order, their priority, near_after 0 or 1), and keeps

@@ -90,12 +90,13 @@ def _batch_inputs(pkg, systems, precision, flags=0):
 
 @pytest.mark.parametrize("precision", [0, 1])
 def test_batch_every_tuning_matches(pkg, systems, precision):
-    """Every near-field shape and CTA count of the batch kernel, and every M2L
-    split and depth, give the same forces up to the order of the additions."""
+    """Every near-field shape and residency of the batch kernel (a CTA per leaf,
+    or resident CTAs walking the queue), and every M2L split and depth, give the
+    same forces up to the order of the additions."""
     b, X, Q, B = _batch_inputs(pkg, systems, precision)
     f0, p0, _ = b.execute(X, Q, B)
     for shape in range(5):
-        for per_sm in (2, 5):
+        for per_sm in (0, 2, 5):
             b.set_tuning(shape, per_sm, 0, 0)
             f, p, _ = b.execute(X, Q, B)
             assert rel_rms(f, f0) < 1e-5, (shape, per_sm)
@@ -108,6 +109,8 @@ def test_batch_every_tuning_matches(pkg, systems, precision):
                 assert rel_rms(f, f0) < 1e-5, (split, stages)
     with pytest.raises(pkg.FmmError):
         b.set_tuning(5, 4, 0, 0)
+    with pytest.raises(pkg.FmmError):
+        b.set_tuning(0, 6, 0, 0)
     b.close()
 
 
@@ -118,7 +121,7 @@ def test_batch_autotune_keeps_a_valid_tuning(pkg, systems):
     xd = torch.from_numpy(X).cuda()
     qd = torch.from_numpy(Q).cuda()
     t = b.autotune(xd.data_ptr(), qd.data_ptr(), B, reps=2)
-    assert t["ms"] > 0 and 0 <= t["p2p_shape"] < 5 and 1 <= t["p2p_per_sm"] <= 5
+    assert t["ms"] > 0 and 0 <= t["p2p_shape"] < 5 and 0 <= t["p2p_per_sm"] <= 5
     assert t["m2l_split"] in (0, 1, 2, 4, 8)
     f1, _, e1 = b.execute(X, Q, B)
     assert rel_rms(f1, f0) < 1e-5
