@@ -805,8 +805,12 @@ __device__ __forceinline__ void p2p_sweep(const float4* __restrict__ src, int sb
 // (target row ii = lane / SL, source lane jj = lane % SL), SL = 32 / LT; thread
 // targets c0 + ii + LT k.  Steps below msteps need the r = 0 test.
 template <int K, int LT>
-__device__ __forceinline__ void p2p_cluster(const float4* __restrict__ src, const float4* __restrict__ tgt, int c0,
-                                            int ntc, int sb, int se, int msteps, int lane, float4* part)
+// Target positions come from the staged records when tsm is set (the targets
+// are the first bodies of window 0, the target leaf's own, unshifted), else
+// from the sorted atoms.
+__device__ __forceinline__ void p2p_cluster(const float4* __restrict__ src, const float4* __restrict__ tgt,
+                                            const float* tsm, int c0, int ntc, int sb, int se, int msteps, int lane,
+                                            float4* part)
 {
     constexpr int SL = 32 / LT;
     const int ii = lane / SL, jj = lane % SL;
@@ -815,10 +819,22 @@ __device__ __forceinline__ void p2p_cluster(const float4* __restrict__ src, cons
     const f2_t zero = f2_pack(0.f, 0.f);
 #pragma unroll
     for (int k = 0; k < K; k++) {
-        const float4 a = tgt[min(c0 + ii + LT * k, ntc - 1)];
-        X[k][0] = f2_pack(a.x, a.x);
-        X[k][1] = f2_pack(a.y, a.y);
-        X[k][2] = f2_pack(a.z, a.z);
+        const int t = min(c0 + ii + LT * k, ntc - 1);
+        float x, y, z;
+        if (tsm) {
+            const float* rec = tsm + 8 * (t >> 1) + (t & 1);
+            x = rec[0];
+            y = rec[2];
+            z = rec[4];
+        } else {
+            const float4 a = tgt[t];
+            x = a.x;
+            y = a.y;
+            z = a.z;
+        }
+        X[k][0] = f2_pack(x, x);
+        X[k][1] = f2_pack(y, y);
+        X[k][2] = f2_pack(z, z);
         acc[k][0] = acc[k][1] = acc[k][2] = acc[k][3] = zero;
     }
     const int mid = min(max(msteps, sb), se);
@@ -1000,12 +1016,14 @@ __device__ __forceinline__ void p2p_leaf(const P2PArgs& a, uint32_t tcode, P2PSh
             const int per = (nsteps + 3) >> 2;
             const int sb = warp * per, se = min(nsteps, sb + per);
             const int msteps = any_edge ? nsteps : max(0, (min(nself, s0 + ns) - s0 + SPS - 1) / SPS);
+            // targets [t0, t0 + ntc) lie in window 0 as the leaf's own bodies
+            const float* tsm = s0 == 0 && t0 + ntc <= ns ? srcf + 8 * (t0 >> 1) : nullptr;
             for (int c0 = 0; c0 < ntc; c0 += KM * LT) {
                 const int rem = ntc - c0;
-                if (KM >= 4 && rem > 3 * LT) p2p_cluster<(KM >= 4 ? 4 : 3), LT>(sh.src, tgt, c0, ntc, sb, se, msteps, lane, sh.part[warp]);
-                else if (rem > 2 * LT) p2p_cluster<3, LT>(sh.src, tgt, c0, ntc, sb, se, msteps, lane, sh.part[warp]);
-                else if (rem > LT) p2p_cluster<2, LT>(sh.src, tgt, c0, ntc, sb, se, msteps, lane, sh.part[warp]);
-                else p2p_cluster<1, LT>(sh.src, tgt, c0, ntc, sb, se, msteps, lane, sh.part[warp]);
+                if (KM >= 4 && rem > 3 * LT) p2p_cluster<(KM >= 4 ? 4 : 3), LT>(sh.src, tgt, tsm, c0, ntc, sb, se, msteps, lane, sh.part[warp]);
+                else if (rem > 2 * LT) p2p_cluster<3, LT>(sh.src, tgt, tsm, c0, ntc, sb, se, msteps, lane, sh.part[warp]);
+                else if (rem > LT) p2p_cluster<2, LT>(sh.src, tgt, tsm, c0, ntc, sb, se, msteps, lane, sh.part[warp]);
+                else p2p_cluster<1, LT>(sh.src, tgt, tsm, c0, ntc, sb, se, msteps, lane, sh.part[warp]);
             }
         }
         __syncthreads();
