@@ -517,6 +517,18 @@ def frames_line(pkg, torch, dev, systems, tuner_mod, n_frames):
     return out
 
 
+def batch_spec(tuner_mod, nat):
+    """Orders and depths of the 64-system batch: each system's order drawn (seeded)
+    from 6..10; its depth the plain depth (16-128 bodies per leaf) or, for a
+    seeded third of the systems, one deeper, clamped to 3..5, so that every
+    depth of 3..5 occurs."""
+    rng = np.random.default_rng(64)
+    orders = [int(v) for v in rng.integers(6, 11, size=len(nat))]
+    deeper = np.random.default_rng(65).random(len(nat)) < 1.0 / 3.0
+    depths = [min(5, max(3, tuner_mod.plain_depth(k) + int(d))) for k, d in zip(nat, deeper)]
+    return orders, depths
+
+
 def batch_line(pkg, torch, dev, systems, steps, warmup):
     """64 independent systems (atom counts log-uniform in [2,000, 200,000], water +
     0.15 M NaCl, one cubic box each), solved in one batched CUDA graph
@@ -524,7 +536,7 @@ def batch_line(pkg, torch, dev, systems, steps, warmup):
     the near fields in one persistent kernel, tiles from gbfmm_batch_autotune),
     device-resident, L2 flushed before every step:
       value  each system's own order drawn (seeded) from 6..10 and its depth in
-             3..5 (16-128 bodies per leaf where that range allows), BF16X3;
+             3..5 (batch_spec), BF16X3;
       tuned  each system's order and depth proposed by the learned tuner for the
              1e-3 tolerance (each proposal checked against the plain order-10
              FMM), each with its own precision (gbfmm_batch_create_mixed);
@@ -594,9 +606,7 @@ def batch_line(pkg, torch, dev, systems, steps, warmup):
                                                 "launches_per_step": seq_launches},
                    "speedup_vs_sequential": ms_seq / ms}, per
 
-    rng = np.random.default_rng(64)
-    spec_orders = [int(v) for v in rng.integers(6, 11, size=len(nat))]
-    spec_depths = [min(5, max(3, tuner_mod.plain_depth(k))) for k in nat]
+    spec_orders, spec_depths = batch_spec(tuner_mod, nat)
     _, spec, spec_per = run_batch(spec_orders, spec_depths, 1)
     spec.update(orders=sorted(set(spec_orders)), depths=sorted(set(spec_depths)),
                 per_system_ms={"min": min(spec_per), "median": float(np.median(spec_per)), "max": max(spec_per)})
@@ -642,7 +652,8 @@ def main():
                     help="skip the 1,002,002-atom line and the 250,002-atom trajectory line")
     ap.add_argument("--frames", type=int, default=200, help="frames of the trajectory line")
     ap.add_argument("--profile", default=None,
-                    help="precision,order,depth[,p2p_variant,m2l_split,m2l_stages], or 'batch': only run "
+                    help="precision,order,depth[,p2p_variant,m2l_split,m2l_stages], or "
+                         "batch[,shape,per_sm,m2l_split,m2l_stages,far_lanes,far_prio,near_after]: only run "
                          "--steps device-resident steps of that configuration and tuning, or of the 64-system "
                          "batch (a short, fixed launch sequence for ncu captures); prints no bench line")
     ap.add_argument("--large-only", action="store_true",
@@ -658,26 +669,30 @@ def main():
         pkg = G.load_package()
         print(json.dumps({"large": large_line(pkg, torch, torch.device("cuda", local), systems, 5)}))
         return
-    if args.profile == "batch":
+    if args.profile and args.profile.split(",")[0] == "batch":
         # device-resident steps of the 64-system batch of the batch line (orders
-        # 6-10, depths 3-5, BF16X3, default tiles)
+        # 6-10, depths 3-5, BF16X3); default tiles and schedule, or
+        # batch,shape,per_sm,m2l_split,m2l_stages,far_lanes,far_prio,near_after
         import torch
         pkg = G.load_package()
         tuner_mod = G.load_module("tuner")
         sy = systems.batch_systems(n_sys=64)
         nat = [len(t[1]) for t in sy]
-        orders = [int(v) for v in np.random.default_rng(64).integers(6, 11, size=len(nat))]
-        depths = [min(5, max(3, tuner_mod.plain_depth(k))) for k in nat]
+        orders, depths = batch_spec(tuner_mod, nat)
         X = np.concatenate([t[0] for t in sy]).astype(np.float32)
         Q = np.concatenate([t[1] for t in sy]).astype(np.float32)
         B = np.array([float(t[2][0]) for t in sy], np.float32)
         b = pkg.BatchSolver(nat, orders, depths, images=4, precision=1)
+        tv = [int(v) for v in args.profile.split(",")[1:]]
+        if len(tv) == 7:
+            b.set_tuning(*tv[:4])
+            b.set_schedule(*tv[4:])
         xd, qd = torch.from_numpy(X).cuda(), torch.from_numpy(Q).cuda()
         st = torch.cuda.current_stream()
         for _ in range(args.steps):
             b.execute_device(xd.data_ptr(), qd.data_ptr(), B, st.cuda_stream)
         torch.cuda.synchronize()
-        print(json.dumps({"profile": "batch", "steps": args.steps, "systems": len(nat), "atoms": int(sum(nat)),
+        print(json.dumps({"profile": args.profile, "steps": args.steps, "systems": len(nat), "atoms": int(sum(nat)),
                           "launches_per_step": b.step_launches()}))
         b.close()
         return
