@@ -872,9 +872,10 @@ struct P2PShared {
     int e_off[128];            // window position of each stencil leaf (even)
     int e_beg[128];            // first body of the leaf in the sorted atoms
     int e_cnt[128];            // its body count
-    float4 e_d[128];
+    char4 e_d[128];            // its stencil offset
     int ws[4];
     uint64_t bar;              // completion of the bulk copies of one window
+    uint8_t tag[P2P_MAXS / 2]; // stencil leaf of each body pair of the window
 };
 
 // Initialises the staging barrier of a CTA (before its first p2p_leaf).
@@ -937,8 +938,8 @@ __device__ __forceinline__ void p2p_leaf(const P2PArgs& a, uint32_t tcode, P2PSh
             sh.e_beg[tid] = 0;
         }
         sh.e_cnt[tid] = cnt;
-        sh.e_d[tid] = make_float4((float)a.stencil[3 * tid], (float)a.stencil[3 * tid + 1],
-                                  (float)a.stencil[3 * tid + 2], 0.f);
+        sh.e_d[tid] = make_char4((signed char)a.stencil[3 * tid], (signed char)a.stencil[3 * tid + 1],
+                                 (signed char)a.stencil[3 * tid + 2], 0);
     }
     // exclusive prefix of the even-rounded counts over the stencil entries (nst <= 128)
     {
@@ -971,8 +972,11 @@ __device__ __forceinline__ void p2p_leaf(const P2PArgs& a, uint32_t tcode, P2PSh
             const int ns = min(P2P_MAXS, total - s0);
             const int nsp = (ns + SPS - 1) / SPS * SPS;
             __syncthreads();  // the previous window's readers are done
-            // one bulk copy per stencil leaf: its bodies inside this window
+            // one bulk copy per stencil leaf: its bodies inside this window; and
+            // the leaf's tag on each of its body pairs in the window
             if (tid < a.nst) {
+                const int q0 = max(sh.e_off[tid], s0), q1 = min(sh.e_off[tid + 1], s0 + ns);
+                for (int g = q0; g < q1; g += 2) sh.tag[(g - s0) >> 1] = (uint8_t)tid;
                 const int b0 = max(sh.e_off[tid], s0), b1 = min(sh.e_off[tid] + sh.e_cnt[tid], s0 + ns);
                 if (b1 > b0) {
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -987,21 +991,19 @@ __device__ __forceinline__ void p2p_leaf(const P2PArgs& a, uint32_t tcode, P2PSh
             if (tid == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&sh.bar)) : "memory");
             if (!mbar_wait(&sh.bar, phase, a.err, 2, a.wait_limit)) mbar_drain(&sh.bar, phase, a.wait_limit);
             phase ^= 1u;
-            // records, in place: warp w turns the body pairs of leaves w, w+4, ...
-            for (int e = warp; e < a.nst; e += 4) {
-                const int eo = sh.e_off[e], real = eo + sh.e_cnt[e];
-                const int p0 = max(eo, s0), p1 = min(sh.e_off[e + 1], s0 + ns);
-                const float4 d = sh.e_d[e];
-                for (int g = p0 + 2 * lane; g < p1; g += 64) {
-                    const int r = g - s0;
-                    const float4 far = make_float4(P2P_FAR, P2P_FAR, P2P_FAR, 0.f);
-                    const float4 ba = g < real ? sh.src[r] : far;
-                    const float4 bb = g + 1 < real ? sh.src[r + 1] : far;
-                    const bool sa = g < real, sb = g + 1 < real;
-                    sh.src[r] = make_float4(sa ? ba.x + d.x : P2P_FAR, sb ? bb.x + d.x : P2P_FAR,
-                                            sa ? ba.y + d.y : P2P_FAR, sb ? bb.y + d.y : P2P_FAR);
-                    sh.src[r + 1] = make_float4(sa ? ba.z + d.z : P2P_FAR, sb ? bb.z + d.z : P2P_FAR, ba.w, bb.w);
-                }
+            // records, in place: thread t turns the body pairs t, t + 128, ... (each
+            // within one stencil leaf: the leaves start at even positions)
+            for (int pr = tid; pr < (ns >> 1); pr += P2P_THREADS) {
+                const int e = sh.tag[pr];
+                const int r = 2 * pr, g = s0 + r, real = sh.e_off[e] + sh.e_cnt[e];
+                const char4 dc = sh.e_d[e];
+                const float dx = (float)dc.x, dy = (float)dc.y, dz = (float)dc.z;
+                const bool sa = g < real, sb = g + 1 < real;
+                const float4 ba = sa ? sh.src[r] : make_float4(0.f, 0.f, 0.f, 0.f);
+                const float4 bb = sb ? sh.src[r + 1] : make_float4(0.f, 0.f, 0.f, 0.f);
+                sh.src[r] = make_float4(sa ? ba.x + dx : P2P_FAR, sb ? bb.x + dx : P2P_FAR, sa ? ba.y + dy : P2P_FAR,
+                                        sb ? bb.y + dy : P2P_FAR);
+                sh.src[r + 1] = make_float4(sa ? ba.z + dz : P2P_FAR, sb ? bb.z + dz : P2P_FAR, ba.w, bb.w);
             }
             // far zero-charge padding of the last step
             if (tid < (nsp - ns) / 2) {
