@@ -869,7 +869,7 @@ __device__ __forceinline__ void p2p_cluster(const float4* __restrict__ src, cons
 struct P2PShared {
     float4 src[P2P_MAXS];      // P2P_MAXS sources in P2P_MAXS/2 records of two float4
     float4 part[4][P2P_MAXT];  // per-warp partial sums, reduced in warp order
-    int e_off[128];            // window position of each stencil leaf (even)
+    int e_off[129];            // window position of each stencil leaf (even), and the total
     int e_beg[128];            // first body of the leaf in the sorted atoms
     int e_cnt[128];            // its body count
     char4 e_d[128];            // its stencil offset
@@ -918,8 +918,7 @@ __device__ __forceinline__ void p2p_leaf(const P2PArgs& a, uint32_t tcode, P2PSh
     int tx, ty, tz;
     morton_decode(tcode, tx, ty, tz);
     const int tb = a.off[tcode], nt = a.off[tcode + 1] - tb;
-    if (nt == 0) return;  // uniform over the CTA
-    // source leaves of the stencil
+    // source leaves of the stencil (their loads overlap the target leaf's)
     int cnt = 0, eflag = 0;
     if (tid < a.nst) {
         int vx = tx + a.stencil[3 * tid], vy = ty + a.stencil[3 * tid + 1], vz = tz + a.stencil[3 * tid + 2];
@@ -941,7 +940,9 @@ __device__ __forceinline__ void p2p_leaf(const P2PArgs& a, uint32_t tcode, P2PSh
         sh.e_d[tid] = make_char4((signed char)a.stencil[3 * tid], (signed char)a.stencil[3 * tid + 1],
                                  (signed char)a.stencil[3 * tid + 2], 0);
     }
-    // exclusive prefix of the even-rounded counts over the stencil entries (nst <= 128)
+    if (nt == 0) return;  // uniform over the CTA
+    // exclusive prefix of the even-rounded counts over the stencil entries (nst <= 128);
+    // entries past nst have no bodies, so every thread from nst on writes the total
     {
         const int c2 = (cnt + 1) & ~1;
         int x = c2;
@@ -954,8 +955,7 @@ __device__ __forceinline__ void p2p_leaf(const P2PArgs& a, uint32_t tcode, P2PSh
         int add = 0;
         for (int w = 0; w < warp; w++) add += sh.ws[w];
         sh.e_off[tid] = x - c2 + add;
-        __syncthreads();
-        if (tid == 0) sh.e_off[a.nst] = sh.ws[0] + sh.ws[1] + sh.ws[2] + sh.ws[3];
+        if (tid == 0 && a.nst == P2P_THREADS) sh.e_off[a.nst] = sh.ws[0] + sh.ws[1] + sh.ws[2] + sh.ws[3];
     }
     // any staged leaf (the target leaf included: a target outside its leaf can
     // meet the image of a body well inside another leaf) with a body at a face:
