@@ -652,7 +652,7 @@ def main():
                     help="skip the 1,002,002-atom line and the 250,002-atom trajectory line")
     ap.add_argument("--frames", type=int, default=200, help="frames of the trajectory line")
     ap.add_argument("--profile", default=None,
-                    help="precision,order,depth[,p2p_variant,m2l_split,m2l_stages], or "
+                    help="precision,order,depth[,p2p_variant,m2l_split,m2l_stages[,near_after]], or "
                          "batch[,shape,per_sm,m2l_split,m2l_stages,far_lanes,far_prio,near_after]: only run "
                          "--steps device-resident steps of that configuration and tuning, or of the 64-system "
                          "batch (a short, fixed launch sequence for ncu captures); prints no bench line")
@@ -703,8 +703,10 @@ def main():
         prec, P, D = vals[:3]
         pkg = G.load_package()
         s = pkg.ZetaFmmSolver(n, q, order=P, max_depth=D, images=4, precision=prec)
-        if len(vals) == 6:
-            s.set_tuning(*vals[3:])
+        if len(vals) >= 6:
+            s.set_tuning(*vals[3:6])
+        if len(vals) == 7:
+            s.set_near_start(vals[6])
         xd = torch.from_numpy(xyz).cuda()
         st = torch.cuda.current_stream()
         for _ in range(args.steps):
@@ -811,6 +813,7 @@ def main():
         sc = run.solver(prec, P, D, flags=pkg.FLAG_HOST_COPY)
         t = s.tuning()
         sc.set_tuning(t["p2p_variant"], t["m2l_split"], t["m2l_stages"])
+        sc.set_near_start(t["near_after"])
         r["e2e_copies"] = n * ws * args.steps / run.time_e2e(sc, args.steps)
         sc.close()
         r["stages"] = run.stages(s, args.steps)

@@ -92,6 +92,8 @@ def lib():
             "gbfmm_debug_harmonics": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, dp, dp]),
             "gbfmm_debug_bounded_wait": (ctypes.c_int, [ctypes.c_uint, vp]),
             "gbfmm_batch_status": (ctypes.c_int, [vp]),
+            "gbfmm_set_near_start": (ctypes.c_int, [vp, ctypes.c_int]),
+            "gbfmm_get_near_start": (ctypes.c_int, [vp, ip]),
             "gbfmm_batch_step_launches": (ctypes.c_int, [vp, ip]),
             "gbfmm_batch_set_schedule": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
             "gbfmm_batch_get_schedule": (ctypes.c_int, [vp, ip, ip, ip]),
@@ -247,9 +249,13 @@ class ZetaFmmSolver:
         return t
 
     def tuning(self):
-        a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        a, b, c, d = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         _check(lib().gbfmm_get_tuning(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
-        return {"p2p_variant": a.value, "m2l_split": b.value, "m2l_stages": c.value}
+        _check(lib().gbfmm_get_near_start(self._h, ctypes.byref(d)))
+        return {"p2p_variant": a.value, "m2l_split": b.value, "m2l_stages": c.value, "near_after": d.value}
+
+    def set_near_start(self, after):
+        _check(lib().gbfmm_set_near_start(self._h, int(after)))
 
     def set_tuning(self, p2p_variant=0, m2l_split=1, m2l_stages=2):
         _check(lib().gbfmm_set_tuning(self._h, int(p2p_variant), int(m2l_split), int(m2l_stages)))

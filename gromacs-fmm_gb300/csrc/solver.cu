@@ -202,6 +202,7 @@ struct gbfmm_handle {
     int tc_split_v = 0;
     int tc_nstage = 2;
     int p2p_variant = 0;  // P2P warp-step shape (autotuned)
+    int near_after = 0;   // the near field starts after the tree (0), the P2M (1) or the upper tree (2)
     StepConst* d_sc = nullptr;
     StepConst* h_sc = nullptr;  // pinned
     int* h_flags = nullptr;     // pinned
@@ -686,23 +687,29 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
                      h->d_counts, s, h->d_leaf_edge);
     mark(h, 1);
     // The near field needs only the tree: in graph mode it forks onto its own
-    // stream and overlaps the far-field chain below (joined before finalize);
-    // the stage-timing pass runs it in line, after L2P.
+    // low-priority stream and overlaps the far-field chain below (joined before
+    // finalize), from the tree on or from a later far-field kernel on
+    // (h->near_after: 1 after the P2M, 2 after the upper tree), so that the
+    // far-field kernels with large shared memory find SMs before the near field's
+    // CTAs fill them; the stage-timing pass runs it in line, after L2P.
     const P2PArgs pa = p2p_args(h);
     const bool near = (mode & STEP_NEAR) != 0;
     const bool fork = near && !h->timing;
     if (tree_done) cudaEventRecord(tree_done, s);
-    if (fork) {
+    auto fork_near = [&](int point) {
+        if (!fork || point != std::min(h->near_after, 2)) return;
         cudaEventRecord(h->ev_fork, s);
         cudaStreamWaitEvent(h->stream_nf, h->ev_fork, 0);
         launch_p2p(pa, h->p2p_variant, h->stream_nf, sync + 2);
         cudaEventRecord(h->ev_join, h->stream_nf);
-    }
+    };
+    fork_near(0);
     // upward pass: P2M with the M2M of the leaf parents in one launch, M2M launches
     // down to level 3, then levels 2 and 1 and the FP64 root in one launch (k_top)
     const bool fused = D >= 2 && launch_p2m_m2m(h->P, h->d_off, h->nleaf, h->d_atoms, h->Mlev[D], h->Mlev[D - 1],
                                                 h->d_m2m_t, h->Rpad, s);
     if (!fused) launch_p2m(h->P, h->d_off, h->nleaf, h->d_atoms, h->Mlev[D], h->Rpad, s);
+    fork_near(1);
     mark(h, 2);
     const int top_from = D == 1 || h->R > TOP_STAGE_MAX_R ? 1 : std::min(3, fused ? D - 1 : D);
     for (int k = fused ? D - 2 : D - 1; k >= top_from; k--)
@@ -740,6 +747,7 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
     top.err = h->d_flags + 2;
     top.umask = (h->shift[0] == 0 ? 4 : 0) | (h->shift[1] == 0 ? 2 : 0) | (h->shift[2] == 0 ? 1 : 0);
     launch_top(top, s);
+    fork_near(2);
     mark(h, 4);
     if (h->tc) {
         // the root L2L rides on the grid conversion, ahead of the M2L
@@ -1201,6 +1209,26 @@ extern "C" int gbfmm_set_tuning(gbfmm_handle* h, int p2p_variant, int m2l_split,
     return GBFMM_OK;
 }
 
+extern "C" int gbfmm_set_near_start(gbfmm_handle* h, int after)
+{
+    if (!h) return fail(GBFMM_ERR_ARG, "handle is NULL");
+    if (after < 0 || after > 2) return fail(GBFMM_ERR_ARG, "near-field start %d outside [0,2]", after);
+    CK(cudaStreamSynchronize(h->stream));
+    h->near_after = after;
+    if (h->gexec) {
+        cudaGraphExecDestroy(h->gexec);
+        h->gexec = nullptr;
+    }
+    return GBFMM_OK;
+}
+
+extern "C" int gbfmm_get_near_start(gbfmm_handle* h, int* after)
+{
+    if (!h || !after) return fail(GBFMM_ERR_ARG, "NULL argument");
+    *after = h->near_after;
+    return GBFMM_OK;
+}
+
 extern "C" int gbfmm_get_tuning(gbfmm_handle* h, int* p2p_variant, int* m2l_split, int* m2l_stages)
 {
     if (!h) return fail(GBFMM_ERR_ARG, "handle is NULL");
@@ -1260,6 +1288,17 @@ extern "C" int gbfmm_autotune(gbfmm_handle* h, const float* coords, const float*
             const float t = measure(bp, bs, ns);
             if (t < bt) { bt = t; bn = ns; }
         }
+    }
+    // where the near field starts in the graph (after the tree, the P2M or the upper tree)
+    {
+        int ba = h->near_after;
+        for (int na = 0; na <= 2 && !err; na++) {
+            if (na == ba) continue;
+            h->near_after = na;
+            const float t = measure(bp, bs, bn);
+            if (t < bt) { bt = t; ba = na; }
+        }
+        h->near_after = ba;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

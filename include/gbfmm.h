@@ -283,6 +283,13 @@ int gbfmm_debug_bounded_wait(unsigned polls, void* stream);
  * reference counterpart: the reference's launch shapes are fixed
  * (gpu_solver.cu:221-248). */
 int gbfmm_autotune(gbfmm_handle* h, const float* coords, const float* box, int reps, float* best_ms);
+/* Where the near field starts in the step's graph: after the tree (0, the
+ * default), after the P2M (1) or after the upper tree (2).  The near field runs
+ * on a low-priority stream beside the far-field chain either way; starting it
+ * later lets the far-field kernels with large shared memory take SMs before its
+ * CTAs fill them.  Results do not depend on it; gbfmm_autotune searches it last. */
+int gbfmm_set_near_start(gbfmm_handle* h, int after);
+int gbfmm_get_near_start(gbfmm_handle* h, int* after);
 int gbfmm_get_tuning(gbfmm_handle* h, int* p2p_variant, int* m2l_split, int* m2l_stages);
 int gbfmm_set_tuning(gbfmm_handle* h, int p2p_variant, int m2l_split, int m2l_stages);
 

@@ -69,3 +69,20 @@ def test_deterministic_handle_keeps_whole_tiles(pkg, systems):
     assert np.array_equal(s.forces(), f2)
     assert rel_rms(f2, f1) < 1e-5
     s.close()
+
+
+def test_near_field_start_leaves_results_unchanged(pkg, systems):
+    """The near field may start after the tree, the P2M or the upper tree: only the
+    order of the graph's nodes changes, so a deterministic handle gives the same bits."""
+    xyz, q, L = _system(systems)
+    s = pkg.ZetaFmmSolver(len(q), q, order=5, max_depth=3, images=4, precision=1, flags=pkg.FLAG_DETERMINISTIC)
+    s.execute(xyz, L)
+    f0, p0 = s.forces(), s.potentials()
+    for after in (1, 2, 0):
+        s.set_near_start(after)
+        assert s.tuning()["near_after"] == after
+        s.execute(xyz, L)
+        assert np.array_equal(s.forces(), f0) and np.array_equal(s.potentials(), p0), after
+    with pytest.raises(pkg.FmmError):
+        s.set_near_start(3)
+    s.close()
