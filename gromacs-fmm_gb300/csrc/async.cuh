@@ -37,13 +37,14 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
 // Default poll limit of the bounded waits: 2^24 polls, well over a second.
 constexpr uint32_t WAIT_POLLS_DEFAULT = 1u << 24;
 
-// Bounded wait: gives up after 'limit' polls and ORs 'bit' into *err.
+// Bounded wait: gives up after 'limit' polls and ORs 'bit' into *err (when err
+// is set).
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int bit = 2,
                                           uint32_t limit = WAIT_POLLS_DEFAULT)
 {
     for (uint32_t i = 0; i < limit; i++)
         if (mbar_try_wait(bar, parity)) return true;
-    atomicOr(err, bit);
+    if (err) atomicOr(err, bit);
     return false;
 }
 

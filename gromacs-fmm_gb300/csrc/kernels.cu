@@ -619,6 +619,10 @@ void launch_l2p(int P, const int* offsets, int nleaf, const float4* atoms, const
 
 __device__ __forceinline__ int real_degree(int r) { return (int)sqrtf((float)r + 0.5f); }
 
+// Orders whose 8 L2L operators (32 (P+1)^4 bytes) the downward pass stages in
+// shared memory: up to 6 (76.8 KB).
+#define DOWN_STAGE(P) (32 * (P + 1) * (P + 1) * (P + 1) * (P + 1) <= 80 * 1024)
+
 // Downward pass in one launch.  CTA = one leaf-parent cell p (level D-1, D >= 2):
 // the locals of p's ancestors are rebuilt from level 1 down (L~_k = M2L part + L2L
 // of the parent, in the order of the one-level kernels: a few R^2 FMAs each, the
@@ -628,16 +632,36 @@ template <int P>
 __device__ __forceinline__ void down_body(const DownArgs& a, const int bid)
 {
     constexpr int R = (P + 1) * (P + 1);
+    // the 8 operators in shared memory (one bulk copy) where they fit: every
+    // L2L below reads them R times per row
+    constexpr bool STAGED = DOWN_STAGE(P);
+    extern __shared__ float4 dsm4[];
+    __shared__ uint64_t dbar;
     __shared__ float Lc[R], Ln[R];
     __shared__ float Lleaf[8][R + 1];
     const int D = a.depth;
     const uint32_t p = bid;
+    const float* At = a.l2l_t;
+    if constexpr (STAGED) {
+        float* sA = reinterpret_cast<float*>(dsm4);
+        if (threadIdx.x == 0) {
+            mbar_init(&dbar, 1);
+            mbar_init_fence();
+            mbar_expect_tx(&dbar, 32u * R * R);
+            bulk_g2s(sA, a.l2l_t, 32u * R * R, &dbar);
+        }
+        At = sA;
+    }
     const uint32_t a1 = p >> (3 * (D - 2));  // level-1 ancestor
     for (int r = threadIdx.x; r < R; r += blockDim.x) Lc[r] = a.L[1][(size_t)a1 * a.Rpad + r];
     __syncthreads();
+    if constexpr (STAGED) {
+        // on a give-up the kernel waits (bounded) for the copy before reading on
+        if (!mbar_wait(&dbar, 0, a.err, 1, a.wait_limit)) mbar_drain(&dbar, 0, a.wait_limit);
+    }
     for (int k = 2; k <= D - 1; k++) {
         const uint32_t anc = p >> (3 * (D - 1 - k));
-        const float* A0 = a.l2l_t + (size_t)(anc & 7) * R * R;
+        const float* A0 = At + (size_t)(anc & 7) * R * R;
         for (int r = threadIdx.x; r < R; r += blockDim.x) {
             const int j = real_degree(r);
             float acc = 0.f;
@@ -650,7 +674,7 @@ __device__ __forceinline__ void down_body(const DownArgs& a, const int bid)
     }
     for (int i = threadIdx.x; i < 8 * R; i += blockDim.x) {
         const int o = i / R, r = i - o * R;
-        const float* A0 = a.l2l_t + (size_t)o * R * R;
+        const float* A0 = At + (size_t)o * R * R;
         const int j = real_degree(r);
         float acc = 0.f;
         for (int c = j * j; c < R; c++) acc = fmaf(A0[(size_t)c * R + r], Lc[c], acc);
@@ -698,10 +722,28 @@ __device__ __forceinline__ void down_body(const DownArgs& a, const int bid)
 template <int P>
 __global__ void __launch_bounds__(256) k_down(const DownArgs a) { down_body<P>(a, blockIdx.x); }
 
+size_t down_smem_bytes(int P)
+{
+    const size_t R = (size_t)(P + 1) * (P + 1);
+    return DOWN_STAGE(P) ? 32 * R * R : 0;
+}
+
+template <int P>
+static void down_dispatch(const DownArgs& a, cudaStream_t s)
+{
+    const size_t shm = down_smem_bytes(P);
+    static bool attr = false;
+    if (!attr && shm > 0) {
+        cudaFuncSetAttribute(k_down<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+        attr = true;
+    }
+    k_down<P><<<a.nparent, 256, shm, s>>>(a);
+}
+
 void launch_down(int P, const DownArgs& a, cudaStream_t s)
 {
     COUNT_LAUNCH();
-    GBFMM_ORDER_SWITCH(P, (k_down<PP><<<a.nparent, 256, 0, s>>>(a)));
+    GBFMM_ORDER_SWITCH(P, down_dispatch<PP>(a, s));
 }
 
 
@@ -1994,6 +2036,18 @@ static void launch_p2m_batch_t(const P2MArgs* args, const int* first, int nsys, 
 }
 
 template <int P>
+static void launch_down_batch_t(const DownArgs* args, const int* first, int nsys, int nblocks, cudaStream_t s)
+{
+    const size_t shm = down_smem_bytes(P);
+    static bool attr = false;
+    if (!attr && shm > 0) {
+        cudaFuncSetAttribute(k_down_batch<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+        attr = true;
+    }
+    k_down_batch<P><<<nblocks, 256, shm, s>>>(args, first, nsys);
+}
+
+template <int P>
 static void launch_p2m_m2m_batch_t(const P2MArgs* args, const int* first, int nsys, int nblocks, size_t smem,
                                    cudaStream_t s)
 {
@@ -2030,7 +2084,7 @@ void launch_batch(BatchKernel k, int P, const void* args, const int* first, int 
             GBFMM_ORDER_SWITCH(P, (k_l2p_batch<PP, 4><<<nblocks, 128, 0, s>>>((const L2PArgs*)args, first, nsys)));
             break;
         case BatchKernel::DOWN:
-            GBFMM_ORDER_SWITCH(P, (k_down_batch<PP><<<nblocks, 256, 0, s>>>((const DownArgs*)args, first, nsys)));
+            GBFMM_ORDER_SWITCH(P, launch_down_batch_t<PP>((const DownArgs*)args, first, nsys, nblocks, s));
             break;
         case BatchKernel::M2M:
             k_m2m_batch<<<nblocks, dim3(32, 8), smem, s>>>((const M2MArgs*)args, first, nsys);

@@ -201,8 +201,8 @@ struct P2PArgs {
     int nst;
     float4* field;            // sorted near field (phi, grad), scaled units
     const int* leaf_edge;     // per leaf: a body on or near its faces or outside it (from the leaf sort)
-    int* err = nullptr;       // bit 2: a bounded wait on the staging copies gave up
-    uint32_t wait_limit = 0;  // polls of that wait
+    int* err = nullptr;              // bit 2: a bounded wait on the staging copies gave up
+    uint32_t wait_limit = 1u << 24;  // polls of that wait
 };
 int p2p_variants();
 // Near fields of many systems in one persistent launch (per_sm CTAs per SM).
@@ -228,8 +228,13 @@ struct DownArgs {
     const float* l2l_t;       // 8 transposed R x R scaled L2L operators
     float4* field;            // sorted far field (phi, grad), scaled units
     int depth, Rpad;
+    int* err = nullptr;              // bit 1: the bounded wait on the staged operators gave up
+    uint32_t wait_limit = 1u << 24;  // polls of that wait
 };
 void launch_down(int P, const DownArgs& a, cudaStream_t s);
+// Dynamic shared memory of the downward pass of order P: the 8 L2L operators,
+// staged by one bulk copy where they fit (orders up to 6), else 0 (read from L2).
+size_t down_smem_bytes(int P);
 
 // One level of M2M (nparent parents from their 8 children each); At = 8
 // transposed R x R scaled operators.

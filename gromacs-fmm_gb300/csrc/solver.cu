@@ -780,6 +780,8 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
         da.field = h->d_far;
         da.depth = D;
         da.Rpad = h->Rpad;
+        da.err = h->d_flags + 2;
+        da.wait_limit = WAIT_POLLS_DEFAULT;
         launch_down(h->P, da, s);
         mark(h, 6);
     } else {
@@ -1139,7 +1141,7 @@ static int fetch(gbfmm_handle* h)
         CK(cudaMemsetAsync(h->d_counts, 0, sizeof(int) * (h->nleaf + 1 + 4), h->stream));
         h->have_result = false;
         return fail(GBFMM_ERR_TIMEOUT, h->h_flags[1]   ? "a bounded device wait in the tensor-core M2L gave up"
-                                       : h->h_flags[2] ? "a bounded device wait in the upper-tree kernel gave up"
+                                       : h->h_flags[2] ? "a bounded device wait in the upper-tree or downward-pass kernel gave up"
                                                        : "a bounded device wait in the near-field kernel gave up");
     }
     if (h->h_flags[0]) {
@@ -1647,6 +1649,8 @@ extern "C" int gbfmm_get_virial(gbfmm_handle* h, double* vir)
             da.field = field;
             da.depth = D;
             da.Rpad = h->Rpad;
+            da.err = h->d_flags + 2;
+            da.wait_limit = WAIT_POLLS_DEFAULT;
             launch_down(h->P, da, s);
         } else {
             launch_l2p(h->P, h->d_off, h->nleaf, h->d_atoms, lam[x][1], h->Rpad, field, s);
@@ -2053,6 +2057,8 @@ static void describe_step(gbfmm_handle* h, StepDesc& d)
         da.field = h->d_far;
         da.depth = D;
         da.Rpad = h->Rpad;
+        da.err = h->d_flags + 2;
+        da.wait_limit = WAIT_POLLS_DEFAULT;
     } else {
         d.l2p = L2PArgs{h->d_off, h->nleaf, h->d_atoms, h->Llev[D], h->Rpad, h->d_far};
     }
@@ -2260,7 +2266,7 @@ static int batch_capture(gbfmm_batch* b)
                         lb.push_back((x.h->nleaf + 3) / 4);
                     }
                 }
-            down[l].add(BatchKernel::DOWN, P, 0, da, db);
+            down[l].add(BatchKernel::DOWN, P, down_smem_bytes(P), da, db);
             down[l].add(BatchKernel::L2P, P, 0, la, lb);
         }
     }
@@ -2621,7 +2627,7 @@ static int batch_check(gbfmm_batch* b)
             if (rc == GBFMM_OK)
                 rc = fail(fl[1] || fl[2] || fl[3] ? GBFMM_ERR_TIMEOUT : GBFMM_ERR_COORD,
                           fl[1]   ? "a bounded device wait in a system's tensor-core M2L gave up"
-                          : fl[2] ? "a bounded device wait in a system's upper-tree kernel gave up"
+                          : fl[2] ? "a bounded device wait in a system's upper-tree or downward-pass kernel gave up"
                           : fl[3] ? "a bounded device wait in a system's near-field kernel gave up"
                                   : "a system of the batch has a non-finite coordinate");
         }
