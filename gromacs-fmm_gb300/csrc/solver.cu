@@ -1282,10 +1282,11 @@ extern "C" int gbfmm_autotune(gbfmm_handle* h, const float* coords, const float*
             if (t < bt) { bt = t; bs = sv; }
         }
         const TcPlan& pl = h->tab->tc;
-        const int cand[3] = {2, tc_pick_stages(pl.k_atoms, pl.img_bytes, h->tca->nprod),
+        // one stage: the most CTAs (and entries in flight) per SM
+        const int cand[4] = {1, 2, tc_pick_stages(pl.k_atoms, pl.img_bytes, h->tca->nprod),
                              tc_max_stages(pl.k_atoms, pl.img_bytes, h->tca->nprod)};
-        for (int c = 0; c < 3 && !err; c++) {
-            const int ns = std::min(cand[c], cand[2]);
+        for (int c = 0; c < 4 && !err; c++) {
+            const int ns = std::min(cand[c], cand[3]);
             if (ns == bn || ns < 1) continue;
             const float t = measure(bp, bs, ns);
             if (t < bt) { bt = t; bn = ns; }
