@@ -58,13 +58,6 @@ __device__ __forceinline__ bool mbar_drain(uint64_t* bar, uint32_t parity, uint3
     return false;
 }
 
-// 4-byte global -> shared copy without a register round trip; completes at
-// cp.async.wait_group (after cp.async.commit_group).
-__device__ __forceinline__ void cp_async4(void* dst, const void* src)
-{
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
-}
-
 // Bulk copy of 'bytes' (a multiple of 16; both addresses 16-byte aligned),
 // completing on bar (tx bytes).
 __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
