@@ -637,7 +637,8 @@ __device__ __forceinline__ void down_body(const DownArgs& a, const int bid)
     constexpr bool STAGED = DOWN_STAGE(P);
     extern __shared__ float4 dsm4[];
     __shared__ uint64_t dbar;
-    __shared__ float Lc[R], Ln[R];
+    __shared__ float Lanc[MAX_DEPTH][R];  // the ancestors' rows (levels 1..D-1)
+    __shared__ float Lbuf[2][R];
     __shared__ float Lleaf[8][R + 1];
     const int D = a.depth;
     const uint32_t p = bid;
@@ -652,33 +653,54 @@ __device__ __forceinline__ void down_body(const DownArgs& a, const int bid)
         }
         At = sA;
     }
-    const uint32_t a1 = p >> (3 * (D - 2));  // level-1 ancestor
-    for (int r = threadIdx.x; r < R; r += blockDim.x) Lc[r] = a.L[1][(size_t)a1 * a.Rpad + r];
+    // every local row the CTA reads, in one pass: the ancestors' (level k's
+    // ancestor of parent p is p >> 3 (D-1-k)) and the 8 leaves'
+    for (int i = threadIdx.x; i < (D + 7) * R; i += blockDim.x) {
+        const int k = 1 + i / R, r = i % R;
+        if (k < D) {
+            const uint32_t anc = p >> (3 * (D - 1 - k));
+            Lanc[k - 1][r] = a.L[k][(size_t)anc * a.Rpad + r];
+        } else {
+            const int o = k - D;
+            Lleaf[o][r] = a.L[D][(size_t)((p << 3) | (uint32_t)o) * a.Rpad + r];
+        }
+    }
     __syncthreads();
     if constexpr (STAGED) {
         // on a give-up the kernel waits (bounded) for the copy before reading on
         if (!mbar_wait(&dbar, 0, a.err, 1, a.wait_limit)) mbar_drain(&dbar, 0, a.wait_limit);
     }
+    // L2L down the ancestors: each output row's dot product split over 4
+    // consecutive lanes (columns c = j^2 + q, + 4, ...), added by a fixed butterfly
+    const float* Lc = Lanc[0];
     for (int k = 2; k <= D - 1; k++) {
         const uint32_t anc = p >> (3 * (D - 1 - k));
         const float* A0 = At + (size_t)(anc & 7) * R * R;
-        for (int r = threadIdx.x; r < R; r += blockDim.x) {
-            const int j = real_degree(r);
+        float* Ln = Lbuf[k & 1];
+        for (int base = 0; base < 4 * R; base += blockDim.x) {
+            const int w = base + threadIdx.x;
+            const bool act = w < 4 * R;
+            const int r = act ? w >> 2 : 0, q = w & 3;
             float acc = 0.f;
-            for (int c = j * j; c < R; c++) acc = fmaf(A0[(size_t)c * R + r], Lc[c], acc);
-            Ln[r] = a.L[k][(size_t)anc * a.Rpad + r] + acc;
+            if (act) {
+                const int j = real_degree(r);
+                for (int c = j * j + q; c < R; c += 4) acc = fmaf(A0[(size_t)c * R + r], Lc[c], acc);
+            }
+            acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+            acc += __shfl_xor_sync(0xffffffffu, acc, 2);
+            if (act && q == 0) Ln[r] = Lanc[k - 1][r] + acc;
         }
         __syncthreads();
-        for (int r = threadIdx.x; r < R; r += blockDim.x) Lc[r] = Ln[r];
-        __syncthreads();
+        Lc = Ln;
     }
+    // the 8 leaves: their M2L part (preloaded) plus the L2L of the parent
     for (int i = threadIdx.x; i < 8 * R; i += blockDim.x) {
         const int o = i / R, r = i - o * R;
         const float* A0 = At + (size_t)o * R * R;
         const int j = real_degree(r);
         float acc = 0.f;
         for (int c = j * j; c < R; c++) acc = fmaf(A0[(size_t)c * R + r], Lc[c], acc);
-        Lleaf[o][r] = a.L[D][(size_t)((p << 3) | (uint32_t)o) * a.Rpad + r] + acc;
+        Lleaf[o][r] += acc;
     }
     __syncthreads();
     const int lane = threadIdx.x & 31, o = threadIdx.x >> 5;
