@@ -366,15 +366,38 @@ __device__ __forceinline__ void m2l_tc_body(const TcArgs& a, const int bid)
         const uint32_t q = wv ? morton_encode(i0 + bi, j0 + bj, l0 + bl) : 0u;
         const size_t trow = (size_t)((q << 3) | (uint32_t)s) * a.Rpad;
         for (int c = 0; c < a.nchunk; c++) {
+            // rows r0 + b .. in groups of 4: one vector add (or atomic vector add) where
+            // the group is whole and 16-byte aligned (Rpad is a multiple of 4)
+            const bool al = (a.chunk_row0[c] & 3) == 0;
             for (int b = 0; b < a.chunk_n[c]; b += 16) {
                 float v[16];
                 tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(a.chunk_col[c] + b), v);
+                if (!wv) continue;
 #pragma unroll
-                for (int e = 0; e < 16; e++) {
+                for (int e = 0; e < 16; e += 4) {
                     const int r = a.chunk_row0[c] + b + e;
-                    if (wv && b + e < a.chunk_rows[c]) {
-                        if (a.atomic) atomicAdd(&dst[trow + r], v[e]);
-                        else dst[trow + r] += v[e];
+                    float* d = &dst[trow + r];
+                    if (al && b + e + 3 < a.chunk_rows[c]) {
+                        if (a.atomic) {
+                            asm volatile("red.relaxed.gpu.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(d), "f"(v[e]),
+                                         "f"(v[e + 1]), "f"(v[e + 2]), "f"(v[e + 3])
+                                         : "memory");
+                        } else {
+                            float4 t = *reinterpret_cast<float4*>(d);
+                            t.x += v[e];
+                            t.y += v[e + 1];
+                            t.z += v[e + 2];
+                            t.w += v[e + 3];
+                            *reinterpret_cast<float4*>(d) = t;
+                        }
+                    } else {
+#pragma unroll
+                        for (int f = 0; f < 4; f++) {
+                            if (b + e + f < a.chunk_rows[c]) {
+                                if (a.atomic) atomicAdd(d + f, v[e + f]);
+                                else d[f] += v[e + f];
+                            }
+                        }
                     }
                 }
             }
