@@ -236,6 +236,12 @@ __device__ __forceinline__ void m2l_tc_body(const TcArgs& a, const int bid)
     const int rows = bx * by * bz;
     const int ox = (s >> 2) & 1, oy = (s >> 1) & 1, oz = s & 1;
 
+    // the task's stencil entries, read once (the producer must not wait on
+    // global loads between its copies); their loads overlap the vacuum test's
+    __shared__ CEntry ent[TC_MAXENT];
+    const int ne = min(task.e_end - task.e_begin, TC_MAXENT);
+    for (int i = tid; i < ne; i += TC_THREADS) ent[i] = a.entries[task.e_begin + i];
+
     // a tile whose targets hold no bodies (vacuum) needs no locals: their only
     // readers are their own descendants' L2P
     if (a.leaf_off) {
@@ -249,11 +255,6 @@ __device__ __forceinline__ void m2l_tc_body(const TcArgs& a, const int bid)
         if (!__syncthreads_or(occupied)) return;
     }
 
-    // the task's stencil entries, read once (the producer must not wait on
-    // global loads between its copies)
-    __shared__ CEntry ent[TC_MAXENT];
-    const int ne = min(task.e_end - task.e_begin, TC_MAXENT);
-    for (int i = tid; i < ne; i += TC_THREADS) ent[i] = a.entries[task.e_begin + i];
     if (tid == 0) {
         for (int q = 0; q < NS; q++) {
             mbar_init(&bar_full[q], 1);
