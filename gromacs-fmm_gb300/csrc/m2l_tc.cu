@@ -327,19 +327,23 @@ __device__ __forceinline__ void m2l_tc_body(const TcArgs& a, const int bid)
             tc_fence_after();
             const uint32_t a_hi = smem_u32(sm + st * stage_bytes), a_lo = a_hi + (uint32_t)a_bytes,
                            b_hi = a_hi + (uint32_t)((split ? 2 : 1) * a_bytes), b_lo = b_hi + (uint32_t)b_bytes;
+            // descriptors of the stage's operands; an offset of o bytes (a multiple
+            // of 16, within the 256 KB shared window) adds o >> 4 to the start field
+            const uint64_t da_hi = sw128_desc(a_hi), da_lo = sw128_desc(a_lo), db_hi = sw128_desc(b_hi),
+                           db_lo = sw128_desc(b_lo);
             for (int c = 0; c < a.nchunk; c++) {
                 const int N = a.chunk_n[c], K = a.chunk_k[c];
                 const uint32_t idesc = idesc_bf16(N);
-                const uint32_t boff = (uint32_t)a.chunk_img[c];
+                const uint32_t dcol = tmem + (uint32_t)a.chunk_col[c];
+                const uint64_t boff = (uint64_t)(a.chunk_img[c] >> 4);
                 for (int p = 0; p < a.nprod; p++) {
-                    const uint32_t abase = p == 2 ? a_lo : a_hi;
-                    const uint32_t bbase = (p == 1 ? b_lo : b_hi) + boff;
+                    const uint64_t da = p == 2 ? da_lo : da_hi;
+                    const uint64_t db = (p == 1 ? db_lo : db_hi) + boff;
                     for (int kk = 0; kk < K / 16; kk++) {
-                        const uint32_t ao = (uint32_t)((kk >> 2) * (128 * 128) + (kk & 3) * 32);
-                        const uint32_t bo = (uint32_t)((kk >> 2) * (N * 128) + (kk & 3) * 32);
+                        const uint64_t ao = (uint64_t)((kk >> 2) * (128 * 128 / 16) + (kk & 3) * 2);
+                        const uint64_t bo = (uint64_t)((kk >> 2) * (N * 128 / 16) + (kk & 3) * 2);
                         const uint32_t acc = (i > 0 || p > 0 || kk > 0) ? 1u : 0u;
-                        mma_bf16(tmem + (uint32_t)a.chunk_col[c], sw128_desc(abase + ao), sw128_desc(bbase + bo),
-                                 idesc, acc);
+                        mma_bf16(dcol, da + ao, db + bo, idesc, acc);
                     }
                 }
             }
