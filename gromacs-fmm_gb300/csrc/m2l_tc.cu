@@ -220,7 +220,9 @@ __device__ __forceinline__ void m2l_tc_body(const TcArgs& a, const int bid)
     const bool split = a.nprod > 1;                    // lo halves are needed only for 3 products
     const int a_bytes = 128 * a.k_atoms * 128;        // one operand (hi or lo) of A
     const int b_bytes = a.img_bytes;                   // one operand of B
-    const int stage_bytes = (split ? 2 : 1) * (a_bytes + b_bytes);
+    const int slot_bytes = (split ? 2 : 1) * (a_bytes + b_bytes);  // the operands of one entry
+    const int G = a.group;                             // entries per pipeline stage
+    const int stage_bytes = G * slot_bytes;
     const int NS = a.nstage;
     uint64_t* bar_full = reinterpret_cast<uint64_t*>(sm + NS * stage_bytes);
     uint64_t* bar_empty = bar_full + TC_MAXSTAGE;
@@ -279,71 +281,79 @@ __device__ __forceinline__ void m2l_tc_body(const TcArgs& a, const int bid)
     // On a bounded wait that gives up, the waiting role records the error, stops
     // issuing work and drains what it issued (again bounded); the CTA then skips
     // the read-back and the adds, and releases TMEM only after the drain.
+    const int ng = (ne + G - 1) / G;  // stage uses: groups of G entries
     if (warp == 0 && lane == 0) {
         // ---------------------------------------------------------------- producer
-        const uint32_t tx_bytes = (split ? 2u : 1u) * (uint32_t)(a.k_atoms * rows * 128 + b_bytes);
+        const uint32_t tx_entry = (split ? 2u : 1u) * (uint32_t)(a.k_atoms * rows * 128 + b_bytes);
         int issued = 0;
-        for (int i = 0; i < ne; i++) {
-            const int st = i % NS, u = i / NS;
-            if (i >= NS && !mbar_wait(&bar_empty[st], (u - 1) & 1, a.err, 2, lim)) {
+        for (int g = 0; g < ng; g++) {
+            const int st = g % NS, u = g / NS;
+            if (g >= NS && !mbar_wait(&bar_empty[st], (u - 1) & 1, a.err, 2, lim)) {
                 ok = false;
                 break;
             }
-            const CEntry en = ent[i];
-            uint8_t* A_hi = sm + st * stage_bytes;
-            uint8_t* A_lo = A_hi + a_bytes;
-            uint8_t* B = A_hi + (split ? 2 : 1) * a_bytes;
-            mbar_expect_tx(&bar_full[st], tx_bytes);
-            if (en.mode == 0) {
-                // same-level source: parity grid of level k
-                const int fx = (ox + en.dx) >> 1, fy = (oy + en.dy) >> 1, fz = (oz + en.dz) >> 1;
-                const int par = ((ox + en.dx) & 1) | (((oy + en.dy) & 1) << 1) | (((oz + en.dz) & 1) << 2);
-                const int cx = i0 + fx + TC_HALO, cy = j0 + fy + TC_HALO, cz = l0 + fz + TC_HALO;
-                for (int at = 0; at < a.k_atoms; at++) {
-                    tma_load_5d(A_hi + at * 128 * 128, &a.p_hi[k], 64 * at, cx, cy, cz, par, &bar_full[st]);
-                    if (split) tma_load_5d(A_lo + at * 128 * 128, &a.p_lo[k], 64 * at, cx, cy, cz, par, &bar_full[st]);
+            const int e0 = g * G, e1 = min(ne, e0 + G);
+            mbar_expect_tx(&bar_full[st], (uint32_t)(e1 - e0) * tx_entry);
+            for (int i = e0; i < e1; i++) {
+                const CEntry en = ent[i];
+                uint8_t* A_hi = sm + st * stage_bytes + (i - e0) * slot_bytes;
+                uint8_t* A_lo = A_hi + a_bytes;
+                uint8_t* B = A_hi + (split ? 2 : 1) * a_bytes;
+                if (en.mode == 0) {
+                    // same-level source: parity grid of level k
+                    const int fx = (ox + en.dx) >> 1, fy = (oy + en.dy) >> 1, fz = (oz + en.dz) >> 1;
+                    const int par = ((ox + en.dx) & 1) | (((oy + en.dy) & 1) << 1) | (((oz + en.dz) & 1) << 2);
+                    const int cx = i0 + fx + TC_HALO, cy = j0 + fy + TC_HALO, cz = l0 + fz + TC_HALO;
+                    for (int at = 0; at < a.k_atoms; at++) {
+                        tma_load_5d(A_hi + at * 128 * 128, &a.p_hi[k], 64 * at, cx, cy, cz, par, &bar_full[st]);
+                        if (split) tma_load_5d(A_lo + at * 128 * 128, &a.p_lo[k], 64 * at, cx, cy, cz, par, &bar_full[st]);
+                    }
+                } else {
+                    // parent-level source: natural grid of level k-1
+                    const int cx = i0 + en.dx + TC_HALO, cy = j0 + en.dy + TC_HALO, cz = l0 + en.dz + TC_HALO;
+                    for (int at = 0; at < a.k_atoms; at++) {
+                        tma_load_4d(A_hi + at * 128 * 128, &a.n_hi[k - 1], 64 * at, cx, cy, cz, &bar_full[st]);
+                        if (split) tma_load_4d(A_lo + at * 128 * 128, &a.n_lo[k - 1], 64 * at, cx, cy, cz, &bar_full[st]);
+                    }
                 }
-            } else {
-                // parent-level source: natural grid of level k-1
-                const int cx = i0 + en.dx + TC_HALO, cy = j0 + en.dy + TC_HALO, cz = l0 + en.dz + TC_HALO;
-                for (int at = 0; at < a.k_atoms; at++) {
-                    tma_load_4d(A_hi + at * 128 * 128, &a.n_hi[k - 1], 64 * at, cx, cy, cz, &bar_full[st]);
-                    if (split) tma_load_4d(A_lo + at * 128 * 128, &a.n_lo[k - 1], 64 * at, cx, cy, cz, &bar_full[st]);
-                }
+                bulk_g2s(B, a.bimg + (size_t)en.op * 2 * b_bytes, (split ? 2u : 1u) * b_bytes, &bar_full[st]);
             }
-            bulk_g2s(B, a.bimg + (size_t)en.op * 2 * b_bytes, (split ? 2u : 1u) * b_bytes, &bar_full[st]);
-            issued = i + 1;
+            issued = g + 1;
         }
         if (!ok)  // the copies this thread issued: the last phase of every stage
             for (int st = 0; st < min(NS, issued); st++) mbar_drain(&bar_full[st], ((issued - 1 - st) / NS) & 1, lim);
     } else if (warp == 1 && lane == 0) {
         // ---------------------------------------------------------------- MMA issuer
-        for (int i = 0; i < ne; i++) {
-            const int st = i % NS, u = i / NS;
+        for (int g = 0; g < ng; g++) {
+            const int st = g % NS, u = g / NS;
             if (!mbar_wait(&bar_full[st], u & 1, a.err, 2, lim)) {
                 ok = false;
                 break;
             }
             tc_fence_after();
-            const uint32_t a_hi = smem_u32(sm + st * stage_bytes), a_lo = a_hi + (uint32_t)a_bytes,
-                           b_hi = a_hi + (uint32_t)((split ? 2 : 1) * a_bytes), b_lo = b_hi + (uint32_t)b_bytes;
-            // descriptors of the stage's operands; an offset of o bytes (a multiple
-            // of 16, within the 256 KB shared window) adds o >> 4 to the start field
-            const uint64_t da_hi = sw128_desc(a_hi), da_lo = sw128_desc(a_lo), db_hi = sw128_desc(b_hi),
-                           db_lo = sw128_desc(b_lo);
-            for (int c = 0; c < a.nchunk; c++) {
-                const int N = a.chunk_n[c], K = a.chunk_k[c];
-                const uint32_t idesc = idesc_bf16(N);
-                const uint32_t dcol = tmem + (uint32_t)a.chunk_col[c];
-                const uint64_t boff = (uint64_t)(a.chunk_img[c] >> 4);
-                for (int p = 0; p < a.nprod; p++) {
-                    const uint64_t da = p == 2 ? da_lo : da_hi;
-                    const uint64_t db = (p == 1 ? db_lo : db_hi) + boff;
-                    for (int kk = 0; kk < K / 16; kk++) {
-                        const uint64_t ao = (uint64_t)((kk >> 2) * (128 * 128 / 16) + (kk & 3) * 2);
-                        const uint64_t bo = (uint64_t)((kk >> 2) * (N * 128 / 16) + (kk & 3) * 2);
-                        const uint32_t acc = (i > 0 || p > 0 || kk > 0) ? 1u : 0u;
-                        mma_bf16(dcol, da + ao, db + bo, idesc, acc);
+            const int e0 = g * G, e1 = min(ne, e0 + G);
+            for (int i = e0; i < e1; i++) {
+                const uint32_t a_hi = smem_u32(sm + st * stage_bytes + (i - e0) * slot_bytes),
+                               a_lo = a_hi + (uint32_t)a_bytes, b_hi = a_hi + (uint32_t)((split ? 2 : 1) * a_bytes),
+                               b_lo = b_hi + (uint32_t)b_bytes;
+                // descriptors of the entry's operands; an offset of o bytes (a multiple
+                // of 16, within the 256 KB shared window) adds o >> 4 to the start field
+                const uint64_t da_hi = sw128_desc(a_hi), da_lo = sw128_desc(a_lo), db_hi = sw128_desc(b_hi),
+                               db_lo = sw128_desc(b_lo);
+                for (int c = 0; c < a.nchunk; c++) {
+                    const int N = a.chunk_n[c], K = a.chunk_k[c];
+                    const uint32_t idesc = idesc_bf16(N);
+                    const uint32_t dcol = tmem + (uint32_t)a.chunk_col[c];
+                    const uint64_t boff = (uint64_t)(a.chunk_img[c] >> 4);
+                    for (int p = 0; p < a.nprod; p++) {
+                        const uint64_t da = p == 2 ? da_lo : da_hi;
+                        const uint64_t db = (p == 1 ? db_lo : db_hi) + boff;
+                        for (int kk = 0; kk < K / 16; kk++) {
+                            const uint64_t ao = (uint64_t)((kk >> 2) * (128 * 128 / 16) + (kk & 3) * 2);
+                            const uint64_t bo = (uint64_t)((kk >> 2) * (N * 128 / 16) + (kk & 3) * 2);
+                            const uint32_t acc = (i > 0 || p > 0 || kk > 0) ? 1u : 0u;
+                            mma_bf16(dcol, da + ao, db + bo, idesc, acc);
+                        }
                     }
                 }
             }
@@ -519,7 +529,7 @@ size_t tc_stage_bytes(int k_atoms, int img_bytes, int nprod)
 
 size_t tc_smem_bytes(const TcArgs& a)
 {
-    return 1024 + (size_t)a.nstage * tc_stage_bytes(a.k_atoms, a.img_bytes, a.nprod) +
+    return 1024 + (size_t)a.nstage * a.group * tc_stage_bytes(a.k_atoms, a.img_bytes, a.nprod) +
            (2 * TC_MAXSTAGE + 1) * sizeof(uint64_t) + 16;
 }
 

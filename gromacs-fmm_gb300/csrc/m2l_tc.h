@@ -24,6 +24,9 @@ constexpr int TC_THREADS = 128;  // producer lane, MMA lane, 4 epilogue warps
 constexpr int TC_HALO = 2;       // halo of the source grids (cells of the grid)
 constexpr int TC_MAXLEV = 8;
 constexpr int TC_MAXENT = 256;
+#ifndef TC_GROUP_DEFAULT
+#define TC_GROUP_DEFAULT 1
+#endif
 constexpr int TC_NSPLIT = 4;     // entry splits 1, 2, 4, 8 of a tile's stencil (autotuned)   // stencil entries of one task (the stencils have at most 182)
 
 // Degree chunks of the M2L operator: chunk c covers output rows [row0, row0+rows)
@@ -101,6 +104,7 @@ struct alignas(64) TcArgs {
     int k_atoms, img_bytes, tmem_cols, nchunk;
     int nprod;                   // 3: hi*hi + hi*lo + lo*hi, 1: hi*hi
     int nstage;                  // pipeline stages, 2..TC_MAXSTAGE (tc_pick_stages)
+    int group;                   // stencil entries per stage (one expect_tx, one wait, one commit)
     int atomic;                  // 1: atomicAdd into L (split entry ranges), 0: plain add
     int shift[3];                // stored cells per axis of level l: grid_n(l, shift[d])
     const int* leaf_off;         // leaf offsets of the step (tiles of empty targets are skipped), or NULL
@@ -113,7 +117,7 @@ struct alignas(64) TcArgs {
 // Returns false when the driver's encoder is unavailable or refuses a map.
 bool tc_encode_maps(TcArgs& a, int D, const TcGrids& g, void* hi, void* lo);
 size_t tc_smem_bytes(const TcArgs& a);
-size_t tc_stage_bytes(int k_atoms, int img_bytes, int nprod);
+size_t tc_stage_bytes(int k_atoms, int img_bytes, int nprod);  // the operands of one entry
 int tc_pick_stages(int k_atoms, int img_bytes, int nprod);
 int tc_max_stages(int k_atoms, int img_bytes, int nprod);  // most that fit one CTA's shared memory
 void launch_m2l_tc(const TcArgs& a, int ntasks, cudaStream_t s);

@@ -523,7 +523,8 @@ static int make_tc_args(gbfmm_handle* h)
     a->tmem_cols = pl.tmem_cols;
     a->nchunk = pl.nchunk;
     a->nprod = h->prm.precision == GBFMM_PREC_BF16X1 ? 1 : 3;
-    a->nstage = tc_pick_stages(pl.k_atoms, pl.img_bytes, a->nprod);
+    a->group = TC_GROUP_DEFAULT;
+    a->nstage = std::max(1, tc_pick_stages(pl.k_atoms, pl.img_bytes, a->nprod) / a->group);
     h->tc_nstage = a->nstage;
     if (tc_smem_bytes(*a) > 227 * 1024 - TC_MAXENT * sizeof(CEntry))
         return fail(GBFMM_ERR_UNSUPPORTED, "tensor-core M2L of order %d: one pipeline stage exceeds shared memory",
@@ -1202,7 +1203,7 @@ extern "C" int gbfmm_set_tuning(gbfmm_handle* h, int p2p_variant, int m2l_split,
     if (h->tc) {
         if (h->tc_ntask_v[v] == 0) return fail(GBFMM_ERR_ARG, "m2l split %d unavailable (deterministic handle)", m2l_split);
         const TcPlan& pl = h->tab->tc;
-        const int mx = tc_max_stages(pl.k_atoms, pl.img_bytes, h->tca->nprod);
+        const int mx = std::max(1, tc_max_stages(pl.k_atoms, pl.img_bytes, h->tca->nprod) / h->tca->group);
         if (m2l_stages < 1 || m2l_stages > mx) return fail(GBFMM_ERR_ARG, "m2l stages %d outside [1,%d]", m2l_stages, mx);
         ns = m2l_stages;
     }
@@ -1283,8 +1284,9 @@ extern "C" int gbfmm_autotune(gbfmm_handle* h, const float* coords, const float*
         }
         const TcPlan& pl = h->tab->tc;
         // one stage: the most CTAs (and entries in flight) per SM
-        const int cand[4] = {1, 2, tc_pick_stages(pl.k_atoms, pl.img_bytes, h->tca->nprod),
-                             tc_max_stages(pl.k_atoms, pl.img_bytes, h->tca->nprod)};
+        const int gs = h->tca->group;
+        const int cand[4] = {1, 2, std::max(1, tc_pick_stages(pl.k_atoms, pl.img_bytes, h->tca->nprod) / gs),
+                             std::max(1, tc_max_stages(pl.k_atoms, pl.img_bytes, h->tca->nprod) / gs)};
         for (int c = 0; c < 4 && !err; c++) {
             const int ns = std::min(cand[c], cand[3]);
             if (ns == bn || ns < 1) continue;
@@ -2438,7 +2440,8 @@ static int apply_batch_tuning(gbfmm_batch* b, int shape, int per_sm, int split_v
         if (split_v >= 0) h->tc_split_v = split_v;
         if (nstage > 0) {
             const TcPlan& pl = h->tab->tc;
-            h->tc_nstage = std::max(1, std::min(nstage, tc_max_stages(pl.k_atoms, pl.img_bytes, h->tca->nprod)));
+            h->tc_nstage = std::max(1, std::min(nstage, tc_max_stages(pl.k_atoms, pl.img_bytes, h->tca->nprod) /
+                                                             h->tca->group));
         }
     }
     if (b->gexec) {
