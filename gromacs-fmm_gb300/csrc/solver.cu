@@ -1177,6 +1177,28 @@ extern "C" int gbfmm_execute(gbfmm_handle* h, const float* coords, const float* 
     return rc;
 }
 
+// A device buffer larger than L2 (129 MB on GB300) written before each timed
+// step of the autotuners; none when it cannot be allocated.
+struct L2Flush {
+    void* buf = nullptr;
+    size_t bytes = 256u << 20;
+    L2Flush()
+    {
+        if (cudaMalloc(&buf, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            buf = nullptr;
+        }
+    }
+    ~L2Flush()
+    {
+        if (buf) cudaFree(buf);
+    }
+    void run(cudaStream_t s) const
+    {
+        if (buf) cudaMemsetAsync(buf, 0, bytes, s);
+    }
+};
+
 // ---- autotuner: warp-step shape of P2P, entry split and pipeline depth of the
 // tensor-core M2L, chosen by timing whole steps (CUDA-graph replays) of the
 // caller's own configuration.
@@ -1252,21 +1274,33 @@ extern "C" int gbfmm_autotune(gbfmm_handle* h, const float* coords, const float*
     CK(cudaMemcpyAsync(h->d_coords, coords, sizeof(float) * 3 * h->n, cudaMemcpyHostToDevice, h->stream));
     const bool timing = h->timing;
     h->timing = false;
-    cudaEvent_t e0, e1;
-    CK(cudaEventCreate(&e0));
-    CK(cudaEventCreate(&e1));
+    // each timed step starts from a flushed L2 (a write larger than L2 before it),
+    // as steps do between which the application's other kernels run
+    L2Flush flush;
+    std::vector<cudaEvent_t> e0(reps), e1(reps);
+    for (int i = 0; i < reps; i++) {
+        CK(cudaEventCreate(&e0[i]));
+        CK(cudaEventCreate(&e1[i]));
+    }
     int err = GBFMM_OK;
     auto measure = [&](int pv, int sv, int ns) -> float {
         apply_tuning(h, pv, sv, ns);
         for (int i = 0; i < 2 && err == GBFMM_OK; i++) err = run_step(h);
         if (err) return 1e30f;
-        cudaEventRecord(e0, h->stream);
-        for (int i = 0; i < reps && err == GBFMM_OK; i++) err = run_step(h);
-        cudaEventRecord(e1, h->stream);
-        if (cudaEventSynchronize(e1) != cudaSuccess) err = GBFMM_ERR_CUDA;
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        return err ? 1e30f : ms / reps;
+        for (int i = 0; i < reps && err == GBFMM_OK; i++) {
+            flush.run(h->stream);
+            cudaEventRecord(e0[i], h->stream);
+            err = run_step(h);
+            cudaEventRecord(e1[i], h->stream);
+        }
+        if (cudaEventSynchronize(e1[reps - 1]) != cudaSuccess) err = GBFMM_ERR_CUDA;
+        float tot = 0.f;
+        for (int i = 0; i < reps && !err; i++) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0[i], e1[i]);
+            tot += ms;
+        }
+        return err ? 1e30f : tot / reps;
     };
     int bp = h->p2p_variant, bs = h->tc_split_v, bn = h->tc_nstage;
     float bt = measure(bp, bs, bn);
@@ -1305,8 +1339,10 @@ extern "C" int gbfmm_autotune(gbfmm_handle* h, const float* coords, const float*
         }
         h->near_after = ba;
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    for (int i = 0; i < reps; i++) {
+        cudaEventDestroy(e0[i]);
+        cudaEventDestroy(e1[i]);
+    }
     apply_tuning(h, bp, bs, bn);
     h->timing = timing;
     if (err) return err;
@@ -2509,23 +2545,32 @@ extern "C" int gbfmm_batch_autotune(gbfmm_batch* b, const void* d_coords, const 
 {
     if (!b || !box_edges || (b->natoms > 0 && (!d_coords || !d_charges))) return fail(GBFMM_ERR_ARG, "NULL argument");
     if (reps <= 0) reps = 3;
-    cudaEvent_t e0, e1;
-    CK(cudaEventCreate(&e0));
-    CK(cudaEventCreate(&e1));
+    L2Flush flush;  // each timed step starts from a flushed L2
+    std::vector<cudaEvent_t> e0(reps), e1(reps);
+    for (int i = 0; i < reps; i++) {
+        CK(cudaEventCreate(&e0[i]));
+        CK(cudaEventCreate(&e1[i]));
+    }
     int err = GBFMM_OK;
     auto measure = [&](int sh, int ps, int sv, int ns) -> float {
         if (apply_batch_tuning(b, sh, ps, sv, ns) != GBFMM_OK) return 1e30f;
         for (int i = 0; i < 2 && err == GBFMM_OK; i++)
             err = gbfmm_batch_execute_device(b, d_coords, d_charges, box_edges, b->master);
         if (err) return 1e30f;
-        cudaEventRecord(e0, b->master);
-        for (int i = 0; i < reps && err == GBFMM_OK; i++)
+        for (int i = 0; i < reps && err == GBFMM_OK; i++) {
+            flush.run(b->master);
+            cudaEventRecord(e0[i], b->master);
             err = gbfmm_batch_execute_device(b, d_coords, d_charges, box_edges, b->master);
-        cudaEventRecord(e1, b->master);
-        if (cudaEventSynchronize(e1) != cudaSuccess) err = GBFMM_ERR_CUDA;
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        return err ? 1e30f : ms / reps;
+            cudaEventRecord(e1[i], b->master);
+        }
+        if (cudaEventSynchronize(e1[reps - 1]) != cudaSuccess) err = GBFMM_ERR_CUDA;
+        float tot = 0.f;
+        for (int i = 0; i < reps && !err; i++) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0[i], e1[i]);
+            tot += ms;
+        }
+        return err ? 1e30f : tot / reps;
     };
     int bs = b->p2p_shape, bp = b->p2p_per_sm, bv = b->m2l_split_v, bn = b->m2l_stages;
     float bt = measure(bs, bp, bv, bn);
@@ -2586,8 +2631,10 @@ extern "C" int gbfmm_batch_autotune(gbfmm_batch* b, const void* d_coords, const 
             if (t < bt) { bt = t; bp = ps; }
         }
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    for (int i = 0; i < reps; i++) {
+        cudaEventDestroy(e0[i]);
+        cudaEventDestroy(e1[i]);
+    }
     if (err) return err;
     const int rc = apply_batch_tuning(b, bs, bp, bv, bn);
     if (rc) return rc;

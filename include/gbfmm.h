@@ -272,7 +272,8 @@ int gbfmm_debug_harmonics(int order, int kind, const double* d, double* out);
 int gbfmm_debug_bounded_wait(unsigned polls, void* stream);
 
 /* ---- autotuner (tile shapes) ----
- * gbfmm_autotune times whole steps (CUDA-graph replays, reps per candidate) of
+ * gbfmm_autotune times whole steps (CUDA-graph replays, reps per candidate, each
+ * after a 256 MB write that flushes L2; the buffer is allocated for the call) of
  * the given configuration for the P2P variants (0-14: warp-step shape 8 x 4,
  * 4 x 8 or 16 x 2 by variant % 3, one CTA per leaf or 2-5 resident CTAs per SM
  * by variant / 3; 15-16: 8 x 4 and 4 x 8 with up to 4 targets per thread, one
@@ -336,7 +337,7 @@ int gbfmm_batch_set_schedule(gbfmm_batch* b, int far_lanes, int far_prio, int ne
 int gbfmm_batch_get_schedule(gbfmm_batch* b, int* far_lanes, int* far_prio, int* near_after);
 
 /* Batch autotuner: times replays of the batch graph on the caller's device
- * inputs (as gbfmm_batch_execute_device) for the near-field kernel's warp-step
+ * inputs (as gbfmm_batch_execute_device; each after an L2 flush) for the near-field kernel's warp-step
  * shape (0: 8 targets x 4 source lanes, 1: 4 x 8, 2: 16 x 2, 3 and 4: 8 x 4 and
  * 4 x 8 with up to 4 targets per thread) and residency (2..5 resident CTAs
  * per SM walking the queue, or 0: one CTA per leaf), then, when
