@@ -130,7 +130,7 @@ __host__ __device__ __forceinline__ void tc_tile_shape_dev(int level, const int*
 __device__ __forceinline__ void tc_grids_body(const TcGridArgs& g, const int bid)
 {
     const int groups = g.KP / 8;
-    const long conv_blocks = (g.rows * groups + 255) / 256;
+    const long conv_blocks = ((g.rows - g.row_begin) * groups + 255) / 256;
     if (bid >= conv_blocks) {
         const int lane = threadIdx.x & 31, R = g.root_R;
         const int w = (int)(bid - conv_blocks) * 8 + (threadIdx.x >> 5);
@@ -144,9 +144,9 @@ __device__ __forceinline__ void tc_grids_body(const TcGridArgs& g, const int bid
         return;
     }
     const long i = (long)bid * blockDim.x + threadIdx.x;
-    if (i >= g.rows * groups) return;
-    const long row = i / groups;
-    const int c0 = (int)(i - row * groups) * 8;
+    if (i >= (g.rows - g.row_begin) * groups) return;
+    const long row = g.row_begin + i / groups;
+    const int c0 = (int)(i - (row - g.row_begin) * groups) * 8;
     int q = 0;
     while (q + 1 < g.ngrid && g.row0[q + 1] <= row) q++;
     long r = row - g.row0[q];
@@ -194,7 +194,7 @@ __global__ void __launch_bounds__(256) k_tc_grids(const TcGridArgs g) { tc_grids
 
 void launch_tc_grids(const TcGridArgs& g, cudaStream_t s)
 {
-    const long n = g.rows * (g.KP / 8);
+    const long n = (g.rows - g.row_begin) * (g.KP / 8);
     if (n <= 0) return;
     const long root_blocks = g.root_l2l ? ((long)g.root_n1 * g.root_R + 7) / 8 : 0;
     g_kernel_launches.fetch_add(1, std::memory_order_relaxed);
@@ -622,7 +622,7 @@ void launch_batch_tc(BatchKernel k, const void* args, const int* first, int nsys
 // Blocks of one system's grid conversion (and root L2L).
 long tc_grids_blocks(const TcGridArgs& g)
 {
-    const long n = g.rows * (g.KP / 8);
+    const long n = (g.rows - g.row_begin) * (g.KP / 8);
     if (n <= 0) return 0;
     return (n + 255) / 256 + (g.root_l2l ? ((long)g.root_n1 * g.root_R + 7) / 8 : 0);
 }

@@ -77,7 +77,8 @@ struct TcGridArgs {
     int level[2 * TC_MAXLEV], parity[2 * TC_MAXLEV], W[2 * TC_MAXLEV][3], n[2 * TC_MAXLEV][3];
     const float* src[2 * TC_MAXLEV];  // FP32 rows of that level (Morton order)
     int R, Rpad, KP, periodic;
-    long rows;
+    long rows;                        // rows [row_begin, rows) of the grid buffers are converted
+    long row_begin = 0;
     __nv_bfloat16 *hi, *lo;           // lo may be NULL (one product)
     // Root L2L, run by extra blocks of the same launch (before the M2L adds to
     // level 1): L1[o][r] += sum_c l2l[o][r][c] L0[c] in FP64, one warp per (o, r),

@@ -147,6 +147,9 @@ struct gbfmm_handle {
     // (captured as a fork/join of the step graph)
     cudaStream_t stream_nf = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // the deep levels' bf16 grids convert beside the upper-tree kernel
+    cudaStream_t stream_g = nullptr;
+    cudaEvent_t ev_gfork = nullptr, ev_gjoin = nullptr;
     cudaEvent_t ev_sc = nullptr;  // the step's copy of h_sc has been made (h_sc may be rewritten)
     // host state
     std::vector<float> h_q;
@@ -293,6 +296,9 @@ static void free_handle(gbfmm_handle* h)
     if (h->stream) cudaStreamDestroy(h->stream);
     if (h->stream_nf) cudaStreamDestroy(h->stream_nf);
     if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    if (h->stream_g) cudaStreamDestroy(h->stream_g);
+    if (h->ev_gfork) cudaEventDestroy(h->ev_gfork);
+    if (h->ev_gjoin) cudaEventDestroy(h->ev_gjoin);
     if (h->ev_sc) cudaEventDestroy(h->ev_sc);
     if (h->ev_join) cudaEventDestroy(h->ev_join);
     delete h;
@@ -716,6 +722,23 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
     for (int k = fused ? D - 2 : D - 1; k >= top_from; k--)
         launch_m2m(h->Mlev[k + 1], h->Mlev[k], h->d_m2m_t, (int)h->ncell[k], h->R, h->Rpad, s);
     mark(h, 3);
+    // the bf16 grids of the levels complete before the upper tree (from top_from
+    // down; they are last in the grid buffers) convert on their own stream beside it
+    const bool gfork = h->tc && !h->timing;
+    long grid_split = 0;  // first row of those levels' grids
+    if (h->tc) {
+        const TcGridArgs all = tc_grid_args(h);
+        grid_split = all.rows;
+        for (int q = all.ngrid - 1; q >= 0 && all.level[q] >= top_from; q--) grid_split = all.row0[q];
+    }
+    if (gfork && grid_split < h->tcg.rows) {
+        TcGridArgs deep = tc_grid_args(h);
+        deep.row_begin = grid_split;
+        cudaEventRecord(h->ev_gfork, s);
+        cudaStreamWaitEvent(h->stream_g, h->ev_gfork, 0);
+        launch_tc_grids(deep, h->stream_g);
+        cudaEventRecord(h->ev_gjoin, h->stream_g);
+    }
     RootArgs ra;
     ra.R = h->R;
     ra.Rpad = h->Rpad;
@@ -751,14 +774,17 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
     fork_near(2);
     mark(h, 4);
     if (h->tc) {
-        // the root L2L rides on the grid conversion, ahead of the M2L
+        // the root L2L rides on the grid conversion, ahead of the M2L; the grids
+        // of the upper levels (all of them in the stage-timing pass) convert here
         TcGridArgs tg = tc_grid_args(h);
+        if (gfork) tg.rows = grid_split;
         tg.root_l2l = h->d_root_l2l;
         tg.L0 = h->d_L0;
         tg.L1 = h->Llev[1];
         tg.root_R = h->R;
         tg.root_n1 = (int)h->ncell[1];
         launch_tc_grids(tg, s);
+        if (gfork && grid_split < h->tcg.rows) cudaStreamWaitEvent(s, h->ev_gjoin, 0);
         TcArgs& ta = *h->tca;  // the current tuning: entry split and pipeline depth
         ta.tasks = h->d_tc_tasks_v[h->tc_split_v];
         ta.atomic = h->tc_split_v > 0 ? 1 : 0;
@@ -892,7 +918,10 @@ extern "C" int gbfmm_create(const gbfmm_params* prm, int natoms, gbfmm_handle** 
             cudaStreamCreateWithPriority(&h->stream_nf, cudaStreamNonBlocking, lo) != cudaSuccess ||
             cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
             cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess ||
-            cudaEventCreateWithFlags(&h->ev_sc, cudaEventDisableTiming) != cudaSuccess)
+            cudaEventCreateWithFlags(&h->ev_sc, cudaEventDisableTiming) != cudaSuccess ||
+            cudaStreamCreateWithPriority(&h->stream_g, cudaStreamNonBlocking, hi) != cudaSuccess ||
+            cudaEventCreateWithFlags(&h->ev_gfork, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&h->ev_gjoin, cudaEventDisableTiming) != cudaSuccess)
             return bail(fail(GBFMM_ERR_CUDA, "stream create failed"));
     }
     Arena sz;
