@@ -806,7 +806,7 @@ def main():
         ms = run.time_device(s, args.steps, args.warmup, clocks=clk)
         value, ms = replica_throughput(n, args.steps, ms, dist if ws > 1 else None, dev)
         r = {"prec": prec, "P": P, "D": D, "ms": ms / args.steps, "value": value,
-             "err": err_of(s), "clocks": clk.summary()}
+             "err": err_of(s), "clocks": clk.summary(), "launches": s.step_launches()}
         r["eerr"] = energy_err(s)
         r["e2e"] = n * ws * args.steps / run.time_e2e(s, args.steps)
         # the same call with staging copies (GBFMM_FLAG_HOST_COPY), for comparison
@@ -817,7 +817,6 @@ def main():
         r["e2e_copies"] = n * ws * args.steps / run.time_e2e(sc, args.steps)
         sc.close()
         r["stages"] = run.stages(s, args.steps)
-        r["launches"] = s.step_launches()
         r["tiles"] = tiles
         _, _, ln = s.tree()
         r["p2p_pairs"] = p2p_pair_count(ln, D)

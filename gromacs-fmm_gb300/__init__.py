@@ -94,6 +94,8 @@ def lib():
             "gbfmm_batch_status": (ctypes.c_int, [vp]),
             "gbfmm_set_near_start": (ctypes.c_int, [vp, ctypes.c_int]),
             "gbfmm_get_near_start": (ctypes.c_int, [vp, ip]),
+            "gbfmm_set_launch_overlap": (ctypes.c_int, [vp, ctypes.c_int]),
+            "gbfmm_get_launch_overlap": (ctypes.c_int, [vp, ip]),
             "gbfmm_batch_step_launches": (ctypes.c_int, [vp, ip]),
             "gbfmm_batch_set_schedule": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
             "gbfmm_batch_get_schedule": (ctypes.c_int, [vp, ip, ip, ip]),
@@ -256,6 +258,16 @@ class ZetaFmmSolver:
 
     def set_near_start(self, after):
         _check(lib().gbfmm_set_near_start(self._h, int(after)))
+
+    def launch_overlap(self):
+        e = ctypes.c_int()
+        _check(lib().gbfmm_get_launch_overlap(self._h, ctypes.byref(e)))
+        return bool(e.value)
+
+    def set_launch_overlap(self, enable):
+        """Programmatic dependent launches between the step's consecutive kernels
+        (gbfmm_set_launch_overlap); on by default."""
+        _check(lib().gbfmm_set_launch_overlap(self._h, 1 if enable else 0))
 
     def set_tuning(self, p2p_variant=0, m2l_split=1, m2l_stages=2):
         _check(lib().gbfmm_set_tuning(self._h, int(p2p_variant), int(m2l_split), int(m2l_stages)))

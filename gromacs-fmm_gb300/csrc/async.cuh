@@ -4,6 +4,10 @@
 
 #include <stdint.h>
 
+#include <utility>
+
+#include <cuda_runtime.h>
+
 namespace gbfmm {
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -33,6 +37,20 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
         : "memory");
     return ok != 0;
 }
+
+// Programmatic dependent launch (sm_90 and later).  A kernel launched with
+// programmatic stream serialization (launch_k with pdl set) may start while the
+// previous kernel of its stream is still running: it may stage constant tables
+// first, but it calls pdl_wait() before it reads or writes anything that kernel
+// touches.  pdl_wait returns once that kernel has completed and its writes are
+// visible; in a plain launch it returns at once.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+// Lets the next kernel of the stream, if it was launched with programmatic
+// serialization, start once every CTA of this grid has called this or exited.
+// It only moves that kernel's start (its pdl_wait still waits for this grid's
+// completion); without the call the next kernel starts when this grid ends.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
 // Default poll limit of the bounded waits: 2^24 polls, well over a second.
 constexpr uint32_t WAIT_POLLS_DEFAULT = 1u << 24;
@@ -66,6 +84,29 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
                      smem_u32(dst)),
                  "l"(src), "r"(bytes), "r"(smem_u32(bar))
                  : "memory");
+}
+
+// Launches kernel k on stream s; with pdl, as a programmatic dependent of the
+// previous kernel of s (the kernel must call pdl_wait before it touches that
+// kernel's data).  Captured into a graph, the dependency becomes a programmatic
+// edge.
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_k(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, bool pdl,
+                            Args&&... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    if (pdl) {
+        at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+    }
+    return cudaLaunchKernelEx(&cfg, k, std::forward<Args>(args)...);
 }
 
 }  // namespace gbfmm

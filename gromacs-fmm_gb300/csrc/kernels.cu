@@ -160,6 +160,7 @@ __device__ __forceinline__ void tree_keys_body(const TreeArgs& a, const int bid,
     if (threadIdx.x == 0) s_last = atomicAdd(a.done, 1) == (int)nb - 1;
     __syncthreads();
     if (!s_last) return;
+    pdl_trigger();  // the other blocks have exited: the scatter may launch
     __threadfence();
     if (threadIdx.x == 0) *a.done = 0;  // every block has counted: ready for the next step
     if (a.sums && warp < 4) {
@@ -335,6 +336,8 @@ void launch_scatter(const uint32_t* code, int n, int* cursor, int* tmp_idx, cuda
 
 __device__ __forceinline__ void scatter_ranked_body(const ScatterArgs& a, const int bid)
 {
+    pdl_wait();
+    pdl_trigger();
     int i = bid * blockDim.x + threadIdx.x;
     if (i < a.n) a.tmp[a.off[a.code[i]] + a.rank[i]] = i;
 }
@@ -342,12 +345,12 @@ __device__ __forceinline__ void scatter_ranked_body(const ScatterArgs& a, const 
 __global__ void k_scatter_ranked(const ScatterArgs a) { scatter_ranked_body(a, blockIdx.x); }
 
 void launch_scatter_ranked(const uint32_t* code, int n, const int* off, const int* rank, int* tmp_idx,
-                           cudaStream_t s)
+                           cudaStream_t s, bool pdl)
 {
     if (n > 0) {
         COUNT_LAUNCH();
         ScatterArgs a{code, n, off, rank, tmp_idx};
-        k_scatter_ranked<<<(n + 255) / 256, 256, 0, s>>>(a);
+        launch_k(k_scatter_ranked, dim3((n + 255) / 256), dim3(256), 0, s, pdl, a);
     }
 }
 
@@ -373,6 +376,8 @@ __device__ __forceinline__ void leaf_sort_body(const LeafSortArgs& la, const int
     int* edge = la.edge;
     const int lane = threadIdx.x & 31;
     const int leaf = (bid * blockDim.x + threadIdx.x) >> 5;
+    pdl_wait();
+    pdl_trigger();
     if (leaf >= nleaf) return;
     if (counts && lane == 0) counts[leaf] = 0;  // consumed by the scan: zero for the next step
     const int b = off[leaf], n = off[leaf + 1] - b;
@@ -410,13 +415,13 @@ __device__ __forceinline__ void leaf_sort_body(const LeafSortArgs& la, const int
 __global__ void __launch_bounds__(256) k_leaf_sort(const LeafSortArgs a) { leaf_sort_body(a, blockIdx.x); }
 
 void launch_leaf_sort(const int* offsets, int nleaf, int* tmp_idx, const float4* uq, const uint32_t* code, int* order,
-                      float4* atoms, int* inv, int* counts, cudaStream_t s, int* edge)
+                      float4* atoms, int* inv, int* counts, cudaStream_t s, int* edge, bool pdl)
 {
     (void)code;
     long threads = (long)nleaf * 32;
     COUNT_LAUNCH();
     LeafSortArgs a{offsets, nleaf, tmp_idx, uq, order, atoms, inv, counts, edge};
-    k_leaf_sort<<<(int)((threads + 255) / 256), 256, 0, s>>>(a);
+    launch_k(k_leaf_sort, dim3((unsigned)((threads + 255) / 256)), dim3(256), 0, s, pdl, a);
 }
 
 // ------------------------------------------------------------------ P2M
@@ -474,6 +479,8 @@ __device__ __forceinline__ void p2m_body(const P2MArgs& pa, const int bid)
     const int Rpad = pa.Rpad;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int leaf = bid * WARPS + warp;
+    pdl_wait();
+    pdl_trigger();
     if (leaf >= nleaf) return;
     float* S = sm + warp * R * LD;
     for (int r = 0; r < R; r++) S[r * LD + lane] = 0.f;
@@ -505,7 +512,7 @@ template <int P, int WARPS>
 __global__ void __launch_bounds__(WARPS * 32) k_p2m(const P2MArgs a) { p2m_body<P, WARPS>(a, blockIdx.x); }
 
 template <int P>
-static void p2m_dispatch(const int* off, int nleaf, const float4* atoms, float* M, int Rpad, cudaStream_t s)
+static void p2m_dispatch(const int* off, int nleaf, const float4* atoms, float* M, int Rpad, cudaStream_t s, bool pdl)
 {
     constexpr int R = (P + 1) * (P + 1);
     constexpr int W = R <= 169 ? 4 : 2;
@@ -517,7 +524,7 @@ static void p2m_dispatch(const int* off, int nleaf, const float4* atoms, float* 
     }
     COUNT_LAUNCH();
     P2MArgs a{off, nleaf, atoms, M, nullptr, nullptr, Rpad};
-    k_p2m<P, W><<<(nleaf + W - 1) / W, W * 32, shm, s>>>(a);
+    launch_k(k_p2m<P, W>, dim3((nleaf + W - 1) / W), dim3(W * 32), shm, s, pdl, a);
 }
 
 #define GBFMM_ORDER_SWITCH(P, CALL)            \
@@ -540,9 +547,10 @@ static void p2m_dispatch(const int* off, int nleaf, const float4* atoms, float* 
         default: break;                       \
     }
 
-void launch_p2m(int P, const int* offsets, int nleaf, const float4* atoms, float* M_leaf, int Rpad, cudaStream_t s)
+void launch_p2m(int P, const int* offsets, int nleaf, const float4* atoms, float* M_leaf, int Rpad, cudaStream_t s,
+                bool pdl)
 {
-    GBFMM_ORDER_SWITCH(P, p2m_dispatch<PP>(offsets, nleaf, atoms, M_leaf, Rpad, s));
+    GBFMM_ORDER_SWITCH(P, p2m_dispatch<PP>(offsets, nleaf, atoms, M_leaf, Rpad, s, pdl));
 }
 
 // ------------------------------------------------------------------ L2P
@@ -649,10 +657,11 @@ __device__ __forceinline__ void down_body(const DownArgs& a, const int bid)
             mbar_init(&dbar, 1);
             mbar_init_fence();
             mbar_expect_tx(&dbar, 32u * R * R);
-            bulk_g2s(sA, a.l2l_t, 32u * R * R, &dbar);
+            bulk_g2s(sA, a.l2l_t, 32u * R * R, &dbar);  // constant: may precede the wait below
         }
         At = sA;
     }
+    pdl_wait();
     // every local row the CTA reads, in one pass: the ancestors' (level k's
     // ancestor of parent p is p >> 3 (D-1-k)) and the 8 leaves'
     for (int i = threadIdx.x; i < (D + 7) * R; i += blockDim.x) {
@@ -751,7 +760,7 @@ size_t down_smem_bytes(int P)
 }
 
 template <int P>
-static void down_dispatch(const DownArgs& a, cudaStream_t s)
+static void down_dispatch(const DownArgs& a, cudaStream_t s, bool pdl)
 {
     const size_t shm = down_smem_bytes(P);
     static bool attr = false;
@@ -759,13 +768,13 @@ static void down_dispatch(const DownArgs& a, cudaStream_t s)
         cudaFuncSetAttribute(k_down<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
         attr = true;
     }
-    k_down<P><<<a.nparent, 256, shm, s>>>(a);
+    launch_k(k_down<P>, dim3(a.nparent), dim3(256), shm, s, pdl, a);
 }
 
-void launch_down(int P, const DownArgs& a, cudaStream_t s)
+void launch_down(int P, const DownArgs& a, cudaStream_t s, bool pdl)
 {
     COUNT_LAUNCH();
-    GBFMM_ORDER_SWITCH(P, down_dispatch<PP>(a, s));
+    GBFMM_ORDER_SWITCH(P, down_dispatch<PP>(a, s, pdl));
 }
 
 
@@ -1266,6 +1275,8 @@ __device__ __forceinline__ void m2m_body(const M2MArgs& ma, const int p, const i
     const int R = ma.R, Rpad = ma.Rpad;
     const int o = threadIdx.y, r = rb * 32 + threadIdx.x;
     const int tid = threadIdx.y * 32 + threadIdx.x;
+    pdl_wait();
+    pdl_trigger();
     for (int i = tid; i < 8 * R; i += 256) {
         const int oo = i / R;
         ms[i] = Mc[(size_t)(8 * p + oo) * Rpad + (i - oo * R)];
@@ -1291,11 +1302,12 @@ __device__ __forceinline__ void m2m_body(const M2MArgs& ma, const int p, const i
 
 __global__ void __launch_bounds__(256) k_m2m(const M2MArgs a) { m2m_body(a, blockIdx.x, blockIdx.y); }
 
-void launch_m2m(const float* M_child, float* M_parent, const float* At, int nparent, int R, int Rpad, cudaStream_t s)
+void launch_m2m(const float* M_child, float* M_parent, const float* At, int nparent, int R, int Rpad, cudaStream_t s,
+                bool pdl)
 {
     COUNT_LAUNCH();
     M2MArgs a{M_child, M_parent, At, nparent, R, Rpad};
-    k_m2m<<<dim3(nparent, (R + 31) / 32), dim3(32, 8), sizeof(float) * 8 * R, s>>>(a);
+    launch_k(k_m2m, dim3(nparent, (R + 31) / 32), dim3(32, 8), sizeof(float) * 8 * R, s, pdl, a);
 }
 
 // P2M of 8 sibling leaves (one warp each, the arithmetic of k_p2m) followed by
@@ -1319,6 +1331,8 @@ __device__ __forceinline__ void p2m_m2m_body(const P2MArgs& pa, const int bid)
     float* S = sm + warp * R * LD;
     float* ch = sm + 8 * R * LD;  // the 8 leaf multipoles
     float* red = ch + 8 * R;      // per-octant partial sums of the parent
+    pdl_wait();
+    pdl_trigger();
     for (int r = 0; r < R; r++) S[r * LD + lane] = 0.f;
     const int b = off[leaf], n = off[leaf + 1] - b;
     for (int c0 = 0; c0 < n; c0 += 32) {
@@ -1371,7 +1385,7 @@ constexpr size_t P2M_M2M_MAX_SMEM = 80 * 1024;
 
 template <int P>
 static bool p2m_m2m_dispatch(const int* off, int nleaf, const float4* atoms, float* M, float* Mp, const float* At,
-                             int Rpad, cudaStream_t s)
+                             int Rpad, cudaStream_t s, bool pdl)
 {
     constexpr int R = (P + 1) * (P + 1);
     const size_t shm = sizeof(float) * (8 * R * 33 + 16 * R);
@@ -1383,15 +1397,15 @@ static bool p2m_m2m_dispatch(const int* off, int nleaf, const float4* atoms, flo
     }
     COUNT_LAUNCH();
     P2MArgs a{off, nleaf, atoms, M, Mp, At, Rpad};
-    k_p2m_m2m<P><<<nleaf / 8, 256, shm, s>>>(a);
+    launch_k(k_p2m_m2m<P>, dim3(nleaf / 8), dim3(256), shm, s, pdl, a);
     return true;
 }
 
 bool launch_p2m_m2m(int P, const int* offsets, int nleaf, const float4* atoms, float* M_leaf, float* M_parent,
-                    const float* At, int Rpad, cudaStream_t s)
+                    const float* At, int Rpad, cudaStream_t s, bool pdl)
 {
     bool ok = false;
-    GBFMM_ORDER_SWITCH(P, ok = p2m_m2m_dispatch<PP>(offsets, nleaf, atoms, M_leaf, M_parent, At, Rpad, s));
+    GBFMM_ORDER_SWITCH(P, ok = p2m_m2m_dispatch<PP>(offsets, nleaf, atoms, M_leaf, M_parent, At, Rpad, s, pdl));
     return ok;
 }
 
@@ -1720,23 +1734,27 @@ __device__ __forceinline__ void top_body(const TopArgs& a, const int bid, const 
         // multiples of 16 bytes; the sources are 16-byte aligned allocations
         const int rows = a.from == 3 ? 64 : a.from == 2 ? 8 : 1;
         const float* src_in = a.from >= 2 ? a.Min + (size_t)rows * g * Rpad : a.M1 + (size_t)g * Rpad;
+        const uint32_t b_in = 4u * rows * Rpad;
         if (tid == 0) {
+            // the operators are constant: their copies may start before the
+            // previous kernel's end (pdl_wait), the input cells' after it
             mbar_init(&bar, 1);
             mbar_init_fence();
-            const uint32_t b_at = a.from >= 2 ? 32u * R * R : 0u, b_ag = 8u * R2p, b_lat = a.lattice ? 8u * R2p : 0u,
-                           b_in = 4u * rows * Rpad;
+            const uint32_t b_at = a.from >= 2 ? 32u * R * R : 0u, b_ag = 8u * R2p, b_lat = a.lattice ? 8u * R2p : 0u;
             mbar_expect_tx(&bar, b_at + b_ag + b_lat + b_in);
             if (b_at) bulk_g2s(At, a.m2m_t, b_at, &bar);
             bulk_g2s(Ag, a.root.m2m + (size_t)g * R2p, b_ag, &bar);
             if (b_lat) bulk_g2s(lat, a.root.lattice, b_lat, &bar);
-            bulk_g2s(a.from == 3 ? in : a.from == 2 ? mid : m1, src_in, b_in, &bar);
         }
+        pdl_wait();
+        if (tid == 0) bulk_g2s(a.from == 3 ? in : a.from == 2 ? mid : m1, src_in, b_in, &bar);
         __syncthreads();
         if (!mbar_wait(&bar, 0, a.err, 1, a.wait_limit))
             mbar_drain(&bar, 0, a.wait_limit);  // no exit while the copies may still land
         if (a.from == 3) top_m2m(in, red, mid, a.M2 + (size_t)8 * g * Rpad, 8, At, R, Rpad);
         if (a.from >= 2) top_m2m(mid, red, m1, a.M1 + (size_t)g * Rpad, 1, At, R, Rpad);
     } else {
+        pdl_wait();
         for (int r = tid; r < R; r += TOP_THREADS) m1[r] = a.M1[(size_t)g * Rpad + r];
         __syncthreads();
     }
@@ -1762,6 +1780,7 @@ __device__ __forceinline__ void top_body(const TopArgs& a, const int bid, const 
     if (tid == 0) s_last = atomicAdd(a.done, 1) == (int)nb - 1;
     __syncthreads();
     if (!s_last) return;
+    pdl_trigger();  // the other CTAs have exited: the next kernel may launch
     __threadfence();
     if (tid == 0) *a.done = 0;  // ready for the next step
     // dipole (3) and total charge of the bodies: the tree-key kernel's per-block
@@ -1824,7 +1843,7 @@ __device__ __forceinline__ void top_body(const TopArgs& a, const int bid, const 
 template <bool STAGED>
 __global__ void __launch_bounds__(TOP_THREADS) k_top(const TopArgs a) { top_body<STAGED>(a, blockIdx.x, gridDim.x); }
 
-void launch_top(const TopArgs& a, cudaStream_t s)
+void launch_top(const TopArgs& a, cudaStream_t s, bool pdl)
 {
     const size_t shm = top_smem_bytes(a.root.R);
     const bool staged = top_staged(a.root.R);
@@ -1835,8 +1854,8 @@ void launch_top(const TopArgs& a, cudaStream_t s)
         attr[staged] = shm;
     }
     COUNT_LAUNCH();
-    if (staged) k_top<true><<<a.root.n1, TOP_THREADS, shm, s>>>(a);
-    else k_top<false><<<a.root.n1, TOP_THREADS, shm, s>>>(a);
+    if (staged) launch_k(k_top<true>, dim3(a.root.n1), dim3(TOP_THREADS), shm, s, pdl, a);
+    else launch_k(k_top<false>, dim3(a.root.n1), dim3(TOP_THREADS), shm, s, pdl, a);
     if (!a.lattice) launch_root_lattice(a.root, s);
 }
 

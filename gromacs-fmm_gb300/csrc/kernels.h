@@ -171,19 +171,23 @@ void launch_tree_keys(const TreeArgs& a, cudaStream_t s);
 void launch_exclusive_scan(const int* in, int* out, int n, int* scratch, cudaStream_t s);
 void launch_scatter(const uint32_t* code, int n, int* cursor, int* tmp_idx, cudaStream_t s);
 // The same without atomics: tmp_idx[off[code[i]] + rank[i]] = i (TreeArgs::rank).
+// The launchers below that take 'pdl' launch, when it is set, as programmatic
+// dependents of the previous kernel of s (launch_k): the kernel may start while
+// that one finishes and waits for it (pdl_wait) before it touches its data.
 void launch_scatter_ranked(const uint32_t* code, int n, const int* off, const int* rank, int* tmp_idx,
-                           cudaStream_t s);
+                           cudaStream_t s, bool pdl = false);
 // Also zeroes counts[0..nleaf) (consumed by then) when counts != NULL.
 // inv[input index] = sorted position (the inverse of order); edge[leaf] (when
 // not NULL) = 1 if a body of the leaf lies on or near its faces or outside it.
 void launch_leaf_sort(const int* offsets, int nleaf, int* tmp_idx, const float4* uq, const uint32_t* code, int* order,
-                      float4* atoms, int* inv, int* counts, cudaStream_t s, int* edge = nullptr);
-void launch_p2m(int P, const int* offsets, int nleaf, const float4* atoms, float* M_leaf, int Rpad, cudaStream_t s);
+                      float4* atoms, int* inv, int* counts, cudaStream_t s, int* edge = nullptr, bool pdl = false);
+void launch_p2m(int P, const int* offsets, int nleaf, const float4* atoms, float* M_leaf, int Rpad, cudaStream_t s,
+                bool pdl = false);
 // P2M of the leaves and M2M of their parents in one launch (8 sibling leaves per
 // CTA).  Returns false, launching nothing, when the order's shared memory does
 // not fit or nleaf is not a multiple of 8.
 bool launch_p2m_m2m(int P, const int* offsets, int nleaf, const float4* atoms, float* M_leaf, float* M_parent,
-                    const float* At, int Rpad, cudaStream_t s);
+                    const float* At, int Rpad, cudaStream_t s, bool pdl = false);
 void launch_l2p(int P, const int* offsets, int nleaf, const float4* atoms, const float* L_leaf, int Rpad, float4* field,
                 cudaStream_t s);
 // Near field.  variant = shape + 3 * persistence: shape = the warp-step shape
@@ -231,14 +235,15 @@ struct DownArgs {
     int* err = nullptr;              // bit 1: the bounded wait on the staged operators gave up
     uint32_t wait_limit = 1u << 24;  // polls of that wait
 };
-void launch_down(int P, const DownArgs& a, cudaStream_t s);
+void launch_down(int P, const DownArgs& a, cudaStream_t s, bool pdl = false);
 // Dynamic shared memory of the downward pass of order P: the 8 L2L operators,
 // staged by one bulk copy where they fit (orders up to 6), else 0 (read from L2).
 size_t down_smem_bytes(int P);
 
 // One level of M2M (nparent parents from their 8 children each); At = 8
 // transposed R x R scaled operators.
-void launch_m2m(const float* M_child, float* M_parent, const float* At, int nparent, int R, int Rpad, cudaStream_t s);
+void launch_m2m(const float* M_child, float* M_parent, const float* At, int nparent, int R, int Rpad, cudaStream_t s,
+                bool pdl = false);
 
 struct RootArgs {
     int R, Rpad;
@@ -289,7 +294,7 @@ struct TopArgs {
 constexpr int TOP_STAGE_MAX_R = 49;
 constexpr int TOP_LATTICE_MAX_R = TOP_STAGE_MAX_R;  // larger: the multi-CTA k_root_lattice
 size_t top_smem_bytes(int R);
-void launch_top(const TopArgs& a, cudaStream_t s);
+void launch_top(const TopArgs& a, cudaStream_t s, bool pdl = false);
 
 // Bounded-wait probe: one warp waits on an mbarrier that nothing completes,
 // with no copies or MMAs in flight; after 'polls' polls the wait gives up and

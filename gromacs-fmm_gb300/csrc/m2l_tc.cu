@@ -129,6 +129,7 @@ __host__ __device__ __forceinline__ void tc_tile_shape_dev(int level, const int*
 // bf16 hi and lo.
 __device__ __forceinline__ void tc_grids_body(const TcGridArgs& g, const int bid)
 {
+    pdl_wait();
     const int groups = g.KP / 8;
     const long conv_blocks = ((g.rows - g.row_begin) * groups + 255) / 256;
     if (bid >= conv_blocks) {
@@ -192,13 +193,13 @@ __device__ __forceinline__ void tc_grids_body(const TcGridArgs& g, const int bid
 
 __global__ void __launch_bounds__(256) k_tc_grids(const TcGridArgs g) { tc_grids_body(g, blockIdx.x); }
 
-void launch_tc_grids(const TcGridArgs& g, cudaStream_t s)
+void launch_tc_grids(const TcGridArgs& g, cudaStream_t s, bool pdl)
 {
     const long n = (g.rows - g.row_begin) * (g.KP / 8);
     if (n <= 0) return;
     const long root_blocks = g.root_l2l ? ((long)g.root_n1 * g.root_R + 7) / 8 : 0;
     g_kernel_launches.fetch_add(1, std::memory_order_relaxed);
-    k_tc_grids<<<(unsigned)((n + 255) / 256 + root_blocks), 256, 0, s>>>(g);
+    launch_k(k_tc_grids, dim3((unsigned)((n + 255) / 256 + root_blocks)), dim3(256), 0, s, pdl, g);
 }
 
 // ------------------------------------------------------------------ M2L
@@ -373,6 +374,7 @@ __device__ __forceinline__ void m2l_tc_body(const TcArgs& a, const int bid)
     tc_fence_before();
     const bool failed = __syncthreads_or(!ok) != 0;
     tc_fence_after();
+    pdl_trigger();  // only the epilogue is left: the next kernel may launch (it waits for this one's end)
     if (ne > 0 && !failed) {
         float* dst = a.dst_lvl[k];
         const int t = 32 * warp + lane;

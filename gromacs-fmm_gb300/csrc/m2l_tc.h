@@ -89,7 +89,7 @@ struct TcGridArgs {
     int root_R = 0;
     int root_n1 = 8;  // stored level-1 cells
 };
-void launch_tc_grids(const TcGridArgs& g, cudaStream_t s);
+void launch_tc_grids(const TcGridArgs& g, cudaStream_t s, bool pdl = false);  // pdl: as launch_down
 long tc_grids_blocks(const TcGridArgs& g);  // CTAs of one system's launch_tc_grids
 
 struct alignas(64) TcArgs {

@@ -206,6 +206,7 @@ struct gbfmm_handle {
     int tc_nstage = 2;
     int p2p_variant = 0;  // P2P warp-step shape (autotuned)
     int near_after = 0;   // the near field starts after the tree (0), the P2M (1) or the upper tree (2)
+    bool pdl = true;      // consecutive kernels of the step's main chain launch as programmatic dependents
     StepConst* d_sc = nullptr;
     StepConst* h_sc = nullptr;  // pinned
     int* h_flags = nullptr;     // pinned
@@ -645,6 +646,10 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
     cudaStream_t s = h->stream;
     const int D = h->D, n = h->n;
     const long launches0 = g_kernel_launches.load();
+    // a kernel that follows another on s without a cross-stream wait between them
+    // starts as its programmatic dependent (off in the stage-timing pass, whose
+    // events bracket each kernel)
+    const bool pdl = h->pdl && !h->timing;
     mark(h, 0);
     // Leaf counts and the step's counters are zero when a step starts: zeroed at
     // creation, then re-zeroed by their last users (leaf sort, the last blocks of
@@ -689,9 +694,9 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
         launch_tree_keys(ta, s);
         if (!ta.off) launch_exclusive_scan(h->d_counts, h->d_off, h->nleaf, h->d_scan, s);
     }
-    launch_scatter_ranked(h->d_code, n, h->d_off, h->d_inv, h->d_tmp, s);
+    launch_scatter_ranked(h->d_code, n, h->d_off, h->d_inv, h->d_tmp, s, pdl);
     launch_leaf_sort(h->d_off, h->nleaf, h->d_tmp, h->d_uq, h->d_code, h->d_order, h->d_atoms, h->d_inv,
-                     h->d_counts, s, h->d_leaf_edge);
+                     h->d_counts, s, h->d_leaf_edge, pdl);
     mark(h, 1);
     // The near field needs only the tree: in graph mode it forks onto its own
     // low-priority stream and overlaps the far-field chain below (joined before
@@ -714,13 +719,13 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
     // upward pass: P2M with the M2M of the leaf parents in one launch, M2M launches
     // down to level 3, then levels 2 and 1 and the FP64 root in one launch (k_top)
     const bool fused = D >= 2 && launch_p2m_m2m(h->P, h->d_off, h->nleaf, h->d_atoms, h->Mlev[D], h->Mlev[D - 1],
-                                                h->d_m2m_t, h->Rpad, s);
-    if (!fused) launch_p2m(h->P, h->d_off, h->nleaf, h->d_atoms, h->Mlev[D], h->Rpad, s);
+                                                h->d_m2m_t, h->Rpad, s, pdl);
+    if (!fused) launch_p2m(h->P, h->d_off, h->nleaf, h->d_atoms, h->Mlev[D], h->Rpad, s, pdl);
     fork_near(1);
     mark(h, 2);
     const int top_from = D == 1 || h->R > TOP_STAGE_MAX_R ? 1 : std::min(3, fused ? D - 1 : D);
     for (int k = fused ? D - 2 : D - 1; k >= top_from; k--)
-        launch_m2m(h->Mlev[k + 1], h->Mlev[k], h->d_m2m_t, (int)h->ncell[k], h->R, h->Rpad, s);
+        launch_m2m(h->Mlev[k + 1], h->Mlev[k], h->d_m2m_t, (int)h->ncell[k], h->R, h->Rpad, s, pdl);
     mark(h, 3);
     // the bf16 grids of the levels complete before the upper tree (from top_from
     // down; they are last in the grid buffers) convert on their own stream beside it
@@ -770,7 +775,7 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
     top.done = sync + 3;
     top.err = h->d_flags + 2;
     top.umask = (h->shift[0] == 0 ? 4 : 0) | (h->shift[1] == 0 ? 2 : 0) | (h->shift[2] == 0 ? 1 : 0);
-    launch_top(top, s);
+    launch_top(top, s, pdl);
     fork_near(2);
     mark(h, 4);
     if (h->tc) {
@@ -783,7 +788,7 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
         tg.L1 = h->Llev[1];
         tg.root_R = h->R;
         tg.root_n1 = (int)h->ncell[1];
-        launch_tc_grids(tg, s);
+        launch_tc_grids(tg, s, pdl);
         if (gfork && grid_split < h->tcg.rows) cudaStreamWaitEvent(s, h->ev_gjoin, 0);
         TcArgs& ta = *h->tca;  // the current tuning: entry split and pipeline depth
         ta.tasks = h->d_tc_tasks_v[h->tc_split_v];
@@ -809,7 +814,7 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
         da.Rpad = h->Rpad;
         da.err = h->d_flags + 2;
         da.wait_limit = WAIT_POLLS_DEFAULT;
-        launch_down(h->P, da, s);
+        launch_down(h->P, da, s, pdl);
         mark(h, 6);
     } else {
         mark(h, 6);  // depth 1: the leaves are level 1, complete after the root L2L
@@ -1280,6 +1285,25 @@ extern "C" int gbfmm_get_near_start(gbfmm_handle* h, int* after)
 {
     if (!h || !after) return fail(GBFMM_ERR_ARG, "NULL argument");
     *after = h->near_after;
+    return GBFMM_OK;
+}
+
+extern "C" int gbfmm_set_launch_overlap(gbfmm_handle* h, int enable)
+{
+    if (!h) return fail(GBFMM_ERR_ARG, "handle is NULL");
+    CK(cudaStreamSynchronize(h->stream));
+    h->pdl = enable != 0;
+    if (h->gexec) {
+        cudaGraphExecDestroy(h->gexec);
+        h->gexec = nullptr;
+    }
+    return GBFMM_OK;
+}
+
+extern "C" int gbfmm_get_launch_overlap(gbfmm_handle* h, int* enable)
+{
+    if (!h || !enable) return fail(GBFMM_ERR_ARG, "NULL argument");
+    *enable = h->pdl ? 1 : 0;
     return GBFMM_OK;
 }
 

@@ -291,6 +291,13 @@ int gbfmm_autotune(gbfmm_handle* h, const float* coords, const float* box, int r
  * CTAs fill them.  Results do not depend on it; gbfmm_autotune searches it last. */
 int gbfmm_set_near_start(gbfmm_handle* h, int after);
 int gbfmm_get_near_start(gbfmm_handle* h, int* after);
+/* Programmatic dependent launches in the step (on by default): each kernel of the
+ * far-field chain that follows another on the same stream may start while that
+ * one finishes (it stages its constant operators meanwhile and waits for the
+ * previous kernel's completion before it touches its data).  Off, every kernel
+ * starts after the previous one ends.  Results do not depend on it. */
+int gbfmm_set_launch_overlap(gbfmm_handle* h, int enable);
+int gbfmm_get_launch_overlap(gbfmm_handle* h, int* enable);
 int gbfmm_get_tuning(gbfmm_handle* h, int* p2p_variant, int* m2l_split, int* m2l_stages);
 int gbfmm_set_tuning(gbfmm_handle* h, int p2p_variant, int m2l_split, int m2l_stages);
 

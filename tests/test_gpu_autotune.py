@@ -86,3 +86,26 @@ def test_near_field_start_leaves_results_unchanged(pkg, systems):
     with pytest.raises(pkg.FmmError):
         s.set_near_start(3)
     s.close()
+
+
+@pytest.mark.parametrize("order,depth,prec", [(5, 3, 1), (5, 4, 2), (4, 4, 0), (8, 5, 0)])
+def test_launch_overlap_leaves_results_unchanged(pkg, systems, order, depth, prec):
+    """Programmatic dependent launches only move kernel starts: each kernel still
+    waits for the previous one before it touches its data, so a deterministic
+    handle gives the same bits with and without them (tensor-core and FP32 M2L,
+    the fused and the level-by-level upward pass, the staged and unstaged upper
+    tree)."""
+    xyz, q, L = _system(systems)
+    s = pkg.ZetaFmmSolver(len(q), q, order=order, max_depth=depth, images=4, precision=prec,
+                          flags=pkg.FLAG_DETERMINISTIC)
+    assert s.launch_overlap()
+    s.execute(xyz, L)
+    f0, p0, e0 = s.forces(), s.potentials(), s.get_energy()
+    for on in (False, True, False):
+        s.set_launch_overlap(on)
+        assert s.launch_overlap() == on
+        for _ in range(2):
+            s.execute(xyz, L)
+            assert np.array_equal(s.forces(), f0) and np.array_equal(s.potentials(), p0), on
+            assert s.get_energy() == e0
+    s.close()
