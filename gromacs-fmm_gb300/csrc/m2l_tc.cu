@@ -130,6 +130,7 @@ __host__ __device__ __forceinline__ void tc_tile_shape_dev(int level, const int*
 __device__ __forceinline__ void tc_grids_body(const TcGridArgs& g, const int bid)
 {
     pdl_wait();
+    pdl_trigger();
     const int groups = g.KP / 8;
     const long conv_blocks = ((g.rows - g.row_begin) * groups + 255) / 256;
     if (bid >= conv_blocks) {
@@ -278,6 +279,9 @@ __device__ __forceinline__ void m2l_tc_body(const TcArgs& a, const int bid)
     const uint32_t tmem = *tmem_slot;
     const uint32_t lim = a.wait_limit;
     bool ok = true;
+    // the set-up above reads only this step's tree and constant lists; the source
+    // grids and the locals belong to the previous kernel (a programmatic launch)
+    pdl_wait();
 
     // On a bounded wait that gives up, the waiting role records the error, stops
     // issuing work and drains what it issued (again bounded); the CTA then skips
@@ -560,7 +564,7 @@ int tc_max_stages(int k_atoms, int img_bytes, int nprod)
     return ns;
 }
 
-void launch_m2l_tc(const TcArgs& a, int ntasks, cudaStream_t s)
+void launch_m2l_tc(const TcArgs& a, int ntasks, cudaStream_t s, bool pdl)
 {
     if (ntasks <= 0) return;
     size_t shm = tc_smem_bytes(a);
@@ -570,7 +574,7 @@ void launch_m2l_tc(const TcArgs& a, int ntasks, cudaStream_t s)
         attr = shm;
     }
     g_kernel_launches.fetch_add(1, std::memory_order_relaxed);
-    k_m2l_tc<<<ntasks, TC_THREADS, shm, s>>>(a);
+    launch_k(k_m2l_tc, dim3(ntasks), dim3(TC_THREADS), shm, s, pdl, a);
 }
 
 }  // namespace gbfmm

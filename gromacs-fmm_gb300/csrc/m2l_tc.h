@@ -121,6 +121,6 @@ size_t tc_smem_bytes(const TcArgs& a);
 size_t tc_stage_bytes(int k_atoms, int img_bytes, int nprod);  // the operands of one entry
 int tc_pick_stages(int k_atoms, int img_bytes, int nprod);
 int tc_max_stages(int k_atoms, int img_bytes, int nprod);  // most that fit one CTA's shared memory
-void launch_m2l_tc(const TcArgs& a, int ntasks, cudaStream_t s);
+void launch_m2l_tc(const TcArgs& a, int ntasks, cudaStream_t s, bool pdl = false);  // pdl: as launch_down
 
 }  // namespace gbfmm

@@ -780,7 +780,11 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
     mark(h, 4);
     if (h->tc) {
         // the root L2L rides on the grid conversion, ahead of the M2L; the grids
-        // of the upper levels (all of them in the stage-timing pass) convert here
+        // of the upper levels (all of them in the stage-timing pass) convert here,
+        // after the deep levels' conversion has joined (the M2L then follows this
+        // launch alone, as its programmatic dependent)
+        const bool gjoin = gfork && grid_split < h->tcg.rows;
+        if (gjoin) cudaStreamWaitEvent(s, h->ev_gjoin, 0);
         TcGridArgs tg = tc_grid_args(h);
         if (gfork) tg.rows = grid_split;
         tg.root_l2l = h->d_root_l2l;
@@ -788,13 +792,12 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
         tg.L1 = h->Llev[1];
         tg.root_R = h->R;
         tg.root_n1 = (int)h->ncell[1];
-        launch_tc_grids(tg, s, pdl);
-        if (gfork && grid_split < h->tcg.rows) cudaStreamWaitEvent(s, h->ev_gjoin, 0);
+        launch_tc_grids(tg, s, pdl && !gjoin);
         TcArgs& ta = *h->tca;  // the current tuning: entry split and pipeline depth
         ta.tasks = h->d_tc_tasks_v[h->tc_split_v];
         ta.atomic = h->tc_split_v > 0 ? 1 : 0;
         ta.nstage = h->tc_nstage;
-        launch_m2l_tc(ta, h->tc_ntask_v[h->tc_split_v], s);
+        launch_m2l_tc(ta, h->tc_ntask_v[h->tc_split_v], s, pdl);
     } else {
         ContractArgs a = contract_args(h, OP_M2L, 2, false, h->m2l_task0);
         launch_contract(a, h->m2l_ntask, s);
