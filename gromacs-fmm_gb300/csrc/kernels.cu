@@ -82,12 +82,21 @@ __device__ __forceinline__ void tree_keys_body(const TreeArgs& a, const int bid,
     extern __shared__ float sh[];
     const int nd = 1 << a.depth;
     const StepConst* sc = a.sc;
+    static_assert(sizeof(StepConst) % 8 == 0, "copied in 8-byte words");
+    if (a.sc_copy && bid == 0) {
+        // the constants where the host wrote them (pinned memory, read in place)
+        // to the device copy that the later kernels of the step read
+        const unsigned long long* src = reinterpret_cast<const unsigned long long*>(sc);
+        unsigned long long* dst = reinterpret_cast<unsigned long long*>(a.sc_copy);
+        for (int i = threadIdx.x; i < (int)(sizeof(StepConst) / 8); i += blockDim.x) dst[i] = src[i];
+    }
     float* th = sh;                                   // 3 x (nd+1)
     float2* ce = reinterpret_cast<float2*>(sh + ((3 * (nd + 1) + 1) & ~1));  // 3 x nd
     for (int i = threadIdx.x; i < 3 * (nd + 1); i += blockDim.x) th[i] = sc->thresh[i / (nd + 1)][i % (nd + 1)];
     for (int i = threadIdx.x; i < 3 * nd; i += blockDim.x) ce[i] = sc->centre[i / nd][i % nd];
     const float inv_h = sc->inv_h;
     const float* coords = sc->coords;
+    const int ndv[3] = {sc->nd[0], sc->nd[1], sc->nd[2]};  // leaf cells per axis (nd, or nd / 2 across a slab)
     if (threadIdx.x == 0) {
         // L2 prefetch of the small operators and lists that the later stages
         // read: 4 KB chunks, spread over the blocks (one chunk list per array)
@@ -115,7 +124,7 @@ __device__ __forceinline__ void tree_keys_body(const TreeArgs& a, const int bid,
         float u[3];
 #pragma unroll
         for (int d = 0; d < 3; d++) {
-            const int ndd = sc->nd[d];  // leaf cells along this axis (nd, or nd / 2 across a slab)
+            const int ndd = ndv[d];
             float kf = fminf(fmaxf(x[d] * inv_h, 0.0f), (float)(ndd - 1));
             int k = (int)kf;
             const float* T = th + d * (nd + 1);

@@ -79,7 +79,8 @@ struct StepConst {
 };
 
 struct TreeArgs {
-    const StepConst* sc;
+    const StepConst* sc;    // this step's constants (device memory, or pinned host memory read in place)
+    StepConst* sc_copy = nullptr;  // when set, block 0 copies *sc here for the step's later kernels
     const float* charges;   // N, input order
     int n;
     int depth;

@@ -150,7 +150,8 @@ struct gbfmm_handle {
     // the deep levels' bf16 grids convert beside the upper-tree kernel
     cudaStream_t stream_g = nullptr;
     cudaEvent_t ev_gfork = nullptr, ev_gjoin = nullptr;
-    cudaEvent_t ev_sc = nullptr;  // the step's copy of h_sc has been made (h_sc may be rewritten)
+    cudaEvent_t ev_sc = nullptr;  // the step's tree keys have read h_sc (it may be rewritten)
+    cudaEvent_t ev_tk = nullptr;  // after the tree keys (the branch that records ev_sc)
     // host state
     std::vector<float> h_q;
     bool have_charges = false, have_result = false, results_on_host = false;
@@ -301,6 +302,7 @@ static void free_handle(gbfmm_handle* h)
     if (h->ev_gfork) cudaEventDestroy(h->ev_gfork);
     if (h->ev_gjoin) cudaEventDestroy(h->ev_gjoin);
     if (h->ev_sc) cudaEventDestroy(h->ev_sc);
+    if (h->ev_tk) cudaEventDestroy(h->ev_tk);
     if (h->ev_join) cudaEventDestroy(h->ev_join);
     delete h;
 }
@@ -657,7 +659,8 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
     int* sync = h->d_counts + h->nleaf + 1;  // [0] tree keys, [1] finalize, [2] P2P queue, [3] upper tree
     {
         TreeArgs ta;
-        ta.sc = h->d_sc;
+        ta.sc = h->h_sc;  // read in place (pinned host memory): no copy node ahead of the tree
+        ta.sc_copy = h->d_sc;
         ta.charges = h->d_q;
         ta.n = n;
         ta.depth = D;
@@ -692,6 +695,19 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
         pf(h->d_entries, h->tasks_bytes);
         pf(h->d_p2p_st, sizeof(int) * 3 * h->n_p2p_st);
         launch_tree_keys(ta, s);
+        // h_sc may be rewritten once the tree keys have read it: ev_sc (set_box waits
+        // on it), recorded on the near-field stream's branch when there is one, so
+        // that the next kernel on s still follows the tree keys directly
+        cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+        cudaStreamIsCapturing(s, &cap);
+        const unsigned ev_flags = cap == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
+        if ((mode & STEP_NEAR) && !h->timing) {
+            cudaEventRecord(h->ev_tk, s);
+            cudaStreamWaitEvent(h->stream_nf, h->ev_tk, 0);
+            cudaEventRecordWithFlags(h->ev_sc, h->stream_nf, ev_flags);
+        } else {
+            cudaEventRecordWithFlags(h->ev_sc, s, ev_flags);
+        }
         if (!ta.off) launch_exclusive_scan(h->d_counts, h->d_off, h->nleaf, h->d_scan, s);
     }
     launch_scatter_ranked(h->d_code, n, h->d_off, h->d_inv, h->d_tmp, s, pdl);
@@ -927,6 +943,7 @@ extern "C" int gbfmm_create(const gbfmm_params* prm, int natoms, gbfmm_handle** 
             cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
             cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess ||
             cudaEventCreateWithFlags(&h->ev_sc, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&h->ev_tk, cudaEventDisableTiming) != cudaSuccess ||
             cudaStreamCreateWithPriority(&h->stream_g, cudaStreamNonBlocking, hi) != cudaSuccess ||
             cudaEventCreateWithFlags(&h->ev_gfork, cudaEventDisableTiming) != cudaSuccess ||
             cudaEventCreateWithFlags(&h->ev_gjoin, cudaEventDisableTiming) != cudaSuccess)
@@ -1051,8 +1068,8 @@ static int set_box(gbfmm_handle* h, const float* box, const float* d_coords, boo
     const double C = h->aspect_z == 2 ? 2.0 * a : a;  // edge of the root cube
     const double E[3] = {a, a, C};                    // the box's extents
     const int D = h->D, nd = 1 << D;
-    // the previous step's copy of the constants must have been made before they
-    // are rewritten (it runs first in that step, so this rarely waits)
+    // the previous step's tree keys must have read the constants before they are
+    // rewritten (that kernel runs first in the step, so this rarely waits)
     if (h->ev_sc) cudaEventSynchronize(h->ev_sc);
     StepConst* sc = h->h_sc;
     sc->coords = d_coords;
@@ -1091,23 +1108,17 @@ static int set_box(gbfmm_handle* h, const float* box, const float* d_coords, boo
 
 static bool graph_mode(const gbfmm_handle* h) { return !(h->prm.flags & GBFMM_FLAG_NO_GRAPH) && !h->timing; }
 
-// One step: the upload of the step constants (the first node of the graph, then
-// an event that set_box waits on) and enqueue_step.  In graph mode the graph is
-// launched on 'launch' when on_launch is set (any stream, the legacy default
-// stream 0 included), else on the handle's stream.
+// One step (enqueue_step: its first kernel reads the step constants from the
+// pinned host copy that set_box wrote).  In graph mode the graph is launched on
+// 'launch' when on_launch is set (any stream, the legacy default stream 0
+// included), else on the handle's stream.
 static int run_step(gbfmm_handle* h, cudaStream_t launch = nullptr, bool on_launch = false)
 {
     const bool use_graph = graph_mode(h);
-    auto upload = [h, use_graph]() {
-        cudaMemcpyAsync(h->d_sc, h->h_sc, sizeof(StepConst), cudaMemcpyHostToDevice, h->stream);
-        // inside the capture: an event-record node of the graph
-        cudaEventRecordWithFlags(h->ev_sc, h->stream, use_graph ? cudaEventRecordExternal : cudaEventRecordDefault);
-    };
     if (use_graph) {
         if (!h->gexec) {
             cudaGraph_t g = nullptr;
             CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-            upload();
             enqueue_step(h);
             cudaError_t e = cudaStreamEndCapture(h->stream, &g);
             if (e != cudaSuccess) return fail(GBFMM_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
@@ -1117,7 +1128,6 @@ static int run_step(gbfmm_handle* h, cudaStream_t launch = nullptr, bool on_laun
         }
         CK(cudaGraphLaunch(h->gexec, on_launch ? launch : h->stream));
     } else {
-        upload();
         enqueue_step(h);
         CK(cudaGetLastError());
     }

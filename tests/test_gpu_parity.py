@@ -251,6 +251,40 @@ def test_graph_replay_follows_new_box_and_coords(pkg, oracle, systems):
     s.close()
 
 
+def test_back_to_back_steps_each_see_their_own_box(pkg, systems):
+    """Device steps queued without a host synchronisation between them, the box
+    and coordinates alternating: the tree kernel of each step reads that step's
+    constants (written by the host into pinned memory that the next call rewrites
+    once the previous step's tree kernel has read it), so every step gives the
+    bits of a separate solve of its own configuration."""
+    torch = pytest.importorskip("torch")
+    xyz, q, box = systems.water_ion_box(3000, 3.0, seed=23)
+    L1 = float(box[0])
+    xyz2 = (xyz * np.float32(1.05)).astype(np.float32)
+    L2 = float(np.float32(L1 * 1.05))
+    cfgs = [(xyz, L1), (xyz2, L2)]
+    ref = []
+    for x, L in cfgs:
+        r = pkg.ZetaFmmSolver(len(q), q, order=5, max_depth=3, images=4, precision=1, flags=pkg.FLAG_DETERMINISTIC)
+        r.execute(x, L)
+        ref.append(r.forces())
+        r.close()
+    s = pkg.ZetaFmmSolver(len(q), q, order=5, max_depth=3, images=4, precision=1, flags=pkg.FLAG_DETERMINISTIC)
+    xd = [torch.from_numpy(x).cuda() for x, _ in cfgs]
+    torch.cuda.synchronize()
+    st = torch.cuda.Stream()
+    outs = []
+    with torch.cuda.stream(st):
+        for k in range(6):
+            s.execute_device(xd[k % 2].data_ptr(), cfgs[k % 2][1], st.cuda_stream)
+            fp, _, _ = s.device_outputs()
+            outs.append(torch.as_tensor(_CudaView(fp, (len(q), 3)), device="cuda").clone())
+    st.synchronize()
+    for k, f in enumerate(outs):
+        assert np.array_equal(f.cpu().numpy(), ref[k % 2]), k
+    s.close()
+
+
 def test_nonfinite_input_reports_error_and_recovers(pkg, systems):
     xyz, q, box = systems.water_ion_box(300, 2.0, seed=15)
     s = pkg.ZetaFmmSolver(len(q), q, order=4, max_depth=2, images=4)
