@@ -84,8 +84,8 @@ __device__ __forceinline__ void tree_keys_body(const TreeArgs& a, const int bid,
     const StepConst* sc = a.sc;
     static_assert(sizeof(StepConst) % 8 == 0, "copied in 8-byte words");
     if (a.sc_copy && bid == 0) {
-        // the constants where the host wrote them (pinned memory, read in place)
-        // to the device copy that the later kernels of the step read
+        // the constants (a kernel parameter) to the device copy that the later
+        // kernels of the step read
         const unsigned long long* src = reinterpret_cast<const unsigned long long*>(sc);
         unsigned long long* dst = reinterpret_cast<unsigned long long*>(a.sc_copy);
         for (int i = threadIdx.x; i < (int)(sizeof(StepConst) / 8); i += blockDim.x) dst[i] = src[i];
@@ -237,13 +237,25 @@ __global__ void __launch_bounds__(256) k_tree_keys(TreeArgs a) { tree_keys_body(
 int tree_blocks(int n) { return n <= 0 ? 1 : (n + 255) / 256 < TREE_MAX_BLOCKS ? (n + 255) / 256 : TREE_MAX_BLOCKS; }
 int final_blocks(int n) { return n <= 0 ? 1 : (n + 255) / 256 < FINAL_MAX_BLOCKS ? (n + 255) / 256 : FINAL_MAX_BLOCKS; }
 
-void launch_tree_keys(const TreeArgs& a, cudaStream_t s)
+// The step's constants as a kernel parameter (copied with the launch, and in a
+// CUDA graph updated on the node before each launch): the kernel reads them from
+// the parameter space and block 0 stores them to a.sc_copy for the later kernels.
+__global__ void __launch_bounds__(256) k_tree_keys_sc(TreeArgs a, const __grid_constant__ StepConst sc)
+{
+    a.sc = &sc;
+    tree_keys_body(a, blockIdx.x, gridDim.x);
+}
+
+const void* tree_keys_sc_kernel() { return reinterpret_cast<const void*>(&k_tree_keys_sc); }
+
+void launch_tree_keys(const TreeArgs& a, cudaStream_t s, const StepConst* by_value)
 {
     int nd = 1 << a.depth;
     size_t shm = sizeof(float) * (((3 * (nd + 1) + 1) & ~1) + 6 * nd);
     int blocks = tree_blocks(a.n);
     COUNT_LAUNCH();
-    k_tree_keys<<<blocks, 256, shm, s>>>(a);
+    if (by_value) k_tree_keys_sc<<<blocks, 256, shm, s>>>(a, *by_value);
+    else k_tree_keys<<<blocks, 256, shm, s>>>(a);
 }
 
 // Exclusive scan of n ints (out[n] = total), three phases of 2048-element blocks.

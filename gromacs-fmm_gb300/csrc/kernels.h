@@ -79,7 +79,7 @@ struct StepConst {
 };
 
 struct TreeArgs {
-    const StepConst* sc;    // this step's constants (device memory, or pinned host memory read in place)
+    const StepConst* sc;    // this step's constants (device memory, or the by-value launch's parameter)
     StepConst* sc_copy = nullptr;  // when set, block 0 copies *sc here for the step's later kernels
     const float* charges;   // N, input order
     int n;
@@ -168,7 +168,10 @@ extern std::atomic<long> g_kernel_launches;
 // cached per device).
 int sm_count();
 
-void launch_tree_keys(const TreeArgs& a, cudaStream_t s);
+// by_value: the step's constants travel as a parameter of the launch (a.sc is
+// ignored; a.sc_copy receives them); else the kernel reads them at a.sc.
+void launch_tree_keys(const TreeArgs& a, cudaStream_t s, const StepConst* by_value = nullptr);
+const void* tree_keys_sc_kernel();  // the by-value kernel (to find its node in a captured graph)
 void launch_exclusive_scan(const int* in, int* out, int n, int* scratch, cudaStream_t s);
 void launch_scatter(const uint32_t* code, int n, int* cursor, int* tmp_idx, cudaStream_t s);
 // The same without atomics: tmp_idx[off[code[i]] + rank[i]] = i (TreeArgs::rank).

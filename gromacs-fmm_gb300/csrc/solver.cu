@@ -150,8 +150,12 @@ struct gbfmm_handle {
     // the deep levels' bf16 grids convert beside the upper-tree kernel
     cudaStream_t stream_g = nullptr;
     cudaEvent_t ev_gfork = nullptr, ev_gjoin = nullptr;
-    cudaEvent_t ev_sc = nullptr;  // the step's tree keys have read h_sc (it may be rewritten)
-    cudaEvent_t ev_tk = nullptr;  // after the tree keys (the branch that records ev_sc)
+    // the tree-key node of the captured graph (its parameters carry the step's
+    // constants) and the arguments it was captured with
+    cudaGraph_t graph = nullptr;
+    cudaGraphNode_t tk_node = nullptr;
+    cudaKernelNodeParams tk_params = {};
+    TreeArgs tk_args;
     // host state
     std::vector<float> h_q;
     bool have_charges = false, have_result = false, results_on_host = false;
@@ -278,6 +282,16 @@ const char* gbfmm_stage_name(int s) { return (s >= 0 && s < 9) ? k_stage_names[s
 
 }  // extern "C"
 
+// Destroys the step's graph (it is captured again on the next step).
+static void drop_graph(gbfmm_handle* h)
+{
+    if (h->gexec) cudaGraphExecDestroy(h->gexec);
+    if (h->graph) cudaGraphDestroy(h->graph);
+    h->gexec = nullptr;
+    h->graph = nullptr;
+    h->tk_node = nullptr;
+}
+
 static void free_handle(gbfmm_handle* h)
 {
     if (!h) return;
@@ -285,7 +299,7 @@ static void free_handle(gbfmm_handle* h)
         h->tca->~TcArgs();
         free(h->tca);
     }
-    if (h->gexec) cudaGraphExecDestroy(h->gexec);
+    drop_graph(h);
     for (int i = 0; i < 16; i++)
         if (h->ev[i]) cudaEventDestroy(h->ev[i]);
     if (h->arena) cudaFree(h->arena);
@@ -301,8 +315,6 @@ static void free_handle(gbfmm_handle* h)
     if (h->stream_g) cudaStreamDestroy(h->stream_g);
     if (h->ev_gfork) cudaEventDestroy(h->ev_gfork);
     if (h->ev_gjoin) cudaEventDestroy(h->ev_gjoin);
-    if (h->ev_sc) cudaEventDestroy(h->ev_sc);
-    if (h->ev_tk) cudaEventDestroy(h->ev_tk);
     if (h->ev_join) cudaEventDestroy(h->ev_join);
     delete h;
 }
@@ -659,7 +671,7 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
     int* sync = h->d_counts + h->nleaf + 1;  // [0] tree keys, [1] finalize, [2] P2P queue, [3] upper tree
     {
         TreeArgs ta;
-        ta.sc = h->h_sc;  // read in place (pinned host memory): no copy node ahead of the tree
+        ta.sc = nullptr;  // the constants travel with the launch (no copy node ahead of the tree)
         ta.sc_copy = h->d_sc;
         ta.charges = h->d_q;
         ta.n = n;
@@ -694,20 +706,10 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
         pf(h->d_l2l_t, sizeof(float) * t->l2l_t.size());
         pf(h->d_entries, h->tasks_bytes);
         pf(h->d_p2p_st, sizeof(int) * 3 * h->n_p2p_st);
-        launch_tree_keys(ta, s);
-        // h_sc may be rewritten once the tree keys have read it: ev_sc (set_box waits
-        // on it), recorded on the near-field stream's branch when there is one, so
-        // that the next kernel on s still follows the tree keys directly
-        cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-        cudaStreamIsCapturing(s, &cap);
-        const unsigned ev_flags = cap == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
-        if ((mode & STEP_NEAR) && !h->timing) {
-            cudaEventRecord(h->ev_tk, s);
-            cudaStreamWaitEvent(h->stream_nf, h->ev_tk, 0);
-            cudaEventRecordWithFlags(h->ev_sc, h->stream_nf, ev_flags);
-        } else {
-            cudaEventRecordWithFlags(h->ev_sc, s, ev_flags);
-        }
+        // the constants are a parameter of this launch: a captured graph gets them
+        // updated on the node before each launch (run_step), from h->tk_args
+        launch_tree_keys(ta, s, h->h_sc);
+        h->tk_args = ta;
         if (!ta.off) launch_exclusive_scan(h->d_counts, h->d_off, h->nleaf, h->d_scan, s);
     }
     launch_scatter_ranked(h->d_code, n, h->d_off, h->d_inv, h->d_tmp, s, pdl);
@@ -942,8 +944,7 @@ extern "C" int gbfmm_create(const gbfmm_params* prm, int natoms, gbfmm_handle** 
             cudaStreamCreateWithPriority(&h->stream_nf, cudaStreamNonBlocking, lo) != cudaSuccess ||
             cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
             cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess ||
-            cudaEventCreateWithFlags(&h->ev_sc, cudaEventDisableTiming) != cudaSuccess ||
-            cudaEventCreateWithFlags(&h->ev_tk, cudaEventDisableTiming) != cudaSuccess ||
+
             cudaStreamCreateWithPriority(&h->stream_g, cudaStreamNonBlocking, hi) != cudaSuccess ||
             cudaEventCreateWithFlags(&h->ev_gfork, cudaEventDisableTiming) != cudaSuccess ||
             cudaEventCreateWithFlags(&h->ev_gjoin, cudaEventDisableTiming) != cudaSuccess)
@@ -1068,9 +1069,6 @@ static int set_box(gbfmm_handle* h, const float* box, const float* d_coords, boo
     const double C = h->aspect_z == 2 ? 2.0 * a : a;  // edge of the root cube
     const double E[3] = {a, a, C};                    // the box's extents
     const int D = h->D, nd = 1 << D;
-    // the previous step's tree keys must have read the constants before they are
-    // rewritten (that kernel runs first in the step, so this rarely waits)
-    if (h->ev_sc) cudaEventSynchronize(h->ev_sc);
     StepConst* sc = h->h_sc;
     sc->coords = d_coords;
     sc->out_forces = host_out ? h->h_forces : h->d_forces;
@@ -1117,14 +1115,43 @@ static int run_step(gbfmm_handle* h, cudaStream_t launch = nullptr, bool on_laun
     const bool use_graph = graph_mode(h);
     if (use_graph) {
         if (!h->gexec) {
+            drop_graph(h);
             cudaGraph_t g = nullptr;
             CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
             enqueue_step(h);
             cudaError_t e = cudaStreamEndCapture(h->stream, &g);
             if (e != cudaSuccess) return fail(GBFMM_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
             e = cudaGraphInstantiate(&h->gexec, g, cudaGraphInstantiateFlagUseNodePriority);
-            cudaGraphDestroy(g);
-            if (e != cudaSuccess) return fail(GBFMM_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+            if (e != cudaSuccess) {
+                cudaGraphDestroy(g);
+                return fail(GBFMM_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+            }
+            h->graph = g;  // kept: its tree-key node is updated before each launch
+            size_t nn = 0;
+            CK(cudaGraphGetNodes(g, nullptr, &nn));
+            std::vector<cudaGraphNode_t> nodes(nn);
+            CK(cudaGraphGetNodes(g, nodes.data(), &nn));
+            for (cudaGraphNode_t node : nodes) {
+                cudaGraphNodeType type;
+                cudaKernelNodeParams p;
+                if (cudaGraphNodeGetType(node, &type) == cudaSuccess && type == cudaGraphNodeTypeKernel &&
+                    cudaGraphKernelNodeGetParams(node, &p) == cudaSuccess && p.func == tree_keys_sc_kernel()) {
+                    h->tk_node = node;
+                    h->tk_params = p;
+                    break;
+                }
+            }
+            if (!h->tk_node) {
+                drop_graph(h);
+                return fail(GBFMM_ERR_CUDA, "graph capture: no tree-key node");
+            }
+        } else {
+            // this step's constants into the tree-key node (copied by the call)
+            void* args[2] = {&h->tk_args, h->h_sc};
+            cudaKernelNodeParams p = h->tk_params;
+            p.kernelParams = args;
+            p.extra = nullptr;
+            CK(cudaGraphExecKernelNodeSetParams(h->gexec, h->tk_node, &p));
         }
         CK(cudaGraphLaunch(h->gexec, on_launch ? launch : h->stream));
     } else {
@@ -1255,10 +1282,7 @@ static void apply_tuning(gbfmm_handle* h, int p2p_variant, int split_v, int nsta
     h->p2p_variant = p2p_variant;
     h->tc_split_v = split_v;
     h->tc_nstage = nstage;
-    if (h->gexec) {
-        cudaGraphExecDestroy(h->gexec);
-        h->gexec = nullptr;
-    }
+    drop_graph(h);
 }
 
 extern "C" int gbfmm_set_tuning(gbfmm_handle* h, int p2p_variant, int m2l_split, int m2l_stages)
@@ -1287,10 +1311,7 @@ extern "C" int gbfmm_set_near_start(gbfmm_handle* h, int after)
     if (after < 0 || after > 2) return fail(GBFMM_ERR_ARG, "near-field start %d outside [0,2]", after);
     CK(cudaStreamSynchronize(h->stream));
     h->near_after = after;
-    if (h->gexec) {
-        cudaGraphExecDestroy(h->gexec);
-        h->gexec = nullptr;
-    }
+    drop_graph(h);
     return GBFMM_OK;
 }
 
@@ -1306,10 +1327,7 @@ extern "C" int gbfmm_set_launch_overlap(gbfmm_handle* h, int enable)
     if (!h) return fail(GBFMM_ERR_ARG, "handle is NULL");
     CK(cudaStreamSynchronize(h->stream));
     h->pdl = enable != 0;
-    if (h->gexec) {
-        cudaGraphExecDestroy(h->gexec);
-        h->gexec = nullptr;
-    }
+    drop_graph(h);
     return GBFMM_OK;
 }
 
