@@ -43,38 +43,35 @@ int sm_count()
 
 // ------------------------------------------------------------------ tree
 
-// FP64 sum of per-block partials held as FP32 pairs (hi, lo) at part[stride * b]
-// for b < nblocks, by one warp: every load issued first (one round trip), each
-// pair made exact in FP64, the lane's blocks added by a fixed pairwise tree, then
-// a butterfly (FP64 addition commutes, so every lane ends with the same sum).
-// The final reductions of the step (energy, dipole, total charge) are FP64.
-__device__ __forceinline__ double sum_partials_f64(const float2* part, int stride, int nblocks)
+// Sum of per-block partials held as FP32 pairs (hi, lo) at part[stride * b] for
+// b < nblocks, by one warp, in FP32-pair arithmetic (about 48 bits, the precision
+// of the partials themselves): every load issued first (one round trip), each
+// lane's blocks added in block order, then the fixed butterfly of f2s_warp_sum
+// (every lane ends with the same sum), returned as an FP64 number.  Not FP64: an
+// SM of this GPU retires two FP64 lanes per clock, and an FP64 sum of a few
+// hundred partials by one CTA took microseconds on the step's serial path.
+__device__ __forceinline__ double sum_partials(const float2* part, int stride, int nblocks)
 {
-    static_assert(TREE_MAX_BLOCKS == FINAL_MAX_BLOCKS, "one tree shape for both reductions");
-    constexpr int K = (TREE_MAX_BLOCKS + 31) / 32, K2 = K <= 16 ? 16 : 32;
+    static_assert(TREE_MAX_BLOCKS == FINAL_MAX_BLOCKS, "one shape for both reductions");
+    constexpr int K = (TREE_MAX_BLOCKS + 31) / 32;
     const int lane = threadIdx.x & 31;
-    double v[K2];
+    float2 p[K];
 #pragma unroll
-    for (int k = 0; k < K2; k++) {
+    for (int k = 0; k < K; k++) {
         const int b = lane + 32 * k;
-        const float2 p = (k < K && b < nblocks) ? __ldcg(&part[(size_t)stride * b]) : make_float2(0.f, 0.f);
-        v[k] = (double)p.x + (double)p.y;
+        p[k] = b < nblocks ? __ldcg(&part[(size_t)stride * b]) : make_float2(0.f, 0.f);
     }
+    f2sum t = {p[0].x, p[0].y};
 #pragma unroll
-    for (int w = K2 / 2; w >= 1; w >>= 1)
-#pragma unroll
-        for (int k = 0; k < w; k++) v[k] = v[k] + v[k + w];
-    double t = v[0];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-    return t;
+    for (int k = 1; k < K; k++) t = f2s_add(t, f2sum{p[k].x, p[k].y});
+    return f2s_value(f2s_warp_sum(t));
 }
 
 // Sum over the tree-key blocks of one of the four per-block partials (dipole x, y,
-// z, total charge; FP32 pairs), in FP64 (sum_partials_f64).
+// z, total charge; FP32 pairs), by sum_partials.
 __device__ __forceinline__ double sum_tree_partials(const double* partials, int nblocks, int quantity)
 {
-    return sum_partials_f64(reinterpret_cast<const float2*>(partials) + quantity, 4, nblocks);
+    return sum_partials(reinterpret_cast<const float2*>(partials) + quantity, 4, nblocks);
 }
 
 __device__ __forceinline__ void tree_keys_body(const TreeArgs& a, const int bid, const int nb)
@@ -1824,11 +1821,13 @@ __device__ __forceinline__ void top_body(const TopArgs& a, const int bid, const 
             // the root cube holds 'copies' copies of the box, whose dipole about
             // the root centre is copies x (box dipole about the box centre)
             const StepConst* sc = a.root.sc;
-            const double Q = sums[3], L = sc->box_len, k = (double)sc->copies;
+            // (divisions by the root edge as products with its host-computed
+            // reciprocal: an FP64 division is a long dependent chain here)
+            const double Q = sums[3], iL = sc->inv_box_len, k = (double)sc->copies;
             if (r == 0) s = k * Q;
-            else if (r == 1) s = -k * (sums[2] - Q * sc->box_centre[2]) / L;
-            else if (r == 2) s = k * (sums[0] - Q * sc->box_centre[0]) / (2.0 * L);
-            else s = -k * (sums[1] - Q * sc->box_centre[1]) / (2.0 * L);
+            else if (r == 1) s = -k * (sums[2] - Q * sc->box_centre[2]) * iL;
+            else if (r == 2) s = k * (sums[0] - Q * sc->box_centre[0]) * (0.5 * iL);
+            else s = -k * (sums[1] - Q * sc->box_centre[1]) * (0.5 * iL);
         }
         M0s[r] = s;
         a.root.M0[r] = s;
@@ -1841,7 +1840,7 @@ __device__ __forceinline__ void top_body(const TopArgs& a, const int bid, const 
         a.fconst[0] = (float)(cK * M0);
         a.fconst[1] = (float)(cK * M1);
         a.fconst[2] = (float)(cK * M2);
-        a.fconst[3] = (float)(cK * (M0 * M0 + M1 * M1 + M2 * M2) / (double)max(a.natoms, 1));
+        a.fconst[3] = (float)(cK * (M0 * M0 + M1 * M1 + M2 * M2) * a.inv_natoms);
     }
     __syncthreads();
     if (!a.lattice) return;
@@ -1957,7 +1956,7 @@ __device__ __forceinline__ void finalize_body(const FinalArgs& a, const int bid,
         if (a.zero_after) *a.zero_after = 0;
     }
     // the energy: the blocks' FP32-pair partials summed in FP64
-    const double t = sum_partials_f64(reinterpret_cast<const float2*>(a.partials), 1, (int)nb);
+    const double t = sum_partials(reinterpret_cast<const float2*>(a.partials), 1, (int)nb);
     if (threadIdx.x == 0) {
         *a.sc->out_energy = t;
         int* fl = a.sc->out_flags;

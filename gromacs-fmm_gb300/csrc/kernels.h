@@ -71,6 +71,7 @@ struct StepConst {
     int copies;                          // copies of the box in the root cube (1 cubic, 4 slab)
     double coef;                         // 4 pi / (3 V), dipole correction (V: box volume)
     double box_len;                      // C, the edge of the root cube (nm): the period of a cubic box
+    double inv_box_len;                  // 1 / C
     double box_centre[3];                // centre of the box (nm)
     int nd[3];                           // leaf cells per axis of the stored grid
     int pad_;
@@ -286,7 +287,7 @@ struct TopArgs {
     int tree_nblocks;
     double* sums;         // out: dipole (3) and total charge, FP64
     float* fconst;        // out: FP32 dipole-correction constants of the finalize (4)
-    int natoms;
+    double inv_natoms;    // 1 / max(atoms, 1)
     int* done;            // zero at launch
     int* err;             // bit 1: the bounded wait for the staged copies gave up
     // CTA g < root.n1 owns stored level-1 cell g and the root-M2M shares of the

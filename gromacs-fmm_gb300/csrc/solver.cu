@@ -789,7 +789,7 @@ static void enqueue_step(gbfmm_handle* h, int mode = STEP_NEAR | STEP_FINAL, cud
     top.tree_nblocks = tree_blocks(h->n);
     top.sums = h->d_sums;
     top.fconst = h->d_fconst;
-    top.natoms = h->n;
+    top.inv_natoms = 1.0 / std::max(h->n, 1);
     top.done = sync + 3;
     top.err = h->d_flags + 2;
     top.umask = (h->shift[0] == 0 ? 4 : 0) | (h->shift[1] == 0 ? 2 : 0) | (h->shift[2] == 0 ? 1 : 0);
@@ -1078,6 +1078,7 @@ static int set_box(gbfmm_handle* h, const float* box, const float* d_coords, boo
     sc->inv_h = (float)(nd / C);
     sc->coef = 4.0 * M_PI / (3.0 * E[0] * E[1] * E[2]);
     sc->box_len = C;
+    sc->inv_box_len = 1.0 / C;
     sc->copies = h->aspect_z == 2 ? 4 : 1;
     for (int d = 0; d < 3; d++) {
         const int n = grid_n(D, h->shift[d]);
@@ -2149,7 +2150,7 @@ static void describe_step(gbfmm_handle* h, StepDesc& d)
     top.tree_nblocks = tree_blocks(h->n);
     top.sums = h->d_sums;
     top.fconst = h->d_fconst;
-    top.natoms = h->n;
+    top.inv_natoms = 1.0 / std::max(h->n, 1);
     top.done = sync + 3;
     top.err = h->d_flags + 2;
     top.umask = (h->shift[0] == 0 ? 4 : 0) | (h->shift[1] == 0 ? 2 : 0) | (h->shift[2] == 0 ? 1 : 0);

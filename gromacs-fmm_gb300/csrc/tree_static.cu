@@ -143,6 +143,7 @@ extern "C" int gbfmm_tree_build_noalloc(const void* d_coords, const void* d_char
     sc.inv_h = (float)(nd / L);
     sc.coef = 4.0 * M_PI / (3.0 * L * L * L);
     sc.box_len = L;
+    sc.inv_box_len = 1.0 / L;
     sc.copies = 1;
     for (int d = 0; d < 3; d++) {
         sc.nd[d] = nd;
