@@ -1926,7 +1926,7 @@ __device__ __forceinline__ void finalize_body(const FinalArgs& a, const int bid,
         forces[3 * o + 1] = qk * gy + q * fM1;
         forces[3 * o + 2] = qk * gz + q * fM2;
         // FP32 per body (no FP64 division); the exact products of the energy are
-        // summed per block as FP32 pairs, and the blocks in FP64
+        // summed as FP32 pairs, per block and then over the blocks
         float pot = phi * (float)KE;
         if (q != 0.f) pot -= corr_f / q;
         pots[o] = pot;
@@ -1955,7 +1955,7 @@ __device__ __forceinline__ void finalize_body(const FinalArgs& a, const int bid,
         *a.done = 0;
         if (a.zero_after) *a.zero_after = 0;
     }
-    // the energy: the blocks' FP32-pair partials summed in FP64
+    // the energy: the blocks' FP32-pair partials summed in FP32 pairs (sum_partials)
     const double t = sum_partials(reinterpret_cast<const float2*>(a.partials), 1, (int)nb);
     if (threadIdx.x == 0) {
         *a.sc->out_energy = t;
