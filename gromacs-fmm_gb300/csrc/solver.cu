@@ -1389,32 +1389,37 @@ extern "C" int gbfmm_autotune(gbfmm_handle* h, const float* coords, const float*
     };
     int bp = h->p2p_variant, bs = h->tc_split_v, bn = h->tc_nstage;
     float bt = measure(bp, bs, bn);
-    // coordinate search: P2P shape, then M2L split, then M2L pipeline depth
-    for (int pv = 0; pv < p2p_variants() && !err; pv++) {
-        if (pv == bp) continue;
-        const float t = measure(pv, bs, bn);
-        if (t < bt) { bt = t; bp = pv; }
-    }
-    if (h->tc) {
-        for (int sv = 0; sv < TC_NSPLIT && !err; sv++) {
-            if (sv == bs || h->tc_ntask_v[sv] == 0) continue;
-            const float t = measure(bp, sv, bn);
-            if (t < bt) { bt = t; bs = sv; }
+    auto search_p2p = [&]() {
+        for (int pv = 0; pv < p2p_variants() && !err; pv++) {
+            if (pv == bp) continue;
+            const float t = measure(pv, bs, bn);
+            if (t < bt) { bt = t; bp = pv; }
         }
+    };
+    // M2L entry split and pipeline depth together (each split with every depth
+    // candidate: the best depth depends on how many CTAs the split makes)
+    auto search_m2l = [&]() {
+        if (!h->tc) return;
         const TcPlan& pl = h->tab->tc;
-        // one stage: the most CTAs (and entries in flight) per SM
         const int gs = h->tca->group;
-        const int cand[4] = {1, 2, std::max(1, tc_pick_stages(pl.k_atoms, pl.img_bytes, h->tca->nprod) / gs),
-                             std::max(1, tc_max_stages(pl.k_atoms, pl.img_bytes, h->tca->nprod) / gs)};
-        for (int c = 0; c < 4 && !err; c++) {
-            const int ns = std::min(cand[c], cand[3]);
-            if (ns == bn || ns < 1) continue;
-            const float t = measure(bp, bs, ns);
-            if (t < bt) { bt = t; bn = ns; }
+        const int mx = std::max(1, tc_max_stages(pl.k_atoms, pl.img_bytes, h->tca->nprod) / gs);
+        // one stage: the most CTAs (and entries in flight) per SM
+        const int cand[4] = {1, 2, std::max(1, tc_pick_stages(pl.k_atoms, pl.img_bytes, h->tca->nprod) / gs), mx};
+        for (int sv = 0; sv < TC_NSPLIT && !err; sv++) {
+            if (h->tc_ntask_v[sv] == 0) continue;
+            for (int c = 0; c < 4 && !err; c++) {
+                const int ns = std::min(cand[c], mx);
+                if (ns < 1 || (sv == bs && ns == bn)) continue;
+                bool dup = false;  // a depth already measured for this split
+                for (int d = 0; d < c; d++) dup |= std::min(cand[d], mx) == ns;
+                if (dup) continue;
+                const float t = measure(bp, sv, ns);
+                if (t < bt) { bt = t; bs = sv; bn = ns; }
+            }
         }
-    }
+    };
     // where the near field starts in the graph (after the tree, the P2M or the upper tree)
-    {
+    auto search_near = [&]() {
         int ba = h->near_after;
         for (int na = 0; na <= 2 && !err; na++) {
             if (na == ba) continue;
@@ -1423,7 +1428,14 @@ extern "C" int gbfmm_autotune(gbfmm_handle* h, const float* coords, const float*
             if (t < bt) { bt = t; ba = na; }
         }
         h->near_after = ba;
-    }
+    };
+    // coordinate search: P2P shape, the M2L (split x depth), the near field's start,
+    // then the M2L and the P2P shape again at that start
+    search_p2p();
+    search_m2l();
+    search_near();
+    search_m2l();
+    search_p2p();
     for (int i = 0; i < reps; i++) {
         cudaEventDestroy(e0[i]);
         cudaEventDestroy(e1[i]);

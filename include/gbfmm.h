@@ -278,8 +278,10 @@ int gbfmm_debug_bounded_wait(unsigned polls, void* stream);
  * 4 x 8 or 16 x 2 by variant % 3, one CTA per leaf or 2-5 resident CTAs per SM
  * by variant / 3; 15-16: 8 x 4 and 4 x 8 with up to 4 targets per thread, one
  * CTA per leaf) and, on the tensor-core
- * path, the M2L entry split (1, 2, 4, 8; 1 only on a deterministic handle) and
- * pipeline depth, and keeps the fastest (best_ms: its step time; may be NULL).
+ * path, the M2L entry split (1, 2, 4, 8; 1 only on a deterministic handle)
+ * together with the pipeline depth, then where the near field starts
+ * (gbfmm_set_near_start), then the split, depth and P2P variant again at that
+ * start, and keeps the fastest (best_ms: its step time; may be NULL).
  * Results are the same up to the order of floating-point additions.  No
  * reference counterpart: the reference's launch shapes are fixed
  * (gpu_solver.cu:221-248). */
@@ -288,7 +290,7 @@ int gbfmm_autotune(gbfmm_handle* h, const float* coords, const float* box, int r
  * default), after the P2M (1) or after the upper tree (2).  The near field runs
  * on a low-priority stream beside the far-field chain either way; starting it
  * later lets the far-field kernels with large shared memory take SMs before its
- * CTAs fill them.  Results do not depend on it; gbfmm_autotune searches it last. */
+ * CTAs fill them.  Results do not depend on it; gbfmm_autotune searches it. */
 int gbfmm_set_near_start(gbfmm_handle* h, int after);
 int gbfmm_get_near_start(gbfmm_handle* h, int* after);
 /* Programmatic dependent launches in the step (on by default): each kernel of the
