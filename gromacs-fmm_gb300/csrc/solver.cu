@@ -156,6 +156,7 @@ struct gbfmm_handle {
     cudaGraphNode_t tk_node = nullptr;
     cudaKernelNodeParams tk_params = {};
     TreeArgs tk_args;
+    StepConst tk_sc;  // the constants the node holds now
     // host state
     std::vector<float> h_q;
     bool have_charges = false, have_result = false, results_on_host = false;
@@ -1139,6 +1140,7 @@ static int run_step(gbfmm_handle* h, cudaStream_t launch = nullptr, bool on_laun
                     cudaGraphKernelNodeGetParams(node, &p) == cudaSuccess && p.func == tree_keys_sc_kernel()) {
                     h->tk_node = node;
                     h->tk_params = p;
+                    h->tk_sc = *h->h_sc;  // captured with these
                     break;
                 }
             }
@@ -1146,13 +1148,15 @@ static int run_step(gbfmm_handle* h, cudaStream_t launch = nullptr, bool on_laun
                 drop_graph(h);
                 return fail(GBFMM_ERR_CUDA, "graph capture: no tree-key node");
             }
-        } else {
-            // this step's constants into the tree-key node (copied by the call)
+        } else if (std::memcmp(&h->tk_sc, h->h_sc, sizeof(StepConst)) != 0) {
+            // this step's constants into the tree-key node (copied by the call),
+            // unless the node holds them already (same box and coordinate array)
             void* args[2] = {&h->tk_args, h->h_sc};
             cudaKernelNodeParams p = h->tk_params;
             p.kernelParams = args;
             p.extra = nullptr;
             CK(cudaGraphExecKernelNodeSetParams(h->gexec, h->tk_node, &p));
+            h->tk_sc = *h->h_sc;
         }
         CK(cudaGraphLaunch(h->gexec, on_launch ? launch : h->stream));
     } else {
