@@ -4,8 +4,9 @@
 // images) -- operators, stencils, contraction task lists -- is built and uploaded
 // once at create time; device buffers are sized once (no per-step allocation,
 // unlike GPUSolver::solve, src/gromacs/zeta_fmm/gpu_solver.cu:79-98, 258-270).
-// Per step only the box-dependent constants (a few KB) are uploaded, and the
-// whole step is replayed from a captured CUDA graph.
+// Per step only the box-dependent constants (a few KB) change: they travel as a
+// parameter of the step's first kernel, and the whole step is replayed from a
+// captured CUDA graph.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -213,8 +214,8 @@ struct gbfmm_handle {
     int p2p_variant = 0;  // P2P warp-step shape (autotuned)
     int near_after = 0;   // the near field starts after the tree (0), the P2M (1) or the upper tree (2)
     bool pdl = true;      // consecutive kernels of the step's main chain launch as programmatic dependents
-    StepConst* d_sc = nullptr;
-    StepConst* h_sc = nullptr;  // pinned
+    StepConst* d_sc = nullptr;  // written by the tree-key kernel's block 0 each step
+    StepConst* h_sc = nullptr;  // this step's constants (set_box), passed by value to that kernel
     int* h_flags = nullptr;     // pinned
     // task ranges
     int m2l_task0 = 0, m2l_ntask = 0;
