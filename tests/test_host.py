@@ -216,6 +216,21 @@ def test_batch_arguments_rejected_before_device_use(pkg):
     assert lib.gbfmm_batch_autotune(None, None, None, None, 3, None) == 1
 
 
+def test_schedule_entry_points_reject_a_null_handle(pkg):
+    """The single-solve scheduling entry points check their arguments before any
+    device use: a NULL handle or output pointer is GBFMM_ERR_ARG."""
+    import ctypes
+    lib = pkg.lib()
+    v = ctypes.c_int()
+    for fn, args in (("gbfmm_set_launch_overlap", (None, 1)), ("gbfmm_get_launch_overlap", (None, ctypes.byref(v))),
+                     ("gbfmm_set_near_start", (None, 1)), ("gbfmm_get_near_start", (None, ctypes.byref(v))),
+                     ("gbfmm_set_tuning", (None, 0, 1, 2)), ("gbfmm_step_launches", (None, ctypes.byref(v))),
+                     ("gbfmm_autotune", (None, None, None, 3, None)),
+                     ("gbfmm_batch_set_schedule", (None, 1, 0, 0)),
+                     ("gbfmm_batch_step_launches", (None, ctypes.byref(v)))):
+        assert getattr(lib, fn)(*args) == 1, fn
+
+
 def test_bench_pair_count_matches_the_reference_lists(oracle, systems):
     """bench.py's P2P pair count (the unit of its roofline) equals the sum over
     the reference-ordered P2P list of |target leaf| x |source leaf|."""
