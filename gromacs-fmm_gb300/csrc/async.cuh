@@ -1,5 +1,6 @@
-// Asynchronous copies into shared memory for sm_100+: mbarrier primitives with
-// bounded waits and the bulk (TMA engine) global -> shared copy.
+// Asynchronous work for sm_100+: mbarrier primitives with bounded waits, the bulk
+// (TMA engine) global -> shared copy, and programmatic dependent launches (the
+// device-side wait and trigger, and the host launcher that requests them).
 #pragma once
 
 #include <stdint.h>
