@@ -76,3 +76,19 @@ def test_slab_box_validation(pkg):
         c.execute(x, [2.0, 2.0, 4.0])  # slab box on a cubic handle
     assert e.value.status == 2
     c.close()
+
+
+@pytest.mark.parametrize("P,depth,prec", [(5, 4, 2), (8, 3, 0)])
+def test_slab_launch_overlap_leaves_results_unchanged(pkg, P, depth, prec):
+    """Programmatic dependent launches on a slab (two stored level-1 cells, per-axis
+    grids): a deterministic handle gives the same bits with and without them."""
+    xyz, q, a = _slab(3000, 4.2, seed=61)
+    s = pkg.ZetaFmmSolver(len(q), q, aspect_z=2, order=P, max_depth=depth, images=4, precision=prec,
+                          flags=pkg.FLAG_DETERMINISTIC)
+    box = [a, a, 2 * a]
+    s.execute(xyz, box)
+    f0, p0, e0 = s.forces(), s.potentials(), s.get_energy()
+    s.set_launch_overlap(False)
+    s.execute(xyz, box)
+    assert np.array_equal(s.forces(), f0) and np.array_equal(s.potentials(), p0) and s.get_energy() == e0
+    s.close()
