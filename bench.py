@@ -442,7 +442,7 @@ def frames_line(pkg, torch, dev, systems, tuner_mod, n_frames):
     """The 250,002-atom box over a trajectory of kicked frames (sigma 0.01 nm per
     frame).  Per tolerance, the tuner proposes and checks on the first frame and
     the choice serves the following frames; every frame is checked against the
-    plain order-10, depth-5 FP32 FMM (the judge, solved on every frame anyway),
+    plain order-10, depth-5 FP32 FMM (the check solve, solved on every frame anyway),
     and a frame whose check misses the tolerance re-runs the checked choice on
     that frame (fallback to the plain FMM if nothing meets it).  On every 25th
     frame both are also held against the FP64 Ewald sum (forces on every 251st
@@ -747,7 +747,7 @@ def main():
     pkg.lib()
     run = Runner(pkg, torch, dev, xyz, q, box)
 
-    # FP64 Ewald forces on sampled atoms and the total energy: the accuracy judge
+    # FP64 Ewald forces on sampled atoms and the total energy: the accuracy reference
     # of every candidate (OpenMP on the host cores)
     from oracle import oracle as O
     O.set_threads(os.cpu_count() or 1)
@@ -765,7 +765,7 @@ def main():
 
     # tuned parameters: the learned tuner's proposal for this system (statistics
     # on the device, MLP forward on the device), checked against the plain
-    # order-10 FMM on this configuration; the plain FMM is judge and fallback
+    # order-10 FMM on this configuration; the plain FMM is check and fallback
     tuner_mod = G.load_module("tuner")
     mlp = tuner_mod.Mlp.load()
     ts = tuner_mod.TunedSolver(q, mlp, tol=TOL)

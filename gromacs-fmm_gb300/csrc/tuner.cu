@@ -735,7 +735,7 @@ extern "C" int gbfmm_tuner_choose(gbfmm_mlp* m, int natoms, const float* charges
         cudaFree(d);
         if (rc) return rc;
     }
-    // the judge: the plain order-10 FP32 FMM of this configuration
+    // the check solve: the plain order-10 FP32 FMM of this configuration
     // (of a slab the depth of a cube of four copies: the same bodies per leaf)
     const int plain_order = 10, plain_depth = gbfmm_plain_depth(feat[56] > 0.5f ? 4 * n : n);
     std::vector<float> fj, fc;
@@ -752,7 +752,7 @@ extern "C" int gbfmm_tuner_choose(gbfmm_mlp* m, int natoms, const float* charges
         out->pred_rel_force_err = pe;
         out->pred_ms = pm;
         // the proposal, then up to two higher orders at the same depth and
-        // precision; each one is checked against the judge
+        // precision; each one is checked against the check solve
         for (int P = P0; P <= std::min(P0 + 2, plain_order); P++) {
             rc = solve_forces(n, charges, coords, box, P, D, prec, images, fc);
             if (rc) return rc;
@@ -767,7 +767,7 @@ extern "C" int gbfmm_tuner_choose(gbfmm_mlp* m, int natoms, const float* charges
                 out->diff_vs_plain = diff;
                 // the network's error model is conservative where it has seen
                 // few systems like this one: a lower order whose measured
-                // difference from the judge stays within tol / margin is cheaper
+                // difference from the check solve stays within tol / margin is cheaper
                 // at the same depth and precision
                 if (P == P0)
                     for (int Q = P - 1; Q >= 4 && out->nchecks < GBFMM_TUNER_MAX_CHECKS; Q--) {

@@ -6,7 +6,7 @@ are the library's own (gbfmm_mlp_*), and the proposal (gbfmm_tuner_propose).
 
 `TunedSolver` checks every proposal through the library's gbfmm_tuner_choose:
 it solves the system once with the proposal and once with the plain
-fixed-parameter FMM (order 10, the judge) and keeps the proposal only if their
+fixed-parameter FMM (order 10, the check solve) and keeps the proposal only if their
 forces agree within the tolerance (retrying one and two orders higher);
 otherwise it falls back to the plain FMM.  Nothing here uses an FP64
 reference: training tuples come from tests/golden/make_tuner_data.py.
@@ -216,7 +216,7 @@ def plain_depth(natoms):
 
 class TunedSolver:
     """Solves a system with the MLP-proposed parameters, checked against the
-    plain fixed-parameter FMM (judge and fallback) whenever a proposal is made."""
+    plain fixed-parameter FMM (check and fallback) whenever a proposal is made."""
 
     def __init__(self, charges, mlp, tol=1e-3, margin=1.5, images=4):
         self.q = _f(charges)

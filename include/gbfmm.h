@@ -215,9 +215,9 @@ int gbfmm_plain_depth(int natoms);
  * depth 3, zeta_fmm_solver.cpp:10-11): statistics of the system on the device,
  * the network's proposal for 'tol' (gbfmm_tuner_propose with 'margin'), then a
  * check of the proposal's forces against the plain order-10 FP32 FMM of the
- * same configuration (the judge), retried at one and two orders higher; an
+ * same configuration (the check solve), retried at one and two orders higher; an
  * accepted order is refined downwards (one order lower at the same depth and
- * precision, while the judge's difference stays within tol / margin, down to
+ * precision, while the difference from the check solve stays within tol / margin, down to
  * order 4); when no candidate meets tol, or none is proposed, the plain FMM's
  * parameters are chosen (fallback = 1).  Host inputs; each solve runs through
  * gbfmm_execute. */
@@ -225,7 +225,7 @@ int gbfmm_plain_depth(int natoms);
 typedef struct {
     int order, depth, precision;  /* the choice */
     int fallback;                 /* 1: the plain FMM */
-    double diff_vs_plain;         /* relative RMS force difference of the choice from the judge */
+    double diff_vs_plain;         /* relative RMS force difference of the choice from the check solve */
     int proposed_order, proposed_depth, proposed_precision;  /* the network's proposal (0 if none) */
     float pred_rel_force_err, pred_ms;
     int nchecks;                  /* checked candidates (orders check_order[k]) */

@@ -34,7 +34,7 @@ def test_million_atoms_depth5_tensor_core_vs_fp32(pkg, systems):
 
 def test_trajectory_frames_keep_the_checked_choice(pkg, systems):
     """The tuner's choice, checked once on the first frame at 5e-4, stays within
-    5e-4 (+20 %: the tuner's own judge is the order-10 FMM at depth 4, about 1e-5
+    5e-4 (+20 %: the tuner's own check solve is the order-10 FMM at depth 4, about 1e-5
     from the depth-5 one) of the order-10, depth-5 FP32 baseline on later frames
     of a trajectory (0.01 nm kicks per frame), and is faster than it."""
     pytest.importorskip("torch")
